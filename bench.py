@@ -1,0 +1,297 @@
+"""Benchmark: verified candidates/s of the exhaustive PCA-16 solve on one GB300.
+
+Workload (one step): the hybrid solve of is_power2 -- 32 test vectors (12
+powers of two below 2^15, 0, 0x8000, 18 uniform non-powers; seed 1),
+branchless subset, iterative deepening to program length 7 (kernel depth 4),
+levels 1..3 built with the exact OEP pruner and the last instruction
+enumerated by the suffix kernel (split depth 3). A step proves whether a
+length-7 program exists. Synthetic data, generated from the seed.
+
+  value       candidates decided per second, device time (CUDA events on the
+              engine's stream around each solve)
+  e2e         the same count per second of wall time around pcagb_solve, the
+              C-ABI call with host buffers (task in, programs out)
+  roofline    the dominant kernel against its bound
+  cpu_baseline the reference algorithm (oracle port of tools/enumerate.c)
+              on the host cores, time-bounded sample of the same workload
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+With N > 1 (torchrun) every rank runs the same solve on its own GPU: the
+search does not shard (one task, one device), so ranks are independent
+replicas and value sums them over the max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = "verified candidates/s"
+UNIT = "candidates/s"
+WORKLOAD = ("is_power2, 32 tests, branchless, IDDFS to kernel depth 4 "
+            "(program length 7), split depth 3")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--max-depth", type=int, default=4)
+    ap.add_argument("--split", type=int, default=3)
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--cpu-budget", type=float, default=12.0,
+                    help="seconds of CPU work in the cpu_baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.t:
+            self.t.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            p = json.load(f)
+        return p, "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0}, "fallback"
+
+
+def cpu_baseline(task, depth: int, budget: float):
+    """The reference algorithm (oracle port of tools/enumerate.c, 32-bit OEP)
+    on every host core for `budget` seconds of the same workload."""
+    from oracle import oracle as O
+    cores = os.cpu_count() or 1
+    n, secs, _ = O.sample_throughput(task, depth, cores, budget)
+    return {"value": n / secs if secs > 0 else 0.0, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": (f"kernel depth {depth} DFS of the same task over (root, level-1) "
+                       f"candidate pairs handed out in DFS order, {secs:.1f} s on {cores} threads, "
+                       f"{n} candidates")}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def run_reference(args):
+    """Reference arm: the reference's CPU solver algorithm on the host cores."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from pca_gb300 import taskgen
+    from oracle.build import build_oracle
+    build_oracle()
+    task = taskgen.is_power2_task(args.seed)
+    per_step = max(2.0, min(10.0, 150.0 / max(1, args.steps + args.warmup)))
+    from oracle import oracle as O
+    cores = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        O.sample_throughput(task, args.max_depth, cores, per_step)
+    tot_n, tot_s = 0, 0.0
+    for _ in range(args.steps):
+        n, s, _ = O.sample_throughput(task, args.max_depth, cores, per_step)
+        tot_n += n
+        tot_s += s
+    v = tot_n / tot_s
+    sample = (f"kernel depth {args.max_depth} DFS of the workload over (root, level-1) candidate "
+              f"pairs, {per_step:.0f} s per step on {cores} threads")
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * tot_s / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u16",
+            "data": "synthetic", "config": {"workload": WORKLOAD, "seed": args.seed},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    rank, world, local = dist_env()
+    import torch
+    from pca_gb300.build import build_engine
+    if rank == 0 or not os.path.exists(os.path.join(REPO, "pca_gb300", "_lib", "libpcagb.so")):
+        build_engine()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        dist.barrier()
+    from pca_gb300 import taskgen
+    from pca_gb300.pcalib import Engine, OEP_EXACT_LIVE
+    torch.cuda.set_device(local)
+    task = taskgen.is_power2_task(args.seed)
+    eng = Engine(local, 0)
+    stream = torch.cuda.ExternalStream(eng.stream, device=local)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+
+    def step():
+        return eng.solve(task, max_depth=args.max_depth, split_depth=args.split,
+                         oep_mode=OEP_EXACT_LIVE, sol_cap=1 << 12)
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    sampler = ClockSampler(local)
+    sampler.start()
+    dev_ms, wall_s, cands, evals = [], [], 0, 0
+    launches, h2d, d2h = 0, 0, 0
+    insert_ms, insert_n, insert_children, suffix_ms, suffix_n = 0.0, 0, 0, 0.0, 0
+    sol = None
+    for _ in range(args.steps):
+        flush.fill_(1)  # L2 flush between timed steps (256 MB > 126 MB L2)
+        torch.cuda.synchronize()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        t0 = time.perf_counter()
+        sol = step()
+        t1 = time.perf_counter()
+        ev1.record(stream)
+        ev1.synchronize()
+        dev_ms.append(ev0.elapsed_time(ev1))
+        wall_s.append(t1 - t0)
+        cands += sum(sol.candidates)
+        evals += sum(sol.evaluations)
+        launches += sol.kernel_launches
+        h2d += sol.h2d_bytes
+        d2h += sol.d2h_bytes
+        insert_ms += sol.gpu_ms_insert
+        insert_n += sol.insert_launches
+        insert_children += sol.insert_children
+        suffix_ms += sol.gpu_ms_suffix
+        suffix_n += sol.suffix_launches
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    clocks = sampler.stop()
+    t_dev = sum(dev_ms) / 1000.0
+    t_wall = sum(wall_s)
+    if world > 1:
+        t = torch.tensor([t_dev, t_wall], dtype=torch.float64, device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_dev, t_wall = float(t[0]), float(t[1])
+        c = torch.tensor([cands], dtype=torch.float64, device=f"cuda:{local}")
+        dist.all_reduce(c)
+        total_cands = float(c[0])
+    else:
+        total_cands = float(cands)
+    if rank != 0:
+        dist.destroy_process_group()
+        return
+    pk, pk_kind = peaks()
+    sm_max = pk.get("sm_max_mhz", 2070.0)
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    # suffix kernel: value classes evaluated per second against the issue
+    # roofline (one warp instruction per SM sub-partition per clock)
+    suffix_evals_per_s = evals / (suffix_ms / 1000.0) if suffix_ms > 0 else 0.0
+    insert_gbs = 0.0
+    line = {
+        "metric": METRIC, "value": total_cands / t_dev, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": max(3, args.warmup),
+        "ms_per_step": 1000.0 * t_dev / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u16", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "seed": args.seed, "max_kernel_depth": args.max_depth,
+                   "split_depth": args.split, "oep": "exact regs+flags+live",
+                   "l2": "flushed between steps (256 MB write)",
+                   "parallelism": f"replicas x{world}"},
+        "optimal_depth": sol.optimal_depth if sol else None,
+        "candidates_per_step": cands // args.steps,
+        "evaluations_per_step": evals // args.steps,
+        "e2e": {"value": total_cands / t_wall, "unit": UNIT,
+                "h2d_bytes_per_step": h2d // args.steps, "d2h_bytes_per_step": d2h // args.steps},
+        "gpu_launches": launches,
+        "clocks": clocks,
+        "kernels_ms_per_step": {"suffix": suffix_ms / args.steps, "insert": insert_ms / args.steps,
+                                "expand_total": sum([]) if False else None},
+    }
+    line["kernels_ms_per_step"]["expand_total"] = None
+    line["roofline"] = {
+        "kernel": "k_suffix (last instruction, value classes)",
+        "bound": "int_issue",
+        "achieved": suffix_evals_per_s / 1e9, "unit": "Geval/s",
+        "peak": None, "frac": None, "traffic": None,
+        "peak_issue_gwarp_inst_s": sms * 4 * sm_max / 1e3,
+        "peak_source": pk_kind,
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(task, args.max_depth, args.cpu_budget)
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

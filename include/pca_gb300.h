@@ -1,0 +1,241 @@
+/*
+ * pca_gb300.h -- C ABI of libpcagb.so, the GB300-native PCA-16
+ * superoptimizer engine.
+ *
+ * Part 1 is a drop-in for the reference's libpca.so (Makefile:23-24), the
+ * library the reference's Python binds through ctypes
+ * (python/search_eval.py:74-188). Same symbol names, same argument meaning,
+ * same return codes, same struct layouts byte for byte. Each declaration
+ * cites the reference declaration it replaces.
+ *
+ * Part 2 is the GPU engine (pcagb_*): the exhaustive iterative-deepening
+ * solver whose hot path runs as CUDA kernels on one GB300. The reference
+ * has no library interface for its GPU path (gpu/hybrid.cu is a standalone
+ * program, gpu/hybrid.cu:631-836); these entry points are what that
+ * program's main loop would bind.
+ *
+ * Plain C types and pointers only. The caller owns every buffer.
+ */
+#ifndef PCA_GB300_H
+#define PCA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------- Part 1: libpca.so ABI ---------------------------------- */
+
+#define PCA_NUM_REGS    8     /* src/pca.h:25 */
+#define PCA_MEM_SIZE    256
+#define PCA_PROG_SIZE   256
+#define PCA_STACK_DEPTH 16
+#define PCA_NUM_PORTS   8
+#define MAX_TESTS       32    /* tasks/spec.h:17 */
+#define MAX_IO_PORTS    8     /* tasks/spec.h:18 */
+#define SEARCH_MAX_DEPTH 16   /* src/search_state.h:17 */
+
+#define PCA_RUNNING 0
+#define PCA_HALTED  1
+#define PCA_TIMEOUT 2
+#define PCA_FAULT   3
+
+/* src/pca.h:105-120 */
+typedef struct pca_vm {
+    uint16_t r[PCA_NUM_REGS];
+    uint16_t mem[PCA_MEM_SIZE];
+    uint16_t prog[PCA_PROG_SIZE];
+    uint8_t  pc;
+    uint8_t  sp;
+    uint16_t stack[PCA_STACK_DEPTH];
+    uint8_t  flags;
+    uint8_t  status;
+    uint64_t cycles;
+    uint16_t ports[PCA_NUM_PORTS];
+    void (*on_write)(struct pca_vm *vm, uint8_t port, uint16_t val);
+    void (*on_read)(struct pca_vm *vm, uint8_t port);
+} pca_vm_t;
+
+/* tasks/spec.h:20-34 */
+typedef struct {
+    uint16_t in[MAX_IO_PORTS];
+    uint16_t out[MAX_IO_PORTS];
+} test_case_t;
+
+typedef struct {
+    char     name[64];
+    uint64_t max_cycles;
+    uint8_t  input_ports[MAX_IO_PORTS];
+    int      num_inputs;
+    uint8_t  output_ports[MAX_IO_PORTS];
+    int      num_outputs;
+    test_case_t tests[MAX_TESTS];
+    int      num_tests;
+} task_spec_t;
+
+/* src/search_state.h:20-25 */
+typedef struct {
+    uint16_t regs[MAX_TESTS][PCA_NUM_REGS];
+    uint8_t  flags[MAX_TESTS];
+    uint8_t  live;
+    uint8_t  depth;
+} search_state_t;
+
+/* src/search_state.h:28-35 */
+typedef struct {
+    task_spec_t task;
+    uint8_t num_tests;
+    uint8_t num_inputs;
+    uint8_t num_outputs;
+    uint8_t input_regs[MAX_IO_PORTS];
+    uint8_t output_port;
+} search_ctx_t;
+
+/* src/search_state.h:38-52 (576-byte label record) */
+typedef struct {
+    uint64_t state_hash;
+    uint64_t oep_hash;
+    uint32_t task_id;
+    uint16_t parent_action;
+    uint8_t  depth;
+    uint8_t  budget_left;
+    uint8_t  live;
+    uint8_t  can_finish_optimally;
+    int8_t   remaining_steps;
+    uint8_t  _pad[2];
+    uint16_t regs[MAX_TESTS][PCA_NUM_REGS];
+    uint8_t  flags[MAX_TESTS];
+} dataset_state_record_t;
+
+/* VM: src/pca.h:123-127 */
+void pca_init(pca_vm_t *vm);
+void pca_load(pca_vm_t *vm, const uint16_t *prog, size_t len);
+void pca_step(pca_vm_t *vm);
+int  pca_run(pca_vm_t *vm, uint64_t max_cycles);
+/* src/pca.h:136-139: "%-4s ..." text of one instruction */
+void pca_disasm(uint16_t insn, char *buf, size_t len);
+void pca_disasm_prog(const uint16_t *prog, int count);
+
+/* Tasks: tasks/spec.h:37-46. task_load returns 0 / -1 (message on stderr). */
+int  task_load(const char *path, task_spec_t *spec);
+int  task_evaluate(const task_spec_t *spec, const uint16_t *prog, int prog_len);
+void task_print(const task_spec_t *spec);
+
+/* Search state: src/search_state.h:66-131 */
+int  search_ctx_init(search_ctx_t *ctx, const task_spec_t *task);         /* 0 / -1 */
+void search_state_init_root(const search_ctx_t *ctx, search_state_t *s);
+int  search_state_step(const search_ctx_t *ctx, const search_state_t *src,
+                       uint16_t insn, search_state_t *dst);               /* 1 ok / 0 illegal */
+uint64_t search_state_oep_hash64(const search_ctx_t *ctx, const search_state_t *s);
+uint64_t search_state_key_hash64(const search_ctx_t *ctx, const search_state_t *s);
+uint8_t  search_state_leaf_outputs(const search_ctx_t *ctx, const search_state_t *s);
+void search_state_serialize(const search_ctx_t *ctx, const search_state_t *s,
+                            uint32_t task_id, uint16_t parent_action,
+                            uint8_t target_depth, uint8_t can_finish_optimally,
+                            int8_t remaining_steps, dataset_state_record_t *out);
+int  search_gen_candidates_branchless(uint16_t *out, int max, const search_state_t *s);
+/* src/search_state.h:108-125. GPU-backed here: returns 1 and the shortest
+ * completion (the lexicographically first in candidate order among the
+ * shortest) or 0 if none exists within max_depth. Reentrant per thread. */
+int  search_exhaustive_complete(const search_ctx_t *ctx, const search_state_t *start,
+                                int max_depth, uint16_t *solution_insns,
+                                int *solution_len);
+/* src/search_state.h:129: states (children) the last completion evaluated */
+uint64_t search_exhaustive_states_explored(void);
+void search_state_dump(const search_ctx_t *ctx, const search_state_t *s, void *fp);
+
+/* ---------------- Part 2: GPU engine ------------------------------------- */
+
+/* Pruning key of the exact observational-equivalence pruner (OEP). */
+#define PCAGB_OEP_NONE       0 /* no pruning: every child kept (small cases) */
+#define PCAGB_OEP_EXACT      1 /* key = regs+flags (the reference's key,
+                                  tools/enumerate.c:379-384), exact compare,
+                                  first child in DFS order represents a key */
+#define PCAGB_OEP_EXACT_LIVE 2 /* key = regs+flags+live, exact compare
+                                  (default: order independent, sound) */
+
+/* Error codes (negative returns). */
+#define PCAGB_OK            0
+#define PCAGB_EINVAL       -1  /* bad task or options */
+#define PCAGB_ENOMEM       -2  /* HBM budget too small for the split chosen */
+#define PCAGB_ECUDA        -3  /* CUDA runtime error (see pcagb_last_error) */
+#define PCAGB_ELIMIT       -4  /* a device-side limit was hit (table full,
+                                  bounded wait expired); the result is void */
+#define PCAGB_ENODEV       -5  /* no CUDA device */
+
+typedef struct pcagb_engine pcagb_engine_t;
+
+typedef struct {
+    int max_depth;      /* largest kernel depth K tried (IDDFS 0..max_depth) */
+    int min_depth;      /* first K tried (0 = from the root check)           */
+    int split_depth;    /* deepest level built with OEP; -1 = automatic      */
+    int oep_mode;       /* PCAGB_OEP_*                                       */
+    int count_levels;   /* 1: build every level up to K with OEP so that the
+                           reference's per-depth counters are reproduced     */
+    int first_only;     /* 1: stop IDDFS at the first depth with a solution
+                           and keep only the first solution in DFS order     */
+    int reserved[6];
+} pcagb_opts_t;
+
+#define PCAGB_MAXD 17
+typedef struct {
+    int      optimal_depth;            /* -1: none within max_depth          */
+    int      stored;                   /* solutions written to the caller    */
+    uint64_t total_solutions;          /* solving programs at optimal depth  */
+    uint64_t candidates[PCAGB_MAXD];   /* programs decided per target depth  */
+    uint64_t evaluations[PCAGB_MAXD];  /* last-instruction value classes run */
+    uint64_t tried[PCAGB_MAXD];        /* the reference's "candidates" count
+                                          (valid with count_levels)          */
+    uint64_t pruned_cum[PCAGB_MAXD];   /* the reference's cumulative "OEP
+                                          pruned" (valid with count_levels)  */
+    uint64_t level_children[PCAGB_MAXD];
+    uint64_t level_survivors[PCAGB_MAXD];
+    double   seconds;                  /* wall time of the solve             */
+    double   gpu_ms_expand;            /* device time building levels        */
+    double   gpu_ms_suffix;            /* device time in the suffix kernels  */
+    double   gpu_ms_insert;            /* device time in the OEP insert kernel */
+    uint64_t kernel_launches;          /* kernels this solve launched        */
+    uint64_t insert_launches;
+    uint64_t suffix_launches;
+    uint64_t h2d_bytes;                /* host->device bytes this solve copied */
+    uint64_t d2h_bytes;                /* device->host bytes                 */
+    uint64_t insert_children;          /* children the insert kernels hashed */
+    int      split_used;
+    int      reserved[7];
+} pcagb_result_t;
+
+const char *pcagb_last_error(void);
+void pcagb_default_opts(pcagb_opts_t *o);
+
+/* One engine per device and host thread; it owns device buffers sized by
+ * hbm_budget_bytes (0 = 60% of the device's free memory). */
+int  pcagb_engine_create(int device, size_t hbm_budget_bytes, pcagb_engine_t **out);
+void pcagb_engine_destroy(pcagb_engine_t *e);
+
+/* Exhaustive shortest-program solve of one task (the loop of
+ * gpu/hybrid.cu:699-824 and tools/enumerate.c:624-662). Solutions are full
+ * programs (IN scaffold + kernel + OUT + HLT), 16 words each, in DFS order of
+ * the reference's candidate generator; at most sol_cap are stored. */
+int  pcagb_solve(pcagb_engine_t *e, const task_spec_t *task, const pcagb_opts_t *opts,
+                 pcagb_result_t *res, uint16_t *sol_progs, int *sol_lens, int sol_cap);
+
+/* IDDFS completion from an arbitrary branchless state (the GPU form of
+ * search_exhaustive_complete, src/search_state.c:418-453). Returns 1 found /
+ * 0 none / negative error. */
+int  pcagb_complete(pcagb_engine_t *e, const search_ctx_t *ctx, const search_state_t *start,
+                    int max_depth, uint16_t *solution_insns, int *solution_len,
+                    uint64_t *states_explored);
+
+/* The CUDA stream (cudaStream_t) every kernel of this engine runs on, so a
+ * caller can time a solve with events on that stream. */
+void *pcagb_engine_stream(pcagb_engine_t *e);
+
+/* Number of generator candidates for a live mask (src/search_state.c:280-330). */
+int  pcagb_num_candidates(uint8_t live);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,53 @@
+"""Build the CPU oracle (test infrastructure): oracle/_build/liborc.so and
+oracle/_build/oracle_enumerate, plus, where the reference tree exists on this
+machine, the reference's own CPU solver via oracle/build_ref.sh.
+
+    python oracle/build.py [--force]
+"""
+from __future__ import annotations
+
+import os
+import platform
+import subprocess
+import sys
+
+ORACLE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(ORACLE, "_build")
+REFERENCE_ROOT = "/root/reference"
+
+
+def _newer(target: str, deps: list[str]) -> bool:
+    return os.path.exists(target) and all(
+        os.path.getmtime(d) <= os.path.getmtime(target) for d in deps)
+
+
+def build_oracle(force: bool = False) -> str:
+    os.makedirs(BUILD, exist_ok=True)
+    stamp = os.path.join(BUILD, ".machine")
+    if not os.path.exists(stamp) or open(stamp).read().strip() != platform.machine():
+        force = True
+    src = os.path.join(ORACLE, "pca_oracle.c")
+    deps = [src, os.path.join(ORACLE, "pca_oracle.h")]
+    flags = ["-O2", "-std=c99", "-Wall", "-Wextra", "-pthread"]
+    lib = os.path.join(BUILD, "liborc.so")
+    cli = os.path.join(BUILD, "oracle_enumerate")
+    procs = []
+    if force or not _newer(lib, deps):
+        procs.append(subprocess.Popen(["gcc", *flags, "-shared", "-fPIC", src, "-o", lib]))
+    cli_src = os.path.join(ORACLE, "oracle_cli.c")
+    if force or not _newer(cli, deps + [cli_src]):
+        procs.append(subprocess.Popen(["gcc", *flags, src, cli_src, "-o", cli]))
+    for p in procs:
+        if p.wait() != 0:
+            raise RuntimeError("oracle build failed")
+    with open(stamp, "w") as f:
+        f.write(platform.machine() + "\n")
+    if os.path.isdir(REFERENCE_ROOT) and (
+            force or not os.path.exists(os.path.join(ORACLE, "_ref", "enumerate"))):
+        subprocess.run(["sh", os.path.join(ORACLE, "build_ref.sh"), REFERENCE_ROOT],
+                       check=True, capture_output=True)
+    return lib
+
+
+if __name__ == "__main__":
+    print(build_oracle("--force" in sys.argv))

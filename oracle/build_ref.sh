@@ -1,0 +1,28 @@
+#!/bin/sh
+# Compile the reference's own CPU solver and its libpca.so from the reference
+# sources, in place, into oracle/_ref/ (git-ignored). Used only as a checker:
+# tests and golden-fixture generation compare against these outputs.
+#
+#   oracle/build_ref.sh [REFERENCE_ROOT]
+#
+# REFERENCE_ROOT defaults to /root/reference. Without it, this script exits 0
+# and builds nothing (the GPU machine has no reference tree).
+set -e
+REF=${1:-/root/reference}
+HERE=$(cd "$(dirname "$0")" && pwd)
+OUT="$HERE/_ref"
+if [ ! -f "$REF/tools/enumerate.c" ]; then
+    echo "build_ref: no reference tree at $REF; skipping" >&2
+    exit 0
+fi
+mkdir -p "$OUT"
+CFLAGS="-O2 -std=c99 -w"
+gcc $CFLAGS -o "$OUT/enumerate" \
+    "$REF/src/vm.c" "$REF/src/asm.c" "$REF/src/search_state.c" \
+    "$REF/tasks/spec.c" "$REF/tools/enumerate.c"
+gcc $CFLAGS -shared -fPIC -o "$OUT/libpca.so" \
+    "$REF/src/vm.c" "$REF/src/asm.c" "$REF/src/search_state.c" "$REF/tasks/spec.c"
+gcc $CFLAGS -o "$OUT/gen_tasks" \
+    "$REF/src/vm.c" "$REF/src/asm.c" "$REF/src/search_state.c" \
+    "$REF/tasks/spec.c" "$REF/tools/gen_tasks.c"
+echo "build_ref: built $OUT/enumerate $OUT/libpca.so $OUT/gen_tasks"

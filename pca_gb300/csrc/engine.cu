@@ -1,0 +1,883 @@
+/*
+ * engine.cu -- the GPU engine behind pcagb_solve / pcagb_complete and the
+ * GPU-backed search_exhaustive_complete of the libpca ABI.
+ *
+ * Iterative deepening over the kernel length K, as in the reference's
+ * tools/enumerate.c:624-662 and gpu/hybrid.cu:699-824, restructured for one
+ * GB300:
+ *   - levels 1..S are built breadth-first on the device, each deduplicated
+ *     by the exact OEP table and kept in HBM in DFS order (levels do not
+ *     depend on K, so each is built once per solve, not once per K);
+ *   - the remaining K-S <= 3 instructions are enumerated by the suffix
+ *     kernel, which takes the role of gpu/hybrid.cu:163-275;
+ *   - the host only reads back sizes, counters and the solving records.
+ * Device memory comes from one arena allocated at engine creation: levels
+ * grow from the bottom, per-expansion scratch (hash table, bitmap, scan
+ * buffers) from the top, so a solve performs no cudaMalloc.
+ */
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/pca_gb300.h"
+#include "engine_kernels.cuh"
+#include "gen_tables.h"
+
+namespace pcagb {
+
+static thread_local std::string g_err;
+
+static void set_err(const char *fmt, ...)
+{
+    char b[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(b, sizeof b, fmt, ap);
+    va_end(ap);
+    g_err = b;
+}
+
+#define CK(call)                                                                       \
+    do {                                                                               \
+        cudaError_t e_ = (call);                                                       \
+        if (e_ != cudaSuccess) {                                                       \
+            set_err("%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, \
+                    __LINE__);                                                         \
+            return PCAGB_ECUDA;                                                        \
+        }                                                                              \
+    } while (0)
+
+struct Level {
+    uint64_t n = 0;
+    uint16_t *regs = nullptr;
+    uint8_t *flags = nullptr;
+    uint8_t *live = nullptr;
+    uint32_t *parent = nullptr;
+    uint16_t *cidx = nullptr;
+    uint64_t *child_off = nullptr;  /* set when this level is expanded */
+    uint64_t children = 0;
+    uint64_t hist[128] = {};
+};
+
+struct PathGather {
+    const uint32_t *parent[SEARCH_MAX_DEPTH + 1];
+    const uint16_t *cidx[SEARCH_MAX_DEPTH + 1];
+};
+
+/* For each record, write the candidate indices of its prefix path. */
+__global__ void k_gather_paths(PathGather G, int S, const ulonglong2 *rec, uint64_t n,
+                               uint16_t *out)
+{
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t q = rec[i].x;
+        for (int d = S; d >= 1; d--) {
+            out[i * SEARCH_MAX_DEPTH + d - 1] = G.cidx[d][q];
+            q = G.parent[d][q];
+        }
+    }
+}
+
+}  // namespace pcagb
+
+using namespace pcagb;
+
+struct pcagb_engine {
+    int device = 0;
+    int sms = 0;
+    cudaStream_t stream = nullptr;
+    char *arena = nullptr;
+    size_t cap = 0, bottom = 0, top = 0;
+    uint32_t *d_cand_uop = nullptr, *d_vc_uop = nullptr;
+    uint16_t *d_vc_first = nullptr;
+    unsigned long long *d_small = nullptr;   /* [0] sol count [1] first [2] count [8..135] hist */
+    uint32_t *d_status = nullptr;
+    ulonglong2 *d_sol = nullptr;
+    uint64_t sol_cap = 1u << 20;
+    uint16_t *d_paths = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
+    uint64_t launches = 0;
+    uint64_t h2d = 0, d2h = 0;
+    uint64_t insert_launches = 0, suffix_launches = 0, insert_children = 0;
+    float ms_insert = 0;
+
+    /* per solve */
+    std::vector<Level> levels;
+    int TPC = 32;
+    int T = 0;
+    bool no_oep = false;
+    int max_feasible = SEARCH_MAX_DEPTH;
+    uint8_t root_live = 0;
+    TaskDev td{};
+    float ms_expand = 0, ms_suffix = 0;
+
+    void *alloc_bottom(size_t bytes)
+    {
+        bytes = (bytes + 255) & ~size_t(255);
+        if (bottom + bytes > top) return nullptr;
+        void *p = arena + bottom;
+        bottom += bytes;
+        return p;
+    }
+    void *alloc_top(size_t bytes)
+    {
+        bytes = (bytes + 255) & ~size_t(255);
+        if (top < bottom + bytes) return nullptr;
+        top -= bytes;
+        return arena + top;
+    }
+    int grid(int per_sm = 4) const { return sms * per_sm; }
+};
+
+namespace {
+
+/* every host<->device copy of a solve goes through here and is counted */
+cudaError_t e_copy(pcagb_engine *e, void *dst, const void *src, size_t n, cudaMemcpyKind kind,
+                   cudaStream_t st)
+{
+    if (kind == cudaMemcpyHostToDevice) e->h2d += n;
+    if (kind == cudaMemcpyDeviceToHost) e->d2h += n;
+    return cudaMemcpyAsync(dst, src, n, kind, st);
+}
+
+int check_launch(pcagb_engine *e)
+{
+    e->launches++;
+    cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) {
+        set_err("kernel launch failed: %s", cudaGetErrorString(err));
+        return PCAGB_ECUDA;
+    }
+    return PCAGB_OK;
+}
+
+/* Exclusive scan of a[0..n) in place; returns the total in *total. */
+int exclusive_scan(pcagb_engine *e, uint64_t *a, uint64_t n, uint64_t *total)
+{
+    if (n == 0) { *total = 0; return PCAGB_OK; }
+    uint64_t nb = (n + kScanBlock - 1) / kScanBlock;
+    size_t saved = e->top;
+    uint64_t *sums = (uint64_t *)e->alloc_top((nb + 1) * sizeof(uint64_t));
+    if (!sums) { set_err("arena exhausted in scan"); return PCAGB_ENOMEM; }
+    k_scan_local<<<(unsigned)nb, 256, 0, e->stream>>>(a, n, sums);
+    int rc = check_launch(e);
+    if (rc) return rc;
+    if (nb == 1) {
+        CK(e_copy(e, total, sums, sizeof(uint64_t), cudaMemcpyDeviceToHost, e->stream));
+        CK(cudaStreamSynchronize(e->stream));
+    } else {
+        rc = exclusive_scan(e, sums, nb, total);
+        if (rc) return rc;
+        k_scan_add<<<(unsigned)nb, 256, 0, e->stream>>>(a, n, sums);
+        rc = check_launch(e);
+        if (rc) return rc;
+    }
+    e->top = saved;
+    return PCAGB_OK;
+}
+
+LevelDev view(const Level &L) { return LevelDev{L.regs, L.flags, L.live, L.child_off, L.n}; }
+
+int alloc_level(pcagb_engine *e, Level &L, uint64_t n)
+{
+    L.n = n;
+    L.regs = (uint16_t *)e->alloc_bottom(n * 8 * e->TPC * 2);
+    L.flags = (uint8_t *)e->alloc_bottom(n * e->TPC);
+    L.live = (uint8_t *)e->alloc_bottom(n);
+    L.parent = (uint32_t *)e->alloc_bottom(n * 4);
+    L.cidx = (uint16_t *)e->alloc_bottom(n * 2);
+    if (!L.regs || !L.flags || !L.live || !L.parent || !L.cidx) return PCAGB_ENOMEM;
+    return PCAGB_OK;
+}
+
+int fetch_hist(pcagb_engine *e, Level &L)
+{
+    unsigned long long *h = e->d_small + 8;
+    CK(cudaMemsetAsync(h, 0, 128 * sizeof(unsigned long long), e->stream));
+    k_live_hist<<<e->grid(2), 256, 0, e->stream>>>(L.live, L.n, h);
+    int rc = check_launch(e);
+    if (rc) return rc;
+    CK(e_copy(e, L.hist, h, sizeof L.hist, cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    return PCAGB_OK;
+}
+
+template <int TPC>
+int launch_expand(pcagb_engine *e, const Level &P, unsigned long long *table, uint64_t tmask)
+{
+    k_expand_insert<TPC><<<e->grid(4), kThreads, 0, e->stream>>>(view(P), e->td, table, tmask,
+                                                                 e->d_status);
+    return check_launch(e);
+}
+
+template <int TPC>
+int launch_materialize(pcagb_engine *e, const Level &P, const uint32_t *bitmap,
+                       const uint64_t *word_off, Level &C)
+{
+    LevelOut out{C.regs, C.flags, C.live, C.parent, C.cidx};
+    k_materialize<TPC><<<e->grid(4), kThreads, 0, e->stream>>>(view(P), e->td, bitmap, word_off,
+                                                               out);
+    return check_launch(e);
+}
+
+/* Build level d+1 from level d. Returns PCAGB_ENOMEM (and leaves the arena
+ * as it was) when the level does not fit. */
+int build_level(pcagb_engine *e, int d)
+{
+    Level &P = e->levels[d];
+    const size_t bottom0 = e->bottom, top0 = e->top;
+    auto fail = [&](int rc) {
+        e->bottom = bottom0;
+        e->top = top0;
+        if (rc == PCAGB_ENOMEM) P.child_off = nullptr;
+        return rc;
+    };
+    if (!P.child_off) {
+        P.child_off = (uint64_t *)e->alloc_bottom((P.n + 1) * sizeof(uint64_t));
+        if (!P.child_off) return fail(PCAGB_ENOMEM);
+        k_child_counts<<<e->grid(2), 256, 0, e->stream>>>(P.live, P.n, P.child_off);
+        int rc = check_launch(e);
+        if (rc) return rc;
+        rc = exclusive_scan(e, P.child_off, P.n + 1, &P.children);
+        if (rc) return fail(rc);
+    }
+    const uint64_t children = P.children;
+    if (children >= (1ull << 38)) return fail(PCAGB_ENOMEM);
+    const uint64_t words = (children + 31) / 32;
+
+    cudaEventRecord(e->ev0, e->stream);
+    uint32_t *bitmap = (uint32_t *)e->alloc_top(words * 4 + 4);
+    if (!bitmap) return fail(PCAGB_ENOMEM);
+    uint64_t survivors = children;
+    if (e->no_oep) {
+        k_mark_all<<<e->grid(2), 256, 0, e->stream>>>(bitmap, words, children);
+        int rc = check_launch(e);
+        if (rc) return rc;
+    } else {
+        if (P.n >= (1ull << 28)) return fail(PCAGB_ENOMEM);
+        uint64_t slots = 1024;
+        while (slots < 2 * children) slots <<= 1;
+        unsigned long long *table = (unsigned long long *)e->alloc_top(slots * 8);
+        if (!table) return fail(PCAGB_ENOMEM);
+        /* rough room check for the new level before spending the time */
+        CK(cudaMemsetAsync(table, 0, slots * 8, e->stream));
+        CK(cudaMemsetAsync(bitmap, 0, words * 4 + 4, e->stream));
+        CK(cudaMemsetAsync(e->d_small + 2, 0, 8, e->stream));
+        cudaEventRecord(e->ev2, e->stream);
+        int rc = e->TPC == 16 ? launch_expand<16>(e, P, table, slots - 1)
+                              : launch_expand<32>(e, P, table, slots - 1);
+        if (rc) return rc;
+        cudaEventRecord(e->ev3, e->stream);
+        k_mark<<<e->grid(4), 256, 0, e->stream>>>(table, slots, P.child_off, bitmap,
+                                                  e->d_small + 2);
+        rc = check_launch(e);
+        if (rc) return rc;
+        uint32_t status = 0;
+        CK(e_copy(e, &status, e->d_status, 4, cudaMemcpyDeviceToHost, e->stream));
+        CK(e_copy(e, &survivors, e->d_small + 2, 8, cudaMemcpyDeviceToHost, e->stream));
+        CK(cudaStreamSynchronize(e->stream));
+        if (status) {
+            set_err("expansion of level %d hit a device limit (status %u)", d + 1, status);
+            return PCAGB_ELIMIT;
+        }
+        float ims = 0;
+        cudaEventElapsedTime(&ims, e->ev2, e->ev3);
+        e->ms_insert += ims;
+        e->insert_launches++;
+        e->insert_children += children;
+    }
+    uint64_t *word_off = (uint64_t *)e->alloc_top((words + 1) * sizeof(uint64_t));
+    if (!word_off) return fail(PCAGB_ENOMEM);
+    k_popc<<<e->grid(2), 256, 0, e->stream>>>(bitmap, words, word_off);
+    int rc = check_launch(e);
+    if (rc) return rc;
+    uint64_t total = 0;
+    rc = exclusive_scan(e, word_off, words, &total);
+    if (rc) return fail(rc);
+    if (total != survivors) {
+        set_err("internal: bitmap holds %llu winners, table %llu", (unsigned long long)total,
+                (unsigned long long)survivors);
+        return PCAGB_ELIMIT;
+    }
+    Level C;
+    if (survivors >= (1ull << 28)) return fail(PCAGB_ENOMEM);
+    if (alloc_level(e, C, survivors) != PCAGB_OK) return fail(PCAGB_ENOMEM);
+    rc = e->TPC == 16 ? launch_materialize<16>(e, P, bitmap, word_off, C)
+                      : launch_materialize<32>(e, P, bitmap, word_off, C);
+    if (rc) return rc;
+    cudaEventRecord(e->ev1, e->stream);
+    rc = fetch_hist(e, C);
+    if (rc) return rc;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e->ev0, e->ev1);
+    e->ms_expand += ms;
+    e->top = top0;
+    e->levels.push_back(C);
+    return PCAGB_OK;
+}
+
+struct RawSol {
+    std::vector<uint16_t> kernel;  /* kernel instructions */
+    uint32_t out_reg;
+    /* DFS-order key */
+    std::vector<uint32_t> key;
+};
+
+/* Run the last stage at depth K from level S (suffix depth K-S, or the leaf
+ * check when K == S). Fills raw solutions in DFS order. */
+int run_stage(pcagb_engine *e, int S, int K, uint64_t *nrec_out, std::vector<RawSol> *sols,
+              bool first_only)
+{
+    const GenTables &gt = gen_tables();
+    Level &L = e->levels[S];
+    const int s = K - S;
+    CK(cudaMemsetAsync(e->d_small, 0, 8, e->stream));
+    CK(cudaMemsetAsync(e->d_small + 1, 0xFF, 8, e->stream));
+    SolBuf sb{e->d_small, e->d_sol, e->sol_cap, e->d_small + 1};
+    cudaEventRecord(e->ev0, e->stream);
+    int rc = PCAGB_OK;
+    const bool t16 = e->TPC == 16;
+    if (s == 0) {
+        if (t16) k_leaf<16><<<e->grid(4), 256, 0, e->stream>>>(view(L), e->td, sb);
+        else k_leaf<32><<<e->grid(4), 256, 0, e->stream>>>(view(L), e->td, sb);
+    } else if (s == 1) {
+        if (t16) k_suffix<16, 1><<<e->grid(8), kThreads, 0, e->stream>>>(view(L), e->td, sb, 1, 1);
+        else k_suffix<32, 1><<<e->grid(8), kThreads, 0, e->stream>>>(view(L), e->td, sb, 1, 1);
+    } else {
+        int ncmax = 0;
+        for (int m = 0; m < 128; m++)
+            if (L.hist[m]) ncmax = std::max(ncmax, gt.nc(m));
+        uint32_t chunk = s == 2 ? 16 : 1;
+        uint32_t cpp = (uint32_t)((ncmax + chunk - 1) / chunk);
+        if (s == 2) {
+            if (t16) k_suffix<16, 2><<<e->grid(8), kThreads, 0, e->stream>>>(view(L), e->td, sb, cpp, chunk);
+            else k_suffix<32, 2><<<e->grid(8), kThreads, 0, e->stream>>>(view(L), e->td, sb, cpp, chunk);
+        } else if (s == 3) {
+            if (t16) k_suffix<16, 3><<<e->grid(8), kThreads, 0, e->stream>>>(view(L), e->td, sb, cpp, chunk);
+            else k_suffix<32, 3><<<e->grid(8), kThreads, 0, e->stream>>>(view(L), e->td, sb, cpp, chunk);
+        } else {
+            set_err("suffix depth %d not supported (split too shallow)", s);
+            return PCAGB_ENOMEM;
+        }
+    }
+    rc = check_launch(e);
+    if (rc) return rc;
+    cudaEventRecord(e->ev1, e->stream);
+    unsigned long long nrec = 0, first = 0;
+    CK(e_copy(e, &nrec, e->d_small, 8, cudaMemcpyDeviceToHost, e->stream));
+    CK(e_copy(e, &first, e->d_small + 1, 8, cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e->ev0, e->ev1);
+    e->ms_suffix += ms;
+    e->suffix_launches++;
+    *nrec_out = nrec;
+    if (!nrec) return PCAGB_OK;
+
+
+    /* Fetch the records (or, past the buffer or in first-only mode, the
+       DFS-first one rebuilt from its packed key) and their prefix paths. */
+    std::vector<ulonglong2> rec;
+    if (first_only || nrec > e->sol_cap) {
+        if (!first_only) {
+            set_err("%llu solving records exceed the buffer of %llu",
+                    (unsigned long long)nrec, (unsigned long long)e->sol_cap);
+            return PCAGB_ELIMIT;
+        }
+        const uint64_t m1 = (first >> 24) & 4095, m2 = (first >> 12) & 4095, fc = first & 4095;
+        /* low 16 bits with bit 15 set: a candidate index, not a class */
+        rec.push_back(make_ulonglong2(first >> 36, (m1 << 32) | (m2 << 16) | (0x8000u | fc)));
+    } else {
+        rec.resize(nrec);
+        CK(e_copy(e, rec.data(), e->d_sol, nrec * sizeof(ulonglong2), cudaMemcpyDeviceToHost,
+                           e->stream));
+        CK(cudaStreamSynchronize(e->stream));
+    }
+    std::vector<uint16_t> paths(rec.size() * SEARCH_MAX_DEPTH, 0);
+    if (S > 0) {
+        const size_t top0 = e->top;
+        ulonglong2 *d_rec = (ulonglong2 *)e->alloc_top(rec.size() * sizeof(ulonglong2));
+        uint16_t *d_paths = (uint16_t *)e->alloc_top(paths.size() * 2);
+        if (!d_rec || !d_paths) { set_err("arena exhausted gathering paths"); return PCAGB_ENOMEM; }
+        CK(e_copy(e, d_rec, rec.data(), rec.size() * sizeof(ulonglong2),
+                           cudaMemcpyHostToDevice, e->stream));
+        PathGather G{};
+        for (int d = 1; d <= S; d++) {
+            G.parent[d] = e->levels[d].parent;
+            G.cidx[d] = e->levels[d].cidx;
+        }
+        k_gather_paths<<<64, 256, 0, e->stream>>>(G, S, d_rec, rec.size(), d_paths);
+        rc = check_launch(e);
+        if (rc) return rc;
+        CK(e_copy(e, paths.data(), d_paths, paths.size() * 2, cudaMemcpyDeviceToHost,
+                           e->stream));
+        CK(cudaStreamSynchronize(e->stream));
+        e->top = top0;
+    }
+    for (size_t i = 0; i < rec.size(); i++) {
+        RawSol base;
+        uint32_t mask = (e->root_live >> 1) & 127u;
+        auto take = [&](uint32_t c) {
+            const uint32_t idx = gt.cand_off[mask] + c;
+            base.kernel.push_back(gt.cand[idx]);
+            base.key.push_back(c);
+            mask |= 1u << (UOP_RD(gt.cand_uop[idx]) - 1);
+        };
+        for (int d = 0; d < S; d++) take(paths[i * SEARCH_MAX_DEPTH + d]);
+        const uint32_t m1 = (uint32_t)(rec[i].y >> 32), m2 = (uint32_t)((rec[i].y >> 16) & 0xFFFF);
+        const uint32_t low = (uint32_t)(rec[i].y & 0xFFFF);
+        if (s >= 2) take(m1);
+        if (s >= 3) take(m2);
+        if (s == 0) {
+            base.out_reg = low;
+            base.key.push_back(0);
+            sols->push_back(base);
+            continue;
+        }
+        if (low & 0x8000u) {
+            RawSol r = base;
+            const uint32_t c = low & 0x7FFF;
+            const uint32_t idx = gt.cand_off[mask] + c;
+            r.kernel.push_back(gt.cand[idx]);
+            r.key.push_back(c);
+            r.out_reg = UOP_RD(gt.cand_uop[idx]);
+            sols->push_back(r);
+            continue;
+        }
+        for (uint32_t c = 0; c < (uint32_t)gt.nc(mask); c++) {
+            const uint32_t idx = gt.cand_off[mask] + c;
+            if (gt.cand_vc[idx] != low) continue;
+            RawSol r = base;
+            r.kernel.push_back(gt.cand[idx]);
+            r.key.push_back(c);
+            r.out_reg = UOP_RD(gt.cand_uop[idx]);
+            sols->push_back(r);
+        }
+    }
+    std::sort(sols->begin(), sols->end(),
+              [](const RawSol &a, const RawSol &b) { return a.key < b.key; });
+    return PCAGB_OK;
+}
+
+/* Host-side step for re-verification and for the reference-key dedup of the
+   solving leaves (tools/enumerate.c:380-384 applies OEP to leaves too). */
+void leaf_key(const task_spec_t *task, const search_state_t &root, const std::vector<uint16_t> &k,
+              std::vector<uint8_t> *key)
+{
+    search_ctx_t ctx;
+    search_ctx_init(&ctx, task);
+    search_state_t s = root, n;
+    for (uint16_t insn : k) {
+        search_state_step(&ctx, &s, insn, &n);
+        s = n;
+    }
+    key->clear();
+    for (int t = 0; t < task->num_tests; t++) {
+        const uint8_t *p = (const uint8_t *)s.regs[t];
+        key->insert(key->end(), p, p + 16);
+        key->push_back(s.flags[t]);
+    }
+}
+
+struct RunSpec {
+    search_state_t root;     /* level-0 state */
+    int T;
+    uint16_t target[MAX_TESTS];
+};
+
+/* Core IDDFS shared by pcagb_solve and pcagb_complete. */
+int run_iddfs(pcagb_engine *e, const RunSpec &rs, const pcagb_opts_t &o, pcagb_result_t *res,
+              std::vector<RawSol> *sols)
+{
+    const GenTables &gt = gen_tables();
+    auto t_start = std::chrono::steady_clock::now();
+    memset(res, 0, sizeof *res);
+    res->optimal_depth = -1;
+    e->levels.clear();
+    e->bottom = 0;
+    e->top = e->cap;
+    e->ms_expand = e->ms_suffix = e->ms_insert = 0;
+    e->launches = 0;
+    e->h2d = e->d2h = 0;
+    e->insert_launches = e->suffix_launches = e->insert_children = 0;
+    e->max_feasible = SEARCH_MAX_DEPTH;
+    e->T = rs.T;
+    e->TPC = rs.T <= 16 ? 16 : 32;
+    e->no_oep = o.oep_mode == PCAGB_OEP_NONE;
+    e->root_live = rs.root.live;
+    memset(&e->td, 0, sizeof e->td);
+    e->td.T = rs.T;
+    e->td.key_live = o.oep_mode == PCAGB_OEP_EXACT_LIVE;
+    for (int t = 0; t < rs.T; t++) e->td.target[t] = rs.target[t];
+    CK(cudaSetDevice(e->device));
+    CK(cudaMemsetAsync(e->d_status, 0, 4, e->stream));
+
+    /* level 0 */
+    Level L0;
+    if (alloc_level(e, L0, 1) != PCAGB_OK) { set_err("arena too small"); return PCAGB_ENOMEM; }
+    {
+        std::vector<uint16_t> regs(8 * e->TPC, 0);
+        std::vector<uint8_t> flags(e->TPC, 0);
+        for (int t = 0; t < rs.T; t++) {
+            for (int r = 1; r < 8; r++) regs[r * e->TPC + t] = rs.root.regs[t][r];
+            flags[t] = rs.root.flags[t];
+        }
+        uint32_t zero32 = 0;
+        uint16_t zero16 = 0;
+        CK(e_copy(e, L0.regs, regs.data(), regs.size() * 2, cudaMemcpyHostToDevice, e->stream));
+        CK(e_copy(e, L0.flags, flags.data(), flags.size(), cudaMemcpyHostToDevice, e->stream));
+        CK(e_copy(e, L0.live, &rs.root.live, 1, cudaMemcpyHostToDevice, e->stream));
+        CK(e_copy(e, L0.parent, &zero32, 4, cudaMemcpyHostToDevice, e->stream));
+        CK(e_copy(e, L0.cidx, &zero16, 2, cudaMemcpyHostToDevice, e->stream));
+        CK(cudaStreamSynchronize(e->stream));
+        L0.hist[(rs.root.live >> 1) & 127] = 1;
+    }
+    e->levels.push_back(L0);
+    res->level_children[0] = res->level_survivors[0] = 1;
+
+    /* K = 0: does a live register already hold the target? */
+    if (o.min_depth <= 0) {
+        for (uint32_t r = 1; r < 8; r++) {
+            if (!((rs.root.live >> r) & 1u)) continue;
+            bool ok = true;
+            for (int t = 0; t < rs.T && ok; t++) ok = rs.root.regs[t][r] == rs.target[t];
+            if (ok) {
+                RawSol s0;
+                s0.out_reg = r;
+                sols->push_back(s0);
+            }
+        }
+        if (!sols->empty()) {
+            res->optimal_depth = 0;
+            res->tried[0] = sols->size();
+            res->total_solutions = sols->size();
+        }
+    }
+    uint64_t pruned_cum = 0;
+    for (int K = std::max(1, o.min_depth); K <= o.max_depth && res->optimal_depth < 0; K++) {
+        int S_target = o.count_levels ? K : K - 1;
+        if (o.split_depth >= 0) S_target = std::min(S_target, o.split_depth);
+        while ((int)e->levels.size() - 1 < S_target && (int)e->levels.size() - 1 < e->max_feasible) {
+            const int d = (int)e->levels.size() - 1;
+            int rc = build_level(e, d);
+            if (rc == PCAGB_ENOMEM) {
+                e->max_feasible = d;
+                break;
+            }
+            if (rc) return rc;
+            res->level_children[d + 1] = e->levels[d].children;
+            res->level_survivors[d + 1] = e->levels[d + 1].n;
+        }
+        const int S = std::min(S_target, (int)e->levels.size() - 1);
+        const int s = K - S;
+        if (o.count_levels && S < S_target) {
+            set_err("count_levels: level %d does not fit the HBM budget", S + 1);
+            return PCAGB_ENOMEM;
+        }
+        if (s > 3) {
+            set_err("depth %d needs level %d in HBM; the budget holds level %d", K, K - 3, S);
+            return PCAGB_ENOMEM;
+        }
+        res->split_used = S;
+        const Level &LS = e->levels[S];
+        uint64_t cands = 0, evals = 0;
+        for (int m = 0; m < 128; m++) {
+            if (!LS.hist[m]) continue;
+            if (s >= 1) cands += LS.hist[m] * gt.f[s][m];
+            /* evaluations: value classes scanned at the last position */
+            if (s == 1) evals += LS.hist[m] * (uint64_t)gt.nvc(m);
+        }
+        if (s >= 2) {
+            /* sum over middle paths of the last mask's class count */
+            std::vector<uint64_t> g(128, 0), g2(128, 0);
+            for (int m = 0; m < 128; m++) g[m] = gt.nvc(m);
+            for (int step = 1; step < s; step++) {
+                for (int m = 0; m < 128; m++) {
+                    uint64_t sum = 0;
+                    for (uint32_t i = gt.cand_off[m]; i < gt.cand_off[m + 1]; i++)
+                        sum += g[(m | (1u << (UOP_RD(gt.cand_uop[i]) - 1))) & 127];
+                    g2[m] = sum;
+                }
+                g.swap(g2);
+            }
+            for (int m = 0; m < 128; m++) evals += LS.hist[m] * g[m];
+        }
+        res->candidates[K] = s == 0 ? LS.n : cands;
+        res->evaluations[K] = s == 0 ? LS.n : evals;
+        uint64_t nrec = 0;
+        std::vector<RawSol> found;
+        int rc = run_stage(e, S, K, &nrec, &found, o.first_only != 0);
+        if (rc) return rc;
+        /* the reference's counters (exact when every level up to K is built) */
+        uint64_t tried = 0, pruned = 0;
+        for (int j = 1; j <= S; j++) {
+            tried += res->level_children[j];
+            pruned += res->level_children[j] - res->level_survivors[j];
+        }
+        for (int i = 1; i <= s; i++)
+            for (int m = 0; m < 128; m++) tried += LS.hist[m] * gt.f[i][m];
+        pruned_cum += pruned;
+        res->tried[K] = tried + (s == 0 ? nrec : 0);
+        res->pruned_cum[K] = pruned_cum;
+        if (nrec) {
+            res->optimal_depth = K;
+            res->total_solutions = s == 0 ? nrec : 0;
+            if (s != 0) {
+                if (o.first_only) res->total_solutions = nrec;  /* class records */
+                else res->total_solutions = found.size();
+            }
+            *sols = std::move(found);
+        }
+    }
+    res->gpu_ms_expand = e->ms_expand;
+    res->gpu_ms_suffix = e->ms_suffix;
+    res->gpu_ms_insert = e->ms_insert;
+    res->kernel_launches = e->launches;
+    res->insert_launches = e->insert_launches;
+    res->suffix_launches = e->suffix_launches;
+    res->insert_children = e->insert_children;
+    res->h2d_bytes = e->h2d;
+    res->d2h_bytes = e->d2h;
+    res->seconds =
+        std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+    return PCAGB_OK;
+}
+
+int engine_init(pcagb_engine *e, int device, size_t budget)
+{
+    CK(cudaSetDevice(device));
+    e->device = device;
+    CK(cudaDeviceGetAttribute(&e->sms, cudaDevAttrMultiProcessorCount, device));
+    CK(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
+    CK(cudaEventCreate(&e->ev0));
+    CK(cudaEventCreate(&e->ev1));
+    CK(cudaEventCreate(&e->ev2));
+    CK(cudaEventCreate(&e->ev3));
+    size_t free_b = 0, total_b = 0;
+    CK(cudaMemGetInfo(&free_b, &total_b));
+    if (budget == 0) budget = (size_t)(free_b * 0.6);
+    if (budget > free_b) budget = free_b - (256u << 20);
+    budget &= ~size_t(4095);
+    CK(cudaMalloc(&e->arena, budget));
+    e->cap = budget;
+    e->top = budget;
+    const GenTables &gt = gen_tables();
+    std::vector<uint16_t> first(gt.vc_uop.size(), 0);
+    for (int m = 0; m < 128; m++) {
+        std::vector<bool> seen(gt.nvc(m), false);
+        for (uint32_t c = 0; c < (uint32_t)gt.nc(m); c++) {
+            uint16_t v = gt.cand_vc[gt.cand_off[m] + c];
+            if (!seen[v]) { seen[v] = true; first[gt.vc_off[m] + v] = (uint16_t)c; }
+        }
+    }
+    CK(cudaMalloc(&e->d_cand_uop, gt.cand_uop.size() * 4));
+    CK(cudaMalloc(&e->d_vc_uop, gt.vc_uop.size() * 4));
+    CK(cudaMalloc(&e->d_vc_first, first.size() * 2));
+    CK(cudaMalloc(&e->d_small, 256 * sizeof(unsigned long long)));
+    CK(cudaMalloc(&e->d_status, 16));
+    CK(cudaMalloc(&e->d_sol, e->sol_cap * sizeof(ulonglong2)));
+    CK(cudaMemcpy(e->d_cand_uop, gt.cand_uop.data(), gt.cand_uop.size() * 4, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(e->d_vc_uop, gt.vc_uop.data(), gt.vc_uop.size() * 4, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(e->d_vc_first, first.data(), first.size() * 2, cudaMemcpyHostToDevice));
+    CK(cudaMemcpyToSymbol(c_cand_off, gt.cand_off.data(), 129 * 4));
+    CK(cudaMemcpyToSymbol(c_vc_off, gt.vc_off.data(), 129 * 4));
+    const uint32_t *cu = e->d_cand_uop, *vu = e->d_vc_uop;
+    const uint16_t *vf = e->d_vc_first;
+    CK(cudaMemcpyToSymbol(c_cand_uop, &cu, sizeof cu));
+    CK(cudaMemcpyToSymbol(c_vc_uop, &vu, sizeof vu));
+    CK(cudaMemcpyToSymbol(c_vc_first, &vf, sizeof vf));
+    return PCAGB_OK;
+}
+
+thread_local pcagb_engine *t_default_engine = nullptr;
+thread_local uint64_t t_last_explored = 0;
+
+}  // namespace
+
+extern "C" {
+
+const char *pcagb_last_error(void) { return g_err.c_str(); }
+
+void pcagb_default_opts(pcagb_opts_t *o)
+{
+    memset(o, 0, sizeof *o);
+    o->max_depth = 4;
+    o->min_depth = 0;
+    o->split_depth = -1;
+    o->oep_mode = PCAGB_OEP_EXACT_LIVE;
+}
+
+int pcagb_engine_create(int device, size_t hbm_budget_bytes, pcagb_engine_t **out)
+{
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        set_err("no CUDA device: the PCA-16 engine runs only on the GPU");
+        return PCAGB_ENODEV;
+    }
+    if (device < 0 || device >= n) { set_err("bad device %d", device); return PCAGB_EINVAL; }
+    pcagb_engine *e = new pcagb_engine();
+    int rc = engine_init(e, device, hbm_budget_bytes);
+    if (rc) {
+        pcagb_engine_destroy(e);
+        return rc;
+    }
+    *out = e;
+    return PCAGB_OK;
+}
+
+void pcagb_engine_destroy(pcagb_engine_t *e)
+{
+    if (!e) return;
+    cudaSetDevice(e->device);
+    if (e->stream) cudaStreamSynchronize(e->stream);
+    cudaFree(e->arena);
+    cudaFree(e->d_cand_uop);
+    cudaFree(e->d_vc_uop);
+    cudaFree(e->d_vc_first);
+    cudaFree(e->d_small);
+    cudaFree(e->d_status);
+    cudaFree(e->d_sol);
+    for (cudaEvent_t ev : {e->ev0, e->ev1, e->ev2, e->ev3})
+        if (ev) cudaEventDestroy(ev);
+    if (e->stream) cudaStreamDestroy(e->stream);
+    delete e;
+}
+
+void *pcagb_engine_stream(pcagb_engine_t *e) { return e ? (void *)e->stream : nullptr; }
+
+int pcagb_solve(pcagb_engine_t *e, const task_spec_t *task, const pcagb_opts_t *opts,
+                pcagb_result_t *res, uint16_t *sol_progs, int *sol_lens, int sol_cap)
+{
+    pcagb_opts_t o;
+    if (opts) o = *opts;
+    else pcagb_default_opts(&o);
+    search_ctx_t ctx;
+    if (!e || !task || !res) { set_err("null argument"); return PCAGB_EINVAL; }
+    if (search_ctx_init(&ctx, task) != 0 || task->num_tests < 1) {
+        set_err("task needs 1..32 tests, one output and at most 7 inputs");
+        return PCAGB_EINVAL;
+    }
+    if (o.max_depth < 0 || o.max_depth > 12 || task->num_inputs + o.max_depth + 2 > 16) {
+        set_err("max_depth %d out of range (program length is limited to 16)", o.max_depth);
+        return PCAGB_EINVAL;
+    }
+    if (o.oep_mode < PCAGB_OEP_NONE || o.oep_mode > PCAGB_OEP_EXACT_LIVE) {
+        set_err("bad oep_mode %d", o.oep_mode);
+        return PCAGB_EINVAL;
+    }
+    RunSpec rs;
+    search_state_init_root(&ctx, &rs.root);
+    rs.T = task->num_tests;
+    for (int t = 0; t < rs.T; t++) rs.target[t] = task->tests[t].out[0];
+    std::vector<RawSol> sols;
+    int rc = run_iddfs(e, rs, o, res, &sols);
+    if (rc) return rc;
+    /* The reference applies its pruner to the last level too: among solving
+       programs with equal final regs+flags only the DFS-first is printed. */
+    if (o.oep_mode == PCAGB_OEP_EXACT && !o.count_levels && res->optimal_depth > 0 &&
+        !o.first_only) {
+        std::vector<RawSol> kept;
+        std::vector<std::vector<uint8_t>> seen;
+        std::vector<uint8_t> key;
+        for (RawSol &s : sols) {
+            leaf_key(task, rs.root, s.kernel, &key);
+            if (std::find(seen.begin(), seen.end(), key) != seen.end()) continue;
+            seen.push_back(key);
+            kept.push_back(s);
+        }
+        sols.swap(kept);
+        res->total_solutions = sols.size();
+    }
+    int stored = 0;
+    for (const RawSol &s : sols) {
+        if (stored >= sol_cap || !sol_progs) break;
+        uint16_t prog[16] = {0};
+        int n = 0;
+        for (int i = 0; i < task->num_inputs; i++)
+            prog[n++] = PCA_ENC_I(PCA_OP_IN, i + 1, task->input_ports[i]);
+        for (uint16_t insn : s.kernel) prog[n++] = insn;
+        prog[n++] = PCA_ENC_I(PCA_OP_OUT, s.out_reg, task->output_ports[0]);
+        prog[n++] = PCA_ENC_R(PCA_OP_HLT, 0, 0, 0);
+        if (task_evaluate(task, prog, n) != task->num_tests) {
+            set_err("internal: a GPU solution failed the VM re-check");
+            return PCAGB_ELIMIT;
+        }
+        memcpy(sol_progs + (size_t)stored * 16, prog, sizeof prog);
+        if (sol_lens) sol_lens[stored] = n;
+        stored++;
+    }
+    res->stored = stored;
+    return PCAGB_OK;
+}
+
+int pcagb_complete(pcagb_engine_t *e, const search_ctx_t *ctx, const search_state_t *start,
+                   int max_depth, uint16_t *solution_insns, int *solution_len,
+                   uint64_t *states_explored)
+{
+    if (!e || !ctx || !start || !solution_len) { set_err("null argument"); return PCAGB_EINVAL; }
+    *solution_len = 0;
+    if (states_explored) *states_explored = 0;
+    int max_r = max_depth - (int)start->depth;
+    if (max_r > SEARCH_MAX_DEPTH) max_r = SEARCH_MAX_DEPTH;
+    RunSpec rs;
+    rs.root = *start;
+    rs.T = ctx->num_tests;
+    if (rs.T < 1 || rs.T > MAX_TESTS) { set_err("bad test count"); return PCAGB_EINVAL; }
+    for (int t = 0; t < rs.T; t++) rs.target[t] = ctx->task.tests[t].out[0];
+    /* depth 0: the start state already solves */
+    for (uint32_t r = 1; r < 8; r++) {
+        if (!((start->live >> r) & 1u)) continue;
+        bool ok = true;
+        for (int t = 0; t < rs.T && ok; t++) ok = start->regs[t][r] == rs.target[t];
+        if (ok) return 1;
+    }
+    if (max_r <= 0) return 0;
+    pcagb_opts_t o;
+    pcagb_default_opts(&o);
+    o.min_depth = 1;
+    o.max_depth = max_r;
+    o.first_only = 1;
+    pcagb_result_t res;
+    std::vector<RawSol> sols;
+    int rc = run_iddfs(e, rs, o, &res, &sols);
+    if (rc) return rc;
+    uint64_t explored = 0;
+    for (int k = 0; k < PCAGB_MAXD; k++) explored += res.candidates[k];
+    if (states_explored) *states_explored = explored;
+    if (res.optimal_depth < 0 || sols.empty()) return 0;
+    const RawSol &s = sols.front();
+    for (size_t i = 0; i < s.kernel.size(); i++) solution_insns[i] = s.kernel[i];
+    *solution_len = (int)s.kernel.size();
+    return 1;
+}
+
+int search_exhaustive_complete(const search_ctx_t *ctx, const search_state_t *start, int max_depth,
+                               uint16_t *solution_insns, int *solution_len)
+{
+    if (!t_default_engine) {
+        int rc = pcagb_engine_create(0, 0, &t_default_engine);
+        if (rc) {
+            fprintf(stderr, "search_exhaustive_complete: %s\n", pcagb_last_error());
+            *solution_len = 0;
+            return rc;
+        }
+    }
+    uint64_t explored = 0;
+    int rc = pcagb_complete(t_default_engine, ctx, start, max_depth, solution_insns, solution_len,
+                            &explored);
+    t_last_explored = explored;
+    if (rc < 0) fprintf(stderr, "search_exhaustive_complete: %s\n", pcagb_last_error());
+    return rc;
+}
+
+uint64_t search_exhaustive_states_explored(void) { return t_last_explored; }
+
+}  // extern "C"

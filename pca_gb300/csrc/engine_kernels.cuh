@@ -1,0 +1,565 @@
+/*
+ * engine_kernels.cuh -- CUDA kernels of the PCA-16 exhaustive engine.
+ *
+ * Search levels. Level d holds the distinct states reached by d kernel
+ * instructions (level 0 = the task root). A state is stored column-major:
+ * regs[n][8][TP] (u16, r0's column kept as zeros), flags[n][TP], live[n],
+ * plus the back pointer (parent rank, candidate index) that rebuilds its
+ * program. TP is 16 or 32 (test count rounded up), and test slots >= T are
+ * zero in every state.
+ *
+ * Level expansion (the OEP kernel): one warp per parent, one lane per child
+ * candidate. Each lane computes the child's new column and flags across all
+ * tests, a 64-bit hash of the whole child state (incrementally from the
+ * parent's per-column hashes), and inserts a 64-bit slot
+ *   [tag: hash bits 40..63][ref + 1: 40 bits]
+ * into an open-addressed HBM table, ref = parent_rank << 12 | candidate.
+ * On a tag match the two child states are rebuilt and compared in full
+ * (every register of every test, flags, and live when it is part of the
+ * key), so a hash collision can never merge two different states. Among
+ * equal states the smallest ref wins (atomicCAS loop), which is the first
+ * child in the reference's DFS order -- the representative the reference's
+ * DFS pruner keeps (tools/enumerate.c:379-384).
+ *
+ * The winners are then marked in a bitmap indexed by the child's linear
+ * index (child_off[parent] + candidate), ranked by a scan, and written out
+ * in that order, so every level stays in DFS order.
+ *
+ * Suffix kernels: one warp per prefix state. The last instruction's value
+ * does not depend on its destination (except ADDI), so the lanes scan the
+ * value classes of the prefix's live mask on test 0, and each survivor is
+ * checked on all tests at once, lane t taking test t, with __ballot_sync /
+ * __all_sync deciding. Suffix depths 2 and 3 enumerate the middle
+ * instructions in the warp, keeping the new columns in spare shared-memory
+ * columns 8 and 9.
+ */
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "pca_isa.h"
+
+namespace pcagb {
+
+constexpr int kWarpsPerBlock = 8;
+constexpr int kThreads = kWarpsPerBlock * 32;
+constexpr uint64_t kRefMask = (1ull << 40) - 1;
+constexpr uint32_t kMaxProbes = 1u << 16;
+
+/* status flags set by kernels (bounded loops that ran out) */
+constexpr uint32_t kStatusTableFull = 1u;
+constexpr uint32_t kStatusRefOverflow = 2u;
+
+/* Candidate tables, uploaded once per device. */
+__constant__ uint32_t c_cand_off[129];
+__constant__ uint32_t c_vc_off[129];
+__constant__ const uint32_t *c_cand_uop;
+__constant__ const uint32_t *c_vc_uop;
+__constant__ const uint16_t *c_vc_first;   /* first candidate index per class */
+
+struct TaskDev {
+    int T;          /* tests */
+    int key_live;   /* OEP key includes live */
+    uint32_t target[32];
+};
+
+struct LevelDev {
+    const uint16_t *regs;   /* [n][8][TP] */
+    const uint8_t *flags;   /* [n][TP] */
+    const uint8_t *live;    /* [n] */
+    const uint64_t *child_off; /* [n+1] */
+    uint64_t n;
+};
+
+struct LevelOut {
+    uint16_t *regs;
+    uint8_t *flags;
+    uint8_t *live;
+    uint32_t *parent;
+    uint16_t *cidx;
+};
+
+/* ---- hashing (a multiply-rotate chain; the table compares full states, so
+        the hash only has to spread well) -------------------------------- */
+
+__device__ __forceinline__ uint64_t fmix64(uint64_t x)
+{
+    x ^= x >> 33;
+    x *= 0xFF51AFD7ED558CCDull;
+    x ^= x >> 33;
+    x *= 0xC4CEB9FE1A85EC53ull;
+    x ^= x >> 33;
+    return x;
+}
+
+__device__ __forceinline__ uint64_t chain(uint64_t h, uint64_t w)
+{
+    h = (h ^ w) * 0x9E3779B97F4A7C15ull;
+    return (h << 27) | (h >> 37);
+}
+
+__device__ __forceinline__ uint64_t col_final(uint32_t r, uint64_t h)
+{
+    return fmix64(h + (uint64_t)r * 0xD6E8FEB86659FD93ull);
+}
+
+__device__ __forceinline__ uint64_t live_final(uint32_t live)
+{
+    return fmix64(0x5851F42D4C957F2Dull ^ live);
+}
+
+template <int TPC>
+__device__ __forceinline__ uint64_t hash_column(const uint32_t *col)
+{
+    uint64_t h = 0x243F6A8885A308D3ull;
+#pragma unroll
+    for (int t = 0; t < TPC; t += 4) {
+        uint64_t w = (uint64_t)col[t] | ((uint64_t)col[t + 1] << 16) |
+                     ((uint64_t)col[t + 2] << 32) | ((uint64_t)col[t + 3] << 48);
+        h = chain(h, w);
+    }
+    return h;
+}
+
+template <int TPC>
+__device__ __forceinline__ uint64_t hash_flags(const uint32_t *f)
+{
+    uint64_t h = 0x13198A2E03707344ull;
+#pragma unroll
+    for (int t = 0; t < TPC; t += 16) {
+        uint64_t w = 0;
+#pragma unroll
+        for (int k = 0; k < 16; k++) w |= (uint64_t)f[t + k] << (4 * k);
+        h = chain(h, w);
+    }
+    return h;
+}
+
+/* ---- shared-memory view of one state per warp ---------------------------- */
+
+template <int TPC>
+struct WarpState {
+    uint32_t R[10][TPC + 1];  /* columns r0..r7 + 2 spare; +1 word pad */
+    uint32_t F[TPC];
+    uint64_t colh[8];         /* colh[r] = col_final(r, hash(col r)); [0] = flags */
+};
+
+template <int TPC>
+__device__ __forceinline__ void load_state(WarpState<TPC> &ws, const uint16_t *regs,
+                                           const uint8_t *flags, uint64_t q, int lane)
+{
+    if (lane < TPC) {
+        const uint16_t *src = regs + q * 8 * TPC + lane;
+#pragma unroll
+        for (int r = 0; r < 8; r++) ws.R[r][lane] = src[r * TPC];
+        ws.F[lane] = flags[q * TPC + lane];
+    }
+}
+
+/* ---- level expansion: insert every child into the exact table ------------ */
+
+template <int TPC>
+__device__ bool child_equal(const LevelDev &P, const TaskDev &task, const WarpState<TPC> &A,
+                            uint32_t liveA, uint32_t uA, uint64_t qB, uint32_t cB)
+{
+    uint32_t liveB = P.live[qB];
+    uint32_t mB = (liveB >> 1) & 127u;
+    uint32_t uB = c_cand_uop[c_cand_off[mB] + cB];
+    uint32_t rdA = UOP_RD(uA), rdB = UOP_RD(uB);
+    if (task.key_live && ((liveA | (1u << rdA)) != (liveB | (1u << rdB)))) return false;
+    const uint16_t *RB = P.regs + qB * 8 * TPC;
+    const uint8_t *FB = P.flags + qB * TPC;
+    for (int t = 0; t < task.T; t++) {
+        uint32_t a1 = A.R[UOP_A(uA)][t], b1 = A.R[UOP_B(uA)][t];
+        uint32_t resA = pca_alu(UOP_OP(uA), a1, b1, UOP_IMM(uA));
+        uint32_t fA = pca_alu_flags(UOP_OP(uA), a1, b1, UOP_IMM(uA), resA, A.F[t]);
+        uint32_t a2 = RB[UOP_A(uB) * TPC + t], b2 = RB[UOP_B(uB) * TPC + t];
+        uint32_t resB = pca_alu(UOP_OP(uB), a2, b2, UOP_IMM(uB));
+        uint32_t fB = pca_alu_flags(UOP_OP(uB), a2, b2, UOP_IMM(uB), resB, FB[t]);
+        if (fA != fB) return false;
+#pragma unroll
+        for (uint32_t r = 1; r < 8; r++) {
+            uint32_t vA = r == rdA ? resA : A.R[r][t];
+            uint32_t vB = r == rdB ? resB : (uint32_t)RB[r * TPC + t];
+            if (vA != vB) return false;
+        }
+    }
+    return true;
+}
+
+template <int TPC>
+__global__ void __launch_bounds__(kThreads)
+k_expand_insert(LevelDev P, TaskDev task, unsigned long long *table, uint64_t tmask,
+                uint32_t *status)
+{
+    __shared__ WarpState<TPC> sws[kWarpsPerBlock];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    WarpState<TPC> &ws = sws[wib];
+    const uint64_t nw = (uint64_t)gridDim.x * kWarpsPerBlock;
+    for (uint64_t q = (uint64_t)blockIdx.x * kWarpsPerBlock + wib; q < P.n; q += nw) {
+        load_state<TPC>(ws, P.regs, P.flags, q, lane);
+        const uint32_t live = P.live[q];
+        __syncwarp();
+        if (lane >= 1 && lane < 8) ws.colh[lane] = col_final(lane, hash_column<TPC>(ws.R[lane]));
+        if (lane == 0) ws.colh[0] = hash_flags<TPC>(ws.F);
+        __syncwarp();
+        uint64_t regsum = 0;
+#pragma unroll
+        for (int r = 1; r < 8; r++) regsum += ws.colh[r];
+        const uint32_t m = (live >> 1) & 127u;
+        const uint32_t base = c_cand_off[m], nc = c_cand_off[m + 1] - base;
+        for (uint32_t c = lane; c < nc; c += 32) {
+            const uint32_t u = c_cand_uop[base + c];
+            const uint32_t op = UOP_OP(u), rd = UOP_RD(u), ra = UOP_A(u), rb = UOP_B(u),
+                           imm = UOP_IMM(u);
+            uint64_t h = 0x243F6A8885A308D3ull, hf = 0x13198A2E03707344ull;
+            uint64_t w = 0, wf = 0;
+#pragma unroll
+            for (int t = 0; t < TPC; t++) {
+                uint32_t a = ws.R[ra][t], b = ws.R[rb][t];
+                uint32_t res = pca_alu(op, a, b, imm);
+                uint32_t f = pca_alu_flags(op, a, b, imm, res, ws.F[t]);
+                if (t >= task.T) { res = 0; f = 0; }
+                w |= (uint64_t)res << (16 * (t & 3));
+                wf |= (uint64_t)f << (4 * (t & 15));
+                if ((t & 3) == 3) { h = chain(h, w); w = 0; }
+                if ((t & 15) == 15) { hf = chain(hf, wf); wf = 0; }
+            }
+            const uint32_t clive = live | (1u << rd);
+            uint64_t H = regsum - ws.colh[rd] + col_final(rd, h) + hf;
+            if (task.key_live) H += live_final(clive);
+            const uint64_t ref = (q << 12) | c;
+            const unsigned long long mine = ((H >> 40) << 40) | (ref + 1);
+            uint64_t idx = H & tmask;
+            uint32_t probes = 0;
+            for (;;) {
+                unsigned long long s = *((volatile unsigned long long *)&table[idx]);
+                if (s == 0) {
+                    unsigned long long old = atomicCAS(&table[idx], 0ull, mine);
+                    if (old == 0) break;
+                    s = old;
+                }
+                if ((s >> 40) == (mine >> 40)) {
+                    uint64_t oref = (s & kRefMask) - 1;
+                    if (child_equal<TPC>(P, task, ws, live, u, oref >> 12, (uint32_t)(oref & 4095))) {
+                        while (ref < oref) {
+                            unsigned long long old = atomicCAS(&table[idx], s, mine);
+                            if (old == s) break;
+                            s = old;
+                            oref = (s & kRefMask) - 1;
+                        }
+                        break;
+                    }
+                }
+                idx = (idx + 1) & tmask;
+                if (++probes >= kMaxProbes) {
+                    atomicOr(status, kStatusTableFull);
+                    break;
+                }
+            }
+        }
+        __syncwarp();
+    }
+}
+
+/* Mark each table winner in the child bitmap; count them. */
+__global__ void k_mark(const unsigned long long *table, uint64_t slots, const uint64_t *child_off,
+                       uint32_t *bitmap, unsigned long long *count)
+{
+    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    uint32_t local = 0;
+    for (; i < slots; i += stride) {
+        unsigned long long s = table[i];
+        if (!s) continue;
+        uint64_t ref = (s & kRefMask) - 1;
+        uint64_t L = child_off[ref >> 12] + (ref & 4095);
+        atomicOr(&bitmap[L >> 5], 1u << (L & 31));
+        local++;
+    }
+    for (int o = 16; o; o >>= 1) local += __shfl_down_sync(0xFFFFFFFFu, local, o);
+    if ((threadIdx.x & 31) == 0 && local) atomicAdd(count, (unsigned long long)local);
+}
+
+/* Keep every child (no pruning): set all bits below `total`. */
+__global__ void k_mark_all(uint32_t *bitmap, uint64_t words, uint64_t total)
+{
+    for (uint64_t w = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; w < words;
+         w += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t lo = w * 32;
+        uint32_t v = 0xFFFFFFFFu;
+        if (lo + 32 > total) v = total > lo ? (uint32_t)((1ull << (total - lo)) - 1) : 0u;
+        bitmap[w] = v;
+    }
+}
+
+__global__ void k_popc(const uint32_t *bitmap, uint64_t words, uint64_t *cnt)
+{
+    for (uint64_t w = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; w < words;
+         w += (uint64_t)gridDim.x * blockDim.x)
+        cnt[w] = __popc(bitmap[w]);
+}
+
+/* child_off[i] = number of candidates of state i (scanned afterwards). */
+__global__ void k_child_counts(const uint8_t *live, uint64_t n, uint64_t *cnt)
+{
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t m = (live[i] >> 1) & 127u;
+        cnt[i] = c_cand_off[m + 1] - c_cand_off[m];
+    }
+}
+
+/* Write the marked children of each parent, in rank (DFS) order. */
+template <int TPC>
+__global__ void __launch_bounds__(kThreads)
+k_materialize(LevelDev P, TaskDev task, const uint32_t *bitmap, const uint64_t *word_off,
+              LevelOut C)
+{
+    __shared__ WarpState<TPC> sws[kWarpsPerBlock];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    WarpState<TPC> &ws = sws[wib];
+    const uint64_t nw = (uint64_t)gridDim.x * kWarpsPerBlock;
+    for (uint64_t q = (uint64_t)blockIdx.x * kWarpsPerBlock + wib; q < P.n; q += nw) {
+        load_state<TPC>(ws, P.regs, P.flags, q, lane);
+        const uint32_t live = P.live[q];
+        __syncwarp();
+        const uint32_t m = (live >> 1) & 127u;
+        const uint32_t base = c_cand_off[m], nc = c_cand_off[m + 1] - base;
+        const uint64_t off = P.child_off[q];
+        for (uint32_t c0 = 0; c0 < nc; c0 += 32) {
+            uint32_t c = c0 + lane;
+            bool keep = false;
+            if (c < nc) {
+                uint64_t L = off + c;
+                keep = (bitmap[L >> 5] >> (L & 31)) & 1u;
+            }
+            uint32_t bal = __ballot_sync(0xFFFFFFFFu, keep);
+            while (bal) {
+                const int j = __ffs(bal) - 1;
+                bal &= bal - 1;
+                const uint32_t cj = c0 + j;
+                const uint64_t L = off + cj;
+                const uint32_t wv = bitmap[L >> 5];
+                const uint64_t rank = word_off[L >> 5] + __popc(wv & ((1u << (L & 31)) - 1u));
+                const uint32_t u = c_cand_uop[base + cj];
+                const uint32_t op = UOP_OP(u), rd = UOP_RD(u);
+                if (lane < TPC) {
+                    uint32_t a = ws.R[UOP_A(u)][lane], b = ws.R[UOP_B(u)][lane];
+                    uint32_t res = pca_alu(op, a, b, UOP_IMM(u));
+                    uint32_t f = pca_alu_flags(op, a, b, UOP_IMM(u), res, ws.F[lane]);
+                    if (lane >= task.T) { res = 0; f = 0; }
+                    uint16_t *dst = C.regs + rank * 8 * TPC + lane;
+#pragma unroll
+                    for (uint32_t r = 0; r < 8; r++)
+                        dst[r * TPC] = (uint16_t)(r == rd ? res : ws.R[r][lane]);
+                    C.flags[rank * TPC + lane] = (uint8_t)f;
+                }
+                if (lane == 0) {
+                    C.live[rank] = (uint8_t)(live | (1u << rd));
+                    C.parent[rank] = (uint32_t)q;
+                    C.cidx[rank] = (uint16_t)cj;
+                }
+            }
+        }
+        __syncwarp();
+    }
+}
+
+__global__ void k_live_hist(const uint8_t *live, uint64_t n, unsigned long long *hist)
+{
+    __shared__ unsigned int sh[128];
+    for (int i = threadIdx.x; i < 128; i += blockDim.x) sh[i] = 0;
+    __syncthreads();
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        atomicAdd(&sh[(live[i] >> 1) & 127u], 1u);
+    __syncthreads();
+    for (int i = threadIdx.x; i < 128; i += blockDim.x)
+        if (sh[i]) atomicAdd(&hist[i], (unsigned long long)sh[i]);
+}
+
+/* ---- solutions ----------------------------------------------------------- */
+
+struct SolBuf {
+    unsigned long long *count;    /* solving (prefix, mids, class) records */
+    ulonglong2 *rec;              /* x = prefix rank, y = m1<<32 | m2<<16 | class */
+    uint64_t cap;
+    unsigned long long *first;    /* atomicMin of a packed DFS-order key */
+};
+
+__device__ __forceinline__ void record_solution(const SolBuf &S, uint64_t q, uint32_t m1,
+                                                uint32_t m2, uint32_t vc, uint32_t first_c)
+{
+    unsigned long long slot = atomicAdd(S.count, 1ull);
+    if (slot < S.cap)
+        S.rec[slot] = make_ulonglong2(q, ((unsigned long long)m1 << 32) | (m2 << 16) | vc);
+    unsigned long long key = ((unsigned long long)(q & 0xFFFFFFFull) << 36) |
+                             ((unsigned long long)m1 << 24) | ((unsigned long long)m2 << 12) |
+                             first_c;
+    atomicMin(S.first, key);
+}
+
+/* Leaf check of a materialized level (count mode): state q solves through
+ * live register r when regs[q][r][t] == target[t] for every test. */
+template <int TPC>
+__global__ void k_leaf(LevelDev P, TaskDev task, SolBuf S)
+{
+    const int lane = threadIdx.x & 31;
+    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    const uint32_t tgt = lane < task.T ? task.target[lane] : 0u;
+    for (uint64_t q = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < P.n; q += nw) {
+        const uint32_t live = P.live[q];
+        for (uint32_t r = 1; r < 8; r++) {
+            if (!((live >> r) & 1u)) continue;
+            bool ok = lane >= task.T || P.regs[q * 8 * TPC + r * TPC + lane] == tgt;
+            if (__all_sync(0xFFFFFFFFu, ok) && lane == 0) record_solution(S, q, 0, 0, r, r);
+        }
+    }
+}
+
+/* Scan the value classes of mask m against the warp's state, with operand
+ * registers remapped: a register equal to rd2 reads spare column 9, else a
+ * register equal to rd1 reads column 8 (rd = 8 means "none"). */
+template <int TPC>
+__device__ __forceinline__ void scan_last(const WarpState<TPC> &ws, const TaskDev &task,
+                                          uint32_t m, uint32_t rd1, uint32_t rd2, uint32_t tgt,
+                                          uint32_t tgt0, int lane, const SolBuf &S, uint64_t q,
+                                          uint32_t m1, uint32_t m2)
+{
+    const uint32_t vbase = c_vc_off[m], nvc = c_vc_off[m + 1] - vbase;
+    for (uint32_t b0 = 0; b0 < nvc; b0 += 32) {
+        const uint32_t i = b0 + lane;
+        uint32_t u = 0;
+        bool pass = false;
+        if (i < nvc) {
+            u = c_vc_uop[vbase + i];
+            uint32_t ra = UOP_A(u), rb = UOP_B(u);
+            ra = ra == rd2 ? 9u : ra == rd1 ? 8u : ra;
+            rb = rb == rd2 ? 9u : rb == rd1 ? 8u : rb;
+            pass = pca_alu(UOP_OP(u), ws.R[ra][0], ws.R[rb][0], UOP_IMM(u)) == tgt0;
+        }
+        uint32_t bal = __ballot_sync(0xFFFFFFFFu, pass);
+        while (bal) {
+            const int j = __ffs(bal) - 1;
+            bal &= bal - 1;
+            const uint32_t uj = __shfl_sync(0xFFFFFFFFu, u, j);
+            uint32_t ra = UOP_A(uj), rb = UOP_B(uj);
+            ra = ra == rd2 ? 9u : ra == rd1 ? 8u : ra;
+            rb = rb == rd2 ? 9u : rb == rd1 ? 8u : rb;
+            bool ok = true;
+            if (lane < task.T) ok = pca_alu(UOP_OP(uj), ws.R[ra][lane], ws.R[rb][lane], UOP_IMM(uj)) == tgt;
+            if (__all_sync(0xFFFFFFFFu, ok) && lane == 0)
+                record_solution(S, q, m1, m2, b0 + j, c_vc_first[vbase + b0 + j]);
+        }
+    }
+}
+
+/* Suffix enumeration of depth SD (1..3) from every state of level P.
+ * Work item = (prefix, chunk of first-suffix candidates); for SD = 1 the
+ * chunk is the whole prefix. */
+template <int TPC, int SD>
+__global__ void __launch_bounds__(kThreads)
+k_suffix(LevelDev P, TaskDev task, SolBuf S, uint32_t chunks_per_prefix, uint32_t chunk)
+{
+    __shared__ WarpState<TPC> sws[kWarpsPerBlock];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    WarpState<TPC> &ws = sws[wib];
+    const uint32_t tgt = lane < task.T ? task.target[lane] : 0u;
+    const uint32_t tgt0 = task.target[0];
+    const uint64_t nw = (uint64_t)gridDim.x * kWarpsPerBlock;
+    const uint64_t items = P.n * chunks_per_prefix;
+    uint64_t loaded = ~0ull;
+    for (uint64_t it = (uint64_t)blockIdx.x * kWarpsPerBlock + wib; it < items; it += nw) {
+        const uint64_t q = it / chunks_per_prefix;
+        const uint32_t ck = (uint32_t)(it - q * chunks_per_prefix);
+        const uint32_t live = P.live[q];
+        if (q != loaded) {
+            __syncwarp();
+            load_state<TPC>(ws, P.regs, P.flags, q, lane);
+            loaded = q;
+            __syncwarp();
+        }
+        const uint32_t m0 = (live >> 1) & 127u;
+        if (SD == 1) {
+            scan_last<TPC>(ws, task, m0, 8, 8, tgt, tgt0, lane, S, q, 0, 0);
+            continue;
+        }
+        const uint32_t cb0 = c_cand_off[m0], nc0 = c_cand_off[m0 + 1] - cb0;
+        const uint32_t lo = ck * chunk, hi = min(nc0, lo + chunk);
+        for (uint32_t i1 = lo; i1 < hi; i1++) {
+            const uint32_t u1 = c_cand_uop[cb0 + i1];
+            const uint32_t rd1 = UOP_RD(u1);
+            __syncwarp();
+            if (lane < TPC)
+                ws.R[8][lane] = lane < task.T ? pca_alu(UOP_OP(u1), ws.R[UOP_A(u1)][lane],
+                                                        ws.R[UOP_B(u1)][lane], UOP_IMM(u1))
+                                              : 0u;
+            __syncwarp();
+            const uint32_t m1 = (m0 | (1u << (rd1 - 1))) & 127u;
+            if (SD == 2) {
+                scan_last<TPC>(ws, task, m1, rd1, 8, tgt, tgt0, lane, S, q, i1, 0);
+                continue;
+            }
+            const uint32_t cb1 = c_cand_off[m1], nc1 = c_cand_off[m1 + 1] - cb1;
+            for (uint32_t i2 = 0; i2 < nc1; i2++) {
+                const uint32_t u2 = c_cand_uop[cb1 + i2];
+                const uint32_t rd2 = UOP_RD(u2);
+                uint32_t ra = UOP_A(u2), rb = UOP_B(u2);
+                ra = ra == rd1 ? 8u : ra;
+                rb = rb == rd1 ? 8u : rb;
+                __syncwarp();
+                if (lane < TPC)
+                    ws.R[9][lane] = lane < task.T ? pca_alu(UOP_OP(u2), ws.R[ra][lane],
+                                                            ws.R[rb][lane], UOP_IMM(u2))
+                                                  : 0u;
+                __syncwarp();
+                const uint32_t m2 = (m1 | (1u << (rd2 - 1))) & 127u;
+                scan_last<TPC>(ws, task, m2, rd2 == rd1 ? 8u : rd1, rd2, tgt, tgt0, lane, S, q,
+                               i1, i2);
+            }
+        }
+    }
+}
+
+/* ---- exclusive scan of u64 (in place), three-phase ----------------------- */
+
+constexpr int kScanBlock = 1024;  /* elements per block (256 threads x 4) */
+
+__global__ void k_scan_local(uint64_t *a, uint64_t n, uint64_t *block_sums)
+{
+    __shared__ uint64_t sh[256];
+    const uint64_t base = (uint64_t)blockIdx.x * kScanBlock + threadIdx.x * 4;
+    uint64_t v[4], s = 0;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        v[k] = base + k < n ? a[base + k] : 0;
+        s += v[k];
+    }
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = 1; o < 256; o <<= 1) {
+        uint64_t x = threadIdx.x >= (unsigned)o ? sh[threadIdx.x - o] : 0;
+        __syncthreads();
+        sh[threadIdx.x] += x;
+        __syncthreads();
+    }
+    uint64_t run = sh[threadIdx.x] - s;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        if (base + k < n) a[base + k] = run;
+        run += v[k];
+    }
+    if (threadIdx.x == 255) block_sums[blockIdx.x] = sh[255];
+}
+
+__global__ void k_scan_add(uint64_t *a, uint64_t n, const uint64_t *block_off)
+{
+    const uint64_t base = (uint64_t)blockIdx.x * kScanBlock;
+    const uint64_t add = block_off[blockIdx.x];
+    for (int k = threadIdx.x; k < kScanBlock; k += blockDim.x)
+        if (base + k < n) a[base + k] += add;
+}
+
+}  // namespace pcagb

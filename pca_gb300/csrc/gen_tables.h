@@ -1,0 +1,55 @@
+/*
+ * gen_tables.h -- the branchless candidate generator, precomputed for all
+ * 128 liveness masks.
+ *
+ * The generator is the reference's src/search_state.c:280-330: nine ALU ops
+ * (ADD SUB MUL AND OR XOR SHL SHR ASR) over rd = r1..r7 and live source
+ * registers (r0 always allowed), with rt >= rs for the commutative ops and
+ * five no-op encodings skipped; then LDI rd, {0,1,2,3,4,5,8,16,32,64,128,255}
+ * for every rd; then ADDI rd, {-1,1,-2,2,-3,3} for live rd. The list order is
+ * the reference's DFS order, which the engine preserves.
+ *
+ * A liveness mask only matters in bits 1..7, so masks are indexed by
+ * live >> 1 (0..127).
+ *
+ * Value classes. The value an instruction writes does not depend on its
+ * destination register unless the op reads it (ADDI). At the last kernel
+ * position only that value matters, so candidates that differ only in rd
+ * form one value class, evaluated once: (op, a, b, imm) with rd cleared, or
+ * with rd kept for ADDI.
+ */
+#ifndef PCA_GEN_TABLES_H
+#define PCA_GEN_TABLES_H
+
+#include <stdint.h>
+#include <vector>
+
+namespace pcagb {
+
+struct GenTables {
+    /* per mask (128): offsets into the flat arrays, size 129 */
+    std::vector<uint32_t> cand_off;
+    std::vector<uint16_t> cand;        /* raw instruction words            */
+    std::vector<uint32_t> cand_uop;    /* pre-decoded micro-ops            */
+    std::vector<uint16_t> cand_vc;     /* value class index within mask    */
+    std::vector<uint32_t> vc_off;      /* size 129                         */
+    std::vector<uint32_t> vc_uop;      /* one micro-op per value class     */
+    /* f[s][m]: programs decided by s more instructions from mask m:
+       f[1][m] = nc(m), f[s][m] = sum over candidates c of f[s-1][m | rd(c)] */
+    std::vector<uint64_t> f[5];
+    int max_nc = 0;
+    int max_nvc = 0;
+
+    int nc(int mask) const { return (int)(cand_off[mask + 1] - cand_off[mask]); }
+    int nvc(int mask) const { return (int)(vc_off[mask + 1] - vc_off[mask]); }
+};
+
+/* Built once (thread-safe, immutable afterwards). */
+const GenTables &gen_tables();
+
+/* The generator for one live mask, in reference order. */
+int gen_candidates(uint8_t live, uint16_t *out, int max);
+
+}  // namespace pcagb
+
+#endif

@@ -1,0 +1,326 @@
+"""ctypes mirror of libpcagb.so.
+
+`PCALib` has the reference's interface (python/search_eval.py:74-185): same
+struct layouts (python/search_eval.py:32-69), same method names, same
+return conventions, so reference-style callers switch by changing the
+library path. `Engine` wraps the GPU solver entry points (pcagb_*).
+
+The library must have been built (python -m pca_gb300.build); nothing here
+falls back to a CPU implementation.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass, field
+
+MAX_TESTS = 32
+PCA_NUM_REGS = 8
+MAX_IO_PORTS = 8
+MAX_CANDIDATES = 4096
+MAXD = 17
+
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "libpcagb.so")
+
+
+class TestCase(ctypes.Structure):
+    _fields_ = [("inputs", ctypes.c_uint16 * MAX_IO_PORTS),
+                ("outputs", ctypes.c_uint16 * MAX_IO_PORTS)]
+
+
+class TaskSpec(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char * 64),
+                ("max_cycles", ctypes.c_uint64),
+                ("input_ports", ctypes.c_uint8 * MAX_IO_PORTS),
+                ("num_inputs", ctypes.c_int),
+                ("output_ports", ctypes.c_uint8 * MAX_IO_PORTS),
+                ("num_outputs", ctypes.c_int),
+                ("tests", TestCase * MAX_TESTS),
+                ("num_tests", ctypes.c_int)]
+
+
+class SearchCtx(ctypes.Structure):
+    _fields_ = [("task", TaskSpec),
+                ("num_tests", ctypes.c_uint8),
+                ("num_inputs", ctypes.c_uint8),
+                ("num_outputs", ctypes.c_uint8),
+                ("input_regs", ctypes.c_uint8 * MAX_IO_PORTS),
+                ("output_port", ctypes.c_uint8)]
+
+
+class SearchState(ctypes.Structure):
+    _fields_ = [("regs", (ctypes.c_uint16 * PCA_NUM_REGS) * MAX_TESTS),
+                ("flags", ctypes.c_uint8 * MAX_TESTS),
+                ("live", ctypes.c_uint8),
+                ("depth", ctypes.c_uint8)]
+
+
+class SolveOpts(ctypes.Structure):
+    _fields_ = [("max_depth", ctypes.c_int),
+                ("min_depth", ctypes.c_int),
+                ("split_depth", ctypes.c_int),
+                ("oep_mode", ctypes.c_int),
+                ("count_levels", ctypes.c_int),
+                ("first_only", ctypes.c_int),
+                ("reserved", ctypes.c_int * 6)]
+
+
+class SolveResult(ctypes.Structure):
+    _fields_ = [("optimal_depth", ctypes.c_int),
+                ("stored", ctypes.c_int),
+                ("total_solutions", ctypes.c_uint64),
+                ("candidates", ctypes.c_uint64 * MAXD),
+                ("evaluations", ctypes.c_uint64 * MAXD),
+                ("tried", ctypes.c_uint64 * MAXD),
+                ("pruned_cum", ctypes.c_uint64 * MAXD),
+                ("level_children", ctypes.c_uint64 * MAXD),
+                ("level_survivors", ctypes.c_uint64 * MAXD),
+                ("seconds", ctypes.c_double),
+                ("gpu_ms_expand", ctypes.c_double),
+                ("gpu_ms_suffix", ctypes.c_double),
+                ("gpu_ms_insert", ctypes.c_double),
+                ("kernel_launches", ctypes.c_uint64),
+                ("insert_launches", ctypes.c_uint64),
+                ("suffix_launches", ctypes.c_uint64),
+                ("h2d_bytes", ctypes.c_uint64),
+                ("d2h_bytes", ctypes.c_uint64),
+                ("insert_children", ctypes.c_uint64),
+                ("split_used", ctypes.c_int),
+                ("reserved", ctypes.c_int * 7)]
+
+
+OEP_NONE, OEP_EXACT, OEP_EXACT_LIVE = 0, 1, 2
+
+# every function declared in include/pca_gb300.h
+EXPORTS = [
+    "pca_init", "pca_load", "pca_step", "pca_run", "pca_disasm", "pca_disasm_prog",
+    "task_load", "task_evaluate", "task_print",
+    "search_ctx_init", "search_state_init_root", "search_state_step",
+    "search_state_oep_hash64", "search_state_key_hash64", "search_state_leaf_outputs",
+    "search_state_serialize", "search_gen_candidates_branchless",
+    "search_exhaustive_complete", "search_exhaustive_states_explored", "search_state_dump",
+    "pcagb_last_error", "pcagb_default_opts", "pcagb_engine_create", "pcagb_engine_destroy",
+    "pcagb_solve", "pcagb_complete", "pcagb_num_candidates", "pcagb_engine_stream",
+]
+
+
+def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: build it with `python -m pca_gb300.build`")
+    lib = ctypes.CDLL(path)
+    P = ctypes.POINTER
+    sig = {
+        "task_load": ([ctypes.c_char_p, P(TaskSpec)], ctypes.c_int),
+        "task_evaluate": ([P(TaskSpec), P(ctypes.c_uint16), ctypes.c_int], ctypes.c_int),
+        "search_ctx_init": ([P(SearchCtx), P(TaskSpec)], ctypes.c_int),
+        "search_state_init_root": ([P(SearchCtx), P(SearchState)], None),
+        "search_state_step": ([P(SearchCtx), P(SearchState), ctypes.c_uint16, P(SearchState)],
+                              ctypes.c_int),
+        "search_state_oep_hash64": ([P(SearchCtx), P(SearchState)], ctypes.c_uint64),
+        "search_state_key_hash64": ([P(SearchCtx), P(SearchState)], ctypes.c_uint64),
+        "search_state_leaf_outputs": ([P(SearchCtx), P(SearchState)], ctypes.c_uint8),
+        "search_gen_candidates_branchless": ([P(ctypes.c_uint16), ctypes.c_int, P(SearchState)],
+                                             ctypes.c_int),
+        "search_exhaustive_complete": ([P(SearchCtx), P(SearchState), ctypes.c_int,
+                                        P(ctypes.c_uint16), P(ctypes.c_int)], ctypes.c_int),
+        "search_exhaustive_states_explored": ([], ctypes.c_uint64),
+        "pca_disasm": ([ctypes.c_uint16, ctypes.c_char_p, ctypes.c_size_t], None),
+        "pcagb_last_error": ([], ctypes.c_char_p),
+        "pcagb_default_opts": ([P(SolveOpts)], None),
+        "pcagb_engine_create": ([ctypes.c_int, ctypes.c_size_t, P(ctypes.c_void_p)], ctypes.c_int),
+        "pcagb_engine_destroy": ([ctypes.c_void_p], None),
+        "pcagb_solve": ([ctypes.c_void_p, P(TaskSpec), P(SolveOpts), P(SolveResult),
+                         P(ctypes.c_uint16), P(ctypes.c_int), ctypes.c_int], ctypes.c_int),
+        "pcagb_complete": ([ctypes.c_void_p, P(SearchCtx), P(SearchState), ctypes.c_int,
+                            P(ctypes.c_uint16), P(ctypes.c_int), P(ctypes.c_uint64)], ctypes.c_int),
+        "pcagb_num_candidates": ([ctypes.c_uint8], ctypes.c_int),
+        "pcagb_engine_stream": ([ctypes.c_void_p], ctypes.c_void_p),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    return lib
+
+
+class PCALib:
+    """The reference's PCALib interface over libpcagb.so."""
+
+    def __init__(self, lib_path: str = LIB_PATH):
+        self.lib = load_library(lib_path)
+
+    def load_task(self, path):
+        spec = TaskSpec()
+        if self.lib.task_load(path.encode(), ctypes.byref(spec)) != 0:
+            raise RuntimeError(f"Failed to load task: {path}")
+        return spec
+
+    def init_ctx(self, spec):
+        ctx = SearchCtx()
+        if self.lib.search_ctx_init(ctypes.byref(ctx), ctypes.byref(spec)) != 0:
+            raise RuntimeError("Failed to init search context")
+        return ctx
+
+    def init_root(self, ctx):
+        root = SearchState()
+        self.lib.search_state_init_root(ctypes.byref(ctx), ctypes.byref(root))
+        return root
+
+    def step(self, ctx, src, insn):
+        dst = SearchState()
+        ok = self.lib.search_state_step(ctypes.byref(ctx), ctypes.byref(src), insn,
+                                        ctypes.byref(dst))
+        return dst if ok else None
+
+    def oep_hash(self, ctx, state):
+        return self.lib.search_state_oep_hash64(ctypes.byref(ctx), ctypes.byref(state))
+
+    def key_hash(self, ctx, state):
+        return self.lib.search_state_key_hash64(ctypes.byref(ctx), ctypes.byref(state))
+
+    def leaf_check(self, ctx, state):
+        return self.lib.search_state_leaf_outputs(ctypes.byref(ctx), ctypes.byref(state))
+
+    def gen_candidates(self, state):
+        buf = (ctypes.c_uint16 * MAX_CANDIDATES)()
+        n = self.lib.search_gen_candidates_branchless(buf, MAX_CANDIDATES, ctypes.byref(state))
+        return [buf[i] for i in range(n)]
+
+    def exhaustive_complete(self, ctx, state, max_depth):
+        """IDDFS completion from state to max_depth on the GPU.
+        Returns (found, sol_len, [insns])."""
+        insns = (ctypes.c_uint16 * 16)()
+        sol_len = ctypes.c_int(0)
+        found = self.lib.search_exhaustive_complete(ctypes.byref(ctx), ctypes.byref(state),
+                                                    max_depth, insns, ctypes.byref(sol_len))
+        if found < 0:
+            raise RuntimeError(self.lib.pcagb_last_error().decode())
+        if found:
+            return True, sol_len.value, [insns[i] for i in range(sol_len.value)]
+        return False, 0, []
+
+    def exhaustive_states_explored(self):
+        return self.lib.search_exhaustive_states_explored()
+
+    def evaluate(self, spec, prog):
+        arr = (ctypes.c_uint16 * len(prog))(*prog)
+        return self.lib.task_evaluate(ctypes.byref(spec), arr, len(prog))
+
+    def disasm(self, insn):
+        buf = ctypes.create_string_buffer(64)
+        self.lib.pca_disasm(insn, buf, 64)
+        return buf.value.decode()
+
+
+def make_task(name, inputs, outputs, max_cycles=100, input_ports=None) -> TaskSpec:
+    """Build a TaskSpec from rows of input values and single outputs."""
+    spec = TaskSpec()
+    spec.name = name.encode()[:63]
+    spec.max_cycles = max_cycles
+    n_in = len(inputs[0]) if len(inputs) else 1
+    ports = input_ports if input_ports is not None else list(range(n_in))
+    spec.num_inputs = n_in
+    for i, p in enumerate(ports):
+        spec.input_ports[i] = p
+    spec.num_outputs = 1
+    spec.output_ports[0] = 0
+    if len(inputs) > MAX_TESTS:
+        raise ValueError("at most 32 tests")
+    for t, (row, out) in enumerate(zip(inputs, outputs)):
+        for i, v in enumerate(row):
+            spec.tests[t].inputs[i] = int(v) & 0xFFFF
+        spec.tests[t].outputs[0] = int(out) & 0xFFFF
+    spec.num_tests = len(inputs)
+    return spec
+
+
+@dataclass
+class Solution:
+    optimal_depth: int
+    programs: list = field(default_factory=list)
+    total_solutions: int = 0
+    candidates: list = field(default_factory=list)
+    evaluations: list = field(default_factory=list)
+    tried: list = field(default_factory=list)
+    pruned_cum: list = field(default_factory=list)
+    level_children: list = field(default_factory=list)
+    level_survivors: list = field(default_factory=list)
+    seconds: float = 0.0
+    gpu_ms_expand: float = 0.0
+    gpu_ms_suffix: float = 0.0
+    gpu_ms_insert: float = 0.0
+    kernel_launches: int = 0
+    insert_launches: int = 0
+    suffix_launches: int = 0
+    h2d_bytes: int = 0
+    d2h_bytes: int = 0
+    insert_children: int = 0
+    split_used: int = 0
+
+
+class EngineError(RuntimeError):
+    pass
+
+
+class Engine:
+    """One GPU engine (device buffers in an HBM arena)."""
+
+    def __init__(self, device: int = 0, hbm_budget_bytes: int = 0, lib: ctypes.CDLL | None = None):
+        self.lib = lib or load_library()
+        self.h = ctypes.c_void_p()
+        rc = self.lib.pcagb_engine_create(device, hbm_budget_bytes, ctypes.byref(self.h))
+        if rc != 0:
+            raise EngineError(f"engine create failed ({rc}): {self.lib.pcagb_last_error().decode()}")
+
+    def close(self):
+        if self.h:
+            self.lib.pcagb_engine_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def solve(self, task: TaskSpec, max_depth=4, oep_mode=OEP_EXACT_LIVE, split_depth=-1,
+              count_levels=False, first_only=False, min_depth=0, sol_cap=4096) -> Solution:
+        o = SolveOpts()
+        self.lib.pcagb_default_opts(ctypes.byref(o))
+        o.max_depth, o.min_depth, o.split_depth = max_depth, min_depth, split_depth
+        o.oep_mode, o.count_levels, o.first_only = oep_mode, int(count_levels), int(first_only)
+        r = SolveResult()
+        progs = (ctypes.c_uint16 * (16 * max(sol_cap, 1)))()
+        lens = (ctypes.c_int * max(sol_cap, 1))()
+        rc = self.lib.pcagb_solve(self.h, ctypes.byref(task), ctypes.byref(o), ctypes.byref(r),
+                                  progs, lens, sol_cap)
+        if rc != 0:
+            raise EngineError(f"solve failed ({rc}): {self.lib.pcagb_last_error().decode()}")
+        sol = Solution(optimal_depth=r.optimal_depth, total_solutions=r.total_solutions)
+        for name in ("seconds", "gpu_ms_expand", "gpu_ms_suffix", "gpu_ms_insert",
+                     "kernel_launches", "insert_launches", "suffix_launches", "h2d_bytes",
+                     "d2h_bytes", "insert_children", "split_used"):
+            setattr(sol, name, getattr(r, name))
+        for i in range(r.stored):
+            sol.programs.append([progs[i * 16 + j] for j in range(lens[i])])
+        last = max(r.optimal_depth, max_depth if r.optimal_depth < 0 else r.optimal_depth)
+        for name in ("candidates", "evaluations", "tried", "pruned_cum", "level_children",
+                     "level_survivors"):
+            arr = getattr(r, name)
+            setattr(sol, name, [arr[k] for k in range(min(last + 1, MAXD))])
+        return sol
+
+    @property
+    def stream(self) -> int:
+        """cudaStream_t of the engine, as an integer handle."""
+        return self.lib.pcagb_engine_stream(self.h) or 0
+
+    def complete(self, ctx: SearchCtx, state: SearchState, max_depth: int):
+        insns = (ctypes.c_uint16 * 16)()
+        n = ctypes.c_int(0)
+        explored = ctypes.c_uint64(0)
+        rc = self.lib.pcagb_complete(self.h, ctypes.byref(ctx), ctypes.byref(state), max_depth,
+                                     insns, ctypes.byref(n), ctypes.byref(explored))
+        if rc < 0:
+            raise EngineError(f"complete failed ({rc}): {self.lib.pcagb_last_error().decode()}")
+        return bool(rc), n.value, [insns[i] for i in range(n.value)], explored.value

@@ -241,6 +241,7 @@ int build_level(pcagb_engine *e, int d)
     if (!P.child_off) {
         P.child_off = (uint64_t *)e->alloc_bottom((P.n + 1) * sizeof(uint64_t));
         if (!P.child_off) return fail(PCAGB_ENOMEM);
+        CK(cudaMemsetAsync(P.child_off + P.n, 0, sizeof(uint64_t), e->stream));
         k_child_counts<<<e->grid(2), 256, 0, e->stream>>>(P.live, P.n, P.child_off);
         int rc = check_launch(e);
         if (rc) return rc;

@@ -235,6 +235,30 @@ void *pcagb_engine_stream(pcagb_engine_t *e);
 /* Number of generator candidates for a live mask (src/search_state.c:280-330). */
 int  pcagb_num_candidates(uint8_t live);
 
+/* ---- Solve without allocating (no counterpart in the reference) ----------
+ * For callers that cannot call cudaMalloc -- a process whose device memory
+ * belongs to another allocator's pool, latency-critical code that must not
+ * risk the synchronisation an allocation can cause, hosts that forbid a
+ * plugin from owning device memory. Needs no engine. Enumerates every kernel
+ * program of length 1..max_depth straight from the task root and returns the
+ * full canonical program set at the optimal length (the programs
+ * pcagb_solve returns with split_depth 0, here in no particular order).
+ * Scratch is one file-scope static __device__ array of
+ * PCAGB_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until
+ * exit; the first call on a device sets it up (call it once before any
+ * stream capture). Calls share the array: calls that overlap on the GPU
+ * race. max_depth above PCAGB_NOALLOC_MAX_DEPTH, or more solving records
+ * than the scratch holds, is rejected (PCAGB_EINVAL / PCAGB_ELIMIT; message
+ * in pcagb_noalloc_last_error). Runs on the current device and the given
+ * stream (NULL = legacy default stream). Returns 1 found / 0 none /
+ * negative error. */
+#define PCAGB_NOALLOC_SCRATCH_BYTES (16u << 20)
+#define PCAGB_NOALLOC_MAX_DEPTH 3
+int  pcagb_solve_small_noalloc(const task_spec_t *task, int max_depth, void *stream,
+                               int *optimal_depth, uint64_t *total_solutions,
+                               uint16_t *sol_progs, int *sol_lens, int sol_cap);
+const char *pcagb_noalloc_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif

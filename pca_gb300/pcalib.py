@@ -101,6 +101,7 @@ EXPORTS = [
     "search_exhaustive_complete", "search_exhaustive_states_explored", "search_state_dump",
     "pcagb_last_error", "pcagb_default_opts", "pcagb_engine_create", "pcagb_engine_destroy",
     "pcagb_solve", "pcagb_complete", "pcagb_num_candidates", "pcagb_engine_stream",
+    "pcagb_solve_small_noalloc", "pcagb_noalloc_last_error",
 ]
 
 
@@ -135,6 +136,10 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
                             P(ctypes.c_uint16), P(ctypes.c_int), P(ctypes.c_uint64)], ctypes.c_int),
         "pcagb_num_candidates": ([ctypes.c_uint8], ctypes.c_int),
         "pcagb_engine_stream": ([ctypes.c_void_p], ctypes.c_void_p),
+        "pcagb_solve_small_noalloc": ([P(TaskSpec), ctypes.c_int, ctypes.c_void_p,
+                                       P(ctypes.c_int), P(ctypes.c_uint64), P(ctypes.c_uint16),
+                                       P(ctypes.c_int), ctypes.c_int], ctypes.c_int),
+        "pcagb_noalloc_last_error": ([], ctypes.c_char_p),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--cpu-budget", type=float, default=12.0,
                     help="seconds of CPU work in the cpu_baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--hbm-gb", type=float, default=0.0,
+                    help="engine arena size in GB (0: 60%% of free HBM)")
     return ap.parse_args()
 
 
@@ -191,7 +193,7 @@ def main():
     from pca_gb300.pcalib import Engine, OEP_EXACT_LIVE
     torch.cuda.set_device(local)
     task = taskgen.is_power2_task(args.seed)
-    eng = Engine(local, 0)
+    eng = Engine(local, int(args.hbm_gb * (1 << 30)))
     stream = torch.cuda.ExternalStream(eng.stream, device=local)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
 
@@ -278,13 +280,24 @@ def main():
                                 "expand_total": sum([]) if False else None},
     }
     line["kernels_ms_per_step"]["expand_total"] = None
+    # Roofline of the suffix kernel: integer-issue bound. Peak = one warp
+    # instruction per SM sub-partition per clock at the measured max clock.
+    # Achieved = this run's value-class evaluations per second of suffix-kernel
+    # time x the kernel's warp instructions per evaluation, measured by ncu
+    # (profiles/k_suffix_is_power2_t32_k4.md: 2.20e9 instructions for the
+    # depth-4 launch's 7.30e8 evaluations).
+    inst_per_eval = 2203637570 / 7.30e8
+    peak_issue = sms * 4 * sm_max * 1e6
+    achieved_issue = suffix_evals_per_s * inst_per_eval
     line["roofline"] = {
-        "kernel": "k_suffix (last instruction, value classes)",
-        "bound": "int_issue",
-        "achieved": suffix_evals_per_s / 1e9, "unit": "Geval/s",
-        "peak": None, "frac": None, "traffic": None,
-        "peak_issue_gwarp_inst_s": sms * 4 * sm_max / 1e3,
-        "peak_source": pk_kind,
+        "kernel": "k_suffix<32,1> (last instruction over value classes)",
+        "bound": "int_issue", "unit": "Gwarp-inst/s",
+        "achieved": achieved_issue / 1e9, "peak": peak_issue / 1e9,
+        "frac": achieved_issue / peak_issue,
+        "traffic": 2888440000 + 3394560,
+        "evaluations_per_s": suffix_evals_per_s,
+        "peak_source": f"{sms} SMs x 4 issue slots x sm_max_mhz from MEASURED_PEAKS.json ({pk_kind})",
+        "ncu": "profiles/k_suffix_is_power2_t32_k4.md",
     }
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(task, args.max_depth, args.cpu_budget)

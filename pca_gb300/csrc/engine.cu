@@ -96,12 +96,14 @@ struct pcagb_engine {
     size_t cap = 0, bottom = 0, top = 0;
     uint32_t *d_cand_uop = nullptr, *d_vc_uop = nullptr;
     uint16_t *d_vc_first = nullptr;
+    uint32_t *d_chunks = nullptr;
     unsigned long long *d_small = nullptr;   /* [0] sol count [1] first [2] count [8..135] hist */
     uint32_t *d_status = nullptr;
     ulonglong2 *d_sol = nullptr;
     uint64_t sol_cap = 1u << 20;
     uint16_t *d_paths = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
+    int occ_insert = 4, occ_suffix = 8, occ_mat = 4;   /* resident blocks per SM */
     uint64_t launches = 0;
     uint64_t h2d = 0, d2h = 0;
     uint64_t insert_launches = 0, suffix_launches = 0, insert_children = 0;
@@ -211,8 +213,8 @@ int fetch_hist(pcagb_engine *e, Level &L)
 template <int TPC>
 int launch_expand(pcagb_engine *e, const Level &P, unsigned long long *table, uint64_t tmask)
 {
-    k_expand_insert<TPC><<<e->grid(4), kThreads, 0, e->stream>>>(view(P), e->td, table, tmask,
-                                                                 e->d_status);
+    k_expand_insert<TPC><<<e->grid(e->occ_insert), kThreads, 0, e->stream>>>(
+        view(P), e->td, table, tmask, e->d_status);
     return check_launch(e);
 }
 
@@ -221,8 +223,8 @@ int launch_materialize(pcagb_engine *e, const Level &P, const uint32_t *bitmap,
                        const uint64_t *word_off, Level &C)
 {
     LevelOut out{C.regs, C.flags, C.live, C.parent, C.cidx};
-    k_materialize<TPC><<<e->grid(4), kThreads, 0, e->stream>>>(view(P), e->td, bitmap, word_off,
-                                                               out);
+    k_materialize<TPC><<<e->grid(e->occ_mat), kThreads, 0, e->stream>>>(view(P), e->td, bitmap,
+                                                                         word_off, out);
     return check_launch(e);
 }
 
@@ -348,8 +350,8 @@ int run_stage(pcagb_engine *e, int S, int K, uint64_t *nrec_out, std::vector<Raw
         if (t16) k_leaf<16><<<e->grid(4), 256, 0, e->stream>>>(view(L), e->td, sb);
         else k_leaf<32><<<e->grid(4), 256, 0, e->stream>>>(view(L), e->td, sb);
     } else if (s == 1) {
-        if (t16) k_suffix<16, 1><<<e->grid(8), kThreads, 0, e->stream>>>(view(L), e->td, sb, 1, 1);
-        else k_suffix<32, 1><<<e->grid(8), kThreads, 0, e->stream>>>(view(L), e->td, sb, 1, 1);
+        if (t16) k_suffix<16, 1><<<e->grid(e->occ_suffix), kThreads, 0, e->stream>>>(view(L), e->td, sb, 1, 1);
+        else k_suffix<32, 1><<<e->grid(e->occ_suffix), kThreads, 0, e->stream>>>(view(L), e->td, sb, 1, 1);
     } else {
         int ncmax = 0;
         for (int m = 0; m < 128; m++)
@@ -357,11 +359,11 @@ int run_stage(pcagb_engine *e, int S, int K, uint64_t *nrec_out, std::vector<Raw
         uint32_t chunk = s == 2 ? 16 : 1;
         uint32_t cpp = (uint32_t)((ncmax + chunk - 1) / chunk);
         if (s == 2) {
-            if (t16) k_suffix<16, 2><<<e->grid(8), kThreads, 0, e->stream>>>(view(L), e->td, sb, cpp, chunk);
-            else k_suffix<32, 2><<<e->grid(8), kThreads, 0, e->stream>>>(view(L), e->td, sb, cpp, chunk);
+            if (t16) k_suffix<16, 2><<<e->grid(e->occ_suffix), kThreads, 0, e->stream>>>(view(L), e->td, sb, cpp, chunk);
+            else k_suffix<32, 2><<<e->grid(e->occ_suffix), kThreads, 0, e->stream>>>(view(L), e->td, sb, cpp, chunk);
         } else if (s == 3) {
-            if (t16) k_suffix<16, 3><<<e->grid(8), kThreads, 0, e->stream>>>(view(L), e->td, sb, cpp, chunk);
-            else k_suffix<32, 3><<<e->grid(8), kThreads, 0, e->stream>>>(view(L), e->td, sb, cpp, chunk);
+            if (t16) k_suffix<16, 3><<<e->grid(e->occ_suffix), kThreads, 0, e->stream>>>(view(L), e->td, sb, cpp, chunk);
+            else k_suffix<32, 3><<<e->grid(e->occ_suffix), kThreads, 0, e->stream>>>(view(L), e->td, sb, cpp, chunk);
         } else {
             set_err("suffix depth %d not supported (split too shallow)", s);
             return PCAGB_ENOMEM;
@@ -492,6 +494,64 @@ struct RunSpec {
     uint16_t target[MAX_TESTS];
 };
 
+/* Test order for the suffix kernel. Its lanes evaluate value classes on
+   the first one or two tests and send survivors to a check of all tests, so
+   the fewer classes pass the first tests the less work is done. The order is
+   chosen greedily on (state, class) pairs sampled from the root and its
+   children: each next test is the one the fewest remaining pairs pass. A
+   permutation of the tests changes no result of the search (pruning keys,
+   DFS order, programs and counts are all independent of it). */
+std::vector<int> choose_test_order(const RunSpec &rs)
+{
+    const GenTables &gt = gen_tables();
+    const int T = rs.T;
+    search_ctx_t ctx;
+    memset(&ctx, 0, sizeof ctx);
+    ctx.num_tests = (uint8_t)T;
+    std::vector<search_state_t> sample(1, rs.root);
+    uint16_t cands[4096];
+    int n = gen_candidates(rs.root.live, cands, 4096);
+    for (int i = 0; i < n; i++) {
+        search_state_t c;
+        if (search_state_step(&ctx, &rs.root, cands[i], &c)) sample.push_back(c);
+    }
+    std::vector<uint32_t> masks;
+    for (const search_state_t &st : sample) {
+        const uint32_t m = (st.live >> 1) & 127u;
+        for (uint32_t i = gt.vc_off[m]; i < gt.vc_off[m + 1]; i++) {
+            const uint32_t u = gt.vc_uop[i];
+            uint32_t pass = 0;
+            for (int t = 0; t < T; t++) {
+                uint32_t v = pca_alu(UOP_OP(u), st.regs[t][UOP_A(u)], st.regs[t][UOP_B(u)],
+                                     UOP_IMM(u));
+                if (v == rs.target[t]) pass |= 1u << t;
+            }
+            masks.push_back(pass);
+        }
+    }
+    std::vector<int> order;
+    uint32_t used = 0;
+    while ((int)order.size() < T && !masks.empty()) {
+        int best = -1;
+        size_t best_n = SIZE_MAX;
+        for (int t = 0; t < T; t++) {
+            if (used >> t & 1u) continue;
+            size_t cnt = 0;
+            for (uint32_t m : masks) cnt += m >> t & 1u;
+            if (cnt < best_n) { best_n = cnt; best = t; }
+        }
+        order.push_back(best);
+        used |= 1u << best;
+        std::vector<uint32_t> keep;
+        for (uint32_t m : masks)
+            if (m >> best & 1u) keep.push_back(m);
+        masks.swap(keep);
+    }
+    for (int t = 0; t < T; t++)
+        if (!(used >> t & 1u)) order.push_back(t);
+    return order;
+}
+
 /* Core IDDFS shared by pcagb_solve and pcagb_complete. */
 int run_iddfs(pcagb_engine *e, const RunSpec &rs, const pcagb_opts_t &o, pcagb_result_t *res,
               std::vector<RawSol> *sols)
@@ -515,7 +575,9 @@ int run_iddfs(pcagb_engine *e, const RunSpec &rs, const pcagb_opts_t &o, pcagb_r
     memset(&e->td, 0, sizeof e->td);
     e->td.T = rs.T;
     e->td.key_live = o.oep_mode == PCAGB_OEP_EXACT_LIVE;
-    for (int t = 0; t < rs.T; t++) e->td.target[t] = rs.target[t];
+    /* the device sees the tests in the suffix kernel's preferred order */
+    const std::vector<int> order = choose_test_order(rs);
+    for (int t = 0; t < rs.T; t++) e->td.target[t] = rs.target[order[t]];
     CK(cudaSetDevice(e->device));
     CK(cudaMemsetAsync(e->d_status, 0, 4, e->stream));
 
@@ -526,8 +588,8 @@ int run_iddfs(pcagb_engine *e, const RunSpec &rs, const pcagb_opts_t &o, pcagb_r
         std::vector<uint16_t> regs(8 * e->TPC, 0);
         std::vector<uint8_t> flags(e->TPC, 0);
         for (int t = 0; t < rs.T; t++) {
-            for (int r = 1; r < 8; r++) regs[r * e->TPC + t] = rs.root.regs[t][r];
-            flags[t] = rs.root.flags[t];
+            for (int r = 1; r < 8; r++) regs[r * e->TPC + t] = rs.root.regs[order[t]][r];
+            flags[t] = rs.root.flags[order[t]];
         }
         uint32_t zero32 = 0;
         uint16_t zero16 = 0;
@@ -660,6 +722,19 @@ int engine_init(pcagb_engine *e, int device, size_t budget)
     CK(cudaEventCreate(&e->ev1));
     CK(cudaEventCreate(&e->ev2));
     CK(cudaEventCreate(&e->ev3));
+    {
+        int nb = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_expand_insert<32>, kThreads, 0) ==
+                cudaSuccess && nb > 0)
+            e->occ_insert = nb;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_suffix<32, 1>, kThreads, 0) ==
+                cudaSuccess && nb > 0)
+            e->occ_suffix = nb;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_materialize<32>, kThreads, 0) ==
+                cudaSuccess && nb > 0)
+            e->occ_mat = nb;
+        cudaGetLastError();
+    }
     size_t free_b = 0, total_b = 0;
     CK(cudaMemGetInfo(&free_b, &total_b));
     if (budget == 0) budget = (size_t)(free_b * 0.6);
@@ -680,6 +755,13 @@ int engine_init(pcagb_engine *e, int device, size_t budget)
     CK(cudaMalloc(&e->d_cand_uop, gt.cand_uop.size() * 4));
     CK(cudaMalloc(&e->d_vc_uop, gt.vc_uop.size() * 4));
     CK(cudaMalloc(&e->d_vc_first, first.size() * 2));
+    CK(cudaMalloc(&e->d_chunks, gt.chunks.size() * 4));
+    CK(cudaMemcpy(e->d_chunks, gt.chunks.data(), gt.chunks.size() * 4, cudaMemcpyHostToDevice));
+    CK(cudaMemcpyToSymbol(c_chunk_off, gt.chunk_off.data(), 129 * 4));
+    {
+        const uint32_t *ck = e->d_chunks;
+        CK(cudaMemcpyToSymbol(c_chunks, &ck, sizeof ck));
+    }
     CK(cudaMalloc(&e->d_small, 256 * sizeof(unsigned long long)));
     CK(cudaMalloc(&e->d_status, 16));
     CK(cudaMalloc(&e->d_sol, e->sol_cap * sizeof(ulonglong2)));
@@ -743,6 +825,7 @@ void pcagb_engine_destroy(pcagb_engine_t *e)
     cudaFree(e->d_cand_uop);
     cudaFree(e->d_vc_uop);
     cudaFree(e->d_vc_first);
+    cudaFree(e->d_chunks);
     cudaFree(e->d_small);
     cudaFree(e->d_status);
     cudaFree(e->d_sol);

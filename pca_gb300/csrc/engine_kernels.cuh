@@ -57,6 +57,8 @@ __constant__ uint32_t c_vc_off[129];
 __constant__ const uint32_t *c_cand_uop;
 __constant__ const uint32_t *c_vc_uop;
 __constant__ const uint16_t *c_vc_first;   /* first candidate index per class */
+__constant__ uint32_t c_chunk_off[129];    /* op-uniform runs of candidates */
+__constant__ const uint32_t *c_chunks;
 
 struct TaskDev {
     int T;          /* tests */
@@ -142,7 +144,7 @@ template <int TPC>
 struct WarpState {
     uint32_t R[10][TPC + 1];  /* columns r0..r7 + 2 spare; +1 word pad */
     uint32_t F[TPC];
-    uint64_t colh[8];         /* colh[r] = col_final(r, hash(col r)); [0] = flags */
+    uint64_t colh[8];         /* colh[r] = col_final(r, hash(col r)), r >= 1 */
 };
 
 template <int TPC>
@@ -159,33 +161,116 @@ __device__ __forceinline__ void load_state(WarpState<TPC> &ws, const uint16_t *r
 
 /* ---- level expansion: insert every child into the exact table ------------ */
 
-template <int TPC>
-__device__ bool child_equal(const LevelDev &P, const TaskDev &task, const WarpState<TPC> &A,
-                            uint32_t liveA, uint32_t uA, uint64_t qB, uint32_t cB)
+/* The op is a template parameter here: a warp expands a run of candidates
+   that share one op, so the switch is resolved at compile time and the
+   lanes never diverge on it. */
+template <int OP>
+__device__ __forceinline__ uint32_t alu_t(uint32_t a, uint32_t b, uint32_t imm)
 {
-    uint32_t liveB = P.live[qB];
-    uint32_t mB = (liveB >> 1) & 127u;
-    uint32_t uB = c_cand_uop[c_cand_off[mB] + cB];
-    uint32_t rdA = UOP_RD(uA), rdB = UOP_RD(uB);
+    if constexpr (OP == PCA_OP_ADD) return (a + b) & 0xFFFFu;
+    else if constexpr (OP == PCA_OP_SUB) return (a - b) & 0xFFFFu;
+    else if constexpr (OP == PCA_OP_MUL) return (a * b) & 0xFFFFu;
+    else if constexpr (OP == PCA_OP_AND) return a & b;
+    else if constexpr (OP == PCA_OP_OR) return a | b;
+    else if constexpr (OP == PCA_OP_XOR) return a ^ b;
+    else if constexpr (OP == PCA_OP_SHL) return (a << (b & 15u)) & 0xFFFFu;
+    else if constexpr (OP == PCA_OP_SHR) return a >> (b & 15u);
+    else if constexpr (OP == PCA_OP_ASR) return (uint32_t)(uint16_t)((int16_t)(uint16_t)a >> (b & 15u));
+    else if constexpr (OP == PCA_OP_LDI) return imm;
+    else return (a + (uint32_t)(int32_t)(int8_t)(uint8_t)imm) & 0xFFFFu; /* ADDI */
+}
+
+template <int OP>
+__device__ __forceinline__ uint32_t flags_t(uint32_t a, uint32_t b, uint32_t imm, uint32_t res,
+                                            uint32_t old)
+{
+    if constexpr (OP == PCA_OP_LDI) return old;
+    else if constexpr (OP == PCA_OP_ADD || OP == PCA_OP_SUB || OP == PCA_OP_MUL ||
+                       OP == PCA_OP_ADDI)
+        return pca_alu_flags(OP, a, b, imm, res, old);
+    else return pca_zn(res);
+}
+
+/* Hash of the child's new column (chain over 4 tests per word) and of its
+   flags (16 tests per word), tests >= T contributing zeros. The loop over
+   word groups is kept rolled: eleven op variants of a fully unrolled loop
+   overflow the instruction cache. */
+template <int TPC, int OP>
+__device__ __forceinline__ void child_hashes(const WarpState<TPC> &ws, uint32_t ra, uint32_t rb,
+                                             uint32_t imm, int T, uint64_t &h, uint64_t &hf)
+{
+    h = 0x243F6A8885A308D3ull;
+    hf = 0x13198A2E03707344ull;
+    uint64_t wf = 0;
+#pragma unroll 1
+    for (int t0 = 0; t0 < TPC; t0 += 4) {
+        uint64_t w = 0;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const int t = t0 + j;
+            const uint32_t a = ws.R[ra][t], b = ws.R[rb][t];
+            uint32_t res = alu_t<OP>(a, b, imm);
+            uint32_t f = flags_t<OP>(a, b, imm, res, ws.F[t]);
+            if (t >= T) { res = 0; f = 0; }
+            w |= (uint64_t)res << (16 * j);
+            wf |= (uint64_t)f << (4 * (t & 15));
+        }
+        h = chain(h, w);
+        if ((t0 & 15) == 12) { hf = chain(hf, wf); wf = 0; }
+    }
+}
+
+template <int TPC>
+__device__ __forceinline__ void child_hashes_any(uint32_t op, const WarpState<TPC> &ws, uint32_t ra,
+                                                 uint32_t rb, uint32_t imm, int T, uint64_t &h,
+                                                 uint64_t &hf)
+{
+    switch (op) {
+    case PCA_OP_ADD: child_hashes<TPC, PCA_OP_ADD>(ws, ra, rb, imm, T, h, hf); break;
+    case PCA_OP_SUB: child_hashes<TPC, PCA_OP_SUB>(ws, ra, rb, imm, T, h, hf); break;
+    case PCA_OP_MUL: child_hashes<TPC, PCA_OP_MUL>(ws, ra, rb, imm, T, h, hf); break;
+    case PCA_OP_AND: child_hashes<TPC, PCA_OP_AND>(ws, ra, rb, imm, T, h, hf); break;
+    case PCA_OP_OR: child_hashes<TPC, PCA_OP_OR>(ws, ra, rb, imm, T, h, hf); break;
+    case PCA_OP_XOR: child_hashes<TPC, PCA_OP_XOR>(ws, ra, rb, imm, T, h, hf); break;
+    case PCA_OP_SHL: child_hashes<TPC, PCA_OP_SHL>(ws, ra, rb, imm, T, h, hf); break;
+    case PCA_OP_SHR: child_hashes<TPC, PCA_OP_SHR>(ws, ra, rb, imm, T, h, hf); break;
+    case PCA_OP_ASR: child_hashes<TPC, PCA_OP_ASR>(ws, ra, rb, imm, T, h, hf); break;
+    case PCA_OP_LDI: child_hashes<TPC, PCA_OP_LDI>(ws, ra, rb, imm, T, h, hf); break;
+    default: child_hashes<TPC, PCA_OP_ADDI>(ws, ra, rb, imm, T, h, hf); break;
+    }
+}
+
+/* Exact compare of child A (the warp's parent in shared memory + micro-op
+   uA) with child B (parent qB of the level in HBM + candidate cB), the whole
+   warp cooperating: lane t rebuilds test t of both children (every register,
+   the flags) and __all_sync decides. All lanes must call it. */
+template <int TPC>
+__device__ bool warp_child_equal(const LevelDev &P, const TaskDev &task, const WarpState<TPC> &A,
+                                 uint32_t liveA, uint32_t uA, uint64_t qB, uint32_t cB, int lane)
+{
+    const uint32_t liveB = P.live[qB];
+    const uint32_t uB = c_cand_uop[c_cand_off[(liveB >> 1) & 127u] + cB];
+    const uint32_t rdA = UOP_RD(uA), rdB = UOP_RD(uB);
     if (task.key_live && ((liveA | (1u << rdA)) != (liveB | (1u << rdB)))) return false;
-    const uint16_t *RB = P.regs + qB * 8 * TPC;
-    const uint8_t *FB = P.flags + qB * TPC;
-    for (int t = 0; t < task.T; t++) {
-        uint32_t a1 = A.R[UOP_A(uA)][t], b1 = A.R[UOP_B(uA)][t];
-        uint32_t resA = pca_alu(UOP_OP(uA), a1, b1, UOP_IMM(uA));
-        uint32_t fA = pca_alu_flags(UOP_OP(uA), a1, b1, UOP_IMM(uA), resA, A.F[t]);
-        uint32_t a2 = RB[UOP_A(uB) * TPC + t], b2 = RB[UOP_B(uB) * TPC + t];
-        uint32_t resB = pca_alu(UOP_OP(uB), a2, b2, UOP_IMM(uB));
-        uint32_t fB = pca_alu_flags(UOP_OP(uB), a2, b2, UOP_IMM(uB), resB, FB[t]);
-        if (fA != fB) return false;
+    bool ok = true;
+    if (lane < task.T) {
+        const uint16_t *RB = P.regs + qB * 8 * TPC + lane;
+        const uint32_t a1 = A.R[UOP_A(uA)][lane], b1 = A.R[UOP_B(uA)][lane];
+        const uint32_t resA = pca_alu(UOP_OP(uA), a1, b1, UOP_IMM(uA));
+        const uint32_t fA = pca_alu_flags(UOP_OP(uA), a1, b1, UOP_IMM(uA), resA, A.F[lane]);
+        const uint32_t a2 = RB[UOP_A(uB) * TPC], b2 = RB[UOP_B(uB) * TPC];
+        const uint32_t resB = pca_alu(UOP_OP(uB), a2, b2, UOP_IMM(uB));
+        const uint32_t fB = pca_alu_flags(UOP_OP(uB), a2, b2, UOP_IMM(uB), resB,
+                                          P.flags[qB * TPC + lane]);
+        ok = fA == fB;
 #pragma unroll
         for (uint32_t r = 1; r < 8; r++) {
-            uint32_t vA = r == rdA ? resA : A.R[r][t];
-            uint32_t vB = r == rdB ? resB : (uint32_t)RB[r * TPC + t];
-            if (vA != vB) return false;
+            const uint32_t vA = r == rdA ? resA : A.R[r][lane];
+            const uint32_t vB = r == rdB ? resB : (uint32_t)RB[r * TPC];
+            ok &= vA == vB;
         }
     }
-    return true;
+    return __all_sync(0xFFFFFFFFu, ok);
 }
 
 template <int TPC>
@@ -198,68 +283,79 @@ k_expand_insert(LevelDev P, TaskDev task, unsigned long long *table, uint64_t tm
     WarpState<TPC> &ws = sws[wib];
     const uint64_t nw = (uint64_t)gridDim.x * kWarpsPerBlock;
     for (uint64_t q = (uint64_t)blockIdx.x * kWarpsPerBlock + wib; q < P.n; q += nw) {
+        __syncwarp();
         load_state<TPC>(ws, P.regs, P.flags, q, lane);
         const uint32_t live = P.live[q];
         __syncwarp();
         if (lane >= 1 && lane < 8) ws.colh[lane] = col_final(lane, hash_column<TPC>(ws.R[lane]));
-        if (lane == 0) ws.colh[0] = hash_flags<TPC>(ws.F);
         __syncwarp();
         uint64_t regsum = 0;
 #pragma unroll
         for (int r = 1; r < 8; r++) regsum += ws.colh[r];
         const uint32_t m = (live >> 1) & 127u;
-        const uint32_t base = c_cand_off[m], nc = c_cand_off[m + 1] - base;
-        for (uint32_t c = lane; c < nc; c += 32) {
+        const uint32_t base = c_cand_off[m];
+        for (uint32_t k = c_chunk_off[m]; k < c_chunk_off[m + 1]; k++) {
+            const uint32_t ch = c_chunks[k], start = ch >> 8, cnt = ch & 255u;
+            const bool valid = (uint32_t)lane < cnt;
+            const uint32_t c = start + (valid ? lane : 0);
             const uint32_t u = c_cand_uop[base + c];
-            const uint32_t op = UOP_OP(u), rd = UOP_RD(u), ra = UOP_A(u), rb = UOP_B(u),
-                           imm = UOP_IMM(u);
-            uint64_t h = 0x243F6A8885A308D3ull, hf = 0x13198A2E03707344ull;
-            uint64_t w = 0, wf = 0;
-#pragma unroll
-            for (int t = 0; t < TPC; t++) {
-                uint32_t a = ws.R[ra][t], b = ws.R[rb][t];
-                uint32_t res = pca_alu(op, a, b, imm);
-                uint32_t f = pca_alu_flags(op, a, b, imm, res, ws.F[t]);
-                if (t >= task.T) { res = 0; f = 0; }
-                w |= (uint64_t)res << (16 * (t & 3));
-                wf |= (uint64_t)f << (4 * (t & 15));
-                if ((t & 3) == 3) { h = chain(h, w); w = 0; }
-                if ((t & 15) == 15) { hf = chain(hf, wf); wf = 0; }
-            }
-            const uint32_t clive = live | (1u << rd);
+            const uint32_t op = UOP_OP(u), rd = UOP_RD(u);
+            uint64_t h, hf;
+            child_hashes_any<TPC>(op, ws, UOP_A(u), UOP_B(u), UOP_IMM(u), task.T, h, hf);
             uint64_t H = regsum - ws.colh[rd] + col_final(rd, h) + hf;
-            if (task.key_live) H += live_final(clive);
+            if (task.key_live) H += live_final(live | (1u << rd));
             const uint64_t ref = (q << 12) | c;
             const unsigned long long mine = ((H >> 40) << 40) | (ref + 1);
             uint64_t idx = H & tmask;
             uint32_t probes = 0;
-            for (;;) {
-                unsigned long long s = *((volatile unsigned long long *)&table[idx]);
-                if (s == 0) {
-                    unsigned long long old = atomicCAS(&table[idx], 0ull, mine);
-                    if (old == 0) break;
-                    s = old;
+            bool done = !valid;
+            /* lanes probe in parallel; a tag match is settled by an exact
+               warp-wide compare, one requesting lane at a time */
+            while (__any_sync(0xFFFFFFFFu, !done)) {
+                bool needcmp = false;
+                unsigned long long s = 0;
+                if (!done) {
+                    s = *((volatile unsigned long long *)&table[idx]);
+                    if (s == 0) {
+                        const unsigned long long old = atomicCAS(&table[idx], 0ull, mine);
+                        if (old == 0) done = true;
+                        else s = old;
+                    }
+                    if (!done) needcmp = (s >> 40) == (mine >> 40);
                 }
-                if ((s >> 40) == (mine >> 40)) {
-                    uint64_t oref = (s & kRefMask) - 1;
-                    if (child_equal<TPC>(P, task, ws, live, u, oref >> 12, (uint32_t)(oref & 4095))) {
+                uint32_t req = __ballot_sync(0xFFFFFFFFu, needcmp);
+                bool eq = false;
+                while (req) {
+                    const int j = __ffs(req) - 1;
+                    req &= req - 1;
+                    const uint32_t uj = __shfl_sync(0xFFFFFFFFu, u, j);
+                    const unsigned long long sj = __shfl_sync(0xFFFFFFFFu, s, j);
+                    const uint64_t oref = (sj & kRefMask) - 1;
+                    const bool e = warp_child_equal<TPC>(P, task, ws, live, uj, oref >> 12,
+                                                         (uint32_t)(oref & 4095), lane);
+                    if (lane == j) eq = e;
+                }
+                if (!done) {
+                    if (needcmp && eq) {
+                        /* same state: keep the smaller ref (the DFS-first child) */
+                        uint64_t oref = (s & kRefMask) - 1;
                         while (ref < oref) {
-                            unsigned long long old = atomicCAS(&table[idx], s, mine);
+                            const unsigned long long old = atomicCAS(&table[idx], s, mine);
                             if (old == s) break;
                             s = old;
                             oref = (s & kRefMask) - 1;
                         }
-                        break;
+                        done = true;
+                    } else {
+                        idx = (idx + 1) & tmask;
+                        if (++probes >= kMaxProbes) {
+                            atomicOr(status, kStatusTableFull);
+                            done = true;
+                        }
                     }
-                }
-                idx = (idx + 1) & tmask;
-                if (++probes >= kMaxProbes) {
-                    atomicOr(status, kStatusTableFull);
-                    break;
                 }
             }
         }
-        __syncwarp();
     }
 }
 
@@ -425,8 +521,8 @@ __global__ void k_leaf(LevelDev P, TaskDev task, SolBuf S)
 template <int TPC>
 __device__ __forceinline__ void scan_last(const WarpState<TPC> &ws, const TaskDev &task,
                                           uint32_t m, uint32_t rd1, uint32_t rd2, uint32_t tgt,
-                                          uint32_t tgt0, int lane, const SolBuf &S, uint64_t q,
-                                          uint32_t m1, uint32_t m2)
+                                          uint32_t tgt0, uint32_t tgt1, int lane,
+                                          const SolBuf &S, uint64_t q, uint32_t m1, uint32_t m2)
 {
     const uint32_t vbase = c_vc_off[m], nvc = c_vc_off[m + 1] - vbase;
     for (uint32_t b0 = 0; b0 < nvc; b0 += 32) {
@@ -434,11 +530,14 @@ __device__ __forceinline__ void scan_last(const WarpState<TPC> &ws, const TaskDe
         uint32_t u = 0;
         bool pass = false;
         if (i < nvc) {
+            /* first two tests per lane; survivors are checked on all tests below */
             u = c_vc_uop[vbase + i];
             uint32_t ra = UOP_A(u), rb = UOP_B(u);
             ra = ra == rd2 ? 9u : ra == rd1 ? 8u : ra;
             rb = rb == rd2 ? 9u : rb == rd1 ? 8u : rb;
-            pass = pca_alu(UOP_OP(u), ws.R[ra][0], ws.R[rb][0], UOP_IMM(u)) == tgt0;
+            const uint32_t op = UOP_OP(u), imm = UOP_IMM(u);
+            pass = pca_alu(op, ws.R[ra][0], ws.R[rb][0], imm) == tgt0 &&
+                   (task.T < 2 || pca_alu(op, ws.R[ra][1], ws.R[rb][1], imm) == tgt1);
         }
         uint32_t bal = __ballot_sync(0xFFFFFFFFu, pass);
         while (bal) {
@@ -467,7 +566,7 @@ k_suffix(LevelDev P, TaskDev task, SolBuf S, uint32_t chunks_per_prefix, uint32_
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     WarpState<TPC> &ws = sws[wib];
     const uint32_t tgt = lane < task.T ? task.target[lane] : 0u;
-    const uint32_t tgt0 = task.target[0];
+    const uint32_t tgt0 = task.target[0], tgt1 = task.target[1];
     const uint64_t nw = (uint64_t)gridDim.x * kWarpsPerBlock;
     const uint64_t items = P.n * chunks_per_prefix;
     uint64_t loaded = ~0ull;
@@ -483,7 +582,7 @@ k_suffix(LevelDev P, TaskDev task, SolBuf S, uint32_t chunks_per_prefix, uint32_
         }
         const uint32_t m0 = (live >> 1) & 127u;
         if (SD == 1) {
-            scan_last<TPC>(ws, task, m0, 8, 8, tgt, tgt0, lane, S, q, 0, 0);
+            scan_last<TPC>(ws, task, m0, 8, 8, tgt, tgt0, tgt1, lane, S, q, 0, 0);
             continue;
         }
         const uint32_t cb0 = c_cand_off[m0], nc0 = c_cand_off[m0 + 1] - cb0;
@@ -499,7 +598,7 @@ k_suffix(LevelDev P, TaskDev task, SolBuf S, uint32_t chunks_per_prefix, uint32_
             __syncwarp();
             const uint32_t m1 = (m0 | (1u << (rd1 - 1))) & 127u;
             if (SD == 2) {
-                scan_last<TPC>(ws, task, m1, rd1, 8, tgt, tgt0, lane, S, q, i1, 0);
+                scan_last<TPC>(ws, task, m1, rd1, 8, tgt, tgt0, tgt1, lane, S, q, i1, 0);
                 continue;
             }
             const uint32_t cb1 = c_cand_off[m1], nc1 = c_cand_off[m1 + 1] - cb1;
@@ -516,8 +615,8 @@ k_suffix(LevelDev P, TaskDev task, SolBuf S, uint32_t chunks_per_prefix, uint32_
                                                   : 0u;
                 __syncwarp();
                 const uint32_t m2 = (m1 | (1u << (rd2 - 1))) & 127u;
-                scan_last<TPC>(ws, task, m2, rd2 == rd1 ? 8u : rd1, rd2, tgt, tgt0, lane, S, q,
-                               i1, i2);
+                scan_last<TPC>(ws, task, m2, rd2 == rd1 ? 8u : rd1, rd2, tgt, tgt0, tgt1, lane,
+                               S, q, i1, i2);
             }
         }
     }

@@ -34,6 +34,11 @@ struct GenTables {
     std::vector<uint16_t> cand_vc;     /* value class index within mask    */
     std::vector<uint32_t> vc_off;      /* size 129                         */
     std::vector<uint32_t> vc_uop;      /* one micro-op per value class     */
+    /* per mask: runs of <= 32 consecutive candidates with one op, so a warp
+       expanding a state works on a single op at a time; entry =
+       start << 8 | count, start relative to the mask's candidate list */
+    std::vector<uint32_t> chunk_off;   /* size 129 */
+    std::vector<uint32_t> chunks;
     /* f[s][m]: programs decided by s more instructions from mask m:
        f[1][m] = nc(m), f[s][m] = sum over candidates c of f[s-1][m | rd(c)] */
     std::vector<uint64_t> f[5];

@@ -93,6 +93,19 @@ static GenTables build_tables()
     }
     t.cand_off[128] = (uint32_t)t.cand.size();
     t.vc_off[128] = (uint32_t)t.vc_uop.size();
+    t.chunk_off.assign(129, 0);
+    for (int m = 0; m < 128; m++) {
+        t.chunk_off[m] = (uint32_t)t.chunks.size();
+        const uint32_t base = t.cand_off[m], n = t.cand_off[m + 1] - base;
+        uint32_t s = 0;
+        while (s < n) {
+            uint32_t e = s;
+            while (e < n && e - s < 32 && UOP_OP(t.cand_uop[base + e]) == UOP_OP(t.cand_uop[base + s])) e++;
+            t.chunks.push_back(s << 8 | (e - s));
+            s = e;
+        }
+    }
+    t.chunk_off[128] = (uint32_t)t.chunks.size();
     for (int s = 0; s < 5; s++) t.f[s].assign(128, 0);
     for (int m = 0; m < 128; m++) t.f[0][m] = 1;
     for (int s = 1; s < 5; s++)

@@ -1,0 +1,131 @@
+/*
+ * cli_enumerate.cpp -- `enumerate`, the reference solver's command line
+ * (tools/enumerate.c:537-755) over libpcagb.so.
+ *
+ *   enumerate <task.json> [-d max_depth] [--no-branch] [--no-oep] [-v] [--count]
+ *
+ * Same argument grammar, the same report lines (task summary, per-depth
+ * "candidates" / "OEP pruned" / "solutions found" / "elapsed", the solutions
+ * with their disassembly and test[0] check, "Optimal solution length: N
+ * instructions (kernel depth K)", "Found N distinct program(s) at this
+ * length.") and the same exit code (0 iff a program was found).
+ *
+ * The search runs on the GPU engine and is branchless: branch mode (CMP/BR)
+ * is not implemented, so the reference's default without --no-branch is
+ * refused with exit code 2. With OEP on, the pruner is exact (key
+ * regs+flags, DFS-first representative, full-state compare); the printed
+ * programs are the reference's (its DFS-first program per final state, at
+ * most 100). --count builds every level with the pruner so the per-depth
+ * counters are the reference's exact-pruner counters; without it the search
+ * builds levels only as deep as HBM allows and enumerates the rest, and the
+ * counters are this engine's. --record (training labels) is not supported.
+ */
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "../../include/pca_gb300.h"
+
+static void print_solution(const task_spec_t &t, const uint16_t *p, int len, int idx)
+{
+    printf("  Solution #%d (%d instructions):\n", idx + 1, len);
+    char buf[64];
+    for (int i = 0; i < len; i++) {
+        pca_disasm(p[i], buf, sizeof buf);
+        printf("    %02X: %04X  %s\n", i, p[i], buf);
+    }
+    pca_vm_t vm;
+    pca_init(&vm);
+    pca_load(&vm, p, (size_t)len);
+    for (int i = 0; i < t.num_inputs; i++) vm.ports[t.input_ports[i]] = t.tests[0].in[i];
+    pca_run(&vm, t.max_cycles);
+    printf("    verify test[0]: in=(");
+    for (int i = 0; i < t.num_inputs; i++) printf("%s%u", i ? "," : "", t.tests[0].in[i]);
+    uint16_t got = vm.ports[t.output_ports[0]];
+    printf(") -> port%d=%u (expected %u) %s\n", t.output_ports[0], got, t.tests[0].out[0],
+           got == t.tests[0].out[0] ? "OK" : "FAIL");
+}
+
+int main(int argc, char **argv)
+{
+    if (argc < 2) {
+        fprintf(stderr,
+                "Usage: enumerate <task.json> [-d max_depth] [--no-branch] [--no-oep] [-v] [--count]\n");
+        return 1;
+    }
+    int max_depth = 4, no_branch = 0, no_oep = 0, count = 0;
+    for (int i = 2; i < argc; i++) {
+        if (!strcmp(argv[i], "-d") && i + 1 < argc) max_depth = atoi(argv[++i]);
+        else if (!strcmp(argv[i], "--no-branch")) no_branch = 1;
+        else if (!strcmp(argv[i], "--no-oep")) no_oep = 1;
+        else if (!strcmp(argv[i], "--count")) count = 1;
+        else if (!strcmp(argv[i], "-v")) {
+        } else if (!strcmp(argv[i], "--record") || !strcmp(argv[i], "--task-id") ||
+                   !strcmp(argv[i], "--neg-stride")) {
+            fprintf(stderr, "enumerate: --record is not supported by the GPU engine\n");
+            return 2;
+        }
+    }
+    task_spec_t task;
+    if (task_load(argv[1], &task) < 0) return 1;
+    task_print(&task);
+    printf("\n");
+    if (!no_branch) {
+        fprintf(stderr, "enumerate: branch mode (CMP/BR) is not implemented on the GPU engine; "
+                        "pass --no-branch\n");
+        return 2;
+    }
+    pcagb_engine_t *e = nullptr;
+    if (pcagb_engine_create(0, 0, &e) != PCAGB_OK) {
+        fprintf(stderr, "enumerate: %s\n", pcagb_last_error());
+        return 1;
+    }
+    printf("Enumerating programs (max kernel depth %d, branches off, OEP %s, search_state)...\n\n",
+           max_depth, no_oep ? "off" : "on");
+    pcagb_opts_t o;
+    pcagb_default_opts(&o);
+    o.max_depth = max_depth;
+    o.oep_mode = no_oep ? PCAGB_OEP_NONE : PCAGB_OEP_EXACT;
+    o.count_levels = count || no_oep;
+    const int cap = 100;
+    std::vector<uint16_t> progs(cap * 16);
+    std::vector<int> lens(cap);
+    pcagb_result_t r;
+    auto t0 = std::chrono::steady_clock::now();
+    int rc = pcagb_solve(e, &task, &o, &r, progs.data(), lens.data(), cap);
+    double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (rc != PCAGB_OK) {
+        fprintf(stderr, "enumerate: %s\n", pcagb_last_error());
+        pcagb_engine_destroy(e);
+        return 1;
+    }
+    const int last = r.optimal_depth >= 0 ? r.optimal_depth : max_depth;
+    uint64_t total_tried = 0;
+    for (int k = 0; k <= last; k++) {
+        printf("--- kernel depth %d (total program length %d) ---\n", k, task.num_inputs + k + 2);
+        total_tried += r.tried[k];
+        const int found = k == r.optimal_depth ? r.stored : 0;
+        printf("  candidates: %llu  (%.1f M/sec)\n", (unsigned long long)r.tried[k],
+               secs > 0 ? r.tried[k] / secs / 1e6 : 0.0);
+        if (!no_oep) printf("  OEP pruned: %llu\n", (unsigned long long)r.pruned_cum[k]);
+        printf("  solutions found: %d (total: %d)\n", found, found);
+        printf("  elapsed: %.2f sec\n\n", secs);
+        if (found)
+            for (int i = 0; i < r.stored; i++) print_solution(task, &progs[i * 16], lens[i], i);
+    }
+    if (r.optimal_depth < 0) {
+        printf("\nNo solutions found up to kernel depth %d.\n", max_depth);
+        pcagb_engine_destroy(e);
+        return 1;
+    }
+    printf("\nOptimal solution length: %d instructions (kernel depth %d)\n",
+           task.num_inputs + r.optimal_depth + 2, r.optimal_depth);
+    printf("Found %d distinct program(s) at this length.\n", r.stored);
+    printf("\nTotal: %llu candidates in %.2f sec", (unsigned long long)total_tried, secs);
+    if (!no_oep) printf(" (OEP pruned: %llu)", (unsigned long long)r.pruned_cum[last]);
+    printf("\n");
+    pcagb_engine_destroy(e);
+    return 0;
+}

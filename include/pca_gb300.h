@@ -221,6 +221,17 @@ void pcagb_engine_destroy(pcagb_engine_t *e);
 int  pcagb_solve(pcagb_engine_t *e, const task_spec_t *task, const pcagb_opts_t *opts,
                  pcagb_result_t *res, uint16_t *sol_progs, int *sol_lens, int sol_cap);
 
+/* Batched solve: many tasks share every launch (level expansion, OEP,
+ * suffix enumeration); a task leaves the search once its optimal depth is
+ * proven or its max_depth is reached. results[i] is task i's result; its
+ * `seconds` is the time from the call until task i was decided (its
+ * time-to-proven-optimal inside the batch), the gpu_ms_* and byte counters
+ * are the batch's. Task i's programs go to
+ * sol_progs[i * sol_cap_per_task * 16 ...]. At most 8192 tasks. */
+int  pcagb_solve_batch(pcagb_engine_t *e, const task_spec_t *tasks, int ntasks,
+                       const pcagb_opts_t *opts, pcagb_result_t *results, uint16_t *sol_progs,
+                       int *sol_lens, int sol_cap_per_task);
+
 /* IDDFS completion from an arbitrary branchless state (the GPU form of
  * search_exhaustive_complete, src/search_state.c:418-453). Returns 1 found /
  * 0 none / negative error. */

@@ -1,16 +1,22 @@
 /*
- * engine.cu -- the GPU engine behind pcagb_solve / pcagb_complete and the
- * GPU-backed search_exhaustive_complete of the libpca ABI.
+ * engine.cu -- the GPU engine behind pcagb_solve, pcagb_solve_batch,
+ * pcagb_complete and the GPU-backed search_exhaustive_complete of the libpca
+ * ABI.
  *
  * Iterative deepening over the kernel length K, as in the reference's
  * tools/enumerate.c:624-662 and gpu/hybrid.cu:699-824, restructured for one
- * GB300:
+ * GB300 and for many tasks at once:
+ *   - a batch of tasks shares every launch: level d holds the distinct
+ *     states of all tasks still searched, each state tagged with its task;
  *   - levels 1..S are built breadth-first on the device, each deduplicated
  *     by the exact OEP table and kept in HBM in DFS order (levels do not
- *     depend on K, so each is built once per solve, not once per K);
+ *     depend on K, so each is built once per batch, not once per K);
  *   - the remaining K-S <= 3 instructions are enumerated by the suffix
  *     kernel, which takes the role of gpu/hybrid.cu:163-275;
- *   - the host only reads back sizes, counters and the solving records.
+ *   - a task leaves the search (its states are skipped) once its optimal
+ *     depth is proven or its depth limit is reached;
+ *   - the host only reads back sizes, per-task histograms, counters and the
+ *     solving records.
  * Device memory comes from one arena allocated at engine creation: levels
  * grow from the bottom, per-expansion scratch (hash table, bitmap, scan
  * buffers) from the top, so a solve performs no cudaMalloc.
@@ -53,30 +59,35 @@ static void set_err(const char *fmt, ...)
         }                                                                              \
     } while (0)
 
+constexpr int kMaxBatch = 8192;
+
 struct Level {
     uint64_t n = 0;
     uint16_t *regs = nullptr;
     uint8_t *flags = nullptr;
     uint8_t *live = nullptr;
+    uint16_t *task = nullptr;
     uint32_t *parent = nullptr;
     uint16_t *cidx = nullptr;
     uint64_t *child_off = nullptr;  /* set when this level is expanded */
     uint64_t children = 0;
-    uint64_t hist[128] = {};
+    std::vector<uint64_t> hist;     /* [task][128] states per liveness mask */
 };
 
 struct PathGather {
     const uint32_t *parent[SEARCH_MAX_DEPTH + 1];
     const uint16_t *cidx[SEARCH_MAX_DEPTH + 1];
+    const uint16_t *task;           /* task of the level-S states */
 };
 
-/* For each record, write the candidate indices of its prefix path. */
+/* For each record, the candidate indices of its prefix path and its task. */
 __global__ void k_gather_paths(PathGather G, int S, const ulonglong2 *rec, uint64_t n,
-                               uint16_t *out)
+                               uint16_t *out, uint16_t *task_out)
 {
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (uint64_t)gridDim.x * blockDim.x) {
         uint64_t q = rec[i].x;
+        task_out[i] = G.task[q];
         for (int d = S; d >= 1; d--) {
             out[i * SEARCH_MAX_DEPTH + d - 1] = G.cidx[d][q];
             q = G.parent[d][q];
@@ -97,11 +108,15 @@ struct pcagb_engine {
     uint32_t *d_cand_uop = nullptr, *d_vc_uop = nullptr;
     uint16_t *d_vc_first = nullptr;
     uint32_t *d_chunks = nullptr;
-    unsigned long long *d_small = nullptr;   /* [0] sol count [1] first [2] count [8..135] hist */
+    unsigned long long *d_small = nullptr;   /* [0] sol count [1] first [2] count */
     uint32_t *d_status = nullptr;
     ulonglong2 *d_sol = nullptr;
     uint64_t sol_cap = 1u << 20;
-    uint16_t *d_paths = nullptr;
+    /* batch task table */
+    int32_t *d_task_T = nullptr;
+    uint32_t *d_task_target = nullptr;
+    uint8_t *d_task_active = nullptr;
+    unsigned long long *d_hist = nullptr;    /* [kMaxBatch][128] */
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
     int occ_insert = 4, occ_suffix = 8, occ_mat = 4;   /* resident blocks per SM */
     uint64_t launches = 0;
@@ -109,13 +124,12 @@ struct pcagb_engine {
     uint64_t insert_launches = 0, suffix_launches = 0, insert_children = 0;
     float ms_insert = 0;
 
-    /* per solve */
+    /* per batch */
     std::vector<Level> levels;
+    int ntasks = 0;
     int TPC = 32;
-    int T = 0;
     bool no_oep = false;
     int max_feasible = SEARCH_MAX_DEPTH;
-    uint8_t root_live = 0;
     TaskDev td{};
     float ms_expand = 0, ms_suffix = 0;
 
@@ -184,7 +198,10 @@ int exclusive_scan(pcagb_engine *e, uint64_t *a, uint64_t n, uint64_t *total)
     return PCAGB_OK;
 }
 
-LevelDev view(const Level &L) { return LevelDev{L.regs, L.flags, L.live, L.child_off, L.n}; }
+LevelDev view(const Level &L)
+{
+    return LevelDev{L.regs, L.flags, L.live, L.task, L.child_off, L.n};
+}
 
 int alloc_level(pcagb_engine *e, Level &L, uint64_t n)
 {
@@ -192,20 +209,23 @@ int alloc_level(pcagb_engine *e, Level &L, uint64_t n)
     L.regs = (uint16_t *)e->alloc_bottom(n * 8 * e->TPC * 2);
     L.flags = (uint8_t *)e->alloc_bottom(n * e->TPC);
     L.live = (uint8_t *)e->alloc_bottom(n);
+    L.task = (uint16_t *)e->alloc_bottom(n * 2);
     L.parent = (uint32_t *)e->alloc_bottom(n * 4);
     L.cidx = (uint16_t *)e->alloc_bottom(n * 2);
-    if (!L.regs || !L.flags || !L.live || !L.parent || !L.cidx) return PCAGB_ENOMEM;
+    if (!L.regs || !L.flags || !L.live || !L.task || !L.parent || !L.cidx) return PCAGB_ENOMEM;
     return PCAGB_OK;
 }
 
 int fetch_hist(pcagb_engine *e, Level &L)
 {
-    unsigned long long *h = e->d_small + 8;
-    CK(cudaMemsetAsync(h, 0, 128 * sizeof(unsigned long long), e->stream));
-    k_live_hist<<<e->grid(2), 256, 0, e->stream>>>(L.live, L.n, h);
+    const size_t nh = (size_t)e->ntasks * 128;
+    CK(cudaMemsetAsync(e->d_hist, 0, nh * sizeof(unsigned long long), e->stream));
+    k_task_hist<<<e->grid(2), 256, 0, e->stream>>>(L.live, L.task, L.n, e->d_hist);
     int rc = check_launch(e);
     if (rc) return rc;
-    CK(e_copy(e, L.hist, h, sizeof L.hist, cudaMemcpyDeviceToHost, e->stream));
+    L.hist.assign(nh, 0);
+    CK(e_copy(e, L.hist.data(), e->d_hist, nh * sizeof(uint64_t), cudaMemcpyDeviceToHost,
+              e->stream));
     CK(cudaStreamSynchronize(e->stream));
     return PCAGB_OK;
 }
@@ -222,14 +242,14 @@ template <int TPC>
 int launch_materialize(pcagb_engine *e, const Level &P, const uint32_t *bitmap,
                        const uint64_t *word_off, Level &C)
 {
-    LevelOut out{C.regs, C.flags, C.live, C.parent, C.cidx};
+    LevelOut out{C.regs, C.flags, C.live, C.task, C.parent, C.cidx};
     k_materialize<TPC><<<e->grid(e->occ_mat), kThreads, 0, e->stream>>>(view(P), e->td, bitmap,
                                                                          word_off, out);
     return check_launch(e);
 }
 
-/* Build level d+1 from level d. Returns PCAGB_ENOMEM (and leaves the arena
- * as it was) when the level does not fit. */
+/* Build level d+1 from level d for the active tasks. Returns PCAGB_ENOMEM
+ * (and leaves the arena as it was) when the level does not fit. */
 int build_level(pcagb_engine *e, int d)
 {
     Level &P = e->levels[d];
@@ -244,7 +264,8 @@ int build_level(pcagb_engine *e, int d)
         P.child_off = (uint64_t *)e->alloc_bottom((P.n + 1) * sizeof(uint64_t));
         if (!P.child_off) return fail(PCAGB_ENOMEM);
         CK(cudaMemsetAsync(P.child_off + P.n, 0, sizeof(uint64_t), e->stream));
-        k_child_counts<<<e->grid(2), 256, 0, e->stream>>>(P.live, P.n, P.child_off);
+        k_child_counts<<<e->grid(2), 256, 0, e->stream>>>(P.live, P.task, e->td.active, P.n,
+                                                          P.child_off);
         int rc = check_launch(e);
         if (rc) return rc;
         rc = exclusive_scan(e, P.child_off, P.n + 1, &P.children);
@@ -268,7 +289,6 @@ int build_level(pcagb_engine *e, int d)
         while (slots < 2 * children) slots <<= 1;
         unsigned long long *table = (unsigned long long *)e->alloc_top(slots * 8);
         if (!table) return fail(PCAGB_ENOMEM);
-        /* rough room check for the new level before spending the time */
         CK(cudaMemsetAsync(table, 0, slots * 8, e->stream));
         CK(cudaMemsetAsync(bitmap, 0, words * 4 + 4, e->stream));
         CK(cudaMemsetAsync(e->d_small + 2, 0, 8, e->stream));
@@ -321,21 +341,35 @@ int build_level(pcagb_engine *e, int d)
     cudaEventElapsedTime(&ms, e->ev0, e->ev1);
     e->ms_expand += ms;
     e->top = top0;
-    e->levels.push_back(C);
+    e->levels.push_back(std::move(C));
     return PCAGB_OK;
 }
 
 struct RawSol {
     std::vector<uint16_t> kernel;  /* kernel instructions */
-    uint32_t out_reg;
-    /* DFS-order key */
-    std::vector<uint32_t> key;
+    uint32_t out_reg = 0;
+    std::vector<uint32_t> key;     /* DFS-order key: candidate indices */
+};
+
+/* One task of a batch, host side. */
+struct TaskRun {
+    search_state_t root;           /* level-0 state */
+    int T = 0;
+    uint16_t target[MAX_TESTS] = {};
+    std::vector<int> order;        /* device test order */
+    int max_depth = 0, min_depth = 0;
+    bool done = false;
+    int optimal_depth = -1;
+    uint64_t nrec = 0;
+    std::vector<RawSol> sols;
+    double t_done = 0;
+    pcagb_result_t res{};
 };
 
 /* Run the last stage at depth K from level S (suffix depth K-S, or the leaf
- * check when K == S). Fills raw solutions in DFS order. */
-int run_stage(pcagb_engine *e, int S, int K, uint64_t *nrec_out, std::vector<RawSol> *sols,
-              bool first_only)
+ * check when K == S) for the active tasks; appends each task's raw
+ * solutions in DFS order. */
+int run_stage(pcagb_engine *e, int S, int K, std::vector<TaskRun> &runs, bool first_only)
 {
     const GenTables &gt = gen_tables();
     Level &L = e->levels[S];
@@ -344,32 +378,32 @@ int run_stage(pcagb_engine *e, int S, int K, uint64_t *nrec_out, std::vector<Raw
     CK(cudaMemsetAsync(e->d_small + 1, 0xFF, 8, e->stream));
     SolBuf sb{e->d_small, e->d_sol, e->sol_cap, e->d_small + 1};
     cudaEventRecord(e->ev0, e->stream);
-    int rc = PCAGB_OK;
     const bool t16 = e->TPC == 16;
+    const int g = e->grid(e->occ_suffix);
     if (s == 0) {
         if (t16) k_leaf<16><<<e->grid(4), 256, 0, e->stream>>>(view(L), e->td, sb);
         else k_leaf<32><<<e->grid(4), 256, 0, e->stream>>>(view(L), e->td, sb);
     } else if (s == 1) {
-        if (t16) k_suffix<16, 1><<<e->grid(e->occ_suffix), kThreads, 0, e->stream>>>(view(L), e->td, sb, 1, 1);
-        else k_suffix<32, 1><<<e->grid(e->occ_suffix), kThreads, 0, e->stream>>>(view(L), e->td, sb, 1, 1);
-    } else {
+        if (t16) k_suffix<16, 1><<<g, kThreads, 0, e->stream>>>(view(L), e->td, sb, 1, 1);
+        else k_suffix<32, 1><<<g, kThreads, 0, e->stream>>>(view(L), e->td, sb, 1, 1);
+    } else if (s <= 3) {
         int ncmax = 0;
-        for (int m = 0; m < 128; m++)
-            if (L.hist[m]) ncmax = std::max(ncmax, gt.nc(m));
-        uint32_t chunk = s == 2 ? 16 : 1;
-        uint32_t cpp = (uint32_t)((ncmax + chunk - 1) / chunk);
+        for (size_t i = 0; i < L.hist.size(); i++)
+            if (L.hist[i]) ncmax = std::max(ncmax, gt.nc((int)(i & 127)));
+        const uint32_t chunk = s == 2 ? 16 : 1;
+        const uint32_t cpp = std::max(1u, (uint32_t)((ncmax + chunk - 1) / chunk));
         if (s == 2) {
-            if (t16) k_suffix<16, 2><<<e->grid(e->occ_suffix), kThreads, 0, e->stream>>>(view(L), e->td, sb, cpp, chunk);
-            else k_suffix<32, 2><<<e->grid(e->occ_suffix), kThreads, 0, e->stream>>>(view(L), e->td, sb, cpp, chunk);
-        } else if (s == 3) {
-            if (t16) k_suffix<16, 3><<<e->grid(e->occ_suffix), kThreads, 0, e->stream>>>(view(L), e->td, sb, cpp, chunk);
-            else k_suffix<32, 3><<<e->grid(e->occ_suffix), kThreads, 0, e->stream>>>(view(L), e->td, sb, cpp, chunk);
+            if (t16) k_suffix<16, 2><<<g, kThreads, 0, e->stream>>>(view(L), e->td, sb, cpp, chunk);
+            else k_suffix<32, 2><<<g, kThreads, 0, e->stream>>>(view(L), e->td, sb, cpp, chunk);
         } else {
-            set_err("suffix depth %d not supported (split too shallow)", s);
-            return PCAGB_ENOMEM;
+            if (t16) k_suffix<16, 3><<<g, kThreads, 0, e->stream>>>(view(L), e->td, sb, cpp, chunk);
+            else k_suffix<32, 3><<<g, kThreads, 0, e->stream>>>(view(L), e->td, sb, cpp, chunk);
         }
+    } else {
+        set_err("suffix depth %d not supported (split too shallow)", s);
+        return PCAGB_ENOMEM;
     }
-    rc = check_launch(e);
+    int rc = check_launch(e);
     if (rc) return rc;
     cudaEventRecord(e->ev1, e->stream);
     unsigned long long nrec = 0, first = 0;
@@ -380,52 +414,58 @@ int run_stage(pcagb_engine *e, int S, int K, uint64_t *nrec_out, std::vector<Raw
     cudaEventElapsedTime(&ms, e->ev0, e->ev1);
     e->ms_suffix += ms;
     e->suffix_launches++;
-    *nrec_out = nrec;
     if (!nrec) return PCAGB_OK;
 
-
-    /* Fetch the records (or, past the buffer or in first-only mode, the
+    /* Fetch the records (or, for one task in first-only mode, just the
        DFS-first one rebuilt from its packed key) and their prefix paths. */
     std::vector<ulonglong2> rec;
-    if (first_only || nrec > e->sol_cap) {
-        if (!first_only) {
-            set_err("%llu solving records exceed the buffer of %llu",
-                    (unsigned long long)nrec, (unsigned long long)e->sol_cap);
-            return PCAGB_ELIMIT;
-        }
+    if (first_only && e->ntasks == 1) {
         const uint64_t m1 = (first >> 24) & 4095, m2 = (first >> 12) & 4095, fc = first & 4095;
         /* low 16 bits with bit 15 set: a candidate index, not a class */
         rec.push_back(make_ulonglong2(first >> 36, (m1 << 32) | (m2 << 16) | (0x8000u | fc)));
     } else {
+        if (nrec > e->sol_cap) {
+            set_err("%llu solving records exceed the buffer of %llu", (unsigned long long)nrec,
+                    (unsigned long long)e->sol_cap);
+            return PCAGB_ELIMIT;
+        }
         rec.resize(nrec);
         CK(e_copy(e, rec.data(), e->d_sol, nrec * sizeof(ulonglong2), cudaMemcpyDeviceToHost,
-                           e->stream));
+                  e->stream));
         CK(cudaStreamSynchronize(e->stream));
     }
     std::vector<uint16_t> paths(rec.size() * SEARCH_MAX_DEPTH, 0);
-    if (S > 0) {
+    std::vector<uint16_t> rtask(rec.size(), 0);
+    {
         const size_t top0 = e->top;
         ulonglong2 *d_rec = (ulonglong2 *)e->alloc_top(rec.size() * sizeof(ulonglong2));
         uint16_t *d_paths = (uint16_t *)e->alloc_top(paths.size() * 2);
-        if (!d_rec || !d_paths) { set_err("arena exhausted gathering paths"); return PCAGB_ENOMEM; }
-        CK(e_copy(e, d_rec, rec.data(), rec.size() * sizeof(ulonglong2),
-                           cudaMemcpyHostToDevice, e->stream));
+        uint16_t *d_task = (uint16_t *)e->alloc_top(rtask.size() * 2);
+        if (!d_rec || !d_paths || !d_task) {
+            set_err("arena exhausted gathering paths");
+            return PCAGB_ENOMEM;
+        }
+        CK(e_copy(e, d_rec, rec.data(), rec.size() * sizeof(ulonglong2), cudaMemcpyHostToDevice,
+                  e->stream));
         PathGather G{};
         for (int d = 1; d <= S; d++) {
             G.parent[d] = e->levels[d].parent;
             G.cidx[d] = e->levels[d].cidx;
         }
-        k_gather_paths<<<64, 256, 0, e->stream>>>(G, S, d_rec, rec.size(), d_paths);
+        G.task = L.task;
+        k_gather_paths<<<64, 256, 0, e->stream>>>(G, S, d_rec, rec.size(), d_paths, d_task);
         rc = check_launch(e);
         if (rc) return rc;
-        CK(e_copy(e, paths.data(), d_paths, paths.size() * 2, cudaMemcpyDeviceToHost,
-                           e->stream));
+        CK(e_copy(e, paths.data(), d_paths, paths.size() * 2, cudaMemcpyDeviceToHost, e->stream));
+        CK(e_copy(e, rtask.data(), d_task, rtask.size() * 2, cudaMemcpyDeviceToHost, e->stream));
         CK(cudaStreamSynchronize(e->stream));
         e->top = top0;
     }
     for (size_t i = 0; i < rec.size(); i++) {
+        TaskRun &tr = runs[rtask[i]];
+        tr.nrec++;
         RawSol base;
-        uint32_t mask = (e->root_live >> 1) & 127u;
+        uint32_t mask = (tr.root.live >> 1) & 127u;
         auto take = [&](uint32_t c) {
             const uint32_t idx = gt.cand_off[mask] + c;
             base.kernel.push_back(gt.cand[idx]);
@@ -440,7 +480,7 @@ int run_stage(pcagb_engine *e, int S, int K, uint64_t *nrec_out, std::vector<Raw
         if (s == 0) {
             base.out_reg = low;
             base.key.push_back(0);
-            sols->push_back(base);
+            tr.sols.push_back(base);
             continue;
         }
         if (low & 0x8000u) {
@@ -450,7 +490,7 @@ int run_stage(pcagb_engine *e, int S, int K, uint64_t *nrec_out, std::vector<Raw
             r.kernel.push_back(gt.cand[idx]);
             r.key.push_back(c);
             r.out_reg = UOP_RD(gt.cand_uop[idx]);
-            sols->push_back(r);
+            tr.sols.push_back(r);
             continue;
         }
         for (uint32_t c = 0; c < (uint32_t)gt.nc(mask); c++) {
@@ -460,16 +500,18 @@ int run_stage(pcagb_engine *e, int S, int K, uint64_t *nrec_out, std::vector<Raw
             r.kernel.push_back(gt.cand[idx]);
             r.key.push_back(c);
             r.out_reg = UOP_RD(gt.cand_uop[idx]);
-            sols->push_back(r);
+            tr.sols.push_back(r);
         }
     }
-    std::sort(sols->begin(), sols->end(),
-              [](const RawSol &a, const RawSol &b) { return a.key < b.key; });
+    for (TaskRun &tr : runs)
+        if (!tr.sols.empty())
+            std::sort(tr.sols.begin(), tr.sols.end(),
+                      [](const RawSol &a, const RawSol &b) { return a.key < b.key; });
     return PCAGB_OK;
 }
 
-/* Host-side step for re-verification and for the reference-key dedup of the
-   solving leaves (tools/enumerate.c:380-384 applies OEP to leaves too). */
+/* Host-side step for the reference-key dedup of the solving leaves
+   (tools/enumerate.c:380-384 applies OEP to leaves too). */
 void leaf_key(const task_spec_t *task, const search_state_t &root, const std::vector<uint16_t> &k,
               std::vector<uint8_t> *key)
 {
@@ -488,12 +530,6 @@ void leaf_key(const task_spec_t *task, const search_state_t &root, const std::ve
     }
 }
 
-struct RunSpec {
-    search_state_t root;     /* level-0 state */
-    int T;
-    uint16_t target[MAX_TESTS];
-};
-
 /* Test order for the suffix kernel. Its lanes evaluate value classes on
    the first one or two tests and send survivors to a check of all tests, so
    the fewer classes pass the first tests the less work is done. The order is
@@ -501,19 +537,19 @@ struct RunSpec {
    children: each next test is the one the fewest remaining pairs pass. A
    permutation of the tests changes no result of the search (pruning keys,
    DFS order, programs and counts are all independent of it). */
-std::vector<int> choose_test_order(const RunSpec &rs)
+std::vector<int> choose_test_order(const TaskRun &tr)
 {
     const GenTables &gt = gen_tables();
-    const int T = rs.T;
+    const int T = tr.T;
     search_ctx_t ctx;
     memset(&ctx, 0, sizeof ctx);
     ctx.num_tests = (uint8_t)T;
-    std::vector<search_state_t> sample(1, rs.root);
+    std::vector<search_state_t> sample(1, tr.root);
     uint16_t cands[4096];
-    int n = gen_candidates(rs.root.live, cands, 4096);
+    int n = gen_candidates(tr.root.live, cands, 4096);
     for (int i = 0; i < n; i++) {
         search_state_t c;
-        if (search_state_step(&ctx, &rs.root, cands[i], &c)) sample.push_back(c);
+        if (search_state_step(&ctx, &tr.root, cands[i], &c)) sample.push_back(c);
     }
     std::vector<uint32_t> masks;
     for (const search_state_t &st : sample) {
@@ -524,7 +560,7 @@ std::vector<int> choose_test_order(const RunSpec &rs)
             for (int t = 0; t < T; t++) {
                 uint32_t v = pca_alu(UOP_OP(u), st.regs[t][UOP_A(u)], st.regs[t][UOP_B(u)],
                                      UOP_IMM(u));
-                if (v == rs.target[t]) pass |= 1u << t;
+                if (v == tr.target[t]) pass |= 1u << t;
             }
             masks.push_back(pass);
         }
@@ -552,14 +588,27 @@ std::vector<int> choose_test_order(const RunSpec &rs)
     return order;
 }
 
-/* Core IDDFS shared by pcagb_solve and pcagb_complete. */
-int run_iddfs(pcagb_engine *e, const RunSpec &rs, const pcagb_opts_t &o, pcagb_result_t *res,
-              std::vector<RawSol> *sols)
+uint64_t hist_sum(const Level &L, int t, const std::vector<uint64_t> &weight)
+{
+    uint64_t s = 0;
+    for (int m = 0; m < 128; m++) s += L.hist[(size_t)t * 128 + m] * weight[m];
+    return s;
+}
+
+/* Core batched IDDFS shared by every solve entry point. */
+int run_batch(pcagb_engine *e, std::vector<TaskRun> &runs, const pcagb_opts_t &o)
 {
     const GenTables &gt = gen_tables();
     auto t_start = std::chrono::steady_clock::now();
-    memset(res, 0, sizeof *res);
-    res->optimal_depth = -1;
+    auto elapsed = [&] {
+        return std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+    };
+    const int nt = (int)runs.size();
+    if (nt < 1 || nt > kMaxBatch) {
+        set_err("batch of %d tasks (1..%d)", nt, kMaxBatch);
+        return PCAGB_EINVAL;
+    }
+    e->ntasks = nt;
     e->levels.clear();
     e->bottom = 0;
     e->top = e->cap;
@@ -568,65 +617,109 @@ int run_iddfs(pcagb_engine *e, const RunSpec &rs, const pcagb_opts_t &o, pcagb_r
     e->h2d = e->d2h = 0;
     e->insert_launches = e->suffix_launches = e->insert_children = 0;
     e->max_feasible = SEARCH_MAX_DEPTH;
-    e->T = rs.T;
-    e->TPC = rs.T <= 16 ? 16 : 32;
+    int maxT = 0, maxK = 0;
+    for (TaskRun &tr : runs) {
+        maxT = std::max(maxT, tr.T);
+        maxK = std::max(maxK, tr.max_depth);
+        memset(&tr.res, 0, sizeof tr.res);
+        tr.res.optimal_depth = -1;
+        tr.order = choose_test_order(tr);
+    }
+    e->TPC = maxT <= 16 ? 16 : 32;
     e->no_oep = o.oep_mode == PCAGB_OEP_NONE;
-    e->root_live = rs.root.live;
-    memset(&e->td, 0, sizeof e->td);
-    e->td.T = rs.T;
-    e->td.key_live = o.oep_mode == PCAGB_OEP_EXACT_LIVE;
-    /* the device sees the tests in the suffix kernel's preferred order */
-    const std::vector<int> order = choose_test_order(rs);
-    for (int t = 0; t < rs.T; t++) e->td.target[t] = rs.target[order[t]];
+    e->td = TaskDev{e->d_task_T, e->d_task_target, e->d_task_active,
+                    o.oep_mode == PCAGB_OEP_EXACT_LIVE};
     CK(cudaSetDevice(e->device));
     CK(cudaMemsetAsync(e->d_status, 0, 4, e->stream));
-
-    /* level 0 */
-    Level L0;
-    if (alloc_level(e, L0, 1) != PCAGB_OK) { set_err("arena too small"); return PCAGB_ENOMEM; }
     {
-        std::vector<uint16_t> regs(8 * e->TPC, 0);
-        std::vector<uint8_t> flags(e->TPC, 0);
-        for (int t = 0; t < rs.T; t++) {
-            for (int r = 1; r < 8; r++) regs[r * e->TPC + t] = rs.root.regs[order[t]][r];
-            flags[t] = rs.root.flags[order[t]];
+        std::vector<int32_t> T(nt);
+        std::vector<uint32_t> tgt((size_t)nt * 32, 0);
+        for (int i = 0; i < nt; i++) {
+            T[i] = runs[i].T;
+            for (int t = 0; t < runs[i].T; t++)
+                tgt[(size_t)i * 32 + t] = runs[i].target[runs[i].order[t]];
         }
-        uint32_t zero32 = 0;
-        uint16_t zero16 = 0;
+        CK(e_copy(e, e->d_task_T, T.data(), nt * 4, cudaMemcpyHostToDevice, e->stream));
+        CK(e_copy(e, e->d_task_target, tgt.data(), tgt.size() * 4, cudaMemcpyHostToDevice,
+                  e->stream));
+    }
+
+    /* level 0: one root per task */
+    Level L0;
+    if (alloc_level(e, L0, nt) != PCAGB_OK) { set_err("arena too small"); return PCAGB_ENOMEM; }
+    {
+        const int TPC = e->TPC;
+        std::vector<uint16_t> regs((size_t)nt * 8 * TPC, 0);
+        std::vector<uint8_t> flags((size_t)nt * TPC, 0), live(nt);
+        std::vector<uint16_t> task(nt), cidx(nt, 0);
+        std::vector<uint32_t> parent(nt, 0);
+        L0.hist.assign((size_t)nt * 128, 0);
+        for (int i = 0; i < nt; i++) {
+            const TaskRun &tr = runs[i];
+            for (int t = 0; t < tr.T; t++) {
+                for (int r = 1; r < 8; r++)
+                    regs[((size_t)i * 8 + r) * TPC + t] = tr.root.regs[tr.order[t]][r];
+                flags[(size_t)i * TPC + t] = tr.root.flags[tr.order[t]];
+            }
+            live[i] = tr.root.live;
+            task[i] = (uint16_t)i;
+            L0.hist[(size_t)i * 128 + ((tr.root.live >> 1) & 127)] = 1;
+        }
         CK(e_copy(e, L0.regs, regs.data(), regs.size() * 2, cudaMemcpyHostToDevice, e->stream));
         CK(e_copy(e, L0.flags, flags.data(), flags.size(), cudaMemcpyHostToDevice, e->stream));
-        CK(e_copy(e, L0.live, &rs.root.live, 1, cudaMemcpyHostToDevice, e->stream));
-        CK(e_copy(e, L0.parent, &zero32, 4, cudaMemcpyHostToDevice, e->stream));
-        CK(e_copy(e, L0.cidx, &zero16, 2, cudaMemcpyHostToDevice, e->stream));
-        CK(cudaStreamSynchronize(e->stream));
-        L0.hist[(rs.root.live >> 1) & 127] = 1;
+        CK(e_copy(e, L0.live, live.data(), nt, cudaMemcpyHostToDevice, e->stream));
+        CK(e_copy(e, L0.task, task.data(), nt * 2, cudaMemcpyHostToDevice, e->stream));
+        CK(e_copy(e, L0.parent, parent.data(), nt * 4, cudaMemcpyHostToDevice, e->stream));
+        CK(e_copy(e, L0.cidx, cidx.data(), nt * 2, cudaMemcpyHostToDevice, e->stream));
     }
-    e->levels.push_back(L0);
-    res->level_children[0] = res->level_survivors[0] = 1;
+    e->levels.push_back(std::move(L0));
 
     /* K = 0: does a live register already hold the target? */
-    if (o.min_depth <= 0) {
+    for (TaskRun &tr : runs) {
+        tr.res.level_children[0] = tr.res.level_survivors[0] = 1;
+        if (tr.min_depth > 0) continue;
         for (uint32_t r = 1; r < 8; r++) {
-            if (!((rs.root.live >> r) & 1u)) continue;
+            if (!((tr.root.live >> r) & 1u)) continue;
             bool ok = true;
-            for (int t = 0; t < rs.T && ok; t++) ok = rs.root.regs[t][r] == rs.target[t];
+            for (int t = 0; t < tr.T && ok; t++) ok = tr.root.regs[t][r] == tr.target[t];
             if (ok) {
                 RawSol s0;
                 s0.out_reg = r;
-                sols->push_back(s0);
+                s0.key.push_back(r);
+                tr.sols.push_back(s0);
             }
         }
-        if (!sols->empty()) {
-            res->optimal_depth = 0;
-            res->tried[0] = sols->size();
-            res->total_solutions = sols->size();
+        if (!tr.sols.empty()) {
+            tr.done = true;
+            tr.optimal_depth = 0;
+            tr.res.tried[0] = tr.sols.size();
+            tr.t_done = elapsed();
         }
     }
-    uint64_t pruned_cum = 0;
-    for (int K = std::max(1, o.min_depth); K <= o.max_depth && res->optimal_depth < 0; K++) {
+    std::vector<uint8_t> active(nt, 0);
+    std::vector<uint64_t> pruned_cum(nt, 0);
+    std::vector<uint64_t> nc_w(128), nvc_w(128), ones(128, 1);
+    for (int m = 0; m < 128; m++) {
+        nc_w[m] = gt.nc(m);
+        nvc_w[m] = gt.nvc(m);
+    }
+    for (int K = 1; K <= maxK; K++) {
+        int nact = 0;
+        for (int i = 0; i < nt; i++) {
+            TaskRun &tr = runs[i];
+            if (!tr.done && K > tr.max_depth) {
+                tr.done = true;
+                tr.t_done = elapsed();
+            }
+            active[i] = !tr.done;
+            nact += active[i];
+        }
+        if (!nact) break;
+        CK(e_copy(e, e->d_task_active, active.data(), nt, cudaMemcpyHostToDevice, e->stream));
         int S_target = o.count_levels ? K : K - 1;
         if (o.split_depth >= 0) S_target = std::min(S_target, o.split_depth);
-        while ((int)e->levels.size() - 1 < S_target && (int)e->levels.size() - 1 < e->max_feasible) {
+        while ((int)e->levels.size() - 1 < S_target &&
+               (int)e->levels.size() - 1 < e->max_feasible) {
             const int d = (int)e->levels.size() - 1;
             int rc = build_level(e, d);
             if (rc == PCAGB_ENOMEM) {
@@ -634,8 +727,6 @@ int run_iddfs(pcagb_engine *e, const RunSpec &rs, const pcagb_opts_t &o, pcagb_r
                 break;
             }
             if (rc) return rc;
-            res->level_children[d + 1] = e->levels[d].children;
-            res->level_survivors[d + 1] = e->levels[d + 1].n;
         }
         const int S = std::min(S_target, (int)e->levels.size() - 1);
         const int s = K - S;
@@ -647,68 +738,68 @@ int run_iddfs(pcagb_engine *e, const RunSpec &rs, const pcagb_opts_t &o, pcagb_r
             set_err("depth %d needs level %d in HBM; the budget holds level %d", K, K - 3, S);
             return PCAGB_ENOMEM;
         }
-        res->split_used = S;
+        /* evaluations: value classes scanned at the last position */
+        std::vector<uint64_t> g(nvc_w);
+        for (int step = 1; step < s; step++) {
+            std::vector<uint64_t> g2(128, 0);
+            for (int m = 0; m < 128; m++)
+                for (uint32_t i = gt.cand_off[m]; i < gt.cand_off[m + 1]; i++)
+                    g2[m] += g[(m | (1u << (UOP_RD(gt.cand_uop[i]) - 1))) & 127];
+            g.swap(g2);
+        }
         const Level &LS = e->levels[S];
-        uint64_t cands = 0, evals = 0;
-        for (int m = 0; m < 128; m++) {
-            if (!LS.hist[m]) continue;
-            if (s >= 1) cands += LS.hist[m] * gt.f[s][m];
-            /* evaluations: value classes scanned at the last position */
-            if (s == 1) evals += LS.hist[m] * (uint64_t)gt.nvc(m);
-        }
-        if (s >= 2) {
-            /* sum over middle paths of the last mask's class count */
-            std::vector<uint64_t> g(128, 0), g2(128, 0);
-            for (int m = 0; m < 128; m++) g[m] = gt.nvc(m);
-            for (int step = 1; step < s; step++) {
-                for (int m = 0; m < 128; m++) {
-                    uint64_t sum = 0;
-                    for (uint32_t i = gt.cand_off[m]; i < gt.cand_off[m + 1]; i++)
-                        sum += g[(m | (1u << (UOP_RD(gt.cand_uop[i]) - 1))) & 127];
-                    g2[m] = sum;
-                }
-                g.swap(g2);
+        for (int i = 0; i < nt; i++) {
+            if (!active[i]) continue;
+            TaskRun &tr = runs[i];
+            tr.res.split_used = S;
+            tr.res.candidates[K] = s == 0 ? hist_sum(LS, i, ones) : hist_sum(LS, i, gt.f[s]);
+            tr.res.evaluations[K] = s == 0 ? tr.res.candidates[K] : hist_sum(LS, i, g);
+            for (int d = 1; d <= S; d++) {
+                tr.res.level_children[d] = hist_sum(e->levels[d - 1], i, nc_w);
+                tr.res.level_survivors[d] = hist_sum(e->levels[d], i, ones);
             }
-            for (int m = 0; m < 128; m++) evals += LS.hist[m] * g[m];
+            tr.nrec = 0;
         }
-        res->candidates[K] = s == 0 ? LS.n : cands;
-        res->evaluations[K] = s == 0 ? LS.n : evals;
-        uint64_t nrec = 0;
-        std::vector<RawSol> found;
-        int rc = run_stage(e, S, K, &nrec, &found, o.first_only != 0);
+        int rc = run_stage(e, S, K, runs, o.first_only != 0);
         if (rc) return rc;
-        /* the reference's counters (exact when every level up to K is built) */
-        uint64_t tried = 0, pruned = 0;
-        for (int j = 1; j <= S; j++) {
-            tried += res->level_children[j];
-            pruned += res->level_children[j] - res->level_survivors[j];
-        }
-        for (int i = 1; i <= s; i++)
-            for (int m = 0; m < 128; m++) tried += LS.hist[m] * gt.f[i][m];
-        pruned_cum += pruned;
-        res->tried[K] = tried + (s == 0 ? nrec : 0);
-        res->pruned_cum[K] = pruned_cum;
-        if (nrec) {
-            res->optimal_depth = K;
-            res->total_solutions = s == 0 ? nrec : 0;
-            if (s != 0) {
-                if (o.first_only) res->total_solutions = nrec;  /* class records */
-                else res->total_solutions = found.size();
+        for (int i = 0; i < nt; i++) {
+            if (!active[i]) continue;
+            TaskRun &tr = runs[i];
+            /* the reference's counters (exact when every level up to K is built) */
+            uint64_t tried = 0, pruned = 0;
+            for (int j = 1; j <= S; j++) {
+                tried += tr.res.level_children[j];
+                pruned += tr.res.level_children[j] - tr.res.level_survivors[j];
             }
-            *sols = std::move(found);
+            for (int k = 1; k <= s; k++) tried += hist_sum(LS, i, gt.f[k]);
+            pruned_cum[i] += pruned;
+            tr.res.tried[K] = tried + (s == 0 ? tr.nrec : 0);
+            tr.res.pruned_cum[K] = pruned_cum[i];
+            if (tr.nrec) {
+                tr.done = true;
+                tr.optimal_depth = K;
+                tr.t_done = elapsed();
+                tr.res.total_solutions =
+                    s == 0 || (o.first_only && nt == 1) ? tr.nrec : tr.sols.size();
+            }
         }
     }
-    res->gpu_ms_expand = e->ms_expand;
-    res->gpu_ms_suffix = e->ms_suffix;
-    res->gpu_ms_insert = e->ms_insert;
-    res->kernel_launches = e->launches;
-    res->insert_launches = e->insert_launches;
-    res->suffix_launches = e->suffix_launches;
-    res->insert_children = e->insert_children;
-    res->h2d_bytes = e->h2d;
-    res->d2h_bytes = e->d2h;
-    res->seconds =
-        std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+    const double total = elapsed();
+    for (TaskRun &tr : runs) {
+        if (!tr.done) tr.t_done = total;
+        tr.res.optimal_depth = tr.optimal_depth;
+        if (tr.optimal_depth == 0) tr.res.total_solutions = tr.sols.size();
+        tr.res.gpu_ms_expand = e->ms_expand;
+        tr.res.gpu_ms_suffix = e->ms_suffix;
+        tr.res.gpu_ms_insert = e->ms_insert;
+        tr.res.kernel_launches = e->launches;
+        tr.res.insert_launches = e->insert_launches;
+        tr.res.suffix_launches = e->suffix_launches;
+        tr.res.insert_children = e->insert_children;
+        tr.res.h2d_bytes = e->h2d;
+        tr.res.d2h_bytes = e->d2h;
+        tr.res.seconds = tr.t_done;
+    }
     return PCAGB_OK;
 }
 
@@ -756,25 +847,89 @@ int engine_init(pcagb_engine *e, int device, size_t budget)
     CK(cudaMalloc(&e->d_vc_uop, gt.vc_uop.size() * 4));
     CK(cudaMalloc(&e->d_vc_first, first.size() * 2));
     CK(cudaMalloc(&e->d_chunks, gt.chunks.size() * 4));
-    CK(cudaMemcpy(e->d_chunks, gt.chunks.data(), gt.chunks.size() * 4, cudaMemcpyHostToDevice));
-    CK(cudaMemcpyToSymbol(c_chunk_off, gt.chunk_off.data(), 129 * 4));
-    {
-        const uint32_t *ck = e->d_chunks;
-        CK(cudaMemcpyToSymbol(c_chunks, &ck, sizeof ck));
-    }
     CK(cudaMalloc(&e->d_small, 256 * sizeof(unsigned long long)));
     CK(cudaMalloc(&e->d_status, 16));
     CK(cudaMalloc(&e->d_sol, e->sol_cap * sizeof(ulonglong2)));
-    CK(cudaMemcpy(e->d_cand_uop, gt.cand_uop.data(), gt.cand_uop.size() * 4, cudaMemcpyHostToDevice));
+    CK(cudaMalloc(&e->d_task_T, kMaxBatch * 4));
+    CK(cudaMalloc(&e->d_task_target, (size_t)kMaxBatch * 32 * 4));
+    CK(cudaMalloc(&e->d_task_active, kMaxBatch));
+    CK(cudaMalloc(&e->d_hist, (size_t)kMaxBatch * 128 * sizeof(unsigned long long)));
+    CK(cudaMemcpy(e->d_cand_uop, gt.cand_uop.data(), gt.cand_uop.size() * 4,
+                  cudaMemcpyHostToDevice));
     CK(cudaMemcpy(e->d_vc_uop, gt.vc_uop.data(), gt.vc_uop.size() * 4, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(e->d_vc_first, first.data(), first.size() * 2, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(e->d_chunks, gt.chunks.data(), gt.chunks.size() * 4, cudaMemcpyHostToDevice));
     CK(cudaMemcpyToSymbol(c_cand_off, gt.cand_off.data(), 129 * 4));
     CK(cudaMemcpyToSymbol(c_vc_off, gt.vc_off.data(), 129 * 4));
-    const uint32_t *cu = e->d_cand_uop, *vu = e->d_vc_uop;
+    CK(cudaMemcpyToSymbol(c_chunk_off, gt.chunk_off.data(), 129 * 4));
+    const uint32_t *cu = e->d_cand_uop, *vu = e->d_vc_uop, *ck = e->d_chunks;
     const uint16_t *vf = e->d_vc_first;
     CK(cudaMemcpyToSymbol(c_cand_uop, &cu, sizeof cu));
     CK(cudaMemcpyToSymbol(c_vc_uop, &vu, sizeof vu));
     CK(cudaMemcpyToSymbol(c_vc_first, &vf, sizeof vf));
+    CK(cudaMemcpyToSymbol(c_chunks, &ck, sizeof ck));
+    return PCAGB_OK;
+}
+
+bool make_run(const task_spec_t *task, const pcagb_opts_t &o, TaskRun *tr)
+{
+    search_ctx_t ctx;
+    if (search_ctx_init(&ctx, task) != 0 || task->num_tests < 1) {
+        set_err("task needs 1..32 tests, one output and at most 7 inputs");
+        return false;
+    }
+    if (o.max_depth < 0 || o.max_depth > 12 || task->num_inputs + o.max_depth + 2 > 16) {
+        set_err("max_depth %d out of range (program length is limited to 16)", o.max_depth);
+        return false;
+    }
+    search_state_init_root(&ctx, &tr->root);
+    tr->T = task->num_tests;
+    for (int t = 0; t < tr->T; t++) tr->target[t] = task->tests[t].out[0];
+    tr->max_depth = o.max_depth;
+    tr->min_depth = o.min_depth;
+    return true;
+}
+
+/* Write a task's solutions (full programs, VM re-checked) to the caller. */
+int emit_solutions(const task_spec_t *task, const pcagb_opts_t &o, TaskRun &tr,
+                   uint16_t *sol_progs, int *sol_lens, int sol_cap)
+{
+    std::vector<RawSol> &sols = tr.sols;
+    /* The reference applies its pruner to the last level too: among solving
+       programs with equal final regs+flags only the DFS-first is printed. */
+    if (o.oep_mode == PCAGB_OEP_EXACT && !o.count_levels && tr.optimal_depth > 0 &&
+        !o.first_only) {
+        std::vector<RawSol> kept;
+        std::vector<std::vector<uint8_t>> seen;
+        std::vector<uint8_t> key;
+        for (RawSol &s : sols) {
+            leaf_key(task, tr.root, s.kernel, &key);
+            if (std::find(seen.begin(), seen.end(), key) != seen.end()) continue;
+            seen.push_back(key);
+            kept.push_back(s);
+        }
+        sols.swap(kept);
+        tr.res.total_solutions = sols.size();
+    }
+    int stored = 0;
+    for (const RawSol &s : sols) {
+        if (stored >= sol_cap || !sol_progs) break;
+        uint16_t prog[16] = {0};
+        int n = 0;
+        for (int i = 0; i < task->num_inputs; i++)
+            prog[n++] = PCA_ENC_I(PCA_OP_IN, i + 1, task->input_ports[i]);
+        for (uint16_t insn : s.kernel) prog[n++] = insn;
+        prog[n++] = PCA_ENC_I(PCA_OP_OUT, s.out_reg, task->output_ports[0]);
+        prog[n++] = PCA_ENC_R(PCA_OP_HLT, 0, 0, 0);
+        if (task_evaluate(task, prog, n) != task->num_tests) {
+            set_err("internal: a GPU solution failed the VM re-check");
+            return PCAGB_ELIMIT;
+        }
+        memcpy(sol_progs + (size_t)stored * 16, prog, sizeof prog);
+        if (sol_lens) sol_lens[stored] = n;
+        stored++;
+    }
+    tr.res.stored = stored;
     return PCAGB_OK;
 }
 
@@ -829,6 +984,10 @@ void pcagb_engine_destroy(pcagb_engine_t *e)
     cudaFree(e->d_small);
     cudaFree(e->d_status);
     cudaFree(e->d_sol);
+    cudaFree(e->d_task_T);
+    cudaFree(e->d_task_target);
+    cudaFree(e->d_task_active);
+    cudaFree(e->d_hist);
     for (cudaEvent_t ev : {e->ev0, e->ev1, e->ev2, e->ev3})
         if (ev) cudaEventDestroy(ev);
     if (e->stream) cudaStreamDestroy(e->stream);
@@ -837,69 +996,38 @@ void pcagb_engine_destroy(pcagb_engine_t *e)
 
 void *pcagb_engine_stream(pcagb_engine_t *e) { return e ? (void *)e->stream : nullptr; }
 
-int pcagb_solve(pcagb_engine_t *e, const task_spec_t *task, const pcagb_opts_t *opts,
-                pcagb_result_t *res, uint16_t *sol_progs, int *sol_lens, int sol_cap)
+int pcagb_solve_batch(pcagb_engine_t *e, const task_spec_t *tasks, int ntasks,
+                      const pcagb_opts_t *opts, pcagb_result_t *results, uint16_t *sol_progs,
+                      int *sol_lens, int sol_cap_per_task)
 {
     pcagb_opts_t o;
     if (opts) o = *opts;
     else pcagb_default_opts(&o);
-    search_ctx_t ctx;
-    if (!e || !task || !res) { set_err("null argument"); return PCAGB_EINVAL; }
-    if (search_ctx_init(&ctx, task) != 0 || task->num_tests < 1) {
-        set_err("task needs 1..32 tests, one output and at most 7 inputs");
-        return PCAGB_EINVAL;
-    }
-    if (o.max_depth < 0 || o.max_depth > 12 || task->num_inputs + o.max_depth + 2 > 16) {
-        set_err("max_depth %d out of range (program length is limited to 16)", o.max_depth);
-        return PCAGB_EINVAL;
-    }
+    if (!e || !tasks || !results || ntasks < 1) { set_err("null argument"); return PCAGB_EINVAL; }
+    if (ntasks > kMaxBatch) { set_err("at most %d tasks per batch", kMaxBatch); return PCAGB_EINVAL; }
     if (o.oep_mode < PCAGB_OEP_NONE || o.oep_mode > PCAGB_OEP_EXACT_LIVE) {
         set_err("bad oep_mode %d", o.oep_mode);
         return PCAGB_EINVAL;
     }
-    RunSpec rs;
-    search_state_init_root(&ctx, &rs.root);
-    rs.T = task->num_tests;
-    for (int t = 0; t < rs.T; t++) rs.target[t] = task->tests[t].out[0];
-    std::vector<RawSol> sols;
-    int rc = run_iddfs(e, rs, o, res, &sols);
+    std::vector<TaskRun> runs(ntasks);
+    for (int i = 0; i < ntasks; i++)
+        if (!make_run(&tasks[i], o, &runs[i])) return PCAGB_EINVAL;
+    int rc = run_batch(e, runs, o);
     if (rc) return rc;
-    /* The reference applies its pruner to the last level too: among solving
-       programs with equal final regs+flags only the DFS-first is printed. */
-    if (o.oep_mode == PCAGB_OEP_EXACT && !o.count_levels && res->optimal_depth > 0 &&
-        !o.first_only) {
-        std::vector<RawSol> kept;
-        std::vector<std::vector<uint8_t>> seen;
-        std::vector<uint8_t> key;
-        for (RawSol &s : sols) {
-            leaf_key(task, rs.root, s.kernel, &key);
-            if (std::find(seen.begin(), seen.end(), key) != seen.end()) continue;
-            seen.push_back(key);
-            kept.push_back(s);
-        }
-        sols.swap(kept);
-        res->total_solutions = sols.size();
+    for (int i = 0; i < ntasks; i++) {
+        uint16_t *p = sol_progs ? sol_progs + (size_t)i * sol_cap_per_task * 16 : nullptr;
+        int *l = sol_lens ? sol_lens + (size_t)i * sol_cap_per_task : nullptr;
+        rc = emit_solutions(&tasks[i], o, runs[i], p, l, sol_cap_per_task);
+        if (rc) return rc;
+        results[i] = runs[i].res;
     }
-    int stored = 0;
-    for (const RawSol &s : sols) {
-        if (stored >= sol_cap || !sol_progs) break;
-        uint16_t prog[16] = {0};
-        int n = 0;
-        for (int i = 0; i < task->num_inputs; i++)
-            prog[n++] = PCA_ENC_I(PCA_OP_IN, i + 1, task->input_ports[i]);
-        for (uint16_t insn : s.kernel) prog[n++] = insn;
-        prog[n++] = PCA_ENC_I(PCA_OP_OUT, s.out_reg, task->output_ports[0]);
-        prog[n++] = PCA_ENC_R(PCA_OP_HLT, 0, 0, 0);
-        if (task_evaluate(task, prog, n) != task->num_tests) {
-            set_err("internal: a GPU solution failed the VM re-check");
-            return PCAGB_ELIMIT;
-        }
-        memcpy(sol_progs + (size_t)stored * 16, prog, sizeof prog);
-        if (sol_lens) sol_lens[stored] = n;
-        stored++;
-    }
-    res->stored = stored;
     return PCAGB_OK;
+}
+
+int pcagb_solve(pcagb_engine_t *e, const task_spec_t *task, const pcagb_opts_t *opts,
+                pcagb_result_t *res, uint16_t *sol_progs, int *sol_lens, int sol_cap)
+{
+    return pcagb_solve_batch(e, task, 1, opts, res, sol_progs, sol_lens, sol_cap);
 }
 
 int pcagb_complete(pcagb_engine_t *e, const search_ctx_t *ctx, const search_state_t *start,
@@ -911,16 +1039,17 @@ int pcagb_complete(pcagb_engine_t *e, const search_ctx_t *ctx, const search_stat
     if (states_explored) *states_explored = 0;
     int max_r = max_depth - (int)start->depth;
     if (max_r > SEARCH_MAX_DEPTH) max_r = SEARCH_MAX_DEPTH;
-    RunSpec rs;
-    rs.root = *start;
-    rs.T = ctx->num_tests;
-    if (rs.T < 1 || rs.T > MAX_TESTS) { set_err("bad test count"); return PCAGB_EINVAL; }
-    for (int t = 0; t < rs.T; t++) rs.target[t] = ctx->task.tests[t].out[0];
+    std::vector<TaskRun> runs(1);
+    TaskRun &tr = runs[0];
+    tr.root = *start;
+    tr.T = ctx->num_tests;
+    if (tr.T < 1 || tr.T > MAX_TESTS) { set_err("bad test count"); return PCAGB_EINVAL; }
+    for (int t = 0; t < tr.T; t++) tr.target[t] = ctx->task.tests[t].out[0];
     /* depth 0: the start state already solves */
     for (uint32_t r = 1; r < 8; r++) {
         if (!((start->live >> r) & 1u)) continue;
         bool ok = true;
-        for (int t = 0; t < rs.T && ok; t++) ok = start->regs[t][r] == rs.target[t];
+        for (int t = 0; t < tr.T && ok; t++) ok = start->regs[t][r] == tr.target[t];
         if (ok) return 1;
     }
     if (max_r <= 0) return 0;
@@ -929,15 +1058,15 @@ int pcagb_complete(pcagb_engine_t *e, const search_ctx_t *ctx, const search_stat
     o.min_depth = 1;
     o.max_depth = max_r;
     o.first_only = 1;
-    pcagb_result_t res;
-    std::vector<RawSol> sols;
-    int rc = run_iddfs(e, rs, o, &res, &sols);
+    tr.max_depth = max_r;
+    tr.min_depth = 1;
+    int rc = run_batch(e, runs, o);
     if (rc) return rc;
     uint64_t explored = 0;
-    for (int k = 0; k < PCAGB_MAXD; k++) explored += res.candidates[k];
+    for (int k = 0; k < PCAGB_MAXD; k++) explored += tr.res.candidates[k];
     if (states_explored) *states_explored = explored;
-    if (res.optimal_depth < 0 || sols.empty()) return 0;
-    const RawSol &s = sols.front();
+    if (tr.optimal_depth < 0 || tr.sols.empty()) return 0;
+    const RawSol &s = tr.sols.front();
     for (size_t i = 0; i < s.kernel.size(); i++) solution_insns[i] = s.kernel[i];
     *solution_len = (int)s.kernel.size();
     return 1;

@@ -60,16 +60,21 @@ __constant__ const uint16_t *c_vc_first;   /* first candidate index per class */
 __constant__ uint32_t c_chunk_off[129];    /* op-uniform runs of candidates */
 __constant__ const uint32_t *c_chunks;
 
+/* Per-task parameters of a batch: device arrays indexed by task id. A
+   state's task id travels with it through the levels; states of different
+   tasks never compare equal. */
 struct TaskDev {
-    int T;          /* tests */
-    int key_live;   /* OEP key includes live */
-    uint32_t target[32];
+    const int32_t *T;          /* tests of each task */
+    const uint32_t *target;    /* [task][32] expected outputs */
+    const uint8_t *active;     /* task still searched at the current depth */
+    int key_live;              /* OEP key includes live */
 };
 
 struct LevelDev {
     const uint16_t *regs;   /* [n][8][TP] */
     const uint8_t *flags;   /* [n][TP] */
     const uint8_t *live;    /* [n] */
+    const uint16_t *task;   /* [n] */
     const uint64_t *child_off; /* [n+1] */
     uint64_t n;
 };
@@ -78,6 +83,7 @@ struct LevelOut {
     uint16_t *regs;
     uint8_t *flags;
     uint8_t *live;
+    uint16_t *task;
     uint32_t *parent;
     uint16_t *cidx;
 };
@@ -109,6 +115,11 @@ __device__ __forceinline__ uint64_t col_final(uint32_t r, uint64_t h)
 __device__ __forceinline__ uint64_t live_final(uint32_t live)
 {
     return fmix64(0x5851F42D4C957F2Dull ^ live);
+}
+
+__device__ __forceinline__ uint64_t task_final(uint32_t task)
+{
+    return fmix64(0x9E3779B97F4A7C15ull * (task + 1));
 }
 
 template <int TPC>
@@ -246,14 +257,16 @@ __device__ __forceinline__ void child_hashes_any(uint32_t op, const WarpState<TP
    the flags) and __all_sync decides. All lanes must call it. */
 template <int TPC>
 __device__ bool warp_child_equal(const LevelDev &P, const TaskDev &task, const WarpState<TPC> &A,
-                                 uint32_t liveA, uint32_t uA, uint64_t qB, uint32_t cB, int lane)
+                                 uint32_t tid, int T, uint32_t liveA, uint32_t uA, uint64_t qB,
+                                 uint32_t cB, int lane)
 {
+    if (P.task[qB] != tid) return false;
     const uint32_t liveB = P.live[qB];
     const uint32_t uB = c_cand_uop[c_cand_off[(liveB >> 1) & 127u] + cB];
     const uint32_t rdA = UOP_RD(uA), rdB = UOP_RD(uB);
     if (task.key_live && ((liveA | (1u << rdA)) != (liveB | (1u << rdB)))) return false;
     bool ok = true;
-    if (lane < task.T) {
+    if (lane < T) {
         const uint16_t *RB = P.regs + qB * 8 * TPC + lane;
         const uint32_t a1 = A.R[UOP_A(uA)][lane], b1 = A.R[UOP_B(uA)][lane];
         const uint32_t resA = pca_alu(UOP_OP(uA), a1, b1, UOP_IMM(uA));
@@ -283,13 +296,16 @@ k_expand_insert(LevelDev P, TaskDev task, unsigned long long *table, uint64_t tm
     WarpState<TPC> &ws = sws[wib];
     const uint64_t nw = (uint64_t)gridDim.x * kWarpsPerBlock;
     for (uint64_t q = (uint64_t)blockIdx.x * kWarpsPerBlock + wib; q < P.n; q += nw) {
+        const uint32_t tid = P.task[q];
+        if (!task.active[tid]) continue;
+        const int T = task.T[tid];
         __syncwarp();
         load_state<TPC>(ws, P.regs, P.flags, q, lane);
         const uint32_t live = P.live[q];
         __syncwarp();
         if (lane >= 1 && lane < 8) ws.colh[lane] = col_final(lane, hash_column<TPC>(ws.R[lane]));
         __syncwarp();
-        uint64_t regsum = 0;
+        uint64_t regsum = task_final(tid);
 #pragma unroll
         for (int r = 1; r < 8; r++) regsum += ws.colh[r];
         const uint32_t m = (live >> 1) & 127u;
@@ -301,7 +317,7 @@ k_expand_insert(LevelDev P, TaskDev task, unsigned long long *table, uint64_t tm
             const uint32_t u = c_cand_uop[base + c];
             const uint32_t op = UOP_OP(u), rd = UOP_RD(u);
             uint64_t h, hf;
-            child_hashes_any<TPC>(op, ws, UOP_A(u), UOP_B(u), UOP_IMM(u), task.T, h, hf);
+            child_hashes_any<TPC>(op, ws, UOP_A(u), UOP_B(u), UOP_IMM(u), T, h, hf);
             uint64_t H = regsum - ws.colh[rd] + col_final(rd, h) + hf;
             if (task.key_live) H += live_final(live | (1u << rd));
             const uint64_t ref = (q << 12) | c;
@@ -331,8 +347,8 @@ k_expand_insert(LevelDev P, TaskDev task, unsigned long long *table, uint64_t tm
                     const uint32_t uj = __shfl_sync(0xFFFFFFFFu, u, j);
                     const unsigned long long sj = __shfl_sync(0xFFFFFFFFu, s, j);
                     const uint64_t oref = (sj & kRefMask) - 1;
-                    const bool e = warp_child_equal<TPC>(P, task, ws, live, uj, oref >> 12,
-                                                         (uint32_t)(oref & 4095), lane);
+                    const bool e = warp_child_equal<TPC>(P, task, ws, tid, T, live, uj,
+                                                         oref >> 12, (uint32_t)(oref & 4095), lane);
                     if (lane == j) eq = e;
                 }
                 if (!done) {
@@ -397,13 +413,15 @@ __global__ void k_popc(const uint32_t *bitmap, uint64_t words, uint64_t *cnt)
         cnt[w] = __popc(bitmap[w]);
 }
 
-/* child_off[i] = number of candidates of state i (scanned afterwards). */
-__global__ void k_child_counts(const uint8_t *live, uint64_t n, uint64_t *cnt)
+/* child_off[i] = number of candidates of state i, 0 when its task is not
+   searched any more (scanned afterwards). */
+__global__ void k_child_counts(const uint8_t *live, const uint16_t *task, const uint8_t *active,
+                               uint64_t n, uint64_t *cnt)
 {
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (uint64_t)gridDim.x * blockDim.x) {
         uint32_t m = (live[i] >> 1) & 127u;
-        cnt[i] = c_cand_off[m + 1] - c_cand_off[m];
+        cnt[i] = active[task[i]] ? c_cand_off[m + 1] - c_cand_off[m] : 0;
     }
 }
 
@@ -418,6 +436,10 @@ k_materialize(LevelDev P, TaskDev task, const uint32_t *bitmap, const uint64_t *
     WarpState<TPC> &ws = sws[wib];
     const uint64_t nw = (uint64_t)gridDim.x * kWarpsPerBlock;
     for (uint64_t q = (uint64_t)blockIdx.x * kWarpsPerBlock + wib; q < P.n; q += nw) {
+        const uint32_t tid = P.task[q];
+        if (!task.active[tid]) continue;
+        const int T = task.T[tid];
+        __syncwarp();
         load_state<TPC>(ws, P.regs, P.flags, q, lane);
         const uint32_t live = P.live[q];
         __syncwarp();
@@ -445,7 +467,7 @@ k_materialize(LevelDev P, TaskDev task, const uint32_t *bitmap, const uint64_t *
                     uint32_t a = ws.R[UOP_A(u)][lane], b = ws.R[UOP_B(u)][lane];
                     uint32_t res = pca_alu(op, a, b, UOP_IMM(u));
                     uint32_t f = pca_alu_flags(op, a, b, UOP_IMM(u), res, ws.F[lane]);
-                    if (lane >= task.T) { res = 0; f = 0; }
+                    if (lane >= T) { res = 0; f = 0; }
                     uint16_t *dst = C.regs + rank * 8 * TPC + lane;
 #pragma unroll
                     for (uint32_t r = 0; r < 8; r++)
@@ -454,26 +476,30 @@ k_materialize(LevelDev P, TaskDev task, const uint32_t *bitmap, const uint64_t *
                 }
                 if (lane == 0) {
                     C.live[rank] = (uint8_t)(live | (1u << rd));
+                    C.task[rank] = (uint16_t)tid;
                     C.parent[rank] = (uint32_t)q;
                     C.cidx[rank] = (uint16_t)cj;
                 }
             }
         }
-        __syncwarp();
     }
 }
 
-__global__ void k_live_hist(const uint8_t *live, uint64_t n, unsigned long long *hist)
+/* hist[task][mask] += states of that task with that liveness mask. Lanes
+   with the same key are counted by one atomic (states of a level are
+   grouped by task and mostly by mask). */
+__global__ void k_task_hist(const uint8_t *live, const uint16_t *task, uint64_t n,
+                            unsigned long long *hist)
 {
-    __shared__ unsigned int sh[128];
-    for (int i = threadIdx.x; i < 128; i += blockDim.x) sh[i] = 0;
-    __syncthreads();
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-         i += (uint64_t)gridDim.x * blockDim.x)
-        atomicAdd(&sh[(live[i] >> 1) & 127u], 1u);
-    __syncthreads();
-    for (int i = threadIdx.x; i < 128; i += blockDim.x)
-        if (sh[i]) atomicAdd(&hist[i], (unsigned long long)sh[i]);
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    const uint64_t n_round = (n + 31) & ~31ull;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_round; i += stride) {
+        const bool valid = i < n;
+        const uint32_t key = valid ? (uint32_t)task[i] * 128u + ((live[i] >> 1) & 127u) : ~0u;
+        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, key);
+        if (valid && (threadIdx.x & 31) == __ffs(peers) - 1)
+            atomicAdd(&hist[key], (unsigned long long)__popc(peers));
+    }
 }
 
 /* ---- solutions ----------------------------------------------------------- */
@@ -504,12 +530,15 @@ __global__ void k_leaf(LevelDev P, TaskDev task, SolBuf S)
 {
     const int lane = threadIdx.x & 31;
     const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-    const uint32_t tgt = lane < task.T ? task.target[lane] : 0u;
     for (uint64_t q = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < P.n; q += nw) {
+        const uint32_t tid = P.task[q];
+        if (!task.active[tid]) continue;
+        const int T = task.T[tid];
+        const uint32_t tgt = lane < T ? task.target[tid * 32 + lane] : 0u;
         const uint32_t live = P.live[q];
         for (uint32_t r = 1; r < 8; r++) {
             if (!((live >> r) & 1u)) continue;
-            bool ok = lane >= task.T || P.regs[q * 8 * TPC + r * TPC + lane] == tgt;
+            bool ok = lane >= T || P.regs[q * 8 * TPC + r * TPC + lane] == tgt;
             if (__all_sync(0xFFFFFFFFu, ok) && lane == 0) record_solution(S, q, 0, 0, r, r);
         }
     }
@@ -519,7 +548,7 @@ __global__ void k_leaf(LevelDev P, TaskDev task, SolBuf S)
  * registers remapped: a register equal to rd2 reads spare column 9, else a
  * register equal to rd1 reads column 8 (rd = 8 means "none"). */
 template <int TPC>
-__device__ __forceinline__ void scan_last(const WarpState<TPC> &ws, const TaskDev &task,
+__device__ __forceinline__ void scan_last(const WarpState<TPC> &ws, int T,
                                           uint32_t m, uint32_t rd1, uint32_t rd2, uint32_t tgt,
                                           uint32_t tgt0, uint32_t tgt1, int lane,
                                           const SolBuf &S, uint64_t q, uint32_t m1, uint32_t m2)
@@ -537,7 +566,7 @@ __device__ __forceinline__ void scan_last(const WarpState<TPC> &ws, const TaskDe
             rb = rb == rd2 ? 9u : rb == rd1 ? 8u : rb;
             const uint32_t op = UOP_OP(u), imm = UOP_IMM(u);
             pass = pca_alu(op, ws.R[ra][0], ws.R[rb][0], imm) == tgt0 &&
-                   (task.T < 2 || pca_alu(op, ws.R[ra][1], ws.R[rb][1], imm) == tgt1);
+                   (T < 2 || pca_alu(op, ws.R[ra][1], ws.R[rb][1], imm) == tgt1);
         }
         uint32_t bal = __ballot_sync(0xFFFFFFFFu, pass);
         while (bal) {
@@ -548,16 +577,16 @@ __device__ __forceinline__ void scan_last(const WarpState<TPC> &ws, const TaskDe
             ra = ra == rd2 ? 9u : ra == rd1 ? 8u : ra;
             rb = rb == rd2 ? 9u : rb == rd1 ? 8u : rb;
             bool ok = true;
-            if (lane < task.T) ok = pca_alu(UOP_OP(uj), ws.R[ra][lane], ws.R[rb][lane], UOP_IMM(uj)) == tgt;
+            if (lane < T) ok = pca_alu(UOP_OP(uj), ws.R[ra][lane], ws.R[rb][lane], UOP_IMM(uj)) == tgt;
             if (__all_sync(0xFFFFFFFFu, ok) && lane == 0)
                 record_solution(S, q, m1, m2, b0 + j, c_vc_first[vbase + b0 + j]);
         }
     }
 }
 
-/* Suffix enumeration of depth SD (1..3) from every state of level P.
- * Work item = (prefix, chunk of first-suffix candidates); for SD = 1 the
- * chunk is the whole prefix. */
+/* Suffix enumeration of depth SD (1..3) from every state of level P whose
+ * task is active. Work item = (prefix, chunk of first-suffix candidates);
+ * for SD = 1 the chunk is the whole prefix. */
 template <int TPC, int SD>
 __global__ void __launch_bounds__(kThreads)
 k_suffix(LevelDev P, TaskDev task, SolBuf S, uint32_t chunks_per_prefix, uint32_t chunk)
@@ -565,14 +594,23 @@ k_suffix(LevelDev P, TaskDev task, SolBuf S, uint32_t chunks_per_prefix, uint32_
     __shared__ WarpState<TPC> sws[kWarpsPerBlock];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     WarpState<TPC> &ws = sws[wib];
-    const uint32_t tgt = lane < task.T ? task.target[lane] : 0u;
-    const uint32_t tgt0 = task.target[0], tgt1 = task.target[1];
     const uint64_t nw = (uint64_t)gridDim.x * kWarpsPerBlock;
     const uint64_t items = P.n * chunks_per_prefix;
     uint64_t loaded = ~0ull;
+    uint32_t cur_task = ~0u, tgt = 0, tgt0 = 0, tgt1 = 0;
+    int T = 0;
     for (uint64_t it = (uint64_t)blockIdx.x * kWarpsPerBlock + wib; it < items; it += nw) {
         const uint64_t q = it / chunks_per_prefix;
         const uint32_t ck = (uint32_t)(it - q * chunks_per_prefix);
+        const uint32_t tid = P.task[q];
+        if (!task.active[tid]) continue;
+        if (tid != cur_task) {
+            cur_task = tid;
+            T = task.T[tid];
+            tgt = lane < T ? task.target[tid * 32 + lane] : 0u;
+            tgt0 = task.target[tid * 32];
+            tgt1 = task.target[tid * 32 + 1];
+        }
         const uint32_t live = P.live[q];
         if (q != loaded) {
             __syncwarp();
@@ -582,7 +620,7 @@ k_suffix(LevelDev P, TaskDev task, SolBuf S, uint32_t chunks_per_prefix, uint32_
         }
         const uint32_t m0 = (live >> 1) & 127u;
         if (SD == 1) {
-            scan_last<TPC>(ws, task, m0, 8, 8, tgt, tgt0, tgt1, lane, S, q, 0, 0);
+            scan_last<TPC>(ws, T, m0, 8, 8, tgt, tgt0, tgt1, lane, S, q, 0, 0);
             continue;
         }
         const uint32_t cb0 = c_cand_off[m0], nc0 = c_cand_off[m0 + 1] - cb0;
@@ -592,13 +630,13 @@ k_suffix(LevelDev P, TaskDev task, SolBuf S, uint32_t chunks_per_prefix, uint32_
             const uint32_t rd1 = UOP_RD(u1);
             __syncwarp();
             if (lane < TPC)
-                ws.R[8][lane] = lane < task.T ? pca_alu(UOP_OP(u1), ws.R[UOP_A(u1)][lane],
-                                                        ws.R[UOP_B(u1)][lane], UOP_IMM(u1))
-                                              : 0u;
+                ws.R[8][lane] = lane < T ? pca_alu(UOP_OP(u1), ws.R[UOP_A(u1)][lane],
+                                                   ws.R[UOP_B(u1)][lane], UOP_IMM(u1))
+                                         : 0u;
             __syncwarp();
             const uint32_t m1 = (m0 | (1u << (rd1 - 1))) & 127u;
             if (SD == 2) {
-                scan_last<TPC>(ws, task, m1, rd1, 8, tgt, tgt0, tgt1, lane, S, q, i1, 0);
+                scan_last<TPC>(ws, T, m1, rd1, 8, tgt, tgt0, tgt1, lane, S, q, i1, 0);
                 continue;
             }
             const uint32_t cb1 = c_cand_off[m1], nc1 = c_cand_off[m1 + 1] - cb1;
@@ -610,13 +648,13 @@ k_suffix(LevelDev P, TaskDev task, SolBuf S, uint32_t chunks_per_prefix, uint32_
                 rb = rb == rd1 ? 8u : rb;
                 __syncwarp();
                 if (lane < TPC)
-                    ws.R[9][lane] = lane < task.T ? pca_alu(UOP_OP(u2), ws.R[ra][lane],
-                                                            ws.R[rb][lane], UOP_IMM(u2))
-                                                  : 0u;
+                    ws.R[9][lane] = lane < T ? pca_alu(UOP_OP(u2), ws.R[ra][lane],
+                                                       ws.R[rb][lane], UOP_IMM(u2))
+                                             : 0u;
                 __syncwarp();
                 const uint32_t m2 = (m1 | (1u << (rd2 - 1))) & 127u;
-                scan_last<TPC>(ws, task, m2, rd2 == rd1 ? 8u : rd1, rd2, tgt, tgt0, tgt1, lane,
-                               S, q, i1, i2);
+                scan_last<TPC>(ws, T, m2, rd2 == rd1 ? 8u : rd1, rd2, tgt, tgt0, tgt1, lane, S,
+                               q, i1, i2);
             }
         }
     }

@@ -100,7 +100,8 @@ EXPORTS = [
     "search_state_serialize", "search_gen_candidates_branchless",
     "search_exhaustive_complete", "search_exhaustive_states_explored", "search_state_dump",
     "pcagb_last_error", "pcagb_default_opts", "pcagb_engine_create", "pcagb_engine_destroy",
-    "pcagb_solve", "pcagb_complete", "pcagb_num_candidates", "pcagb_engine_stream",
+    "pcagb_solve", "pcagb_solve_batch", "pcagb_complete", "pcagb_num_candidates",
+    "pcagb_engine_stream",
     "pcagb_solve_small_noalloc", "pcagb_noalloc_last_error",
 ]
 
@@ -132,6 +133,9 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
         "pcagb_engine_destroy": ([ctypes.c_void_p], None),
         "pcagb_solve": ([ctypes.c_void_p, P(TaskSpec), P(SolveOpts), P(SolveResult),
                          P(ctypes.c_uint16), P(ctypes.c_int), ctypes.c_int], ctypes.c_int),
+        "pcagb_solve_batch": ([ctypes.c_void_p, P(TaskSpec), ctypes.c_int, P(SolveOpts),
+                               P(SolveResult), P(ctypes.c_uint16), P(ctypes.c_int), ctypes.c_int],
+                              ctypes.c_int),
         "pcagb_complete": ([ctypes.c_void_p, P(SearchCtx), P(SearchState), ctypes.c_int,
                             P(ctypes.c_uint16), P(ctypes.c_int), P(ctypes.c_uint64)], ctypes.c_int),
         "pcagb_num_candidates": ([ctypes.c_uint8], ctypes.c_int),
@@ -314,6 +318,42 @@ class Engine:
             arr = getattr(r, name)
             setattr(sol, name, [arr[k] for k in range(min(last + 1, MAXD))])
         return sol
+
+    def solve_batch(self, tasks, max_depth=4, oep_mode=OEP_EXACT_LIVE, split_depth=-1,
+                    count_levels=False, sol_cap=64):
+        """Solve many tasks in shared launches; returns one Solution per task
+        (its `seconds` is that task's time-to-proven-optimal in the batch)."""
+        n = len(tasks)
+        arr = (TaskSpec * n)(*tasks)
+        o = SolveOpts()
+        self.lib.pcagb_default_opts(ctypes.byref(o))
+        o.max_depth, o.split_depth, o.oep_mode = max_depth, split_depth, oep_mode
+        o.count_levels = int(count_levels)
+        res = (SolveResult * n)()
+        cap = max(sol_cap, 1)
+        progs = (ctypes.c_uint16 * (16 * cap * n))()
+        lens = (ctypes.c_int * (cap * n))()
+        rc = self.lib.pcagb_solve_batch(self.h, arr, n, ctypes.byref(o), res, progs, lens, cap)
+        if rc != 0:
+            raise EngineError(f"batch solve failed ({rc}): {self.lib.pcagb_last_error().decode()}")
+        out = []
+        for i in range(n):
+            r = res[i]
+            sol = Solution(optimal_depth=r.optimal_depth, total_solutions=r.total_solutions)
+            for name in ("seconds", "gpu_ms_expand", "gpu_ms_suffix", "gpu_ms_insert",
+                         "kernel_launches", "insert_launches", "suffix_launches", "h2d_bytes",
+                         "d2h_bytes", "insert_children", "split_used"):
+                setattr(sol, name, getattr(r, name))
+            base = i * cap
+            for k in range(r.stored):
+                sol.programs.append([progs[(base + k) * 16 + j] for j in range(lens[base + k])])
+            last = r.optimal_depth if r.optimal_depth >= 0 else max_depth
+            for name in ("candidates", "evaluations", "tried", "pruned_cum", "level_children",
+                         "level_survivors"):
+                arr2 = getattr(r, name)
+                setattr(sol, name, [arr2[k] for k in range(min(last + 1, MAXD))])
+            out.append(sol)
+        return out
 
     @property
     def stream(self) -> int:

@@ -232,6 +232,15 @@ int  pcagb_solve_batch(pcagb_engine_t *e, const task_spec_t *tasks, int ntasks,
                        const pcagb_opts_t *opts, pcagb_result_t *results, uint16_t *sol_progs,
                        int *sol_lens, int sol_cap_per_task);
 
+/* The batched solve with early delivery: on_done(i, &results[i], user) is
+ * called on the calling thread as soon as task i is decided (its programs
+ * are already in sol_progs), not at the end of the batch. A server returns
+ * each request's answer from there. */
+typedef void (*pcagb_done_cb)(int task, const pcagb_result_t *result, void *user);
+int  pcagb_solve_batch_cb(pcagb_engine_t *e, const task_spec_t *tasks, int ntasks,
+                          const pcagb_opts_t *opts, pcagb_result_t *results, uint16_t *sol_progs,
+                          int *sol_lens, int sol_cap_per_task, pcagb_done_cb on_done, void *user);
+
 /* IDDFS completion from an arbitrary branchless state (the GPU form of
  * search_exhaustive_complete, src/search_state.c:418-453). Returns 1 found /
  * 0 none / negative error. */
@@ -242,6 +251,10 @@ int  pcagb_complete(pcagb_engine_t *e, const search_ctx_t *ctx, const search_sta
 /* The CUDA stream (cudaStream_t) every kernel of this engine runs on, so a
  * caller can time a solve with events on that stream. */
 void *pcagb_engine_stream(pcagb_engine_t *e);
+
+/* Free and total device memory, for sizing engines (a server admits work by
+ * free HBM). */
+int  pcagb_device_memory(int device, size_t *free_bytes, size_t *total_bytes);
 
 /* Number of generator candidates for a live mask (src/search_state.c:280-330). */
 int  pcagb_num_candidates(uint8_t live);

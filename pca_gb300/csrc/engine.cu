@@ -28,6 +28,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -105,9 +106,6 @@ struct pcagb_engine {
     cudaStream_t stream = nullptr;
     char *arena = nullptr;
     size_t cap = 0, bottom = 0, top = 0;
-    uint32_t *d_cand_uop = nullptr, *d_vc_uop = nullptr;
-    uint16_t *d_vc_first = nullptr;
-    uint32_t *d_chunks = nullptr;
     unsigned long long *d_small = nullptr;   /* [0] sol count [1] first [2] count */
     uint32_t *d_status = nullptr;
     ulonglong2 *d_sol = nullptr;
@@ -544,10 +542,12 @@ std::vector<int> choose_test_order(const TaskRun &tr)
     search_ctx_t ctx;
     memset(&ctx, 0, sizeof ctx);
     ctx.num_tests = (uint8_t)T;
+    /* the root and up to 24 of its children, spread over the op blocks */
     std::vector<search_state_t> sample(1, tr.root);
     uint16_t cands[4096];
     int n = gen_candidates(tr.root.live, cands, 4096);
-    for (int i = 0; i < n; i++) {
+    const int stride = std::max(1, n / 24);
+    for (int i = 0; i < n; i += stride) {
         search_state_t c;
         if (search_state_step(&ctx, &tr.root, cands[i], &c)) sample.push_back(c);
     }
@@ -595,8 +595,13 @@ uint64_t hist_sum(const Level &L, int t, const std::vector<uint64_t> &weight)
     return s;
 }
 
+/* Called once per task as soon as it is decided (proven optimal depth or
+   depth limit reached), before the batch ends. */
+typedef void (*done_fn)(int task, void *user);
+
 /* Core batched IDDFS shared by every solve entry point. */
-int run_batch(pcagb_engine *e, std::vector<TaskRun> &runs, const pcagb_opts_t &o)
+int run_batch(pcagb_engine *e, std::vector<TaskRun> &runs, const pcagb_opts_t &o,
+              done_fn on_done = nullptr, void *user = nullptr)
 {
     const GenTables &gt = gen_tables();
     auto t_start = std::chrono::steady_clock::now();
@@ -696,6 +701,17 @@ int run_batch(pcagb_engine *e, std::vector<TaskRun> &runs, const pcagb_opts_t &o
             tr.t_done = elapsed();
         }
     }
+    std::vector<uint8_t> notified(nt, 0);
+    auto notify = [&](int i) {
+        if (notified[i]) return;
+        notified[i] = 1;
+        TaskRun &tr = runs[i];
+        tr.res.optimal_depth = tr.optimal_depth;
+        tr.res.seconds = tr.t_done;
+        if (on_done) on_done(i, user);
+    };
+    for (int i = 0; i < nt; i++)
+        if (runs[i].done) notify(i);
     std::vector<uint8_t> active(nt, 0);
     std::vector<uint64_t> pruned_cum(nt, 0);
     std::vector<uint64_t> nc_w(128), nvc_w(128), ones(128, 1);
@@ -710,6 +726,7 @@ int run_batch(pcagb_engine *e, std::vector<TaskRun> &runs, const pcagb_opts_t &o
             if (!tr.done && K > tr.max_depth) {
                 tr.done = true;
                 tr.t_done = elapsed();
+                notify(i);
             }
             active[i] = !tr.done;
             nact += active[i];
@@ -781,6 +798,7 @@ int run_batch(pcagb_engine *e, std::vector<TaskRun> &runs, const pcagb_opts_t &o
                 tr.t_done = elapsed();
                 tr.res.total_solutions =
                     s == 0 || (o.first_only && nt == 1) ? tr.nrec : tr.sols.size();
+                notify(i);
             }
         }
     }
@@ -800,6 +818,53 @@ int run_batch(pcagb_engine *e, std::vector<TaskRun> &runs, const pcagb_opts_t &o
         tr.res.d2h_bytes = e->d2h;
         tr.res.seconds = tr.t_done;
     }
+    for (int i = 0; i < nt; i++) notify(i);
+    return PCAGB_OK;
+}
+
+/* The candidate tables are the same for every engine on a device, and the
+   kernels reach them through __constant__ symbols shared by the whole
+   device. They are uploaded once per device and live until the process
+   exits, so destroying one engine never leaves another engine's kernels
+   reading freed memory. */
+std::mutex g_tables_mu;
+bool g_tables_ready[64];
+
+int ensure_device_tables(int device)
+{
+    std::lock_guard<std::mutex> lk(g_tables_mu);
+    if (device < 0 || device >= 64) { set_err("device %d out of range", device); return PCAGB_EINVAL; }
+    if (g_tables_ready[device]) return PCAGB_OK;
+    const GenTables &gt = gen_tables();
+    std::vector<uint16_t> first(gt.vc_uop.size(), 0);
+    for (int m = 0; m < 128; m++) {
+        std::vector<bool> seen(gt.nvc(m), false);
+        for (uint32_t c = 0; c < (uint32_t)gt.nc(m); c++) {
+            uint16_t v = gt.cand_vc[gt.cand_off[m] + c];
+            if (!seen[v]) { seen[v] = true; first[gt.vc_off[m] + v] = (uint16_t)c; }
+        }
+    }
+    uint32_t *cand_uop = nullptr, *vc_uop = nullptr, *chunks = nullptr;
+    uint16_t *vc_first = nullptr;
+    CK(cudaMalloc(&cand_uop, gt.cand_uop.size() * 4));
+    CK(cudaMalloc(&vc_uop, gt.vc_uop.size() * 4));
+    CK(cudaMalloc(&vc_first, first.size() * 2));
+    CK(cudaMalloc(&chunks, gt.chunks.size() * 4));
+    CK(cudaMemcpy(cand_uop, gt.cand_uop.data(), gt.cand_uop.size() * 4, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(vc_uop, gt.vc_uop.data(), gt.vc_uop.size() * 4, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(vc_first, first.data(), first.size() * 2, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(chunks, gt.chunks.data(), gt.chunks.size() * 4, cudaMemcpyHostToDevice));
+    CK(cudaMemcpyToSymbol(c_cand_off, gt.cand_off.data(), 129 * 4));
+    CK(cudaMemcpyToSymbol(c_vc_off, gt.vc_off.data(), 129 * 4));
+    CK(cudaMemcpyToSymbol(c_chunk_off, gt.chunk_off.data(), 129 * 4));
+    const uint32_t *cu = cand_uop, *vu = vc_uop, *ck = chunks;
+    const uint16_t *vf = vc_first;
+    CK(cudaMemcpyToSymbol(c_cand_uop, &cu, sizeof cu));
+    CK(cudaMemcpyToSymbol(c_vc_uop, &vu, sizeof vu));
+    CK(cudaMemcpyToSymbol(c_vc_first, &vf, sizeof vf));
+    CK(cudaMemcpyToSymbol(c_chunks, &ck, sizeof ck));
+    CK(cudaDeviceSynchronize());
+    g_tables_ready[device] = true;
     return PCAGB_OK;
 }
 
@@ -834,19 +899,8 @@ int engine_init(pcagb_engine *e, int device, size_t budget)
     CK(cudaMalloc(&e->arena, budget));
     e->cap = budget;
     e->top = budget;
-    const GenTables &gt = gen_tables();
-    std::vector<uint16_t> first(gt.vc_uop.size(), 0);
-    for (int m = 0; m < 128; m++) {
-        std::vector<bool> seen(gt.nvc(m), false);
-        for (uint32_t c = 0; c < (uint32_t)gt.nc(m); c++) {
-            uint16_t v = gt.cand_vc[gt.cand_off[m] + c];
-            if (!seen[v]) { seen[v] = true; first[gt.vc_off[m] + v] = (uint16_t)c; }
-        }
-    }
-    CK(cudaMalloc(&e->d_cand_uop, gt.cand_uop.size() * 4));
-    CK(cudaMalloc(&e->d_vc_uop, gt.vc_uop.size() * 4));
-    CK(cudaMalloc(&e->d_vc_first, first.size() * 2));
-    CK(cudaMalloc(&e->d_chunks, gt.chunks.size() * 4));
+    int trc = ensure_device_tables(device);
+    if (trc) return trc;
     CK(cudaMalloc(&e->d_small, 256 * sizeof(unsigned long long)));
     CK(cudaMalloc(&e->d_status, 16));
     CK(cudaMalloc(&e->d_sol, e->sol_cap * sizeof(ulonglong2)));
@@ -854,20 +908,6 @@ int engine_init(pcagb_engine *e, int device, size_t budget)
     CK(cudaMalloc(&e->d_task_target, (size_t)kMaxBatch * 32 * 4));
     CK(cudaMalloc(&e->d_task_active, kMaxBatch));
     CK(cudaMalloc(&e->d_hist, (size_t)kMaxBatch * 128 * sizeof(unsigned long long)));
-    CK(cudaMemcpy(e->d_cand_uop, gt.cand_uop.data(), gt.cand_uop.size() * 4,
-                  cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(e->d_vc_uop, gt.vc_uop.data(), gt.vc_uop.size() * 4, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(e->d_vc_first, first.data(), first.size() * 2, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(e->d_chunks, gt.chunks.data(), gt.chunks.size() * 4, cudaMemcpyHostToDevice));
-    CK(cudaMemcpyToSymbol(c_cand_off, gt.cand_off.data(), 129 * 4));
-    CK(cudaMemcpyToSymbol(c_vc_off, gt.vc_off.data(), 129 * 4));
-    CK(cudaMemcpyToSymbol(c_chunk_off, gt.chunk_off.data(), 129 * 4));
-    const uint32_t *cu = e->d_cand_uop, *vu = e->d_vc_uop, *ck = e->d_chunks;
-    const uint16_t *vf = e->d_vc_first;
-    CK(cudaMemcpyToSymbol(c_cand_uop, &cu, sizeof cu));
-    CK(cudaMemcpyToSymbol(c_vc_uop, &vu, sizeof vu));
-    CK(cudaMemcpyToSymbol(c_vc_first, &vf, sizeof vf));
-    CK(cudaMemcpyToSymbol(c_chunks, &ck, sizeof ck));
     return PCAGB_OK;
 }
 
@@ -977,10 +1017,6 @@ void pcagb_engine_destroy(pcagb_engine_t *e)
     cudaSetDevice(e->device);
     if (e->stream) cudaStreamSynchronize(e->stream);
     cudaFree(e->arena);
-    cudaFree(e->d_cand_uop);
-    cudaFree(e->d_vc_uop);
-    cudaFree(e->d_vc_first);
-    cudaFree(e->d_chunks);
     cudaFree(e->d_small);
     cudaFree(e->d_status);
     cudaFree(e->d_sol);
@@ -995,6 +1031,19 @@ void pcagb_engine_destroy(pcagb_engine_t *e)
 }
 
 void *pcagb_engine_stream(pcagb_engine_t *e) { return e ? (void *)e->stream : nullptr; }
+
+int pcagb_device_memory(int device, size_t *free_bytes, size_t *total_bytes)
+{
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) {
+        cudaGetLastError();
+        set_err("no CUDA device %d", device);
+        return PCAGB_ENODEV;
+    }
+    CK(cudaSetDevice(device));
+    CK(cudaMemGetInfo(free_bytes, total_bytes));
+    return PCAGB_OK;
+}
 
 int pcagb_solve_batch(pcagb_engine_t *e, const task_spec_t *tasks, int ntasks,
                       const pcagb_opts_t *opts, pcagb_result_t *results, uint16_t *sol_progs,
@@ -1028,6 +1077,53 @@ int pcagb_solve(pcagb_engine_t *e, const task_spec_t *task, const pcagb_opts_t *
                 pcagb_result_t *res, uint16_t *sol_progs, int *sol_lens, int sol_cap)
 {
     return pcagb_solve_batch(e, task, 1, opts, res, sol_progs, sol_lens, sol_cap);
+}
+
+namespace {
+struct DoneCtx {
+    const task_spec_t *tasks;
+    const pcagb_opts_t *o;
+    std::vector<TaskRun> *runs;
+    pcagb_result_t *results;
+    uint16_t *sol_progs;
+    int *sol_lens;
+    int cap;
+    pcagb_done_cb cb;
+    void *user;
+    int rc;
+};
+
+void deliver(int i, void *p)
+{
+    DoneCtx &c = *(DoneCtx *)p;
+    TaskRun &tr = (*c.runs)[i];
+    uint16_t *sp = c.sol_progs ? c.sol_progs + (size_t)i * c.cap * 16 : nullptr;
+    int *sl = c.sol_lens ? c.sol_lens + (size_t)i * c.cap : nullptr;
+    int rc = emit_solutions(&c.tasks[i], *c.o, tr, sp, sl, c.cap);
+    if (rc && !c.rc) c.rc = rc;
+    c.results[i] = tr.res;
+    if (c.cb) c.cb(i, &c.results[i], c.user);
+}
+}  // namespace
+
+int pcagb_solve_batch_cb(pcagb_engine_t *e, const task_spec_t *tasks, int ntasks,
+                         const pcagb_opts_t *opts, pcagb_result_t *results, uint16_t *sol_progs,
+                         int *sol_lens, int sol_cap_per_task, pcagb_done_cb on_done, void *user)
+{
+    pcagb_opts_t o;
+    if (opts) o = *opts;
+    else pcagb_default_opts(&o);
+    if (!e || !tasks || !results || ntasks < 1) { set_err("null argument"); return PCAGB_EINVAL; }
+    if (ntasks > kMaxBatch) { set_err("at most %d tasks per batch", kMaxBatch); return PCAGB_EINVAL; }
+    std::vector<TaskRun> runs(ntasks);
+    for (int i = 0; i < ntasks; i++)
+        if (!make_run(&tasks[i], o, &runs[i])) return PCAGB_EINVAL;
+    DoneCtx c{tasks, &o, &runs, results, sol_progs, sol_lens, sol_cap_per_task, on_done, user, 0};
+    int rc = run_batch(e, runs, o, deliver, &c);
+    if (rc) return rc;
+    /* the batch totals are known only now */
+    for (int i = 0; i < ntasks; i++) results[i] = runs[i].res;
+    return c.rc;
 }
 
 int pcagb_complete(pcagb_engine_t *e, const search_ctx_t *ctx, const search_state_t *start,

@@ -91,6 +91,8 @@ class SolveResult(ctypes.Structure):
 
 OEP_NONE, OEP_EXACT, OEP_EXACT_LIVE = 0, 1, 2
 
+DONE_CB = ctypes.CFUNCTYPE(None, ctypes.c_int, ctypes.POINTER(SolveResult), ctypes.c_void_p)
+
 # every function declared in include/pca_gb300.h
 EXPORTS = [
     "pca_init", "pca_load", "pca_step", "pca_run", "pca_disasm", "pca_disasm_prog",
@@ -100,8 +102,9 @@ EXPORTS = [
     "search_state_serialize", "search_gen_candidates_branchless",
     "search_exhaustive_complete", "search_exhaustive_states_explored", "search_state_dump",
     "pcagb_last_error", "pcagb_default_opts", "pcagb_engine_create", "pcagb_engine_destroy",
-    "pcagb_solve", "pcagb_solve_batch", "pcagb_complete", "pcagb_num_candidates",
-    "pcagb_engine_stream",
+    "pcagb_solve", "pcagb_solve_batch", "pcagb_solve_batch_cb", "pcagb_complete",
+    "pcagb_num_candidates",
+    "pcagb_engine_stream", "pcagb_device_memory",
     "pcagb_solve_small_noalloc", "pcagb_noalloc_last_error",
 ]
 
@@ -136,10 +139,15 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
         "pcagb_solve_batch": ([ctypes.c_void_p, P(TaskSpec), ctypes.c_int, P(SolveOpts),
                                P(SolveResult), P(ctypes.c_uint16), P(ctypes.c_int), ctypes.c_int],
                               ctypes.c_int),
+        "pcagb_solve_batch_cb": ([ctypes.c_void_p, P(TaskSpec), ctypes.c_int, P(SolveOpts),
+                                  P(SolveResult), P(ctypes.c_uint16), P(ctypes.c_int),
+                                  ctypes.c_int, DONE_CB, ctypes.c_void_p], ctypes.c_int),
         "pcagb_complete": ([ctypes.c_void_p, P(SearchCtx), P(SearchState), ctypes.c_int,
                             P(ctypes.c_uint16), P(ctypes.c_int), P(ctypes.c_uint64)], ctypes.c_int),
         "pcagb_num_candidates": ([ctypes.c_uint8], ctypes.c_int),
         "pcagb_engine_stream": ([ctypes.c_void_p], ctypes.c_void_p),
+        "pcagb_device_memory": ([ctypes.c_int, P(ctypes.c_size_t), P(ctypes.c_size_t)],
+                                ctypes.c_int),
         "pcagb_solve_small_noalloc": ([P(TaskSpec), ctypes.c_int, ctypes.c_void_p,
                                        P(ctypes.c_int), P(ctypes.c_uint64), P(ctypes.c_uint16),
                                        P(ctypes.c_int), ctypes.c_int], ctypes.c_int),
@@ -271,6 +279,16 @@ class EngineError(RuntimeError):
     pass
 
 
+def device_memory(device: int = 0, lib: ctypes.CDLL | None = None):
+    """(free, total) bytes of a CUDA device."""
+    lib = lib or load_library()
+    free, total = ctypes.c_size_t(0), ctypes.c_size_t(0)
+    rc = lib.pcagb_device_memory(device, ctypes.byref(free), ctypes.byref(total))
+    if rc != 0:
+        raise EngineError(lib.pcagb_last_error().decode())
+    return free.value, total.value
+
+
 class Engine:
     """One GPU engine (device buffers in an HBM arena)."""
 
@@ -320,9 +338,10 @@ class Engine:
         return sol
 
     def solve_batch(self, tasks, max_depth=4, oep_mode=OEP_EXACT_LIVE, split_depth=-1,
-                    count_levels=False, sol_cap=64):
+                    count_levels=False, sol_cap=64, on_done=None):
         """Solve many tasks in shared launches; returns one Solution per task
-        (its `seconds` is that task's time-to-proven-optimal in the batch)."""
+        (its `seconds` is that task's time-to-proven-optimal in the batch).
+        on_done(i, Solution), if given, runs as soon as task i is decided."""
         n = len(tasks)
         arr = (TaskSpec * n)(*tasks)
         o = SolveOpts()
@@ -333,12 +352,8 @@ class Engine:
         cap = max(sol_cap, 1)
         progs = (ctypes.c_uint16 * (16 * cap * n))()
         lens = (ctypes.c_int * (cap * n))()
-        rc = self.lib.pcagb_solve_batch(self.h, arr, n, ctypes.byref(o), res, progs, lens, cap)
-        if rc != 0:
-            raise EngineError(f"batch solve failed ({rc}): {self.lib.pcagb_last_error().decode()}")
-        out = []
-        for i in range(n):
-            r = res[i]
+
+        def convert(i, r):
             sol = Solution(optimal_depth=r.optimal_depth, total_solutions=r.total_solutions)
             for name in ("seconds", "gpu_ms_expand", "gpu_ms_suffix", "gpu_ms_insert",
                          "kernel_launches", "insert_launches", "suffix_launches", "h2d_bytes",
@@ -352,8 +367,17 @@ class Engine:
                          "level_survivors"):
                 arr2 = getattr(r, name)
                 setattr(sol, name, [arr2[k] for k in range(min(last + 1, MAXD))])
-            out.append(sol)
-        return out
+            return sol
+
+        if on_done is None:
+            rc = self.lib.pcagb_solve_batch(self.h, arr, n, ctypes.byref(o), res, progs, lens, cap)
+        else:
+            cb = DONE_CB(lambda i, rp, _u: on_done(i, convert(i, rp.contents)))
+            rc = self.lib.pcagb_solve_batch_cb(self.h, arr, n, ctypes.byref(o), res, progs, lens,
+                                               cap, cb, None)
+        if rc != 0:
+            raise EngineError(f"batch solve failed ({rc}): {self.lib.pcagb_last_error().decode()}")
+        return [convert(i, res[i]) for i in range(n)]
 
     @property
     def stream(self) -> int:

@@ -1,0 +1,158 @@
+"""Continuous-batching solve server.
+
+`Server` keeps `slots` GPU engines (each with its own CUDA stream and HBM
+arena, sized from the device's free memory) and one worker thread per
+engine. Requests wait in a queue; whenever a worker is free it takes every
+request queued at that moment (up to `max_batch`) as one batch, so requests
+that arrive while others are on the GPU join the next free slot, batches on
+different slots overlap on the device, and each request's answer is
+delivered as soon as its own task is decided (pcagb_solve_batch_cb), not
+when its batch ends. A solve's state (levels, OEP tables, test order) lives
+only in its batch's arena and is keyed by task, so each result is the same
+alone and in the mix.
+
+`replay(trace)` drives a server from an arrival trace ((seconds, task)
+pairs, e.g. taskgen.poisson_stream) in real time and returns per-request
+records: arrival, completion, latency (time-to-proven-optimal), optimal
+depth and programs.
+"""
+from __future__ import annotations
+
+import queue
+import threading
+import time
+from dataclasses import dataclass, field
+
+from .pcalib import Engine, OEP_EXACT_LIVE, Solution, device_memory
+
+
+@dataclass
+class Request:
+    rid: int
+    task: object
+    arrival: float
+    max_depth: int
+    done: threading.Event = field(default_factory=threading.Event)
+    finish: float = 0.0
+    solution: Solution | None = None
+    batch_size: int = 0
+
+    @property
+    def latency(self) -> float:
+        return self.finish - self.arrival
+
+
+class Server:
+    def __init__(self, slots: int = 4, max_batch: int = 256, max_depth: int = 4, device: int = 0,
+                 hbm_fraction: float = 0.8, sol_cap: int = 16, oep_mode: int = OEP_EXACT_LIVE):
+        free, _ = device_memory(device)
+        budget = int(free * hbm_fraction / max(1, slots))
+        self.engines = [Engine(device, budget) for _ in range(slots)]
+        self.max_batch = max_batch
+        self.max_depth = max_depth
+        self.sol_cap = sol_cap
+        self.oep_mode = oep_mode
+        self.q: queue.Queue[Request | None] = queue.Queue()
+        self.t0 = time.perf_counter()
+        self.batches: list[int] = []
+        self._stop = False
+        self._lock = threading.Lock()
+        self.threads = [threading.Thread(target=self._worker, args=(e,), daemon=True)
+                        for e in self.engines]
+        for t in self.threads:
+            t.start()
+
+    def now(self) -> float:
+        return time.perf_counter() - self.t0
+
+    def submit(self, rid: int, task, max_depth: int | None = None) -> Request:
+        r = Request(rid, task, self.now(), self.max_depth if max_depth is None else max_depth)
+        self.q.put(r)
+        return r
+
+    def _take_batch(self) -> list[Request]:
+        first = self.q.get()
+        if first is None:
+            return []
+        batch = [first]
+        while len(batch) < self.max_batch:
+            try:
+                r = self.q.get_nowait()
+            except queue.Empty:
+                break
+            if r is None:
+                self.q.put(None)
+                break
+            batch.append(r)
+        return batch
+
+    def _worker(self, eng: Engine):
+        while not self._stop:
+            batch = self._take_batch()
+            if not batch:
+                self.q.put(None)
+                return
+            with self._lock:
+                self.batches.append(len(batch))
+            depth = max(r.max_depth for r in batch)
+
+            def deliver(i, sol, batch=batch):
+                r = batch[i]
+                r.solution = sol
+                r.finish = self.now()
+                r.batch_size = len(batch)
+                r.done.set()
+
+            eng.solve_batch([r.task for r in batch], max_depth=depth, oep_mode=self.oep_mode,
+                            sol_cap=self.sol_cap, on_done=deliver)
+
+    def close(self):
+        self._stop = True
+        self.q.put(None)
+        for t in self.threads:
+            t.join(timeout=60)
+        for e in self.engines:
+            e.close()
+
+
+class SerialServer(Server):
+    """The plain baseline: one engine, one task at a time, first come first
+    served (the reference's one-task-per-run model, on the GPU)."""
+
+    def __init__(self, max_depth: int = 4, device: int = 0, hbm_fraction: float = 0.8,
+                 sol_cap: int = 16, oep_mode: int = OEP_EXACT_LIVE):
+        super().__init__(slots=1, max_batch=1, max_depth=max_depth, device=device,
+                         hbm_fraction=hbm_fraction, sol_cap=sol_cap, oep_mode=oep_mode)
+
+
+def replay(server: Server, trace, max_depth: int | None = None) -> list[Request]:
+    """Submit the trace's tasks at their arrival times (real time) and wait
+    for every answer."""
+    start = server.now()
+    reqs = []
+    for rid, (t_arr, task) in enumerate(trace):
+        wait = start + t_arr - server.now()
+        if wait > 0:
+            time.sleep(wait)
+        reqs.append(server.submit(rid, task, max_depth))
+    for r in reqs:
+        r.done.wait()
+    return reqs
+
+
+def latency_summary(reqs: list[Request]) -> dict:
+    lat = sorted(r.latency for r in reqs)
+
+    def pct(p):
+        if not lat:
+            return None
+        k = min(len(lat) - 1, max(0, int(round(p / 100.0 * len(lat) + 0.5)) - 1))
+        return lat[k]
+
+    span = max(r.finish for r in reqs) - min(r.arrival for r in reqs)
+    cands = sum(sum(r.solution.candidates) for r in reqs if r.solution)
+    return {"requests": len(reqs), "p50_s": pct(50), "p99_s": pct(99), "max_s": lat[-1],
+            "mean_s": sum(lat) / len(lat),
+            "proven_optimal": sum(1 for r in reqs if r.solution and r.solution.optimal_depth >= 0),
+            "span_s": span, "candidates": cands,
+            "candidates_per_s": cands / span if span > 0 else 0.0}

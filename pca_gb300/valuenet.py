@@ -1,0 +1,241 @@
+"""Value network: forward, backward and Adam on the GPU with the project's
+own BF16 tensor-core kernels (pca_gb300/csrc/valuenet.cu).
+
+torch provides device memory and the stream; every layer, gradient and
+optimizer update is one of the C kernels, called through the C ABI.
+
+Network (the reference's ValueNetwork, python/model.py:16-84, with bit
+features): per-test encoder 176 -> 256 -> 256 (ReLU), mean + max pooling
+over the task's tests with the live mask and depth, trunk 528 -> 256 -> 128
+(ReLU), head 128 -> 16 (column 0: can finish optimally; 1..9: remaining
+steps). Loss: the reference's recipe (python/train.py:48-60): BCE with
+pos_weight 50 on column 0 plus 0.5 x cross entropy on the positives.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+
+import torch
+
+from .pcalib import load_library
+
+LAYERS = [("E1", 256, 176), ("E2", 256, 256), ("T1", 256, 528), ("T2", 128, 256),
+          ("H", 16, 128)]
+FEATURES = 176
+ROWS = 32  # feature rows per state
+
+
+def _lib():
+    lib = load_library()
+    vp, i, f = ctypes.c_void_p, ctypes.c_int, ctypes.c_float
+    sz = ctypes.c_size_t
+    sigs = {
+        "pcagb_vnet_gemm_nt": [vp, vp, vp, vp, vp, i, i, i, i, i, i, i, vp],
+        "pcagb_vnet_gemm_tn_acc": [vp, vp, vp, i, i, i, i, i, vp],
+        "pcagb_vnet_colsum": [vp, vp, i, i, i, vp],
+        "pcagb_vnet_features": [vp, vp, vp, i, i, vp, vp, vp, vp],
+        "pcagb_vnet_pool": [vp, vp, vp, vp, vp, i, vp, vp, vp],
+        "pcagb_vnet_pool_bwd": [vp, vp, vp, vp, i, vp, vp],
+        "pcagb_vnet_relu_bwd": [vp, vp, sz, vp],
+        "pcagb_vnet_loss": [vp, vp, vp, i, f, f, vp, vp, vp],
+        "pcagb_vnet_adam": [vp, vp, vp, vp, i, i, f, f, f, f, i, vp, vp, vp],
+        "pcagb_vnet_to_bf16": [vp, vp, sz, vp],
+    }
+    for name, args in sigs.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = ctypes.c_int
+    return lib
+
+
+def _p(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+class ValueNet:
+    def __init__(self, device="cuda", seed=0, lr=3e-4, pos_weight=50.0):
+        self.lib = _lib()
+        self.dev = torch.device(device)
+        self.lr, self.pos_weight = lr, pos_weight
+        g = torch.Generator().manual_seed(seed)
+        self.W, self.b, self.Wb, self.Wt = {}, {}, {}, {}
+        self.mW, self.vW, self.mb, self.vb = {}, {}, {}, {}
+        for name, out, inp in LAYERS:
+            bound = 1.0 / math.sqrt(inp)
+            w = (torch.rand(out, inp, generator=g) * 2 - 1) * bound
+            if name == "T1":
+                w[:, 521:] = 0.0  # padding columns of the trunk input
+            self.W[name] = w.to(self.dev).contiguous()
+            self.b[name] = ((torch.rand(out, generator=g) * 2 - 1) * bound).to(self.dev)
+            for d in (self.mW, self.vW):
+                d[name] = torch.zeros_like(self.W[name])
+            for d in (self.mb, self.vb):
+                d[name] = torch.zeros_like(self.b[name])
+        self.step_n = 0
+        self._refresh_bf16()
+
+    @property
+    def stream(self):
+        return ctypes.c_void_p(torch.cuda.current_stream(self.dev).cuda_stream)
+
+    def _ck(self, rc):
+        if rc != 0:
+            raise RuntimeError(f"value-net kernel failed ({rc})")
+
+    def _refresh_bf16(self):
+        for name, out, inp in LAYERS:
+            self.Wb[name] = self.W[name].to(torch.bfloat16).contiguous()
+            self.Wt[name] = self.W[name].t().contiguous().to(torch.bfloat16)
+
+    def n_params(self):
+        return sum(w.numel() + self.b[k].numel() for k, w in self.W.items())
+
+    # ---- kernels -----------------------------------------------------------
+    def _gemm(self, A, name, relu, out_f32=False, transposed=False):
+        """A[M,K] . W^T (+b) or, for the input gradient, A[M,N] . W."""
+        M, K = A.shape
+        if transposed:
+            B = self.Wt[name]          # [in][out]: rows are the output
+            N = B.shape[0]
+            bias = None
+        else:
+            B = self.Wb[name]          # [out][in]
+            N = B.shape[0]
+            bias = self.b[name]
+        C = torch.empty(M, N, device=self.dev, dtype=torch.float32 if out_f32 else torch.bfloat16)
+        self._ck(self.lib.pcagb_vnet_gemm_nt(
+            _p(A), _p(B), _p(bias), None if out_f32 else _p(C), _p(C) if out_f32 else None,
+            M, N, K, K, B.shape[1], N, int(relu), self.stream))
+        return C
+
+    def features(self, regs, flags, task, TP, task_io, task_T):
+        n = task.shape[0]
+        X = torch.empty(n * ROWS, FEATURES, device=self.dev, dtype=torch.bfloat16)
+        self._ck(self.lib.pcagb_vnet_features(_p(regs), _p(flags), _p(task), TP, n, _p(task_io),
+                                              _p(task_T), _p(X), self.stream))
+        return X
+
+    def forward(self, X, live, task, task_T, depth):
+        n = task.shape[0]
+        H1 = self._gemm(X, "E1", True)
+        H2 = self._gemm(H1, "E2", True)
+        P = torch.empty(n, 528, device=self.dev, dtype=torch.bfloat16)
+        am = torch.empty(n, 256, device=self.dev, dtype=torch.uint8)
+        self._ck(self.lib.pcagb_vnet_pool(_p(H2), _p(live), _p(task), _p(task_T), _p(depth), n,
+                                          _p(P), _p(am), self.stream))
+        Z1 = self._gemm(P, "T1", True)
+        Z2 = self._gemm(Z1, "T2", True)
+        L = self._gemm(Z2, "H", False, out_f32=True)
+        self._acts = dict(X=X, H1=H1, H2=H2, P=P, am=am, Z1=Z1, Z2=Z2, task=task, task_T=task_T)
+        return L
+
+    def _wgrad(self, dY, X, name):
+        out, inp = self.W[name].shape
+        G = torch.zeros(out, inp, device=self.dev, dtype=torch.float32)
+        self._ck(self.lib.pcagb_vnet_gemm_tn_acc(_p(dY), _p(X), _p(G), dY.shape[0], out, inp,
+                                                 dY.shape[1], X.shape[1], self.stream))
+        gb = torch.zeros(out, device=self.dev, dtype=torch.float32)
+        self._ck(self.lib.pcagb_vnet_colsum(_p(dY), _p(gb), dY.shape[0], out, dY.shape[1],
+                                            self.stream))
+        return G, gb
+
+    def _relu_bwd(self, dY, Y):
+        self._ck(self.lib.pcagb_vnet_relu_bwd(_p(dY), _p(Y), dY.numel(), self.stream))
+
+    def backward(self, dL):
+        """dL: bf16 [n,16] gradient of the loss w.r.t. the logits. Returns
+        {name: (dW, db)} in fp32."""
+        a = self._acts
+        grads = {}
+        grads["H"] = self._wgrad(dL, a["Z2"], "H")
+        dZ2 = self._gemm(dL, "H", False, transposed=True)
+        self._relu_bwd(dZ2, a["Z2"])
+        grads["T2"] = self._wgrad(dZ2, a["Z1"], "T2")
+        dZ1 = self._gemm(dZ2, "T2", False, transposed=True)
+        self._relu_bwd(dZ1, a["Z1"])
+        grads["T1"] = self._wgrad(dZ1, a["P"], "T1")
+        dP = self._gemm(dZ1, "T1", False, transposed=True)
+        n = a["task"].shape[0]
+        dH2 = torch.empty(n * ROWS, 256, device=self.dev, dtype=torch.bfloat16)
+        self._ck(self.lib.pcagb_vnet_pool_bwd(_p(dP), _p(a["am"]), _p(a["task"]),
+                                              _p(a["task_T"]), n, _p(dH2), self.stream))
+        self._relu_bwd(dH2, a["H2"])
+        grads["E2"] = self._wgrad(dH2, a["H1"], "E2")
+        dH1 = self._gemm(dH2, "E2", False, transposed=True)
+        self._relu_bwd(dH1, a["H1"])
+        grads["E1"] = self._wgrad(dH1, a["X"], "E1")
+        return grads
+
+    def loss(self, L, label, remaining):
+        n = L.shape[0]
+        dL = torch.empty(n, 16, device=self.dev, dtype=torch.bfloat16)
+        stats = torch.zeros(3, device=self.dev, dtype=torch.float32)
+        npos = float((label > 0.5).sum().item())
+        self._ck(self.lib.pcagb_vnet_loss(_p(L), _p(label), _p(remaining), n, self.pos_weight,
+                                          npos, _p(dL), _p(stats), self.stream))
+        bce, ce, _ = stats.tolist()
+        return bce / n + (0.5 * ce / npos if npos else 0.0), dL
+
+    def adam(self, grads, b1=0.9, b2=0.999, eps=1e-8):
+        self.step_n += 1
+        for name, out, inp in LAYERS:
+            G, gb = grads[name]
+            self._ck(self.lib.pcagb_vnet_adam(_p(self.W[name]), _p(G), _p(self.mW[name]),
+                                              _p(self.vW[name]), out, inp, self.lr, b1, b2, eps,
+                                              self.step_n, _p(self.Wb[name]), _p(self.Wt[name]),
+                                              self.stream))
+            self._ck(self.lib.pcagb_vnet_adam(_p(self.b[name]), _p(gb), _p(self.mb[name]),
+                                              _p(self.vb[name]), 1, out, self.lr, b1, b2, eps,
+                                              self.step_n, None, None, self.stream))
+        with torch.no_grad():
+            self.W["T1"][:, 521:] = 0.0
+            self.Wb["T1"][:, 521:] = 0.0
+            self.Wt["T1"][521:, :] = 0.0
+
+    def train_step(self, batch):
+        """One step on a batch dict (device tensors): regs, flags, live, task,
+        task_io, task_T, TP, depth (uint8 per state), label, remaining.
+        Returns the loss."""
+        X = self.features(batch["regs"], batch["flags"], batch["task"], batch["TP"],
+                          batch["task_io"], batch["task_T"])
+        L = self.forward(X, batch["live"], batch["task"], batch["task_T"], batch["depth"])
+        loss, dL = self.loss(L, batch["label"], batch["remaining"])
+        self.adam(self.backward(dL))
+        return loss
+
+    def score(self, regs, flags, live, task, task_io, task_T, TP, depth):
+        X = self.features(regs, flags, task, TP, task_io, task_T)
+        return self.forward(X, live, task, task_T, depth)[:, 0]
+
+    def state_dict(self):
+        return {k: v.detach().cpu() for k, v in {**{"W." + n: w for n, w in self.W.items()},
+                                                  **{"b." + n: b for n, b in self.b.items()}}.items()}
+
+    def load_state_dict(self, sd):
+        for k, v in sd.items():
+            kind, name = k.split(".", 1)
+            (self.W if kind == "W" else self.b)[name].copy_(v.to(self.dev))
+        self._refresh_bf16()
+
+
+def reference_forward(W, b, X, live, task_T, task, depth, bf16=True):
+    """fp32 CPU restatement of the same network (for gradient checks): X
+    [n*32,176], returns logits [n,16]; autograd-ready when W/b require grad.
+    With bf16=True the activations (and, through autograd, their gradients)
+    are rounded to bf16 where the kernels store them."""
+    r = (lambda x: x.to(torch.bfloat16).float()) if bf16 else (lambda x: x)
+    n = live.shape[0]
+    H1 = r(torch.relu(X @ W["E1"].t() + b["E1"]))
+    H2 = r(torch.relu(H1 @ W["E2"].t() + b["E2"])).view(n, ROWS, 256)
+    T = task_T[task].long()
+    mask = (torch.arange(ROWS)[None, :] < T[:, None]).float()
+    mean = (H2 * mask[:, :, None]).sum(1) / T[:, None].float()
+    mx = torch.where(mask[:, :, None] > 0, H2, torch.full_like(H2, -1e30)).max(1).values
+    g = torch.zeros(n, 16)
+    g[:, :8] = ((live.long()[:, None] >> torch.arange(8)[None, :]) & 1).float()
+    g[:, 8] = depth.float()
+    P = r(torch.cat([mean, mx, g], 1))
+    Z1 = r(torch.relu(P @ W["T1"].t() + b["T1"]))
+    Z2 = r(torch.relu(Z1 @ W["T2"].t() + b["T2"]))
+    return Z2 @ W["H"].t() + b["H"]

@@ -203,7 +203,14 @@ typedef struct {
     uint64_t d2h_bytes;                /* device->host bytes                 */
     uint64_t insert_children;          /* children the insert kernels hashed */
     int      split_used;
-    int      reserved[7];
+    int      reserved0;
+    /* ordered solves (pcagb_solve_ordered) at the optimal depth: prefixes of
+       the split level, prefixes visited up to and including the first chunk
+       that held a solution, and the device time that took */
+    uint64_t prefixes_at_optimal;
+    uint64_t prefixes_to_first;
+    double   ms_to_first;
+    int      reserved[2];
 } pcagb_result_t;
 
 const char *pcagb_last_error(void);
@@ -240,6 +247,41 @@ typedef void (*pcagb_done_cb)(int task, const pcagb_result_t *result, void *user
 int  pcagb_solve_batch_cb(pcagb_engine_t *e, const task_spec_t *tasks, int ntasks,
                           const pcagb_opts_t *opts, pcagb_result_t *results, uint16_t *sol_progs,
                           int *sol_lens, int sol_cap_per_task, pcagb_done_cb on_done, void *user);
+
+/* A device view of the split level a suffix stage starts from, handed to
+ * an ordering callback. Valid only during the callback. regs is
+ * u16[n][8][tp] (column-major per state), flags u8[n][tp], live u8[n],
+ * task u16[n]; task_io is u16[ntasks][3][32] (input 0, input 1, target per
+ * test, in the engine's test order) and task_T int32[ntasks]. */
+typedef struct {
+    const uint16_t *regs;
+    const uint8_t  *flags;
+    const uint8_t  *live;
+    const uint16_t *task;
+    uint64_t n;
+    int tp;
+    int depth;          /* instructions in each prefix */
+    int target_depth;   /* K of the stage */
+    int ntasks;
+    const uint16_t *task_io;
+    const int32_t  *task_T;
+    void *stream;       /* cudaStream_t to work on */
+} pcagb_level_view_t;
+
+/* Returns a device array of uint32 holding a permutation of 0..n-1 (the
+ * order to visit prefixes in; it must stay valid until the stage ends), or
+ * NULL for the plain DFS order. */
+typedef const uint32_t *(*pcagb_order_cb)(const pcagb_level_view_t *view, void *user);
+
+/* Solve with the suffix stages visiting prefixes in an order chosen by the
+ * callback (e.g. by a value network) in chunks of `chunk` prefixes, and
+ * stopping at the first chunk of the optimal depth that holds a solution.
+ * Exact: every depth below the optimum is still searched completely, so the
+ * optimal depth is proven; only the order of work at the optimal depth
+ * changes (its programs are those of the visited chunks). */
+int  pcagb_solve_ordered(pcagb_engine_t *e, const task_spec_t *task, const pcagb_opts_t *opts,
+                         pcagb_order_cb order, void *user, uint64_t chunk,
+                         pcagb_result_t *res, uint16_t *sol_progs, int *sol_lens, int sol_cap);
 
 /* IDDFS completion from an arbitrary branchless state (the GPU form of
  * search_exhaustive_complete, src/search_state.c:418-453). Returns 1 found /

@@ -114,6 +114,7 @@ struct pcagb_engine {
     int32_t *d_task_T = nullptr;
     uint32_t *d_task_target = nullptr;
     uint8_t *d_task_active = nullptr;
+    uint16_t *d_task_io = nullptr;           /* [kMaxBatch][3][32] in0, in1, target */
     unsigned long long *d_hist = nullptr;    /* [kMaxBatch][128] */
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
     int occ_insert = 4, occ_suffix = 8, occ_mat = 4;   /* resident blocks per SM */
@@ -364,10 +365,23 @@ struct TaskRun {
     pcagb_result_t res{};
 };
 
+/* Visiting order of a suffix stage: a permutation of the level's prefixes
+ * (null = DFS order), processed `chunk` prefixes per launch; with
+ * stop_at_first the stage ends after the first launch that found a
+ * solution. Reports how far it got. */
+struct StageOrder {
+    const uint32_t *order = nullptr;
+    uint64_t chunk = 0;
+    bool stop_at_first = false;
+    uint64_t prefixes_to_first = 0;
+    float ms_to_first = 0;
+};
+
 /* Run the last stage at depth K from level S (suffix depth K-S, or the leaf
  * check when K == S) for the active tasks; appends each task's raw
  * solutions in DFS order. */
-int run_stage(pcagb_engine *e, int S, int K, std::vector<TaskRun> &runs, bool first_only)
+int run_stage(pcagb_engine *e, int S, int K, std::vector<TaskRun> &runs, bool first_only,
+              StageOrder *so = nullptr)
 {
     const GenTables &gt = gen_tables();
     Level &L = e->levels[S];
@@ -378,31 +392,50 @@ int run_stage(pcagb_engine *e, int S, int K, std::vector<TaskRun> &runs, bool fi
     cudaEventRecord(e->ev0, e->stream);
     const bool t16 = e->TPC == 16;
     const int g = e->grid(e->occ_suffix);
+    int rc = PCAGB_OK;
     if (s == 0) {
         if (t16) k_leaf<16><<<e->grid(4), 256, 0, e->stream>>>(view(L), e->td, sb);
         else k_leaf<32><<<e->grid(4), 256, 0, e->stream>>>(view(L), e->td, sb);
-    } else if (s == 1) {
-        if (t16) k_suffix<16, 1><<<g, kThreads, 0, e->stream>>>(view(L), e->td, sb, 1, 1);
-        else k_suffix<32, 1><<<g, kThreads, 0, e->stream>>>(view(L), e->td, sb, 1, 1);
+        rc = check_launch(e);
+        if (rc) return rc;
     } else if (s <= 3) {
         int ncmax = 0;
         for (size_t i = 0; i < L.hist.size(); i++)
             if (L.hist[i]) ncmax = std::max(ncmax, gt.nc((int)(i & 127)));
-        const uint32_t chunk = s == 2 ? 16 : 1;
-        const uint32_t cpp = std::max(1u, (uint32_t)((ncmax + chunk - 1) / chunk));
-        if (s == 2) {
-            if (t16) k_suffix<16, 2><<<g, kThreads, 0, e->stream>>>(view(L), e->td, sb, cpp, chunk);
-            else k_suffix<32, 2><<<g, kThreads, 0, e->stream>>>(view(L), e->td, sb, cpp, chunk);
-        } else {
-            if (t16) k_suffix<16, 3><<<g, kThreads, 0, e->stream>>>(view(L), e->td, sb, cpp, chunk);
-            else k_suffix<32, 3><<<g, kThreads, 0, e->stream>>>(view(L), e->td, sb, cpp, chunk);
+        const uint32_t chunk = s == 1 ? 1 : s == 2 ? 16 : 1;
+        const uint32_t cpp =
+            s == 1 ? 1 : std::max(1u, (uint32_t)((ncmax + chunk - 1) / chunk));
+        const uint64_t step = so && so->chunk ? so->chunk : std::max<uint64_t>(L.n, 1);
+        for (uint64_t b0 = 0; b0 < L.n; b0 += step) {
+            const PrefixRange R{so ? so->order : nullptr, b0, std::min(step, L.n - b0)};
+            if (s == 1) {
+                if (t16) k_suffix<16, 1><<<g, kThreads, 0, e->stream>>>(view(L), e->td, sb, 1, 1, R);
+                else k_suffix<32, 1><<<g, kThreads, 0, e->stream>>>(view(L), e->td, sb, 1, 1, R);
+            } else if (s == 2) {
+                if (t16) k_suffix<16, 2><<<g, kThreads, 0, e->stream>>>(view(L), e->td, sb, cpp, chunk, R);
+                else k_suffix<32, 2><<<g, kThreads, 0, e->stream>>>(view(L), e->td, sb, cpp, chunk, R);
+            } else {
+                if (t16) k_suffix<16, 3><<<g, kThreads, 0, e->stream>>>(view(L), e->td, sb, cpp, chunk, R);
+                else k_suffix<32, 3><<<g, kThreads, 0, e->stream>>>(view(L), e->td, sb, cpp, chunk, R);
+            }
+            rc = check_launch(e);
+            if (rc) return rc;
+            if (so && so->stop_at_first) {
+                unsigned long long hits = 0;
+                CK(e_copy(e, &hits, e->d_small, 8, cudaMemcpyDeviceToHost, e->stream));
+                cudaEventRecord(e->ev1, e->stream);
+                CK(cudaStreamSynchronize(e->stream));
+                if (hits) {
+                    so->prefixes_to_first = R.begin + R.count;
+                    cudaEventElapsedTime(&so->ms_to_first, e->ev0, e->ev1);
+                    break;
+                }
+            }
         }
     } else {
         set_err("suffix depth %d not supported (split too shallow)", s);
         return PCAGB_ENOMEM;
     }
-    int rc = check_launch(e);
-    if (rc) return rc;
     cudaEventRecord(e->ev1, e->stream);
     unsigned long long nrec = 0, first = 0;
     CK(e_copy(e, &nrec, e->d_small, 8, cudaMemcpyDeviceToHost, e->stream));
@@ -600,8 +633,14 @@ uint64_t hist_sum(const Level &L, int t, const std::vector<uint64_t> &weight)
 typedef void (*done_fn)(int task, void *user);
 
 /* Core batched IDDFS shared by every solve entry point. */
+struct OrderSpec {
+    pcagb_order_cb cb = nullptr;
+    void *user = nullptr;
+    uint64_t chunk = 0;
+};
+
 int run_batch(pcagb_engine *e, std::vector<TaskRun> &runs, const pcagb_opts_t &o,
-              done_fn on_done = nullptr, void *user = nullptr)
+              done_fn on_done = nullptr, void *user = nullptr, const OrderSpec *ord = nullptr)
 {
     const GenTables &gt = gen_tables();
     auto t_start = std::chrono::steady_clock::now();
@@ -644,9 +683,18 @@ int run_batch(pcagb_engine *e, std::vector<TaskRun> &runs, const pcagb_opts_t &o
             for (int t = 0; t < runs[i].T; t++)
                 tgt[(size_t)i * 32 + t] = runs[i].target[runs[i].order[t]];
         }
+        std::vector<uint16_t> io((size_t)nt * 3 * 32, 0);
+        for (int i = 0; i < nt; i++)
+            for (int t = 0; t < runs[i].T; t++) {
+                const int o = runs[i].order[t];
+                io[((size_t)i * 3 + 0) * 32 + t] = runs[i].root.regs[o][1];
+                io[((size_t)i * 3 + 1) * 32 + t] = runs[i].root.regs[o][2];
+                io[((size_t)i * 3 + 2) * 32 + t] = runs[i].target[o];
+            }
         CK(e_copy(e, e->d_task_T, T.data(), nt * 4, cudaMemcpyHostToDevice, e->stream));
         CK(e_copy(e, e->d_task_target, tgt.data(), tgt.size() * 4, cudaMemcpyHostToDevice,
                   e->stream));
+        CK(e_copy(e, e->d_task_io, io.data(), io.size() * 2, cudaMemcpyHostToDevice, e->stream));
     }
 
     /* level 0: one root per task */
@@ -777,7 +825,17 @@ int run_batch(pcagb_engine *e, std::vector<TaskRun> &runs, const pcagb_opts_t &o
             }
             tr.nrec = 0;
         }
-        int rc = run_stage(e, S, K, runs, o.first_only != 0);
+        StageOrder so;
+        StageOrder *sop = nullptr;
+        if (ord && s >= 1) {
+            pcagb_level_view_t lv{LS.regs, LS.flags, LS.live, LS.task, LS.n, e->TPC, S, K, nt,
+                                  e->d_task_io, e->d_task_T, (void *)e->stream};
+            so.order = ord->cb ? ord->cb(&lv, ord->user) : nullptr;
+            so.chunk = ord->chunk;
+            so.stop_at_first = true;
+            sop = &so;
+        }
+        int rc = run_stage(e, S, K, runs, o.first_only != 0, sop);
         if (rc) return rc;
         for (int i = 0; i < nt; i++) {
             if (!active[i]) continue;
@@ -796,6 +854,9 @@ int run_batch(pcagb_engine *e, std::vector<TaskRun> &runs, const pcagb_opts_t &o
                 tr.done = true;
                 tr.optimal_depth = K;
                 tr.t_done = elapsed();
+                tr.res.prefixes_at_optimal = LS.n;
+                tr.res.prefixes_to_first = sop ? sop->prefixes_to_first : LS.n;
+                tr.res.ms_to_first = sop ? sop->ms_to_first : 0.0;
                 tr.res.total_solutions =
                     s == 0 || (o.first_only && nt == 1) ? tr.nrec : tr.sols.size();
                 notify(i);
@@ -907,6 +968,7 @@ int engine_init(pcagb_engine *e, int device, size_t budget)
     CK(cudaMalloc(&e->d_task_T, kMaxBatch * 4));
     CK(cudaMalloc(&e->d_task_target, (size_t)kMaxBatch * 32 * 4));
     CK(cudaMalloc(&e->d_task_active, kMaxBatch));
+    CK(cudaMalloc(&e->d_task_io, (size_t)kMaxBatch * 3 * 32 * 2));
     CK(cudaMalloc(&e->d_hist, (size_t)kMaxBatch * 128 * sizeof(unsigned long long)));
     return PCAGB_OK;
 }
@@ -1023,6 +1085,7 @@ void pcagb_engine_destroy(pcagb_engine_t *e)
     cudaFree(e->d_task_T);
     cudaFree(e->d_task_target);
     cudaFree(e->d_task_active);
+    cudaFree(e->d_task_io);
     cudaFree(e->d_hist);
     for (cudaEvent_t ev : {e->ev0, e->ev1, e->ev2, e->ev3})
         if (ev) cudaEventDestroy(ev);
@@ -1124,6 +1187,24 @@ int pcagb_solve_batch_cb(pcagb_engine_t *e, const task_spec_t *tasks, int ntasks
     /* the batch totals are known only now */
     for (int i = 0; i < ntasks; i++) results[i] = runs[i].res;
     return c.rc;
+}
+
+int pcagb_solve_ordered(pcagb_engine_t *e, const task_spec_t *task, const pcagb_opts_t *opts,
+                        pcagb_order_cb order, void *user, uint64_t chunk, pcagb_result_t *res,
+                        uint16_t *sol_progs, int *sol_lens, int sol_cap)
+{
+    pcagb_opts_t o;
+    if (opts) o = *opts;
+    else pcagb_default_opts(&o);
+    if (!e || !task || !res) { set_err("null argument"); return PCAGB_EINVAL; }
+    std::vector<TaskRun> runs(1);
+    if (!make_run(task, o, &runs[0])) return PCAGB_EINVAL;
+    OrderSpec spec{order, user, chunk};
+    int rc = run_batch(e, runs, o, nullptr, nullptr, &spec);
+    if (rc) return rc;
+    rc = emit_solutions(task, o, runs[0], sol_progs, sol_lens, sol_cap);
+    *res = runs[0].res;
+    return rc;
 }
 
 int pcagb_complete(pcagb_engine_t *e, const search_ctx_t *ctx, const search_state_t *start,

@@ -584,24 +584,34 @@ __device__ __forceinline__ void scan_last(const WarpState<TPC> &ws, int T,
     }
 }
 
-/* Suffix enumeration of depth SD (1..3) from every state of level P whose
- * task is active. Work item = (prefix, chunk of first-suffix candidates);
- * for SD = 1 the chunk is the whole prefix. */
+/* A contiguous range of prefixes, optionally through a permutation: the
+ * suffix kernel visits prefixes order[begin .. begin + count) (or begin ..
+ * begin + count when order is null). */
+struct PrefixRange {
+    const uint32_t *order;
+    uint64_t begin, count;
+};
+
+/* Suffix enumeration of depth SD (1..3) from the prefixes of level P in
+ * range R whose task is active. Work item = (prefix, chunk of first-suffix
+ * candidates); for SD = 1 the chunk is the whole prefix. */
 template <int TPC, int SD>
 __global__ void __launch_bounds__(kThreads)
-k_suffix(LevelDev P, TaskDev task, SolBuf S, uint32_t chunks_per_prefix, uint32_t chunk)
+k_suffix(LevelDev P, TaskDev task, SolBuf S, uint32_t chunks_per_prefix, uint32_t chunk,
+         PrefixRange R)
 {
     __shared__ WarpState<TPC> sws[kWarpsPerBlock];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     WarpState<TPC> &ws = sws[wib];
     const uint64_t nw = (uint64_t)gridDim.x * kWarpsPerBlock;
-    const uint64_t items = P.n * chunks_per_prefix;
+    const uint64_t items = R.count * chunks_per_prefix;
     uint64_t loaded = ~0ull;
     uint32_t cur_task = ~0u, tgt = 0, tgt0 = 0, tgt1 = 0;
     int T = 0;
     for (uint64_t it = (uint64_t)blockIdx.x * kWarpsPerBlock + wib; it < items; it += nw) {
-        const uint64_t q = it / chunks_per_prefix;
-        const uint32_t ck = (uint32_t)(it - q * chunks_per_prefix);
+        const uint64_t qi = it / chunks_per_prefix;
+        const uint32_t ck = (uint32_t)(it - qi * chunks_per_prefix);
+        const uint64_t q = R.order ? (uint64_t)R.order[R.begin + qi] : R.begin + qi;
         const uint32_t tid = P.task[q];
         if (!task.active[tid]) continue;
         if (tid != cur_task) {

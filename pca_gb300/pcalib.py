@@ -86,7 +86,22 @@ class SolveResult(ctypes.Structure):
                 ("d2h_bytes", ctypes.c_uint64),
                 ("insert_children", ctypes.c_uint64),
                 ("split_used", ctypes.c_int),
-                ("reserved", ctypes.c_int * 7)]
+                ("reserved0", ctypes.c_int),
+                ("prefixes_at_optimal", ctypes.c_uint64),
+                ("prefixes_to_first", ctypes.c_uint64),
+                ("ms_to_first", ctypes.c_double),
+                ("reserved", ctypes.c_int * 2)]
+
+
+class LevelView(ctypes.Structure):
+    _fields_ = [("regs", ctypes.c_void_p), ("flags", ctypes.c_void_p), ("live", ctypes.c_void_p),
+                ("task", ctypes.c_void_p), ("n", ctypes.c_uint64), ("tp", ctypes.c_int),
+                ("depth", ctypes.c_int), ("target_depth", ctypes.c_int), ("ntasks", ctypes.c_int),
+                ("task_io", ctypes.c_void_p), ("task_T", ctypes.c_void_p),
+                ("stream", ctypes.c_void_p)]
+
+
+ORDER_CB = ctypes.CFUNCTYPE(ctypes.c_void_p, ctypes.POINTER(LevelView), ctypes.c_void_p)
 
 
 OEP_NONE, OEP_EXACT, OEP_EXACT_LIVE = 0, 1, 2
@@ -102,7 +117,8 @@ EXPORTS = [
     "search_state_serialize", "search_gen_candidates_branchless",
     "search_exhaustive_complete", "search_exhaustive_states_explored", "search_state_dump",
     "pcagb_last_error", "pcagb_default_opts", "pcagb_engine_create", "pcagb_engine_destroy",
-    "pcagb_solve", "pcagb_solve_batch", "pcagb_solve_batch_cb", "pcagb_complete",
+    "pcagb_solve", "pcagb_solve_batch", "pcagb_solve_batch_cb", "pcagb_solve_ordered",
+    "pcagb_complete",
     "pcagb_num_candidates",
     "pcagb_engine_stream", "pcagb_device_memory",
     "pcagb_solve_small_noalloc", "pcagb_noalloc_last_error",
@@ -142,6 +158,9 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
         "pcagb_solve_batch_cb": ([ctypes.c_void_p, P(TaskSpec), ctypes.c_int, P(SolveOpts),
                                   P(SolveResult), P(ctypes.c_uint16), P(ctypes.c_int),
                                   ctypes.c_int, DONE_CB, ctypes.c_void_p], ctypes.c_int),
+        "pcagb_solve_ordered": ([ctypes.c_void_p, P(TaskSpec), P(SolveOpts), ORDER_CB,
+                                 ctypes.c_void_p, ctypes.c_uint64, P(SolveResult),
+                                 P(ctypes.c_uint16), P(ctypes.c_int), ctypes.c_int], ctypes.c_int),
         "pcagb_complete": ([ctypes.c_void_p, P(SearchCtx), P(SearchState), ctypes.c_int,
                             P(ctypes.c_uint16), P(ctypes.c_int), P(ctypes.c_uint64)], ctypes.c_int),
         "pcagb_num_candidates": ([ctypes.c_uint8], ctypes.c_int),
@@ -273,6 +292,9 @@ class Solution:
     d2h_bytes: int = 0
     insert_children: int = 0
     split_used: int = 0
+    prefixes_at_optimal: int = 0
+    prefixes_to_first: int = 0
+    ms_to_first: float = 0.0
 
 
 class EngineError(RuntimeError):
@@ -326,7 +348,8 @@ class Engine:
         sol = Solution(optimal_depth=r.optimal_depth, total_solutions=r.total_solutions)
         for name in ("seconds", "gpu_ms_expand", "gpu_ms_suffix", "gpu_ms_insert",
                      "kernel_launches", "insert_launches", "suffix_launches", "h2d_bytes",
-                     "d2h_bytes", "insert_children", "split_used"):
+                     "d2h_bytes", "insert_children", "split_used", "prefixes_at_optimal",
+                     "prefixes_to_first", "ms_to_first"):
             setattr(sol, name, getattr(r, name))
         for i in range(r.stored):
             sol.programs.append([progs[i * 16 + j] for j in range(lens[i])])
@@ -378,6 +401,42 @@ class Engine:
         if rc != 0:
             raise EngineError(f"batch solve failed ({rc}): {self.lib.pcagb_last_error().decode()}")
         return [convert(i, res[i]) for i in range(n)]
+
+    def solve_ordered(self, task: TaskSpec, order_fn, chunk=4096, max_depth=4,
+                      oep_mode=OEP_EXACT_LIVE, split_depth=-1, sol_cap=256) -> Solution:
+        """Solve with the suffix stages visiting the split level's prefixes in
+        the order order_fn(view) returns (a device tensor of uint32/int32
+        prefix indices, or None for DFS order), `chunk` prefixes per launch,
+        stopping at the first chunk of the optimal depth with a solution."""
+        o = SolveOpts()
+        self.lib.pcagb_default_opts(ctypes.byref(o))
+        o.max_depth, o.split_depth, o.oep_mode = max_depth, split_depth, oep_mode
+        keep = []
+
+        def cb(vp, _user):
+            out = order_fn(vp.contents)
+            if out is None:
+                return None
+            keep.append(out)
+            return out.data_ptr()
+
+        ccb = ORDER_CB(cb)
+        r = SolveResult()
+        progs = (ctypes.c_uint16 * (16 * max(sol_cap, 1)))()
+        lens = (ctypes.c_int * max(sol_cap, 1))()
+        rc = self.lib.pcagb_solve_ordered(self.h, ctypes.byref(task), ctypes.byref(o), ccb, None,
+                                          chunk, ctypes.byref(r), progs, lens, sol_cap)
+        if rc != 0:
+            raise EngineError(f"ordered solve failed ({rc}): {self.lib.pcagb_last_error().decode()}")
+        sol = Solution(optimal_depth=r.optimal_depth, total_solutions=r.total_solutions)
+        for name in ("seconds", "gpu_ms_expand", "gpu_ms_suffix", "gpu_ms_insert",
+                     "kernel_launches", "split_used", "prefixes_at_optimal", "prefixes_to_first",
+                     "ms_to_first"):
+            setattr(sol, name, getattr(r, name))
+        for i in range(r.stored):
+            sol.programs.append([progs[i * 16 + j] for j in range(lens[i])])
+        sol.candidates = [r.candidates[k] for k in range(MAXD)]
+        return sol
 
     @property
     def stream(self) -> int:

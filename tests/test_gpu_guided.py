@@ -1,0 +1,83 @@
+"""The learned part's contract with the exhaustive engine.
+
+* Labels come from the solver: every positive state really finishes
+  optimally in its labelled number of steps (checked by an exact GPU
+  completion from that state).
+* Ordering never changes what is proven: an ordered solve (value network,
+  random, DFS) reports the task's optimal depth, and its programs are correct
+  and belong to the plain solve's program set at the same split.
+* The trained network gains over the plain (DFS) order on held-out tasks:
+  fewer prefixes of the optimal depth are visited before the first correct
+  program.
+"""
+import random
+
+import pytest
+
+from pca_gb300 import taskgen
+from pca_gb300.pcalib import PCALib
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+def pick(engine, seed, n, depths):
+    tasks = taskgen.synthetic_batch(n, seed=seed)
+    sols = engine.solve_batch(tasks, max_depth=4, sol_cap=1)
+    return [t for t, s in zip(tasks, sols) if s.optimal_depth in depths]
+
+
+def test_positive_labels_are_exact(engine):
+    from pca_gb300.guided import label_task
+    lib = PCALib()
+    rng = random.Random(3)
+    tasks = pick(engine, 31, 300, (2, 3))[:8]
+    assert tasks
+    checked = 0
+    for task in tasks:
+        sol = engine.solve(task, max_depth=4, sol_cap=256)
+        states, depth, label, remaining = label_task(lib, task, sol.programs, sol.optimal_depth, rng, 2)
+        ctx = lib.init_ctx(task)
+        for s, d, y, r in zip(states, depth, label, remaining):
+            if y < 0.5:
+                continue
+            found, n, insns, _ = engine.complete(ctx, s, d + r)
+            assert found and n == r
+            checked += 1
+    assert checked > 0
+
+
+@pytest.mark.parametrize("order", ["dfs", "random", "value"])
+def test_ordered_solve_is_exact(engine, order):
+    from pca_gb300.guided import RandomOrder, ValueOrder
+    from pca_gb300.valuenet import ValueNet
+    lib = PCALib()
+    fn = {"dfs": lambda v: None, "random": RandomOrder(5),
+          "value": ValueOrder(ValueNet(seed=1), min_states=1)}[order]
+    for task in pick(engine, 41, 300, (3, 4))[:6]:
+        plain = engine.solve(task, max_depth=4, split_depth=2, sol_cap=1 << 14)
+        got = engine.solve_ordered(task, fn, chunk=64, max_depth=4, split_depth=2, sol_cap=1 << 14)
+        assert got.optimal_depth == plain.optimal_depth
+        assert got.programs and set(map(tuple, got.programs)) <= set(map(tuple, plain.programs))
+        for p in got.programs:
+            assert lib.evaluate(task, p) == task.num_tests
+        assert 0 < got.prefixes_to_first <= got.prefixes_at_optimal
+
+
+def test_trained_network_beats_dfs_order(engine):
+    from pca_gb300.guided import ValueOrder, build_dataset, train
+    from pca_gb300.valuenet import ValueNet
+    ds, used = build_dataset(engine, taskgen.synthetic_batch(1500, seed=101), max_depth=4, seed=1)
+    assert used > 50
+    net = ValueNet(seed=0, lr=1e-3, pos_weight=8.0)
+    losses = train(net, ds, epochs=6)
+    assert losses[-1] < losses[0]
+    vo = ValueOrder(net, min_states=1)
+    frac_dfs, frac_val = [], []
+    for task in pick(engine, 202, 800, (3, 4))[:24]:
+        a = engine.solve_ordered(task, lambda v: None, chunk=256, max_depth=4, split_depth=2)
+        b = engine.solve_ordered(task, vo, chunk=256, max_depth=4, split_depth=2)
+        assert a.optimal_depth == b.optimal_depth
+        frac_dfs.append(a.prefixes_to_first / a.prefixes_at_optimal)
+        frac_val.append(b.prefixes_to_first / b.prefixes_at_optimal)
+    assert sum(frac_val) < 0.5 * sum(frac_dfs)

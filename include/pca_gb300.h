@@ -174,8 +174,11 @@ typedef struct {
     int oep_mode;       /* PCAGB_OEP_*                                       */
     int count_levels;   /* 1: build every level up to K with OEP so that the
                            reference's per-depth counters are reproduced     */
-    int first_only;     /* 1: stop IDDFS at the first depth with a solution
-                           and keep only the first solution in DFS order     */
+    int first_only;     /* 1: return only the first optimal program in DFS
+                           order; the split level is then chosen by the
+                           engine's autotuner (the answer does not depend on
+                           it). 0: every program found at the optimal depth
+                           from the deepest level that fits                  */
     int reserved[6];
 } pcagb_opts_t;
 

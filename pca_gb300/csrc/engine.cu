@@ -122,6 +122,11 @@ struct pcagb_engine {
     uint64_t h2d = 0, d2h = 0;
     uint64_t insert_launches = 0, suffix_launches = 0, insert_children = 0;
     float ms_insert = 0;
+    /* autotuner: unit costs measured on this engine (running averages) */
+    double t_child_ms = 2.5e-7;     /* device ms per child of a level build */
+    double t_build_fixed_ms = 0.3;  /* device ms of a level build's fixed part */
+    double t_eval_ms = 4.0e-9;      /* device ms per value-class evaluation */
+    double dedup_ratio = 0.35;      /* survivors / children of the last build */
 
     /* per batch */
     std::vector<Level> levels;
@@ -340,6 +345,13 @@ int build_level(pcagb_engine *e, int d)
     cudaEventElapsedTime(&ms, e->ev0, e->ev1);
     e->ms_expand += ms;
     e->top = top0;
+    if (children > 100000) {
+        const double per = std::max(0.0, (ms - e->t_build_fixed_ms) / (double)children);
+        e->t_child_ms = 0.7 * e->t_child_ms + 0.3 * per;
+        if (!e->no_oep) e->dedup_ratio = 0.7 * e->dedup_ratio + 0.3 * ((double)survivors / children);
+    } else if (children > 0) {
+        e->t_build_fixed_ms = 0.7 * e->t_build_fixed_ms + 0.3 * ms;
+    }
     e->levels.push_back(std::move(C));
     return PCAGB_OK;
 }
@@ -445,6 +457,22 @@ int run_stage(pcagb_engine *e, int S, int K, std::vector<TaskRun> &runs, bool fi
     cudaEventElapsedTime(&ms, e->ev0, e->ev1);
     e->ms_suffix += ms;
     e->suffix_launches++;
+    if (s >= 1 && !(so && so->stop_at_first)) {
+        /* value-class evaluations of this stage, for the autotuner */
+        std::vector<uint64_t> g(128);
+        for (int m = 0; m < 128; m++) g[m] = gt.nvc(m);
+        for (int step = 1; step < s; step++) {
+            std::vector<uint64_t> g2(128, 0);
+            for (int m = 0; m < 128; m++)
+                for (uint32_t i = gt.cand_off[m]; i < gt.cand_off[m + 1]; i++)
+                    g2[m] += g[(m | (1u << (UOP_RD(gt.cand_uop[i]) - 1))) & 127];
+            g.swap(g2);
+        }
+        uint64_t evals = 0;
+        for (size_t i = 0; i < L.hist.size(); i++) evals += L.hist[i] * g[i & 127];
+        if (evals > 10000000ull)
+            e->t_eval_ms = 0.7 * e->t_eval_ms + 0.3 * (ms / (double)evals);
+    }
     if (!nrec) return PCAGB_OK;
 
     /* Fetch the records (or, for one task in first-only mode, just the
@@ -632,6 +660,69 @@ uint64_t hist_sum(const Level &L, int t, const std::vector<uint64_t> &weight)
    depth limit reached), before the batch ends. */
 typedef void (*done_fn)(int task, void *user);
 
+/* Split-depth autotuner (first-only solves: the DFS-first optimal program
+ * is the same whatever level the stage starts from, so the choice changes
+ * the work, never the answer). The stage at depth K can start from any level S in
+ * [K-3, K-1]; levels deeper than the ones built cost a build each (children
+ * x measured ms per child + a fixed part), shrink the suffix work by the
+ * measured dedup ratio, and are reused by later depths. The predicted
+ * device time of each S is
+ *   builds(D+1..S) + evals(S, K-S) x ms per evaluation,
+ * with evals of a level not built yet extrapolated from the deepest built
+ * level D: evals(S, K-S) ~ evals(D, K-D) x dedup_ratio^(S-D). The cheapest
+ * S within the HBM budget (max_feasible) wins. */
+int autotune_split(pcagb_engine *e, int K, const std::vector<uint8_t> &active)
+{
+    const GenTables &gt = gen_tables();
+    const int D = (int)e->levels.size() - 1;
+    const int hi = std::min(K - 1, e->max_feasible);
+    const int lo = std::max(0, K - 3);
+    if (hi <= D) return std::max(hi, lo);
+    auto evals_from = [&](int S, int s) {
+        std::vector<uint64_t> g(128);
+        for (int m = 0; m < 128; m++) g[m] = gt.nvc(m);
+        for (int step = 1; step < s; step++) {
+            std::vector<uint64_t> g2(128, 0);
+            for (int m = 0; m < 128; m++)
+                for (uint32_t i = gt.cand_off[m]; i < gt.cand_off[m + 1]; i++)
+                    g2[m] += g[(m | (1u << (UOP_RD(gt.cand_uop[i]) - 1))) & 127];
+            g.swap(g2);
+        }
+        double ev = 0;
+        const Level &L = e->levels[S];
+        for (size_t i = 0; i < L.hist.size(); i++)
+            if (active[i >> 7]) ev += (double)L.hist[i] * g[i & 127];
+        return ev;
+    };
+    auto children_of = [&](int S) {
+        double c = 0;
+        const Level &L = e->levels[S];
+        for (size_t i = 0; i < L.hist.size(); i++)
+            if (active[i >> 7]) c += (double)L.hist[i] * gt.nc((int)(i & 127));
+        return c;
+    };
+    int best = -1;
+    double best_ms = 1e300;
+    for (int S = std::max(lo, 0); S <= hi; S++) {
+        if (K - S > 3) continue;
+        double ms;
+        if (S <= D) {
+            ms = evals_from(S, K - S) * e->t_eval_ms;
+        } else {
+            /* build D+1..S from D, then the suffix from S */
+            double kids = children_of(D), build = 0, states_scale = 1.0;
+            for (int d = D + 1; d <= S; d++) {
+                build += kids * e->t_child_ms + e->t_build_fixed_ms;
+                states_scale *= e->dedup_ratio;
+                kids *= e->dedup_ratio * 800.0;  /* ~children per state deeper down */
+            }
+            ms = build + evals_from(D, K - D) * states_scale * e->t_eval_ms;
+        }
+        if (ms < best_ms) { best_ms = ms; best = S; }
+    }
+    return best < 0 ? std::max(hi, lo) : best;
+}
+
 /* Core batched IDDFS shared by every solve entry point. */
 struct OrderSpec {
     pcagb_order_cb cb = nullptr;
@@ -783,6 +874,7 @@ int run_batch(pcagb_engine *e, std::vector<TaskRun> &runs, const pcagb_opts_t &o
         CK(e_copy(e, e->d_task_active, active.data(), nt, cudaMemcpyHostToDevice, e->stream));
         int S_target = o.count_levels ? K : K - 1;
         if (o.split_depth >= 0) S_target = std::min(S_target, o.split_depth);
+        else if (o.first_only && !o.count_levels) S_target = autotune_split(e, K, active);
         while ((int)e->levels.size() - 1 < S_target &&
                (int)e->levels.size() - 1 < e->max_feasible) {
             const int d = (int)e->levels.size() - 1;
@@ -1015,7 +1107,7 @@ int emit_solutions(const task_spec_t *task, const pcagb_opts_t &o, TaskRun &tr,
     }
     int stored = 0;
     for (const RawSol &s : sols) {
-        if (stored >= sol_cap || !sol_progs) break;
+        if (stored >= sol_cap || !sol_progs || (o.first_only && stored == 1)) break;
         uint16_t prog[16] = {0};
         int n = 0;
         for (int i = 0; i < task->num_inputs; i++)

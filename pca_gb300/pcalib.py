@@ -361,7 +361,7 @@ class Engine:
         return sol
 
     def solve_batch(self, tasks, max_depth=4, oep_mode=OEP_EXACT_LIVE, split_depth=-1,
-                    count_levels=False, sol_cap=64, on_done=None):
+                    count_levels=False, sol_cap=64, on_done=None, first_only=False):
         """Solve many tasks in shared launches; returns one Solution per task
         (its `seconds` is that task's time-to-proven-optimal in the batch).
         on_done(i, Solution), if given, runs as soon as task i is decided."""
@@ -370,7 +370,7 @@ class Engine:
         o = SolveOpts()
         self.lib.pcagb_default_opts(ctypes.byref(o))
         o.max_depth, o.split_depth, o.oep_mode = max_depth, split_depth, oep_mode
-        o.count_levels = int(count_levels)
+        o.count_levels, o.first_only = int(count_levels), int(first_only)
         res = (SolveResult * n)()
         cap = max(sol_cap, 1)
         progs = (ctypes.c_uint16 * (16 * cap * n))()

@@ -7,9 +7,11 @@ request queued at that moment (up to `max_batch`) as one batch, so requests
 that arrive while others are on the GPU join the next free slot, batches on
 different slots overlap on the device, and each request's answer is
 delivered as soon as its own task is decided (pcagb_solve_batch_cb), not
-when its batch ends. A solve's state (levels, OEP tables, test order) lives
-only in its batch's arena and is keyed by task, so each result is the same
-alone and in the mix.
+when its batch ends. An answer is the task's proven optimal depth and its
+first optimal program in DFS order, which does not depend on the batch it
+ran in or the split level the engine's autotuner chose; a solve's state
+(levels, OEP tables, test order) lives only in its batch's arena and is
+keyed by task, so each result is the same alone and in the mix.
 
 `replay(trace)` drives a server from an arrival trace ((seconds, task)
 pairs, e.g. taskgen.poisson_stream) in real time and returns per-request
@@ -104,7 +106,7 @@ class Server:
                 r.done.set()
 
             eng.solve_batch([r.task for r in batch], max_depth=depth, oep_mode=self.oep_mode,
-                            sol_cap=self.sol_cap, on_done=deliver)
+                            sol_cap=self.sol_cap, on_done=deliver, first_only=True)
 
     def close(self):
         self._stop = True

@@ -25,7 +25,7 @@ def test_served_results_equal_single_solves(engine):
     # a burst: requests arriving while the slots are busy share batches
     assert len(srv.batches) < len(tr), "requests were not batched"
     for r, (_, task) in zip(reqs, tr):
-        alone = engine.solve(task, max_depth=3, sol_cap=16)
+        alone = engine.solve(task, max_depth=3, sol_cap=16, first_only=True)
         assert r.solution.optimal_depth == alone.optimal_depth
         assert r.solution.programs == alone.programs
         assert r.latency >= 0

@@ -55,6 +55,14 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--hbm-gb", type=float, default=0.0,
                     help="engine arena size in GB (0: 60%% of free HBM)")
+    ap.add_argument("--workload", default="power2",
+                    choices=["power2", "batched", "served", "guided"],
+                    help="power2: the headline solve (default); batched: 1,000 synthetic "
+                         "tasks plain vs batched; served: Poisson arrivals, served vs plain; "
+                         "guided: value-ordered vs DFS-ordered search")
+    ap.add_argument("--rate", type=float, default=50.0, help="served: arrivals per second")
+    ap.add_argument("--requests", type=int, default=200, help="served: number of requests")
+    ap.add_argument("--tasks", type=int, default=1000, help="batched: number of tasks")
     return ap.parse_args()
 
 
@@ -176,10 +184,144 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def pct(xs, p):
+    xs = sorted(xs)
+    if not xs:
+        return None
+    return xs[min(len(xs) - 1, max(0, int(round(p / 100.0 * len(xs) + 0.5)) - 1))]
+
+
+def run_batched(args):
+    """1,000 seeded synthetic tasks (source length 3..8, 16..32 tests, 1..2
+    inputs), proven optimal up to kernel depth 4 (or proven longer): one task
+    at a time vs shared batched launches. Metric: tasks decided per second."""
+    from pca_gb300 import taskgen
+    from pca_gb300.pcalib import Engine
+    tasks = taskgen.synthetic_batch(args.tasks, seed=7)
+    eng = Engine(0, int(args.hbm_gb * (1 << 30)))
+    eng.solve_batch(tasks[:50], max_depth=4, sol_cap=1, first_only=True)  # warm-up
+    t0 = time.perf_counter()
+    plain, plain_done = [], []
+    for t in tasks:
+        plain.append(eng.solve(t, max_depth=4, sol_cap=1, first_only=True))
+        plain_done.append(time.perf_counter() - t0)
+    t_plain = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    batched, group = [], 250
+    for g0 in range(0, len(tasks), group):
+        base = time.perf_counter() - t0
+        for sol in eng.solve_batch(tasks[g0:g0 + group], max_depth=4, sol_cap=1, first_only=True):
+            sol.seconds += base
+            batched.append(sol)
+    t_batch = time.perf_counter() - t0
+    same = all((a.optimal_depth, a.programs) == (b.optimal_depth, b.programs)
+               for a, b in zip(plain, batched))
+    cands = sum(sum(s.candidates) for s in batched)
+    hist = {}
+    for s in batched:
+        hist[s.optimal_depth] = hist.get(s.optimal_depth, 0) + 1
+    line = {"metric": "tasks proven per second (batched)", "value": len(tasks) / t_batch,
+            "unit": "tasks/s", "higher_is_better": True, "n_gpus": 1, "data": "synthetic",
+            "config": {"workload": f"{len(tasks)} synthetic tasks, source length 3-8, "
+                                   "16-32 tests, 1-2 inputs, kernel depth <= 4, groups of 250"},
+            "plain_tasks_per_s": len(tasks) / t_plain, "speedup_vs_plain": t_plain / t_batch,
+            "plain_seconds": t_plain, "batched_seconds": t_batch,
+            "time_to_proven_optimal_in_mix": {
+                "note": "per task, from the moment the whole mix is submitted",
+                "plain_mean_s": statistics.mean(plain_done), "plain_p50_s": pct(plain_done, 50),
+                "plain_p99_s": pct(plain_done, 99),
+                "batched_mean_s": statistics.mean(s.seconds for s in batched),
+                "batched_p50_s": pct([s.seconds for s in batched], 50),
+                "batched_p99_s": pct([s.seconds for s in batched], 99)},
+            "plain_solve_p50_s": pct([s.seconds for s in plain], 50),
+            "plain_solve_p99_s": pct([s.seconds for s in plain], 99),
+            "same_answers": same, "candidates_per_s": cands / t_batch,
+            "optimal_depth_histogram": {str(k): v for k, v in sorted(hist.items())}}
+    print(json.dumps(line), flush=True)
+
+
+def run_served(args):
+    """Poisson arrivals of synthetic tasks (source length mix 4:30%, 5:30%,
+    6:25%, 7:10%, 8:5%), each proven optimal up to kernel depth 4: the
+    continuous-batching server vs one task at a time."""
+    from pca_gb300 import taskgen
+    from pca_gb300.serve import SerialServer, Server, latency_summary, replay
+    trace = taskgen.poisson_stream(args.requests, rate=args.rate, seed=11)
+    out = {}
+    for name, make in (("served", lambda: Server(slots=4, max_batch=256, max_depth=4)),
+                       ("plain", lambda: SerialServer(max_depth=4))):
+        srv = make()
+        replay(srv, trace[:20])  # warm-up
+        srv.close()
+        srv = make()
+        reqs = replay(srv, trace)
+        srv.close()
+        out[name] = latency_summary(reqs)
+        out[name]["batches"] = len(srv.batches)
+    s, p = out["served"], out["plain"]
+    line = {"metric": "p99 time-to-proven-optimal (served)", "value": s["p99_s"], "unit": "s",
+            "higher_is_better": False, "n_gpus": 1, "data": "synthetic",
+            "config": {"workload": f"Poisson {args.rate:g} req/s, {args.requests} requests, "
+                                   "source length mix 4-8, kernel depth <= 4, 4 engine slots"},
+            "served": s, "plain": p,
+            "p99_ratio_plain_over_served": p["p99_s"] / s["p99_s"] if s["p99_s"] else None,
+            "p50_ratio_plain_over_served": p["p50_s"] / s["p50_s"] if s["p50_s"] else None}
+    print(json.dumps(line), flush=True)
+
+
+def run_guided(args):
+    """The value network trained on the solver's own labels, then the
+    optimal depth searched in value order vs DFS order on held-out tasks:
+    fraction of the optimal depth's prefixes visited before the first
+    correct program, and device time to it."""
+    import torch
+    from pca_gb300 import taskgen
+    from pca_gb300.guided import RandomOrder, ValueOrder, build_dataset, train
+    from pca_gb300.pcalib import Engine
+    from pca_gb300.valuenet import ValueNet
+    eng = Engine(0, int(args.hbm_gb * (1 << 30)))
+    t0 = time.perf_counter()
+    ds, used = build_dataset(eng, taskgen.synthetic_batch(3000, seed=101), max_depth=4, seed=1)
+    t_label = time.perf_counter() - t0
+    net = ValueNet(seed=0, lr=1e-3, pos_weight=8.0)
+    t0 = time.perf_counter()
+    losses = train(net, ds, epochs=10)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    ev = taskgen.synthetic_batch(2000, seed=202)
+    sols = eng.solve_batch(ev, max_depth=4, sol_cap=1, first_only=True)
+    sel = [t for t, s in zip(ev, sols) if s.optimal_depth in (3, 4)]
+    vo = ValueOrder(net, min_states=1)
+    res = {"dfs": [], "random": [], "value": []}
+    for t in sel:
+        for name, fn in (("dfs", lambda v: None), ("random", RandomOrder(1)), ("value", vo)):
+            s = eng.solve_ordered(t, fn, chunk=256, max_depth=4, split_depth=2)
+            res[name].append((s.prefixes_to_first / max(s.prefixes_at_optimal, 1), s.ms_to_first,
+                              s.seconds))
+    summ = {k: {"mean_fraction_to_first": statistics.mean(a[0] for a in v),
+                "median_fraction_to_first": statistics.median(a[0] for a in v),
+                "mean_ms_to_first": statistics.mean(a[1] for a in v),
+                "mean_solve_s": statistics.mean(a[2] for a in v)} for k, v in res.items()}
+    line = {"metric": "prefixes visited before the first correct program (value order / DFS)",
+            "value": summ["value"]["mean_fraction_to_first"] / summ["dfs"]["mean_fraction_to_first"],
+            "unit": "ratio", "higher_is_better": False, "n_gpus": 1, "data": "synthetic",
+            "config": {"workload": f"{len(sel)} held-out synthetic tasks with optimal kernel depth "
+                                   "3-4, split level 2, 256 prefixes per chunk",
+                       "train_tasks_used": used, "train_states": ds.n,
+                       "params": net.n_params(), "epochs": 10},
+            "label_seconds": t_label, "train_seconds": t_train, "train_loss": losses,
+            "orders": summ, "value_scoring_ms_total": vo.score_ms}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload != "power2":
+        from pca_gb300.build import build_engine
+        build_engine()
+        return {"batched": run_batched, "served": run_served, "guided": run_guided}[args.workload](args)
     rank, world, local = dist_env()
     import torch
     from pca_gb300.build import build_engine

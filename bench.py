@@ -206,15 +206,19 @@ def run_batched(args):
         plain.append(eng.solve(t, max_depth=4, sol_cap=1, first_only=True))
         plain_done.append(time.perf_counter() - t0)
     t_plain = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    batched, group = [], 250
-    for g0 in range(0, len(tasks), group):
-        base = time.perf_counter() - t0
-        for sol in eng.solve_batch(tasks[g0:g0 + group], max_depth=4, sol_cap=1, first_only=True):
-            sol.seconds += base
-            batched.append(sol)
-    t_batch = time.perf_counter() - t0
-    same = all((a.optimal_depth, a.programs) == (b.optimal_depth, b.programs)
+    eng.close()
+    from pca_gb300.serve import Server, replay
+    srv = Server(slots=4, max_batch=256, max_depth=4, sol_cap=1)
+    replay(srv, [(0.0, t) for t in tasks[:50]])  # warm-up
+    srv.close()
+    srv = Server(slots=4, max_batch=256, max_depth=4, sol_cap=1)
+    reqs = replay(srv, [(0.0, t) for t in tasks])
+    srv.close()
+    t_batch = max(r.finish for r in reqs) - min(r.arrival for r in reqs)
+    batched = [r.solution for r in reqs]
+    for r in reqs:
+        r.solution.seconds = r.latency
+    same = all((a.optimal_depth, a.programs[:1]) == (b.optimal_depth, b.programs[:1])
                for a, b in zip(plain, batched))
     cands = sum(sum(s.candidates) for s in batched)
     hist = {}
@@ -223,7 +227,8 @@ def run_batched(args):
     line = {"metric": "tasks proven per second (batched)", "value": len(tasks) / t_batch,
             "unit": "tasks/s", "higher_is_better": True, "n_gpus": 1, "data": "synthetic",
             "config": {"workload": f"{len(tasks)} synthetic tasks, source length 3-8, "
-                                   "16-32 tests, 1-2 inputs, kernel depth <= 4, groups of 250"},
+                                   "16-32 tests, 1-2 inputs, kernel depth <= 4, all submitted at once; "
+                                   "batched = 4 engine slots x up to 256 tasks per launch"},
             "plain_tasks_per_s": len(tasks) / t_plain, "speedup_vs_plain": t_plain / t_batch,
             "plain_seconds": t_plain, "batched_seconds": t_batch,
             "time_to_proven_optimal_in_mix": {
@@ -270,10 +275,12 @@ def run_served(args):
 
 
 def run_guided(args):
-    """The value network trained on the solver's own labels, then the
-    optimal depth searched in value order vs DFS order on held-out tasks:
-    fraction of the optimal depth's prefixes visited before the first
-    correct program, and device time to it."""
+    """The value network trained on the solver's own labels, then held-out
+    tasks solved by the plain engine (the whole optimal-depth stage) and by
+    ordered solves (DFS, random and value order, 256 prefixes per launch,
+    stopping at the first launch with a correct program): time to proven
+    optimal and the fraction of the optimal depth's prefixes visited before
+    the first correct program."""
     import torch
     from pca_gb300 import taskgen
     from pca_gb300.guided import RandomOrder, ValueOrder, build_dataset, train
@@ -291,26 +298,47 @@ def run_guided(args):
     ev = taskgen.synthetic_batch(2000, seed=202)
     sols = eng.solve_batch(ev, max_depth=4, sol_cap=1, first_only=True)
     sel = [t for t, s in zip(ev, sols) if s.optimal_depth in (3, 4)]
-    vo = ValueOrder(net, min_states=1)
-    res = {"dfs": [], "random": [], "value": []}
+    vo = ValueOrder(net)
+    orders = (("dfs", lambda v: None), ("random", RandomOrder(1)), ("value", vo),
+              ("value_every_stage", ValueOrder(net, min_states=1, gain=0.0)))
+    for t in sel[:3]:  # warm-up (lazy kernel loading)
+        eng.solve(t, max_depth=4, sol_cap=1, first_only=True)
+        for name, fn in orders:
+            eng.solve_ordered(t, fn, chunk=256, max_depth=4, split_depth=2)
+    vo.score_ms = 0.0
+    res = {"plain": [], "dfs": [], "random": [], "value": [], "value_every_stage": []}
     for t in sel:
-        for name, fn in (("dfs", lambda v: None), ("random", RandomOrder(1)), ("value", vo)):
+        p = eng.solve(t, max_depth=4, sol_cap=1, first_only=True)
+        res["plain"].append((1.0, None, p.seconds))
+        for name, fn in orders:
             s = eng.solve_ordered(t, fn, chunk=256, max_depth=4, split_depth=2)
+            assert s.optimal_depth == p.optimal_depth
             res[name].append((s.prefixes_to_first / max(s.prefixes_at_optimal, 1), s.ms_to_first,
                               s.seconds))
-    summ = {k: {"mean_fraction_to_first": statistics.mean(a[0] for a in v),
-                "median_fraction_to_first": statistics.median(a[0] for a in v),
-                "mean_ms_to_first": statistics.mean(a[1] for a in v),
-                "mean_solve_s": statistics.mean(a[2] for a in v)} for k, v in res.items()}
-    line = {"metric": "prefixes visited before the first correct program (value order / DFS)",
-            "value": summ["value"]["mean_fraction_to_first"] / summ["dfs"]["mean_fraction_to_first"],
-            "unit": "ratio", "higher_is_better": False, "n_gpus": 1, "data": "synthetic",
+    summ = {}
+    for k, v in res.items():
+        summ[k] = {"mean_fraction_to_first": statistics.mean(a[0] for a in v),
+                   "median_fraction_to_first": statistics.median(a[0] for a in v),
+                   "mean_time_to_proven_optimal_s": statistics.mean(a[2] for a in v),
+                   "median_time_to_proven_optimal_s": statistics.median(a[2] for a in v)}
+        if k != "plain":
+            summ[k]["mean_ms_to_first_in_optimal_stage"] = statistics.mean(a[1] for a in v)
+    plain_t = summ["plain"]["mean_time_to_proven_optimal_s"]
+    for k in ("dfs", "random", "value", "value_every_stage"):
+        summ[k]["speedup_vs_plain"] = plain_t / summ[k]["mean_time_to_proven_optimal_s"]
+    line = {"metric": "time-to-proven-optimal, plain engine / value-ordered (mean over tasks)",
+            "value": summ["value"]["speedup_vs_plain"],
+            "unit": "x", "higher_is_better": True, "n_gpus": 1, "data": "synthetic",
+            "prefixes_before_first_value_over_dfs":
+                summ["value_every_stage"]["mean_fraction_to_first"]
+                / summ["dfs"]["mean_fraction_to_first"],
             "config": {"workload": f"{len(sel)} held-out synthetic tasks with optimal kernel depth "
-                                   "3-4, split level 2, 256 prefixes per chunk",
+                                   "3-4; ordered solves from split level 2, first launch 256 "
+                                   "prefixes, doubling",
                        "train_tasks_used": used, "train_states": ds.n,
                        "params": net.n_params(), "epochs": 10},
             "label_seconds": t_label, "train_seconds": t_train, "train_loss": losses,
-            "orders": summ, "value_scoring_ms_total": vo.score_ms}
+            "orders": summ, "value_scoring_ms_per_task": vo.score_ms / max(len(sel), 1)}
     print(json.dumps(line), flush=True)
 
 

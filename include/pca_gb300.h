@@ -269,6 +269,8 @@ typedef struct {
     const uint16_t *task_io;
     const int32_t  *task_T;
     void *stream;       /* cudaStream_t to work on */
+    double est_stage_ms; /* the engine's estimate of the whole stage's device time
+                            (evaluations x measured ms per evaluation) */
 } pcagb_level_view_t;
 
 /* Returns a device array of uint32 holding a permutation of 0..n-1 (the
@@ -277,8 +279,9 @@ typedef struct {
 typedef const uint32_t *(*pcagb_order_cb)(const pcagb_level_view_t *view, void *user);
 
 /* Solve with the suffix stages visiting prefixes in an order chosen by the
- * callback (e.g. by a value network) in chunks of `chunk` prefixes, and
- * stopping at the first chunk of the optimal depth that holds a solution.
+ * callback (e.g. by a value network) in launches of `chunk` prefixes,
+ * doubling after each launch that finds nothing, and stopping at the first
+ * launch of the optimal depth that holds a solution.
  * Exact: every depth below the optimum is still searched completely, so the
  * optimal depth is proven; only the order of work at the optimal depth
  * changes (its programs are those of the visited chunks). */

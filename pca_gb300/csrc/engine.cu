@@ -21,6 +21,7 @@
  * grow from the bottom, per-expansion scratch (hash table, bitmap, scan
  * buffers) from the top, so a solve performs no cudaMalloc.
  */
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -378,9 +379,9 @@ struct TaskRun {
 };
 
 /* Visiting order of a suffix stage: a permutation of the level's prefixes
- * (null = DFS order), processed `chunk` prefixes per launch; with
- * stop_at_first the stage ends after the first launch that found a
- * solution. Reports how far it got. */
+ * (null = DFS order), processed `chunk` prefixes in the first launch and
+ * twice as many in each next one; with stop_at_first the stage ends after
+ * the first launch that found a solution. Reports how far it got. */
 struct StageOrder {
     const uint32_t *order = nullptr;
     uint64_t chunk = 0;
@@ -417,8 +418,11 @@ int run_stage(pcagb_engine *e, int S, int K, std::vector<TaskRun> &runs, bool fi
         const uint32_t chunk = s == 1 ? 1 : s == 2 ? 16 : 1;
         const uint32_t cpp =
             s == 1 ? 1 : std::max(1u, (uint32_t)((ncmax + chunk - 1) / chunk));
-        const uint64_t step = so && so->chunk ? so->chunk : std::max<uint64_t>(L.n, 1);
-        for (uint64_t b0 = 0; b0 < L.n; b0 += step) {
+        /* ordered stages start with `chunk` prefixes per launch and double
+           it after every launch without a solution, so a stage that has to
+           be searched completely takes O(log n) launches */
+        uint64_t step = so && so->chunk ? so->chunk : std::max<uint64_t>(L.n, 1);
+        for (uint64_t b0 = 0; b0 < L.n; b0 += step, step = so && so->chunk ? step * 2 : step) {
             const PrefixRange R{so ? so->order : nullptr, b0, std::min(step, L.n - b0)};
             if (s == 1) {
                 if (t16) k_suffix<16, 1><<<g, kThreads, 0, e->stream>>>(view(L), e->td, sb, 1, 1, R);
@@ -723,6 +727,74 @@ int autotune_split(pcagb_engine *e, int K, const std::vector<uint8_t> &active)
     return best < 0 ? std::max(hi, lo) : best;
 }
 
+typedef CUresult (*AddressRangeFn)(CUdeviceptr *, size_t *, CUdeviceptr);
+
+AddressRangeFn address_range_fn()
+{
+    static AddressRangeFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuMemGetAddressRange", &p, 12000, cudaEnableDefault,
+                                             &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (AddressRangeFn)p;
+    });
+    return fn;
+}
+
+/* An order callback's array must be device memory of this engine's GPU
+ * holding n uint32 values that form a permutation of 0..n-1: anything else
+ * would skip prefixes (a depth left unproven) or index outside the level. */
+int validate_order(pcagb_engine *e, const uint32_t *order, uint64_t n)
+{
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, order) != cudaSuccess ||
+        (a.type != cudaMemoryTypeDevice && a.type != cudaMemoryTypeManaged) ||
+        a.device != e->device) {
+        cudaGetLastError();
+        set_err("order callback returned %p: not device memory of GPU %d", (const void *)order,
+                e->device);
+        return PCAGB_EINVAL;
+    }
+    if (AddressRangeFn fn = address_range_fn()) {
+        CUdeviceptr base = 0;
+        size_t size = 0;
+        const CUdeviceptr p = (CUdeviceptr)(uintptr_t)order;
+        if (fn(&base, &size, p) != CUDA_SUCCESS || p + n * sizeof(uint32_t) > base + size) {
+            set_err("order callback returned an array shorter than the level (%llu prefixes)",
+                    (unsigned long long)n);
+            return PCAGB_EINVAL;
+        }
+    }
+    const size_t saved = e->top;
+    unsigned long long *bad = (unsigned long long *)e->alloc_top(sizeof(unsigned long long));
+    uint32_t *seen = (uint32_t *)e->alloc_top(((n + 31) / 32) * sizeof(uint32_t));
+    if (!bad || !seen) {
+        e->top = saved;
+        set_err("arena exhausted checking an order");
+        return PCAGB_ENOMEM;
+    }
+    CK(cudaMemsetAsync(bad, 0, sizeof *bad, e->stream));
+    CK(cudaMemsetAsync(seen, 0, ((n + 31) / 32) * sizeof(uint32_t), e->stream));
+    k_check_perm<<<e->grid(4), 256, 0, e->stream>>>(order, n, seen, bad);
+    int rc = check_launch(e);
+    unsigned long long nbad = 0;
+    if (!rc) {
+        CK(e_copy(e, &nbad, bad, sizeof nbad, cudaMemcpyDeviceToHost, e->stream));
+        CK(cudaStreamSynchronize(e->stream));
+    }
+    e->top = saved;
+    if (rc) return rc;
+    if (nbad) {
+        set_err("order callback returned no permutation of the %llu prefixes (%llu bad entries)",
+                (unsigned long long)n, nbad);
+        return PCAGB_EINVAL;
+    }
+    return PCAGB_OK;
+}
+
 /* Core batched IDDFS shared by every solve entry point. */
 struct OrderSpec {
     pcagb_order_cb cb = nullptr;
@@ -920,9 +992,17 @@ int run_batch(pcagb_engine *e, std::vector<TaskRun> &runs, const pcagb_opts_t &o
         StageOrder so;
         StageOrder *sop = nullptr;
         if (ord && s >= 1) {
+            double evals = 0;
+            for (int i = 0; i < nt; i++)
+                if (active[i]) evals += (double)runs[i].res.evaluations[K];
             pcagb_level_view_t lv{LS.regs, LS.flags, LS.live, LS.task, LS.n, e->TPC, S, K, nt,
-                                  e->d_task_io, e->d_task_T, (void *)e->stream};
+                                  e->d_task_io, e->d_task_T, (void *)e->stream,
+                                  evals * e->t_eval_ms};
             so.order = ord->cb ? ord->cb(&lv, ord->user) : nullptr;
+            if (so.order) {
+                const int vrc = validate_order(e, so.order, LS.n);
+                if (vrc) return vrc;
+            }
             so.chunk = ord->chunk;
             so.stop_at_first = true;
             sop = &so;

@@ -587,6 +587,23 @@ __device__ __forceinline__ void scan_last(const WarpState<TPC> &ws, int T,
 /* A contiguous range of prefixes, optionally through a permutation: the
  * suffix kernel visits prefixes order[begin .. begin + count) (or begin ..
  * begin + count when order is null). */
+/* Counts entries of order[0..n) that are >= n or repeat an earlier value
+ * (seen: zeroed bitmap of n bits). Zero means order is a permutation. */
+__global__ void k_check_perm(const uint32_t *order, uint64_t n, uint32_t *seen,
+                             unsigned long long *bad)
+{
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t v = order[i];
+        if (v >= n) {
+            atomicAdd(bad, 1ull);
+            continue;
+        }
+        const uint32_t bit = 1u << (v & 31);
+        if (atomicOr(&seen[v >> 5], bit) & bit) atomicAdd(bad, 1ull);
+    }
+}
+
 struct PrefixRange {
     const uint32_t *order;
     uint64_t begin, count;
@@ -612,6 +629,7 @@ k_suffix(LevelDev P, TaskDev task, SolBuf S, uint32_t chunks_per_prefix, uint32_
         const uint64_t qi = it / chunks_per_prefix;
         const uint32_t ck = (uint32_t)(it - qi * chunks_per_prefix);
         const uint64_t q = R.order ? (uint64_t)R.order[R.begin + qi] : R.begin + qi;
+        if (q >= P.n) continue;  /* orders are checked on the host; never index outside */
         const uint32_t tid = P.task[q];
         if (!task.active[tid]) continue;
         if (tid != cur_task) {

@@ -1,0 +1,579 @@
+/*
+ * valuenet_tc.cu -- the value network's per-test encoder on the fifth-
+ * generation tensor cores (tcgen05 + TMEM + TMA), fused from the level's
+ * states to the pooled state vector.
+ *
+ * One persistent CTA per SM walks tiles of 128 feature rows (4 states x 32
+ * test rows). Roles: warp 0 streams the weights by TMA (256 x 64 bf16 slabs
+ * of W1 then W2, 128-byte swizzle) through a 3-stage ring; warp 1 owns TMEM
+ * and one of its threads issues tcgen05.mma (M=128, N=256, K=16, BF16 in,
+ * FP32 accumulate); warps 2..17 are the epilogue, four per TMEM lane quarter
+ * (one state), each owning 64 of the 256 units. Per tile:
+ *   features  the 176 bit features of each (state, test) row (the columns
+ *             of k_features in valuenet.cu), expanded to BF16 in registers
+ *             straight into the swizzled K-major operand A1;
+ *   layer E1  A1 x W1^T into TMEM columns 0..255;
+ *   epi 1     tcgen05.ld, + bias, ReLU and BF16 rounding in one packed
+ *             convert, into the operand A2 (swizzled, K-major);
+ *   layer E2  A2 x W2^T into TMEM columns 256..511;
+ *   epi 2     the same on E2's accumulators, written back over the warp's
+ *             own part of A2, then pooled: each lane sums (fp32, tests in
+ *             order) and maxes (packed bf16) 2 units over the task's T test
+ *             rows and writes P[528] = mean(256) | max(256) | live bits(8) |
+ *             depth | zeros -- the same values as k_pool on the same H2.
+ * A1 and A2 are separate buffers, so the next tile's features and E1 run on
+ * the tensor core while the epilogue finishes the current tile's E2.
+ * The activations X, H1 and H2 never reach HBM: per state the kernel reads
+ * the level record (17 x T bytes) and writes 1,056 bytes; the weights (224
+ * KB) are re-read from L2 once per tile.
+ *
+ * Synchronisation is by mbarriers only; every wait is bounded by the global
+ * timer (kWaitNs). A wait that runs out sets the CTA's abort flag and the
+ * status word, every role leaves its loop, the producer waits for its own
+ * TMA copies, the MMA thread waits for its own MMAs, and TMEM is freed
+ * before the CTA returns.
+ */
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <mutex>
+
+#include "../../include/pca_gb300.h"
+
+namespace {
+
+constexpr int kRows = 128;            /* feature rows per tile */
+constexpr int kStatesPerTile = 4;
+constexpr int kUnits = 256;           /* N of both encoder layers */
+constexpr int kFeat = 176;            /* feature columns (164 used) */
+constexpr int kKB1 = 3, kKB2 = 4;     /* 64-column K blocks of E1 (176 -> 192) and E2 */
+constexpr int kSlabs = kKB1 + kKB2;   /* weight slabs per tile */
+constexpr int kStages = 3;
+constexpr int kEpiWarps = 16;
+constexpr int kEpiThreads = 32 * kEpiWarps;
+constexpr int kThreads = 64 + kEpiThreads; /* warp 0 TMA, warp 1 MMA + TMEM, 2..17 epilogue */
+constexpr int kABlock = kRows * 128;  /* 16 KB: 128 rows x 64 bf16 */
+constexpr int kWBlock = kUnits * 128; /* 32 KB: 256 rows x 64 bf16 */
+constexpr int kOffA1 = 0;                             /* 48 KB */
+constexpr int kOffA2 = kOffA1 + kKB1 * kABlock;       /* 64 KB */
+constexpr int kOffW = kOffA2 + kKB2 * kABlock;        /* 96 KB */
+constexpr int kOffBias = kOffW + kStages * kWBlock;   /* 2 x 256 fp32 */
+constexpr int kOffBar = kOffBias + 2 * kUnits * 4;
+constexpr int kSmemBytes = kOffBar + 256 + 1024;      /* + alignment slack */
+constexpr int kPoolCols = 528;
+constexpr unsigned long long kWaitNs = 1000000000ull; /* 1 s per wait */
+static_assert(kOffA2 % 1024 == 0 && kOffW % 1024 == 0, "swizzle atoms need 1024-byte alignment");
+static_assert(kSmemBytes <= 227 * 1024, "shared memory");
+
+/* barrier slots (8 bytes each) */
+constexpr int kBarWFull = 0, kBarWEmpty = kStages, kBarA1 = 2 * kStages, kBarA2 = kBarA1 + 1,
+              kBarD1 = kBarA1 + 2, kBarD2 = kBarA1 + 3, kBarDrain = kBarA1 + 4,
+              kBarCount = kBarA1 + 5;
+constexpr int kOffTmemSlot = kBarCount * 8;
+constexpr int kOffAbort = kOffTmemSlot + 4;
+static_assert(kOffAbort + 4 <= 256, "barrier area");
+
+/* Instruction descriptor of tcgen05.mma kind::f16: D f32 (bits 4-5 = 1),
+   A and B bf16 (bits 7-9, 10-12 = 1), both K-major, N >> 3 at bits 17-22,
+   M >> 4 at bits 24-28. */
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kUnits >> 3) << 17) |
+                            ((uint32_t)(kRows >> 4) << 24);
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p)
+{
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_test(uint32_t bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+/* Wait for the phase of `parity` to complete, at most kWaitNs; on time-out
+   (or an abort raised elsewhere) set the abort flag and return false. */
+__device__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int *abort_flag, int *status,
+                          int code)
+{
+    const unsigned long long t0 = global_ns();
+    for (uint32_t i = 0;; i++) {
+        if (mbar_test(bar, parity)) return true;
+        if ((i & 15) == 15) {
+            if (*abort_flag) return false;
+            if (global_ns() - t0 > kWaitNs) {
+                *abort_flag = 1;
+                atomicExch(status, code);
+                return false;
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ void fence_async_smem()
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void tc_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, uint32_t bar,
+                                            int x, int y)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes "
+        "[%0], [%1, {%3, %4}], [%2];" ::"r"(dst),
+        "l"((uint64_t)map), "r"(bar), "r"(x), "r"(y)
+        : "memory");
+}
+
+/* Shared-memory matrix descriptor: K-major operand in 128-byte swizzle
+   atoms (8 rows x 128 B), 8-row groups 1024 B apart. */
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr)
+{
+    uint64_t d = (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)1 << 16;            /* leading byte offset: unused for swizzled K-major */
+    d |= (uint64_t)(1024 >> 4) << 32;  /* stride byte offset */
+    d |= (uint64_t)1 << 46;            /* descriptor version */
+    d |= (uint64_t)2 << 61;            /* 128-byte swizzle */
+    return d;
+}
+
+__device__ __forceinline__ void mma_f16(uint32_t dtmem, uint64_t a, uint64_t b, uint32_t acc)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(dtmem),
+        "l"(a), "l"(b), "r"(kIdesc), "r"(acc)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar)
+{
+    asm volatile(
+        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+        : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32])
+{
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+          "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
+          "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
+          "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+/* Byte offset of 16-byte chunk c (0..7) of row r in a 128-byte-swizzled
+   block (the layout TMA's 128B swizzle writes and the descriptor reads). */
+__device__ __forceinline__ uint32_t sw128_off(int r, int c)
+{
+    return (uint32_t)(r * 128 + ((c ^ (r & 7)) << 4));
+}
+
+/* 8 bits of b as 8 bf16 values 0.0 / 1.0 (bit 0 first): bit 2j selects
+   0x3F80 in the low half of word j, bit 2j+1 0x3F80 in the high half. */
+__device__ __forceinline__ uint4 bits_to_bf16x8(uint32_t b)
+{
+    uint32_t w[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        const uint32_t t = b >> (2 * j);
+        w[j] = (t & 1u) * 0x3F80u + (t & 2u) * 0x1FC00000u;
+    }
+    return make_uint4(w[0], w[1], w[2], w[3]);
+}
+
+/* relu(lo), relu(hi) rounded to bf16, lo in the low half. */
+__device__ __forceinline__ uint32_t relu_bf16x2(float lo, float hi)
+{
+    uint32_t d;
+    asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(hi), "f"(lo));
+    return d;
+}
+
+__device__ __forceinline__ uint32_t max_bf16x2(uint32_t a, uint32_t b)
+{
+    uint32_t d;
+    asm("max.bf16x2 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
+    return d;
+}
+
+__global__ void __launch_bounds__(kThreads, 1)
+k_encode_pool_tc(const __grid_constant__ CUtensorMap map_w1, const __grid_constant__ CUtensorMap map_w2,
+                 const float *__restrict__ b1, const float *__restrict__ b2,
+                 const uint16_t *__restrict__ regs, const uint8_t *__restrict__ flags,
+                 const uint8_t *__restrict__ live, const uint16_t *__restrict__ task,
+                 const uint8_t *__restrict__ depth, int TP, int n,
+                 const uint16_t *__restrict__ task_io, const int32_t *__restrict__ task_T,
+                 __nv_bfloat16 *__restrict__ P, int *status)
+{
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    const uint32_t sA1 = smem_u32(smem + kOffA1), sA2 = smem_u32(smem + kOffA2);
+    const uint32_t sW = smem_u32(smem + kOffW);
+    const uint32_t sBar = smem_u32(smem + kOffBar);
+    uint32_t *tmem_slot = (uint32_t *)(smem + kOffBar + kOffTmemSlot);
+    volatile int *abort_flag = (volatile int *)(smem + kOffBar + kOffAbort);
+    float *sb1 = (float *)(smem + kOffBias);
+    float *sb2 = sb1 + kUnits;
+    auto bar = [&](int i) { return sBar + 8u * (uint32_t)i; };
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int ntiles = (n + kStatesPerTile - 1) / kStatesPerTile;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kStages; s++) {
+            mbar_init(bar(kBarWFull + s), 1);
+            mbar_init(bar(kBarWEmpty + s), 1);
+        }
+        mbar_init(bar(kBarA1), kEpiThreads);
+        mbar_init(bar(kBarA2), kEpiThreads);
+        mbar_init(bar(kBarD1), 1);
+        mbar_init(bar(kBarD2), 1);
+        mbar_init(bar(kBarDrain), 1);
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        fence_async_smem();
+    }
+    for (int i = threadIdx.x; i < kUnits; i += kThreads) {
+        sb1[i] = b1[i];
+        sb2[i] = b2[i];
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(
+                         smem_u32(tmem_slot))
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_before();
+    __syncthreads();
+    tc_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0) {
+        /* ---- TMA producer: weight slabs through the ring ---- */
+        if (lane == 0) {
+            uint32_t j = 0;
+            bool ok = true;
+            for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+                for (int s = 0; s < kSlabs && ok; s++, j++) {
+                    const uint32_t st = j % kStages, ph = (j / kStages) & 1u;
+                    ok = mbar_wait(bar(kBarWEmpty + st), ph ^ 1u, abort_flag, status, 1);
+                    if (!ok) break;
+                    mbar_expect_tx(bar(kBarWFull + st), kWBlock);
+                    if (s < kKB1)
+                        tma_load_2d(sW + st * kWBlock, &map_w1, bar(kBarWFull + st), s * 64, 0);
+                    else
+                        tma_load_2d(sW + st * kWBlock, &map_w2, bar(kBarWFull + st),
+                                    (s - kKB1) * 64, 0);
+                }
+            }
+            /* wait for the copies this thread issued (the last one per stage) */
+            const uint32_t issued = j;
+            for (uint32_t st = 0; st < kStages && st < issued; st++) {
+                const uint32_t last = issued - 1 - ((issued - 1 - st) % kStages);
+                const unsigned long long t0 = global_ns();
+                while (!mbar_test(bar(kBarWFull + st), (last / kStages) & 1u) &&
+                       global_ns() - t0 < kWaitNs) {
+                }
+            }
+        }
+    } else if (warp == 1) {
+        /* ---- MMA issuer ---- */
+        if (lane == 0) {
+            uint32_t j = 0;
+            bool ok = true;
+            int it = 0;
+            for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x, it++) {
+                for (int layer = 0; layer < 2 && ok; layer++) {
+                    ok = mbar_wait(bar(layer ? kBarA2 : kBarA1), it & 1, abort_flag, status, 2);
+                    if (!ok) break;
+                    tc_after();
+                    const int nkb = layer ? kKB2 : kKB1;
+                    const uint32_t d = tmem + (layer ? (uint32_t)kUnits : 0u);
+                    const uint32_t a = layer ? sA2 : sA1;
+                    for (int kb = 0; kb < nkb; kb++, j++) {
+                        const uint32_t st = j % kStages, ph = (j / kStages) & 1u;
+                        ok = mbar_wait(bar(kBarWFull + st), ph, abort_flag, status, 3);
+                        if (!ok) break;
+                        tc_after();
+                        const uint32_t a0 = a + kb * kABlock, b0 = sW + st * kWBlock;
+#pragma unroll
+                        for (int k = 0; k < 4; k++)
+                            mma_f16(d, sw128_desc(a0 + 32 * k), sw128_desc(b0 + 32 * k),
+                                    (kb | k) != 0);
+                        mma_commit(bar(kBarWEmpty + st));
+                    }
+                    if (!ok) break;
+                    mma_commit(bar(layer ? kBarD2 : kBarD1));
+                }
+            }
+            /* every MMA this thread issued has finished before TMEM is freed */
+            mma_commit(bar(kBarDrain));
+            const unsigned long long t0 = global_ns();
+            while (!mbar_test(bar(kBarDrain), 0) && global_ns() - t0 < kWaitNs) {
+            }
+        }
+    } else {
+        /* ---- epilogue warps ---- */
+        const int q = warp & 3;              /* TMEM lane quarter = the tile's state */
+        const int h = (warp - 2) >> 2;       /* units [64h, 64h + 64) */
+        const int r = q * 32 + lane;         /* tile row = TMEM lane */
+        const uint32_t lane_base = (uint32_t)(q * 32) << 16;
+
+        /* A state's level record, loaded one tile ahead of its features:
+           the three 16-bit words of this warp's quarter of the feature row
+           (h = 0: in0 in1 target; 1: r1 r2 r3; 2: r4 r5 r6; 3: r7 flags 0)
+           for test `lane`, the task's T and (h = 0, lanes 0..15) the pooled
+           row's tail. The task id is loaded a tile earlier still, so no
+           load waits on another in the loop. */
+        struct Rec {
+            int s, T;
+            uint32_t w[3];
+            float g;  /* P column 512 + lane: live bit / depth / 0 */
+        };
+        auto task_of = [&](int tile) -> int {
+            const int st = tile * kStatesPerTile + q;
+            return (tile < ntiles && st < n) ? (int)task[st] : -1;
+        };
+        auto load_rec = [&](int tile, int tid, Rec &rc) {
+            rc.s = tile * kStatesPerTile + q;
+            rc.T = 0;
+            rc.g = 0.f;
+            rc.w[0] = rc.w[1] = rc.w[2] = 0;
+            if (tid < 0) return;
+            rc.T = min(task_T[tid], TP);
+            if (h == 0 && lane < 8) rc.g = (float)((live[rc.s] >> lane) & 1u);
+            else if (h == 0 && lane == 8) rc.g = (float)depth[rc.s];
+            if (lane >= TP) return;
+            const size_t s8 = (size_t)rc.s * 8;
+            if (h == 0) {
+#pragma unroll
+                for (int k = 0; k < 3; k++) rc.w[k] = task_io[((size_t)tid * 3 + k) * 32 + lane];
+            } else if (h < 3) {
+#pragma unroll
+                for (int k = 0; k < 3; k++) rc.w[k] = regs[(s8 + 3 * h - 2 + k) * TP + lane];
+            } else {
+                rc.w[0] = regs[(s8 + 7) * TP + lane];
+                rc.w[1] = flags[(size_t)rc.s * TP + lane] & 0xFu;
+            }
+        };
+        /* bit features of (state, test lane), chunks [6h, 6h + 6) of the
+           row's 24 16-byte chunks, into A1 (rows of tests >= T are zero) */
+        auto features = [&](const Rec &rc) {
+            const bool valid = lane < rc.T;
+#pragma unroll
+            for (int k = 0; k < 6; k++) {
+                const int c = 6 * h + k;
+                const uint32_t byte = valid ? (rc.w[k >> 1] >> ((k & 1) * 8)) & 0xFFu : 0u;
+                *(uint4 *)(smem + kOffA1 + (c >> 3) * kABlock + sw128_off(r, c & 7)) =
+                    bits_to_bf16x8(byte);
+            }
+            fence_async_smem();
+            mbar_arrive(bar(kBarA1));
+        };
+
+        /* accumulators of units [64h, 64h + 64) of one layer: + bias, ReLU,
+           bf16, into this warp's part of A2 */
+        auto drain = [&](uint32_t col_base, const float *bias) {
+#pragma unroll 1
+            for (int g = 0; g < 2; g++) {
+            const int col0 = 64 * h + 32 * g;
+            uint32_t acc[32];
+            tmem_ld32(tmem + col_base + lane_base + col0, acc);
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                const float4 bl = *(const float4 *)(bias + col0 + 8 * c);
+                const float4 bh = *(const float4 *)(bias + col0 + 8 * c + 4);
+                const uint32_t *a = acc + 8 * c;
+                const uint32_t w0 = relu_bf16x2(__uint_as_float(a[0]) + bl.x, __uint_as_float(a[1]) + bl.y);
+                const uint32_t w1 = relu_bf16x2(__uint_as_float(a[2]) + bl.z, __uint_as_float(a[3]) + bl.w);
+                const uint32_t w2 = relu_bf16x2(__uint_as_float(a[4]) + bh.x, __uint_as_float(a[5]) + bh.y);
+                const uint32_t w3 = relu_bf16x2(__uint_as_float(a[6]) + bh.z, __uint_as_float(a[7]) + bh.w);
+                const int chunk = (col0 >> 3) + c;
+                *(uint4 *)(smem + kOffA2 + (chunk >> 3) * kABlock + sw128_off(r, chunk & 7)) =
+                    make_uint4(w0, w1, w2, w3);
+            }
+            }
+        };
+
+        /* mean (fp32 over tests in order, as k_pool) and max of units
+           64h + 2 lane, + 1 over the state's T rows of H2 in A2 */
+        auto pool = [&](const Rec &rc) {
+            const int chunk = 8 * h + (lane >> 2);
+            const uint8_t *base = smem + kOffA2 + (chunk >> 3) * kABlock + ((lane & 3) << 2);
+            float s0 = 0.f, s1 = 0.f;
+            uint32_t m01 = 0u;                /* ReLU outputs are >= 0 */
+            for (int t0 = 0; t0 < rc.T; t0 += 8) {
+                uint32_t v[8];
+#pragma unroll
+                for (int k = 0; k < 8; k++)
+                    v[k] = *(const uint32_t *)(base + sw128_off(32 * q + t0 + k, chunk & 7));
+                const bool full = t0 + 8 <= rc.T;
+#pragma unroll
+                for (int k = 0; k < 8; k++) {
+                    const uint32_t x = (full || t0 + k < rc.T) ? v[k] : 0u;
+                    s0 += __uint_as_float(x << 16);
+                    s1 += __uint_as_float(x & 0xFFFF0000u);
+                    m01 = max_bf16x2(m01, x);
+                }
+            }
+            const float fT = (float)(rc.T > 0 ? rc.T : 1);
+            __nv_bfloat162 mean = __floats2bfloat162_rn(s0 / fT, s1 / fT);
+            __nv_bfloat16 *row = P + (size_t)rc.s * kPoolCols;
+            *(uint32_t *)(row + 64 * h + 2 * lane) = *reinterpret_cast<uint32_t *>(&mean);
+            *(uint32_t *)(row + kUnits + 64 * h + 2 * lane) = m01;
+            if (h == 0 && lane < 16) row[2 * kUnits + lane] = __float2bfloat16(rc.g);
+        };
+
+        const int G = (int)gridDim.x;
+        int it = 0;
+        int tile = blockIdx.x;
+        Rec cur, nxt;
+        load_rec(tile, task_of(tile), cur);
+        int tid_next = task_of(tile + G);
+        if (tile < ntiles) features(cur);
+        for (; tile < ntiles; tile += G, it++) {
+            /* the next tile's record, in flight while E1 drains */
+            load_rec(tile + G, tid_next, nxt);
+            tid_next = task_of(tile + 2 * G);
+            /* E1 -> A2 */
+            bool ok = mbar_wait(bar(kBarD1), it & 1, abort_flag, status, 4);
+            if (!__all_sync(0xffffffffu, ok)) break;
+            tc_after();
+            drain(0u, sb1);
+            tc_before();
+            fence_async_smem();
+            mbar_arrive(bar(kBarA2));
+            /* next tile's features while E2 runs */
+            if (tile + G < ntiles) features(nxt);
+            /* E2 -> H2 (over this warp's part of A2) -> pooling */
+            ok = mbar_wait(bar(kBarD2), it & 1, abort_flag, status, 5);
+            if (!__all_sync(0xffffffffu, ok)) break;
+            tc_after();
+            drain((uint32_t)kUnits, sb2);
+            tc_before();
+            __syncwarp();
+            if (cur.s < n) pool(cur);
+            __syncwarp();
+            cur = nxt;
+        }
+    }
+    __syncwarp();
+    tc_before();
+    __syncthreads();
+    tc_after();
+    if (warp == 1)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem)
+                     : "memory");
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn()
+{
+    static EncodeTiledFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                             &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (EncodeTiledFn)p;
+    });
+    return fn;
+}
+
+/* Tensor map of a row-major [256][K] bf16 weight, 64 x 256 boxes, 128B swizzle. */
+bool weight_map(CUtensorMap *m, const void *W, int K)
+{
+    EncodeTiledFn fn = encode_fn();
+    if (!fn) return false;
+    cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)kUnits};
+    cuuint64_t strides[1] = {(cuuint64_t)K * 2};
+    cuuint32_t box[2] = {64, (cuuint32_t)kUnits};
+    cuuint32_t estr[2] = {1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(W), dims, strides, box,
+              estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+              CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+}  // namespace
+
+extern "C" int pcagb_vnet_encode_pool_tc(const void *W1, const float *b1, const void *W2,
+                                         const float *b2, const uint16_t *regs,
+                                         const uint8_t *flags, const uint8_t *live,
+                                         const uint16_t *task, const uint8_t *depth, int TP, int n,
+                                         const uint16_t *task_io, const int32_t *task_T, void *P,
+                                         int *status, void *stream)
+{
+    if (n <= 0) return PCAGB_OK;
+    if ((TP != 16 && TP != 32) || !W1 || !W2 || !b1 || !b2 || !P || !status ||
+        ((uintptr_t)W1 & 15) || ((uintptr_t)W2 & 15))
+        return PCAGB_EINVAL;
+    CUtensorMap m1, m2;
+    if (!weight_map(&m1, W1, kFeat) || !weight_map(&m2, W2, kUnits)) return PCAGB_ECUDA;
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return PCAGB_ECUDA;
+    static std::once_flag attr_once;
+    static cudaError_t attr_err = cudaSuccess;
+    std::call_once(attr_once, [] {
+        attr_err = cudaFuncSetAttribute(k_encode_pool_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        kSmemBytes);
+    });
+    if (attr_err != cudaSuccess) return PCAGB_ECUDA;
+    const int ntiles = (n + kStatesPerTile - 1) / kStatesPerTile;
+    const int grid = ntiles < sms ? ntiles : sms;
+    k_encode_pool_tc<<<grid, kThreads, kSmemBytes, (cudaStream_t)stream>>>(
+        m1, m2, b1, b2, regs, flags, live, task, depth, TP, n, task_io, task_T,
+        (__nv_bfloat16 *)P, status);
+    return cudaGetLastError() == cudaSuccess ? PCAGB_OK : PCAGB_ECUDA;
+}

@@ -11,7 +11,8 @@ negatives.
 Ordering: at each suffix stage the engine hands the split level to
 `ValueOrder`, which scores every prefix state with the network (chunks of
 the level through the project's BF16 kernels, on the engine's stream) and
-returns the prefixes by decreasing score. The engine visits them in that
+returns the prefixes by decreasing score (the encoder runs as one fused
+tcgen05 kernel per chunk, the trunk on the pooled rows). The engine visits them in that
 order, chunk by chunk, and stops the optimal depth's stage at the first
 chunk with a correct program. Depths below the optimum are searched
 completely in any order, so the optimal depth stays proven: the network
@@ -166,13 +167,17 @@ def train(net: ValueNet, ds: Dataset, epochs=8, batch=2048, seed=0, log=None):
 class ValueOrder:
     """Order callback for Engine.solve_ordered: prefixes by decreasing
     predicted probability of finishing optimally. A level is scored once
-    (stages at several depths reuse its order); levels below `min_states`
-    keep DFS order, enumerating them costs less than scoring them."""
+    (stages at several depths reuse its order). Stages keep DFS order when
+    scoring would cost more than it can save: levels below `min_states`,
+    and stages the engine expects to finish in less than `gain` x the
+    scoring time (fixed_ms + n / states_per_ms)."""
 
-    def __init__(self, net: ValueNet, chunk_states=65536, min_states=4096):
+    def __init__(self, net: ValueNet, chunk_states=1 << 20, min_states=4096, gain=2.0,
+                 fixed_ms=0.25, states_per_ms=1.0e5):
         self.net = net
         self.chunk_states = chunk_states
         self.min_states = min_states
+        self.gain, self.fixed_ms, self.states_per_ms = gain, fixed_ms, states_per_ms
         self.score_ms = 0.0
         self._cache = {}
 
@@ -181,6 +186,9 @@ class ValueOrder:
         if n < self.min_states:
             return None
         key = (view.regs, n, view.depth)
+        if key not in self._cache and \
+                view.est_stage_ms < self.gain * (self.fixed_ms + n / self.states_per_ms):
+            return None
         if key in self._cache:
             return self._cache[key]
         dev = self.net.dev
@@ -200,11 +208,12 @@ class ValueOrder:
                 live = _device_view(view.live + b0, m, torch.uint8, dev)
                 task = _device_view(view.task + b0 * 2, m, torch.int16, dev)
                 depth = torch.full((m,), view.depth, device=dev, dtype=torch.uint8)
-                X = self.net.features(regs, flags, task, tp, task_io, task_T)
-                scores[b0:b0 + m] = self.net.forward(X, live, task, task_T, depth)[:, 0]
+                scores[b0:b0 + m] = self.net.forward_fused(regs, flags, live, task, depth, tp,
+                                                           task_io, task_T)[:, 0]
             order = torch.argsort(scores, descending=True, stable=True).to(torch.int32)
             ev1.record(stream)
         ev1.synchronize()
+        self.net.check_status()
         self.score_ms += ev0.elapsed_time(ev1)
         self._cache = {key: order}
         return order

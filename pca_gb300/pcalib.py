@@ -98,7 +98,7 @@ class LevelView(ctypes.Structure):
                 ("task", ctypes.c_void_p), ("n", ctypes.c_uint64), ("tp", ctypes.c_int),
                 ("depth", ctypes.c_int), ("target_depth", ctypes.c_int), ("ntasks", ctypes.c_int),
                 ("task_io", ctypes.c_void_p), ("task_T", ctypes.c_void_p),
-                ("stream", ctypes.c_void_p)]
+                ("stream", ctypes.c_void_p), ("est_stage_ms", ctypes.c_double)]
 
 
 ORDER_CB = ctypes.CFUNCTYPE(ctypes.c_void_p, ctypes.POINTER(LevelView), ctypes.c_void_p)
@@ -406,19 +406,34 @@ class Engine:
                       oep_mode=OEP_EXACT_LIVE, split_depth=-1, sol_cap=256) -> Solution:
         """Solve with the suffix stages visiting the split level's prefixes in
         the order order_fn(view) returns (a device tensor of uint32/int32
-        prefix indices, or None for DFS order), `chunk` prefixes per launch,
-        stopping at the first chunk of the optimal depth with a solution."""
+        prefix indices, or None for DFS order), `chunk` prefixes in the first
+        launch of a stage and twice as many in each next one, stopping at the
+        first launch of the optimal depth with a solution."""
         o = SolveOpts()
         self.lib.pcagb_default_opts(ctypes.byref(o))
         o.max_depth, o.split_depth, o.oep_mode = max_depth, split_depth, oep_mode
-        keep = []
+        keep, errors = [], []
 
         def cb(vp, _user):
-            out = order_fn(vp.contents)
-            if out is None:
+            # An exception must not cross the C boundary (ctypes would hand
+            # the engine an undefined pointer): record it, visit this stage in
+            # DFS order, and raise once the solve returns.
+            try:
+                view = vp.contents
+                out = order_fn(view)
+                if out is None:
+                    return None
+                import torch
+                if (not isinstance(out, torch.Tensor) or not out.is_cuda or out.dim() != 1
+                        or out.numel() != view.n or out.element_size() != 4
+                        or out.dtype.is_floating_point or not out.is_contiguous()):
+                    raise EngineError("order callback must return None or a contiguous 1-D "
+                                      f"int32 CUDA tensor of {view.n} prefix indices")
+                keep.append(out)
+                return out.data_ptr()
+            except BaseException as exc:  # noqa: BLE001 - re-raised after the solve
+                errors.append(exc)
                 return None
-            keep.append(out)
-            return out.data_ptr()
 
         ccb = ORDER_CB(cb)
         r = SolveResult()
@@ -426,6 +441,8 @@ class Engine:
         lens = (ctypes.c_int * max(sol_cap, 1))()
         rc = self.lib.pcagb_solve_ordered(self.h, ctypes.byref(task), ctypes.byref(o), ccb, None,
                                           chunk, ctypes.byref(r), progs, lens, sol_cap)
+        if errors:
+            raise errors[0]
         if rc != 0:
             raise EngineError(f"ordered solve failed ({rc}): {self.lib.pcagb_last_error().decode()}")
         sol = Solution(optimal_depth=r.optimal_depth, total_solutions=r.total_solutions)

@@ -41,6 +41,8 @@ def _lib():
         "pcagb_vnet_loss": [vp, vp, vp, i, f, f, vp, vp, vp],
         "pcagb_vnet_adam": [vp, vp, vp, vp, i, i, f, f, f, f, i, vp, vp, vp],
         "pcagb_vnet_to_bf16": [vp, vp, sz, vp],
+        "pcagb_vnet_encode_pool_tc": [vp, vp, vp, vp, vp, vp, vp, vp, vp, i, i, vp, vp, vp, vp,
+                                      vp],
     }
     for name, args in sigs.items():
         fn = getattr(lib, name)
@@ -73,6 +75,7 @@ class ValueNet:
             for d in (self.mb, self.vb):
                 d[name] = torch.zeros_like(self.b[name])
         self.step_n = 0
+        self._status = []
         self._refresh_bf16()
 
     @property
@@ -129,6 +132,37 @@ class ValueNet:
         L = self._gemm(Z2, "H", False, out_f32=True)
         self._acts = dict(X=X, H1=H1, H2=H2, P=P, am=am, Z1=Z1, Z2=Z2, task=task, task_T=task_T)
         return L
+
+    def encode_pool(self, regs, flags, live, task, depth, TP, task_io, task_T):
+        """Features -> E1 -> E2 -> pooling in one tcgen05 kernel (inference):
+        the pooled rows P[n][528] without X, H1 or H2 in HBM."""
+        n = task.shape[0]
+        P = torch.empty(n, 528, device=self.dev, dtype=torch.bfloat16)
+        status = torch.zeros(1, device=self.dev, dtype=torch.int32)
+        self._ck(self.lib.pcagb_vnet_encode_pool_tc(
+            _p(self.Wb["E1"]), _p(self.b["E1"]), _p(self.Wb["E2"]), _p(self.b["E2"]), _p(regs),
+            _p(flags), _p(live), _p(task), _p(depth), TP, n, _p(task_io), _p(task_T), _p(P),
+            _p(status), self.stream))
+        self._status.append(status)
+        return P
+
+    def check_status(self):
+        """Raise if a fused encoder launch gave up on a barrier wait (reads
+        the status words: synchronises with their stream)."""
+        st, self._status = self._status, []
+        for s in st:
+            v = int(s.item())
+            if v:
+                raise RuntimeError(f"fused encoder aborted (barrier wait {v} timed out)")
+
+    def trunk(self, P):
+        Z1 = self._gemm(P, "T1", True)
+        Z2 = self._gemm(Z1, "T2", True)
+        return self._gemm(Z2, "H", False, out_f32=True)
+
+    def forward_fused(self, regs, flags, live, task, depth, TP, task_io, task_T):
+        """Logits [n][16] through the fused encoder and the trunk."""
+        return self.trunk(self.encode_pool(regs, flags, live, task, depth, TP, task_io, task_T))
 
     def _wgrad(self, dY, X, name):
         out, inp = self.W[name].shape

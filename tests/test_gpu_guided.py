@@ -53,7 +53,7 @@ def test_ordered_solve_is_exact(engine, order):
     from pca_gb300.valuenet import ValueNet
     lib = PCALib()
     fn = {"dfs": lambda v: None, "random": RandomOrder(5),
-          "value": ValueOrder(ValueNet(seed=1), min_states=1)}[order]
+          "value": ValueOrder(ValueNet(seed=1), min_states=1, gain=0.0)}[order]
     for task in pick(engine, 41, 300, (3, 4))[:6]:
         plain = engine.solve(task, max_depth=4, split_depth=2, sol_cap=1 << 14)
         got = engine.solve_ordered(task, fn, chunk=64, max_depth=4, split_depth=2, sol_cap=1 << 14)
@@ -72,7 +72,7 @@ def test_trained_network_beats_dfs_order(engine):
     net = ValueNet(seed=0, lr=1e-3, pos_weight=8.0)
     losses = train(net, ds, epochs=6)
     assert losses[-1] < losses[0]
-    vo = ValueOrder(net, min_states=1)
+    vo = ValueOrder(net, min_states=1, gain=0.0)
     frac_dfs, frac_val = [], []
     for task in pick(engine, 202, 800, (3, 4))[:24]:
         a = engine.solve_ordered(task, lambda v: None, chunk=256, max_depth=4, split_depth=2)
@@ -81,3 +81,68 @@ def test_trained_network_beats_dfs_order(engine):
         frac_dfs.append(a.prefixes_to_first / a.prefixes_at_optimal)
         frac_val.append(b.prefixes_to_first / b.prefixes_at_optimal)
     assert sum(frac_val) < 0.5 * sum(frac_dfs)
+
+
+def _orders_task(engine):
+    return pick(engine, 41, 300, (3, 4))[0]
+
+
+@pytest.mark.parametrize("kind", ["duplicate", "out_of_range", "short", "float", "raises"])
+def test_bad_orders_are_refused(engine, kind):
+    """An order that is not a permutation of the level (it would skip
+    prefixes and leave a depth unproven, or index outside the level) is
+    refused before any kernel reads it; an exception in the callback comes
+    back to the caller. The engine stays usable afterwards."""
+    from pca_gb300.pcalib import EngineError
+    task = _orders_task(engine)
+
+    class Boom(Exception):
+        pass
+
+    def fn(view):
+        n = view.n
+        if kind == "raises":
+            raise Boom()
+        if kind == "short":
+            return torch.arange(max(n - 1, 0), dtype=torch.int32, device="cuda")
+        if kind == "float":
+            return torch.arange(n, dtype=torch.float32, device="cuda")
+        o = torch.arange(n, dtype=torch.int32, device="cuda")
+        if n >= 2 and kind == "duplicate":
+            o[1] = 0
+        if kind == "out_of_range":
+            o[-1] = n
+        return o
+
+    expect = Boom if kind == "raises" else EngineError
+    with pytest.raises(expect):
+        engine.solve_ordered(task, fn, chunk=64, max_depth=4, split_depth=2)
+    plain = engine.solve(task, max_depth=4, split_depth=2, sol_cap=1)
+    again = engine.solve_ordered(task, lambda v: None, chunk=64, max_depth=4, split_depth=2)
+    assert again.optimal_depth == plain.optimal_depth
+
+
+def test_host_pointer_order_is_refused(engine):
+    """Through the raw C ABI: a callback that hands back host memory is
+    refused (the engine checks the pointer's memory type and range before
+    launching anything on it)."""
+    import ctypes
+
+    import numpy as np
+
+    from pca_gb300.pcalib import ORDER_CB, SolveOpts, SolveResult
+    task = _orders_task(engine)
+    lib = engine.lib
+    host = np.arange(1 << 16, dtype=np.uint32)
+    cb = ORDER_CB(lambda vp, _u: host.ctypes.data)
+    o = SolveOpts()
+    lib.pcagb_default_opts(ctypes.byref(o))
+    o.max_depth, o.split_depth = 4, 2
+    r = SolveResult()
+    progs = (ctypes.c_uint16 * 16)()
+    lens = (ctypes.c_int * 1)()
+    rc = lib.pcagb_solve_ordered(engine.h, ctypes.byref(task), ctypes.byref(o), cb, None, 64,
+                                 ctypes.byref(r), progs, lens, 1)
+    assert rc != 0
+    assert b"not device memory" in lib.pcagb_last_error()
+    assert engine.solve(task, max_depth=4, split_depth=2, sol_cap=1).optimal_depth >= 0

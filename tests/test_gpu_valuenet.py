@@ -101,3 +101,62 @@ def test_training_lowers_loss():
     for _ in range(150):
         last = net.train_step(b)
     assert last < 0.5 * first
+
+
+def _batch_tp(n, TP, seed):
+    """States in a level layout of TP test columns (16 or 32)."""
+    rng = np.random.default_rng(seed)
+    Ts = np.array([3, 10, 16] if TP == 16 else [7, 16, 25, 32], dtype=np.int32)
+    regs = rng.integers(0, 1 << 16, size=(n, 8, TP), dtype=np.uint16)
+    regs[:, 0, :] = 0
+    flags = rng.integers(0, 16, size=(n, TP), dtype=np.uint8)
+    task = rng.integers(0, len(Ts), size=n).astype(np.uint16)
+    for i in range(n):
+        regs[i, :, Ts[task[i]]:] = 0
+        flags[i, Ts[task[i]]:] = 0
+    live = (rng.integers(0, 256, size=n) & 0xFE).astype(np.uint8)
+    depth = rng.integers(0, 9, size=n).astype(np.uint8)
+    task_io = rng.integers(0, 1 << 16, size=(len(Ts), 3, 32), dtype=np.uint16)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to("cuda")  # noqa: E731
+    return (dict(regs=t(regs.astype(np.int16)), flags=t(flags), task=t(task.astype(np.int16)),
+                 live=t(live), depth=t(depth), task_io=t(task_io.astype(np.int16)),
+                 task_T=t(Ts)), (regs, flags, task, live, depth, task_io, Ts))
+
+
+@pytest.mark.parametrize("TP,n", [(32, 203), (16, 61), (32, 5003)])
+def test_fused_tcgen05_encoder_matches(TP, n):
+    """The fused tcgen05 encoder (features -> E1 -> E2 -> pooling) against the
+    unfused kernels and the fp32 CPU network: pooled rows within BF16
+    rounding, logits within the same tolerance as the unfused path. n not a
+    multiple of 4 leaves a partial last tile; n = 5003 gives each CTA several
+    tiles (ring and barrier phases wrap)."""
+    from pca_gb300.valuenet import ValueNet, reference_forward
+    net = ValueNet(seed=5)
+    b, (regs, flags, task, live, depth, task_io, Ts) = _batch_tp(n, TP, seed=TP + n)
+    Pf = net.encode_pool(b["regs"], b["flags"], b["live"], b["task"], b["depth"], TP,
+                         b["task_io"], b["task_T"])
+    Lf = net.trunk(Pf)
+    net.check_status()
+    # unfused path on the same states (features need 32-column rows)
+    regs32 = np.zeros((n, 8, 32), dtype=np.uint16)
+    regs32[:, :, :TP] = regs
+    flags32 = np.zeros((n, 32), dtype=np.uint8)
+    flags32[:, :TP] = flags
+    X = net.features(torch.from_numpy(regs32.astype(np.int16)).cuda(),
+                     torch.from_numpy(flags32).cuda(), b["task"], 32, b["task_io"], b["task_T"])
+    Lu = net.forward(X, b["live"], b["task"], b["task_T"], b["depth"])
+    Pu = net._acts["P"]
+    torch.cuda.synchronize()
+    assert torch.isfinite(Pf.float()).all()
+    assert rel(Pf.float().cpu(), Pu.float().cpu()) < 1e-2
+    # columns 512.. (live bits, depth, zeros) are exact
+    assert torch.equal(Pf[:, 512:].cpu(), Pu[:, 512:].cpu())
+    assert rel(Lf.cpu(), Lu.cpu()) < 2e-2
+    if n <= 256:
+        W = {k: net.Wb[k].float().cpu() for k in net.W}
+        bb = {k: v.cpu() for k, v in net.b.items()}
+        Lr = reference_forward(W, bb, X.float().cpu(), torch.from_numpy(live),
+                               torch.from_numpy(Ts), torch.from_numpy(task.astype(np.int64)),
+                               torch.from_numpy(depth))
+        assert rel(Lf.cpu(), Lr) < 5e-2
+        assert cos(Lf[:, 0].cpu(), Lr[:, 0]) > 0.999

@@ -1,0 +1,145 @@
+"""Fixed small workloads, one per kernel family, for profiling under ncu.
+
+    python -m pca_gb300.profile_cases engine_depths   # k_suffix<32, 2/3>, k_leaf
+    python -m pca_gb300.profile_cases noalloc         # k_suffix_noalloc
+    python -m pca_gb300.profile_cases valuenet        # training and scoring kernels
+    python -m pca_gb300.profile_cases orders          # k_check_perm
+
+Each case runs its work `--reps` times (default 2) and prints one timing line
+per repetition (CUDA events); the device memory it holds stays below a few
+GB so that a capture of any of its launches ends quickly. The headline solve
+(bench.py) covers the level kernels and k_suffix<32, 1>.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import time
+
+import numpy as np
+
+
+def _events():
+    import torch
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def case_engine_depths(reps: int):
+    """is_power2 (32 tests) to kernel depth 4 with the suffix stage started
+    from level 1 and level 2 (suffix depths 3 and 2), and depth 3 from level
+    3 (the leaf check)."""
+    from .pcalib import Engine
+    from .taskgen import is_power2_task
+    eng = Engine(0, 4 << 30)
+    task = is_power2_task()
+    for _ in range(reps):
+        for split, depth in ((1, 4), (2, 4), (3, 3)):
+            t0 = time.perf_counter()
+            s = eng.solve(task, max_depth=depth, split_depth=split, sol_cap=1, count_levels=split == 3)
+            print(f"engine_depths split={split} depth={depth}: K*={s.optimal_depth} "
+                  f"{time.perf_counter() - t0:.4f} s, suffix {s.gpu_ms_suffix:.3f} ms", flush=True)
+
+
+def case_noalloc(reps: int):
+    """The no-allocation entry point to kernel depth 3 on is_power2 (32
+    tests, no program that short: every depth searched completely) and on a
+    2-input synthetic task (27 tests)."""
+    from .pcalib import load_library
+    from .taskgen import is_power2_task, synthetic_task
+    lib = load_library()
+    cap = 1 << 12
+    progs = (ctypes.c_uint16 * (16 * cap))()
+    lens = (ctypes.c_int * cap)()
+    for _ in range(reps):
+        for name, task in (("is_power2", is_power2_task()), ("synthetic_2in", synthetic_task(5, 6)[0])):
+            opt, total = ctypes.c_int(-9), ctypes.c_uint64(0)
+            t0 = time.perf_counter()
+            rc = lib.pcagb_solve_small_noalloc(ctypes.byref(task), 3, None, ctypes.byref(opt),
+                                               ctypes.byref(total), progs, lens, cap)
+            if rc < 0:
+                raise RuntimeError(lib.pcagb_noalloc_last_error().decode())
+            print(f"noalloc {name}: K*={opt.value} programs={total.value} "
+                  f"{time.perf_counter() - t0:.4f} s", flush=True)
+
+
+def _random_states(n, TP, seed=0):
+    import torch
+    rng = np.random.default_rng(seed)
+    dev = "cuda"
+    Ts = np.array([16, 24, 32], dtype=np.int32) if TP == 32 else np.array([16], dtype=np.int32)
+    task = rng.integers(0, len(Ts), size=n)
+    regs = rng.integers(0, 1 << 16, size=(n, 8, TP), dtype=np.uint16)
+    regs[:, 0, :] = 0
+    flags = rng.integers(0, 16, size=(n, TP), dtype=np.uint8)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)  # noqa: E731
+    return dict(regs=t(regs.astype(np.int16)), flags=t(flags),
+                live=t((rng.integers(0, 256, size=n) & 0xFE).astype(np.uint8)),
+                task=t(task.astype(np.int16)), depth=t(rng.integers(1, 4, size=n).astype(np.uint8)),
+                task_io=t(rng.integers(0, 1 << 16, size=(len(Ts), 3, 32),
+                                       dtype=np.uint16).astype(np.int16)),
+                task_T=t(Ts), label=t((rng.random(n) < 0.1).astype(np.float32)),
+                remaining=t(rng.integers(0, 4, size=n).astype(np.int32)), TP=TP)
+
+
+def case_valuenet(reps: int):
+    """Training steps on 8,192 states (features, BF16 GEMMs forward and
+    backward, pooling, loss, Adam) and scoring of 131,072 states through the
+    fused tcgen05 encoder and the trunk."""
+    import torch
+    from .valuenet import ValueNet
+    net = ValueNet(seed=0, lr=1e-3, pos_weight=8.0)
+    train = _random_states(8192, 32, seed=1)
+    score = _random_states(131072, 32, seed=2)
+    for _ in range(reps):
+        e0, e1 = _events()
+        e0.record()
+        loss = net.train_step(train)
+        e1.record()
+        torch.cuda.synchronize()
+        print(f"valuenet train step (8192 states): {e0.elapsed_time(e1):.3f} ms loss {loss:.4f}",
+              flush=True)
+        e0, e1 = _events()
+        e0.record()
+        L = net.forward_fused(score["regs"], score["flags"], score["live"], score["task"],
+                              score["depth"], 32, score["task_io"], score["task_T"])
+        e1.record()
+        torch.cuda.synchronize()
+        net.check_status()
+        print(f"valuenet score (131072 states): {e0.elapsed_time(e1):.3f} ms "
+              f"mean logit {float(L[:, 0].mean()):.4f}", flush=True)
+
+
+def case_orders(reps: int):
+    """An ordered solve (random order) of is_power2 to depth 4 from level 2:
+    every stage's order is checked on the device before use."""
+    import torch
+    from .pcalib import Engine
+    from .taskgen import is_power2_task
+    eng = Engine(0, 4 << 30)
+    gen = torch.Generator().manual_seed(0)
+
+    def order(view):
+        return torch.randperm(view.n, generator=gen).to(torch.int32).cuda()
+
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        s = eng.solve_ordered(is_power2_task(), order, chunk=4096, max_depth=4, split_depth=2)
+        print(f"orders: K*={s.optimal_depth} {time.perf_counter() - t0:.4f} s", flush=True)
+
+
+CASES = {"engine_depths": case_engine_depths, "noalloc": case_noalloc,
+         "valuenet": case_valuenet, "orders": case_orders}
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("case", choices=sorted(CASES))
+    ap.add_argument("--reps", type=int, default=2)
+    args = ap.parse_args(argv)
+    from .build import build_engine
+    build_engine()
+    CASES[args.case](args.reps)
+
+
+if __name__ == "__main__":
+    main()

@@ -257,13 +257,39 @@ __device__ __forceinline__ void child_hashes_any(uint32_t op, const WarpState<TP
    the flags) and __all_sync decides. All lanes must call it. */
 template <int TPC>
 __device__ bool warp_child_equal(const LevelDev &P, const TaskDev &task, const WarpState<TPC> &A,
-                                 uint32_t tid, int T, uint32_t liveA, uint32_t uA, uint64_t qB,
-                                 uint32_t cB, int lane)
+                                 uint64_t qA, uint32_t tid, int T, uint32_t liveA, uint32_t uA,
+                                 uint64_t qB, uint32_t cB, int lane)
 {
+    const uint32_t rdA = UOP_RD(uA);
+    if (qB == qA) {
+        /* same parent (about a fifth of the duplicates): only the written
+           columns and the flags can differ, and the parent is in shared
+           memory */
+        const uint32_t uB = c_cand_uop[c_cand_off[(liveA >> 1) & 127u] + cB];
+        const uint32_t rdB = UOP_RD(uB);
+        if (task.key_live && ((liveA | (1u << rdA)) != (liveA | (1u << rdB)))) return false;
+        bool ok = true;
+        if (lane < T) {
+            const uint32_t a1 = A.R[UOP_A(uA)][lane], b1 = A.R[UOP_B(uA)][lane];
+            const uint32_t resA = pca_alu(UOP_OP(uA), a1, b1, UOP_IMM(uA));
+            const uint32_t fA = pca_alu_flags(UOP_OP(uA), a1, b1, UOP_IMM(uA), resA, A.F[lane]);
+            const uint32_t a2 = A.R[UOP_A(uB)][lane], b2 = A.R[UOP_B(uB)][lane];
+            const uint32_t resB = pca_alu(UOP_OP(uB), a2, b2, UOP_IMM(uB));
+            const uint32_t fB = pca_alu_flags(UOP_OP(uB), a2, b2, UOP_IMM(uB), resB, A.F[lane]);
+            ok = fA == fB;
+            if (rdA == rdB) {
+                ok &= resA == resB;
+            } else {
+                ok &= resA == A.R[rdA][lane];   /* B keeps the parent's rdA column */
+                ok &= resB == A.R[rdB][lane];   /* A keeps the parent's rdB column */
+            }
+        }
+        return __all_sync(0xFFFFFFFFu, ok);
+    }
     if (P.task[qB] != tid) return false;
     const uint32_t liveB = P.live[qB];
     const uint32_t uB = c_cand_uop[c_cand_off[(liveB >> 1) & 127u] + cB];
-    const uint32_t rdA = UOP_RD(uA), rdB = UOP_RD(uB);
+    const uint32_t rdB = UOP_RD(uB);
     if (task.key_live && ((liveA | (1u << rdA)) != (liveB | (1u << rdB)))) return false;
     bool ok = true;
     if (lane < T) {
@@ -286,8 +312,10 @@ __device__ bool warp_child_equal(const LevelDev &P, const TaskDev &task, const W
     return __all_sync(0xFFFFFFFFu, ok);
 }
 
+/* Eight CTAs per SM (32 registers a thread): the exact compares are
+   latency bound, and more resident warps hide more of them. */
 template <int TPC>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 8)
 k_expand_insert(LevelDev P, TaskDev task, unsigned long long *table, uint64_t tmask,
                 uint32_t *status)
 {
@@ -347,7 +375,7 @@ k_expand_insert(LevelDev P, TaskDev task, unsigned long long *table, uint64_t tm
                     const uint32_t uj = __shfl_sync(0xFFFFFFFFu, u, j);
                     const unsigned long long sj = __shfl_sync(0xFFFFFFFFu, s, j);
                     const uint64_t oref = (sj & kRefMask) - 1;
-                    const bool e = warp_child_equal<TPC>(P, task, ws, tid, T, live, uj,
+                    const bool e = warp_child_equal<TPC>(P, task, ws, q, tid, T, live, uj,
                                                          oref >> 12, (uint32_t)(oref & 4095), lane);
                     if (lane == j) eq = e;
                 }

@@ -109,6 +109,15 @@ typedef struct {
     uint8_t  flags[MAX_TESTS];
 } dataset_state_record_t;
 
+/* src/search_state.h:54-61 (24-byte edge record of the recording pass) */
+typedef struct {
+    uint64_t parent_hash;
+    uint64_t child_hash;
+    uint16_t action;
+    uint8_t  child_depth;
+    uint8_t  _pad[5];
+} dataset_edge_record_t;
+
 /* VM: src/pca.h:123-127 */
 void pca_init(pca_vm_t *vm);
 void pca_load(pca_vm_t *vm, const uint16_t *prog, size_t len);
@@ -295,6 +304,32 @@ int  pcagb_solve_ordered(pcagb_engine_t *e, const task_spec_t *task, const pcagb
 int  pcagb_complete(pcagb_engine_t *e, const search_ctx_t *ctx, const search_state_t *start,
                     int max_depth, uint16_t *solution_insns, int *solution_len,
                     uint64_t *states_explored);
+
+/* The GPU form of `enumerate --record` (tools/enumerate.c:316-355 records,
+ * :480-533 optimal state sets, :676-740 the recording pass). Solves the task
+ * with the exact pruner (key regs+flags, DFS-first representative, every
+ * level built) and, when a program of kernel depth <= max_depth exists,
+ * writes <dir>/states_<task_id>.bin and <dir>/edges_<task_id>.bin as the
+ * reference's recording pass does: the states its depth-first pass visits
+ * at the optimal depth K* (levels 0..K*, in depth-first preorder), every
+ * state on the path of one of the first 100 optimal programs (positive,
+ * with its remaining steps) and every neg_stride-th other state (negative),
+ * as dataset_state_record_t; and one dataset_edge_record_t per visited
+ * child. The levels come from HBM; keys, hashes and records are computed on
+ * the device. Returns 0 when recorded, 1 when no program exists (nothing
+ * written), negative on error. */
+typedef struct {
+    int      optimal_depth;
+    int      optimal_states;    /* distinct path states over all depths */
+    uint64_t states_written;
+    uint64_t positives;
+    uint64_t negatives;
+    uint64_t edges_written;
+    uint64_t visited;           /* states of levels 0..K* */
+} pcagb_record_stats_t;
+
+int  pcagb_record(pcagb_engine_t *e, const task_spec_t *task, int max_depth, uint32_t task_id,
+                  int neg_stride, const char *dir, pcagb_record_stats_t *stats);
 
 /* The CUDA stream (cudaStream_t) every kernel of this engine runs on, so a
  * caller can time a solve with events on that stream. */

@@ -3,6 +3,8 @@
  * (tools/enumerate.c:537-755) over libpcagb.so.
  *
  *   enumerate <task.json> [-d max_depth] [--no-branch] [--no-oep] [-v] [--count]
+ *   enumerate <task.json> [-d max_depth] --no-branch --record <output_dir>
+ *             [--task-id N] [--neg-stride N]
  *
  * Same argument grammar, the same report lines (task summary, per-depth
  * "candidates" / "OEP pruned" / "solutions found" / "elapsed", the solutions
@@ -18,7 +20,13 @@
  * most 100). --count builds every level with the pruner so the per-depth
  * counters are the reference's exact-pruner counters; without it the search
  * builds levels only as deep as HBM allows and enumerates the rest, and the
- * counters are this engine's. --record (training labels) is not supported.
+ * counters are this engine's.
+ *
+ * --record writes the reference's training records (tools/enumerate.c:
+ * 676-740) from the GPU levels through pcagb_record: states_<id>.bin and
+ * edges_<id>.bin with the same records in the same order, and the same
+ * report lines; as in the reference, the closing "Total" line then counts
+ * the recording pass (the optimal depth's search) alone.
  */
 #include <chrono>
 #include <cstdio>
@@ -52,21 +60,32 @@ int main(int argc, char **argv)
 {
     if (argc < 2) {
         fprintf(stderr,
-                "Usage: enumerate <task.json> [-d max_depth] [--no-branch] [--no-oep] [-v] [--count]\n");
+                "Usage: enumerate <task.json> [-d max_depth] [--no-branch] [--no-oep] [-v] [--count]\n"
+                "       enumerate <task.json> [-d max_depth] --record <output_dir> "
+                "[--task-id N] [--neg-stride N]\n");
         return 1;
     }
-    int max_depth = 4, no_branch = 0, no_oep = 0, count = 0;
+    int max_depth = 4, no_branch = 0, no_oep = 0, count = 0, neg_stride = 8;
+    const char *record_dir = nullptr;
+    uint32_t task_id = 0;
     for (int i = 2; i < argc; i++) {
         if (!strcmp(argv[i], "-d") && i + 1 < argc) max_depth = atoi(argv[++i]);
         else if (!strcmp(argv[i], "--no-branch")) no_branch = 1;
         else if (!strcmp(argv[i], "--no-oep")) no_oep = 1;
         else if (!strcmp(argv[i], "--count")) count = 1;
         else if (!strcmp(argv[i], "-v")) {
-        } else if (!strcmp(argv[i], "--record") || !strcmp(argv[i], "--task-id") ||
-                   !strcmp(argv[i], "--neg-stride")) {
-            fprintf(stderr, "enumerate: --record is not supported by the GPU engine\n");
+        } else if (!strcmp(argv[i], "--record") && i + 1 < argc) record_dir = argv[++i];
+        else if (!strcmp(argv[i], "--task-id") && i + 1 < argc) task_id = (uint32_t)atoi(argv[++i]);
+        else if (!strcmp(argv[i], "--neg-stride") && i + 1 < argc) neg_stride = atoi(argv[++i]);
+    }
+    /* recording is branchless and builds every level with the pruner */
+    if (record_dir) {
+        if (no_oep) {
+            fprintf(stderr, "enumerate: --record without the pruner (--no-oep) is not supported\n");
             return 2;
         }
+        no_branch = 1;
+        count = 1;
     }
     task_spec_t task;
     if (task_load(argv[1], &task) < 0) return 1;
@@ -123,8 +142,32 @@ int main(int argc, char **argv)
     printf("\nOptimal solution length: %d instructions (kernel depth %d)\n",
            task.num_inputs + r.optimal_depth + 2, r.optimal_depth);
     printf("Found %d distinct program(s) at this length.\n", r.stored);
+    uint64_t pruned_total = r.pruned_cum[last];
+    if (record_dir) {
+        const int K = r.optimal_depth;
+        printf("\n===== Recording dataset (Pass 2) =====\n");
+        printf("  building optimal state sets from %d solutions...\n", r.stored);
+        auto r0 = std::chrono::steady_clock::now();
+        pcagb_record_stats_t st;
+        int rrc = pcagb_record(e, &task, max_depth, task_id, neg_stride, record_dir, &st);
+        double rsecs = std::chrono::duration<double>(std::chrono::steady_clock::now() - r0).count();
+        if (rrc < 0) {
+            fprintf(stderr, "enumerate: %s\n", pcagb_last_error());
+            pcagb_engine_destroy(e);
+            return 1;
+        }
+        printf("  optimal state set: %d states across %d depths\n", st.optimal_states, K + 1);
+        printf("  recording done in %.2f sec\n", rsecs);
+        printf("  states: %llu written (%llu positive, %llu negative)\n",
+               (unsigned long long)st.states_written, (unsigned long long)st.positives,
+               (unsigned long long)st.negatives);
+        printf("  edges: %llu written\n", (unsigned long long)st.edges_written);
+        /* the reference resets its counters for the recording pass */
+        total_tried = r.tried[K];
+        pruned_total = r.pruned_cum[K] - (K > 0 ? r.pruned_cum[K - 1] : 0);
+    }
     printf("\nTotal: %llu candidates in %.2f sec", (unsigned long long)total_tried, secs);
-    if (!no_oep) printf(" (OEP pruned: %llu)", (unsigned long long)r.pruned_cum[last]);
+    if (!no_oep) printf(" (OEP pruned: %llu)", (unsigned long long)pruned_total);
     printf("\n");
     pcagb_engine_destroy(e);
     return 0;

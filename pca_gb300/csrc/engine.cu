@@ -31,6 +31,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <unordered_set>
 #include <vector>
 
 #include "../../include/pca_gb300.h"
@@ -1207,6 +1208,175 @@ int emit_solutions(const task_spec_t *task, const pcagb_opts_t &o, TaskRun &tr,
     return PCAGB_OK;
 }
 
+/* The recording pass over the levels of a solved task (see pcagb_record). */
+int record_levels(pcagb_engine *e, const task_spec_t *task, const TaskRun &tr,
+                  const uint16_t *progs, const int *lens, int nprogs, uint32_t task_id,
+                  int neg_stride, const char *dir, pcagb_record_stats_t *st)
+{
+    const GenTables &gt = gen_tables();
+    const int K = tr.optimal_depth;
+    if ((int)e->levels.size() < K + 1) {
+        set_err("internal: levels 0..%d are not built", K);
+        return PCAGB_ELIMIT;
+    }
+    /* states on the optimal programs' paths (tools/enumerate.c:480-520) */
+    search_ctx_t ctx;
+    search_ctx_init(&ctx, task);
+    search_state_t root;
+    search_state_init_root(&ctx, &root);
+    std::vector<std::unordered_set<uint64_t>> opt(K + 1);
+    opt[0].insert(search_state_key_hash64(&ctx, &root));
+    for (int si = 0; si < nprogs; si++) {
+        search_state_t cur = root;
+        const int kl = lens[si] - task->num_inputs - 2;
+        for (int k = 0; k < kl; k++) {
+            search_state_t next;
+            if (!search_state_step(&ctx, &cur, progs[si * 16 + task->num_inputs + k], &next)) break;
+            opt[next.depth].insert(search_state_key_hash64(&ctx, &next));
+            cur = next;
+        }
+    }
+    st->optimal_states = 0;
+    for (auto &o : opt) st->optimal_states += (int)o.size();
+
+    TestPos tp{};
+    for (int j = 0; j < tr.T; j++) tp.pos[tr.order[j]] = (uint8_t)j;
+    const size_t top0 = e->top;
+    auto done = [&](int rc) {
+        e->top = top0;
+        return rc;
+    };
+    /* keys of every state, on the device, in the reference's byte order */
+    std::vector<std::vector<uint64_t>> keys(K + 1);
+    std::vector<uint64_t *> d_key(K + 1), d_oep(K + 1);
+    std::vector<std::vector<uint32_t>> parent(K + 1);
+    std::vector<std::vector<uint16_t>> cidx(K + 1);
+    std::vector<std::vector<uint8_t>> live(K + 1);
+    st->visited = 0;
+    for (int d = 0; d <= K; d++) {
+        const Level &L = e->levels[d];
+        st->visited += L.n;
+        d_key[d] = (uint64_t *)e->alloc_top(L.n * 8);
+        d_oep[d] = (uint64_t *)e->alloc_top(L.n * 8);
+        if (!d_key[d] || !d_oep[d]) {
+            set_err("arena exhausted recording level %d", d);
+            return done(PCAGB_ENOMEM);
+        }
+        if (e->TPC == 16)
+            k_record_keys<16><<<e->grid(4), 256, 0, e->stream>>>(view(L), tp, tr.T, d, d_key[d], d_oep[d]);
+        else
+            k_record_keys<32><<<e->grid(4), 256, 0, e->stream>>>(view(L), tp, tr.T, d, d_key[d], d_oep[d]);
+        int rc = check_launch(e);
+        if (rc) return done(rc);
+        keys[d].resize(L.n);
+        live[d].resize(L.n);
+        CK(e_copy(e, keys[d].data(), d_key[d], L.n * 8, cudaMemcpyDeviceToHost, e->stream));
+        CK(e_copy(e, live[d].data(), L.live, L.n, cudaMemcpyDeviceToHost, e->stream));
+        if (d > 0) {
+            parent[d].resize(L.n);
+            cidx[d].resize(L.n);
+            CK(e_copy(e, parent[d].data(), L.parent, L.n * 4, cudaMemcpyDeviceToHost, e->stream));
+            CK(e_copy(e, cidx[d].data(), L.cidx, L.n * 2, cudaMemcpyDeviceToHost, e->stream));
+        }
+    }
+    CK(cudaStreamSynchronize(e->stream));
+    /* children of each state are contiguous in the next level (DFS order) */
+    std::vector<std::vector<uint64_t>> first(K);
+    for (int d = 0; d < K; d++) {
+        first[d].assign(e->levels[d].n + 1, 0);
+        for (uint32_t p : parent[d + 1]) first[d][p + 1]++;
+        for (uint64_t i = 0; i < e->levels[d].n; i++) first[d][i + 1] += first[d][i];
+    }
+    auto action = [&](int d, uint64_t j) -> uint16_t {
+        const uint32_t p = parent[d][j];
+        const uint32_t m = (live[d - 1][p] >> 1) & 127u;
+        return gt.cand[gt.cand_off[m] + cidx[d][j]];
+    };
+    /* the depth-first pass (tools/enumerate.c:316-402): states in preorder,
+       every non-positive one counted, every neg_stride-th recorded */
+    std::vector<std::vector<RecordMeta>> meta(K + 1);
+    std::vector<uint64_t> order;  /* preorder of recorded states: depth << 40 | slot */
+    std::vector<dataset_edge_record_t> edges;
+    uint64_t neg_seen = 0;
+    auto visit = [&](auto &&self, int d, uint64_t i, uint16_t act) -> void {
+        const uint64_t key = keys[d][i];
+        const bool pos = opt[d].count(key) != 0;
+        bool rec = pos;
+        if (!pos) {
+            neg_seen++;
+            rec = neg_stride > 0 && neg_seen % (uint64_t)neg_stride == 0;
+        }
+        if (rec) {
+            meta[d].push_back(RecordMeta{(uint32_t)i, act, (uint8_t)(pos ? 1 : 0),
+                                         (int8_t)(pos ? K - d : -1)});
+            order.push_back((uint64_t)d << 40 | (meta[d].size() - 1));
+            if (pos) st->positives++;
+            else st->negatives++;
+        }
+        if (d == K) return;
+        for (uint64_t j = first[d][i]; j < first[d][i + 1]; j++) {
+            const uint16_t a = action(d + 1, j);
+            dataset_edge_record_t er;
+            memset(&er, 0, sizeof er);
+            er.parent_hash = key;
+            er.child_hash = keys[d + 1][j];
+            er.action = a;
+            er.child_depth = (uint8_t)(d + 1);
+            edges.push_back(er);
+            self(self, d + 1, j, a);
+        }
+    };
+    visit(visit, 0, 0, (uint16_t)0xFFFF);
+    /* the records, serialized on the device */
+    std::vector<std::vector<dataset_state_record_t>> recs(K + 1);
+    for (int d = 0; d <= K; d++) {
+        const uint64_t c = meta[d].size();
+        if (!c) continue;
+        RecordMeta *dm = (RecordMeta *)e->alloc_top(c * sizeof(RecordMeta));
+        dataset_state_record_t *dr =
+            (dataset_state_record_t *)e->alloc_top(c * sizeof(dataset_state_record_t));
+        if (!dm || !dr) {
+            set_err("arena exhausted recording level %d", d);
+            return done(PCAGB_ENOMEM);
+        }
+        CK(e_copy(e, dm, meta[d].data(), c * sizeof(RecordMeta), cudaMemcpyHostToDevice, e->stream));
+        CK(cudaMemsetAsync(dr, 0, c * sizeof(dataset_state_record_t), e->stream));
+        const Level &L = e->levels[d];
+        if (e->TPC == 16)
+            k_record_states<16><<<e->grid(4), 256, 0, e->stream>>>(view(L), tp, tr.T, d, task_id, K, dm, c,
+                                                                 d_key[d], d_oep[d], dr);
+        else
+            k_record_states<32><<<e->grid(4), 256, 0, e->stream>>>(view(L), tp, tr.T, d, task_id, K, dm, c,
+                                                                 d_key[d], d_oep[d], dr);
+        int rc = check_launch(e);
+        if (rc) return done(rc);
+        recs[d].resize(c);
+        CK(e_copy(e, recs[d].data(), dr, c * sizeof(dataset_state_record_t),
+                  cudaMemcpyDeviceToHost, e->stream));
+    }
+    CK(cudaStreamSynchronize(e->stream));
+    char path[1024];
+    snprintf(path, sizeof path, "%s/states_%06u.bin", dir, task_id);
+    FILE *fs = fopen(path, "wb");
+    if (!fs) {
+        set_err("cannot open %s for writing", path);
+        return done(PCAGB_EINVAL);
+    }
+    for (uint64_t x : order) fwrite(&recs[x >> 40][x & ((1ull << 40) - 1)], sizeof(dataset_state_record_t), 1, fs);
+    fclose(fs);
+    snprintf(path, sizeof path, "%s/edges_%06u.bin", dir, task_id);
+    FILE *fe = fopen(path, "wb");
+    if (!fe) {
+        set_err("cannot open %s for writing", path);
+        return done(PCAGB_EINVAL);
+    }
+    if (!edges.empty()) fwrite(edges.data(), sizeof(dataset_edge_record_t), edges.size(), fe);
+    fclose(fe);
+    st->states_written = order.size();
+    st->edges_written = edges.size();
+    return done(PCAGB_OK);
+}
+
 thread_local pcagb_engine *t_default_engine = nullptr;
 thread_local uint64_t t_last_explored = 0;
 
@@ -1377,6 +1547,36 @@ int pcagb_solve_ordered(pcagb_engine_t *e, const task_spec_t *task, const pcagb_
     rc = emit_solutions(task, o, runs[0], sol_progs, sol_lens, sol_cap);
     *res = runs[0].res;
     return rc;
+}
+
+int pcagb_record(pcagb_engine_t *e, const task_spec_t *task, int max_depth, uint32_t task_id,
+                 int neg_stride, const char *dir, pcagb_record_stats_t *stats)
+{
+    if (!e || !task || !dir) { set_err("null argument"); return PCAGB_EINVAL; }
+    pcagb_record_stats_t st;
+    memset(&st, 0, sizeof st);
+    st.optimal_depth = -1;
+    pcagb_opts_t o;
+    pcagb_default_opts(&o);
+    o.max_depth = max_depth;
+    o.oep_mode = PCAGB_OEP_EXACT;
+    o.count_levels = 1;
+    std::vector<TaskRun> runs(1);
+    if (!make_run(task, o, &runs[0])) return PCAGB_EINVAL;
+    int rc = run_batch(e, runs, o);
+    if (rc) return rc;
+    const int cap = 100;  /* the reference's MAX_SOLUTIONS */
+    std::vector<uint16_t> progs((size_t)cap * 16);
+    std::vector<int> lens(cap);
+    rc = emit_solutions(task, o, runs[0], progs.data(), lens.data(), cap);
+    if (rc) return rc;
+    st.optimal_depth = runs[0].optimal_depth;
+    if (st.optimal_depth >= 0)
+        rc = record_levels(e, task, runs[0], progs.data(), lens.data(), runs[0].res.stored, task_id,
+                           neg_stride, dir, &st);
+    if (stats) *stats = st;
+    if (rc) return rc;
+    return st.optimal_depth >= 0 ? 0 : 1;
 }
 
 int pcagb_complete(pcagb_engine_t *e, const search_ctx_t *ctx, const search_state_t *start,

@@ -716,6 +716,83 @@ k_suffix(LevelDev P, TaskDev task, SolBuf S, uint32_t chunks_per_prefix, uint32_
     }
 }
 
+/* ---- recording: the reference's keys and records of level states --------- */
+
+/* Engine column of each original test (the engine reorders tests). */
+struct TestPos {
+    uint8_t pos[MAX_TESTS];
+};
+
+/* FNV-1a-64 over the state's bytes in the reference's order (per original
+ * test: r0..r7 low byte then high byte, then the flags): the oep hash; the
+ * key adds live and depth (src/search_state.c:191-219). One thread per
+ * state. */
+template <int TPC>
+__global__ void k_record_keys(LevelDev L, TestPos tp, int T, int depth, uint64_t *key,
+                              uint64_t *oep)
+{
+    const uint64_t prime = 0x00000100000001B3ull;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < L.n;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t h = 0xCBF29CE484222325ull;
+        for (int u = 0; u < T; u++) {
+            const int c = tp.pos[u];
+#pragma unroll
+            for (int r = 0; r < 8; r++) {
+                const uint32_t v = L.regs[(i * 8 + r) * TPC + c];
+                h = (h ^ (v & 0xFFu)) * prime;
+                h = (h ^ (v >> 8)) * prime;
+            }
+            h = (h ^ L.flags[i * TPC + c]) * prime;
+        }
+        oep[i] = h;
+        h = (h ^ L.live[i]) * prime;
+        h = (h ^ (uint32_t)depth) * prime;
+        key[i] = h;
+    }
+}
+
+/* What the recording pass writes for one state (src/search_state.c:243-268). */
+struct RecordMeta {
+    uint32_t index;          /* state in its level */
+    uint16_t parent_action;  /* 0xFFFF for the root */
+    uint8_t  positive;
+    int8_t   remaining;
+};
+
+/* One warp per record, lane = original test; `out` is zeroed beforehand. */
+template <int TPC>
+__global__ void k_record_states(LevelDev L, TestPos tp, int T, int depth, uint32_t task_id,
+                                int target_depth, const RecordMeta *meta, uint64_t count,
+                                const uint64_t *key, const uint64_t *oep,
+                                dataset_state_record_t *out)
+{
+    const int lane = threadIdx.x & 31;
+    const uint64_t nw = (uint64_t)gridDim.x * (blockDim.x >> 5);
+    for (uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < count; w += nw) {
+        const RecordMeta m = meta[w];
+        const uint64_t i = m.index;
+        dataset_state_record_t &o = out[w];
+        if (lane == 0) {
+            o.state_hash = key[i];
+            o.oep_hash = oep[i];
+            o.task_id = task_id;
+            o.parent_action = m.parent_action;
+            o.depth = (uint8_t)depth;
+            o.budget_left = (uint8_t)(target_depth - depth);
+            o.live = L.live[i];
+            o.can_finish_optimally = m.positive;
+            o.remaining_steps = m.remaining;
+        }
+        if (lane < T) {
+            const int c = tp.pos[lane];
+#pragma unroll
+            for (int r = 0; r < 8; r++) o.regs[lane][r] = L.regs[(i * 8 + r) * TPC + c];
+            o.flags[lane] = L.flags[i * TPC + c];
+        }
+    }
+}
+
 /* ---- exclusive scan of u64 (in place), three-phase ----------------------- */
 
 constexpr int kScanBlock = 1024;  /* elements per block (256 threads x 4) */

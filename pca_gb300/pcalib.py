@@ -104,6 +104,13 @@ class LevelView(ctypes.Structure):
 ORDER_CB = ctypes.CFUNCTYPE(ctypes.c_void_p, ctypes.POINTER(LevelView), ctypes.c_void_p)
 
 
+class RecordStats(ctypes.Structure):
+    _fields_ = [("optimal_depth", ctypes.c_int), ("optimal_states", ctypes.c_int),
+                ("states_written", ctypes.c_uint64), ("positives", ctypes.c_uint64),
+                ("negatives", ctypes.c_uint64), ("edges_written", ctypes.c_uint64),
+                ("visited", ctypes.c_uint64)]
+
+
 OEP_NONE, OEP_EXACT, OEP_EXACT_LIVE = 0, 1, 2
 
 DONE_CB = ctypes.CFUNCTYPE(None, ctypes.c_int, ctypes.POINTER(SolveResult), ctypes.c_void_p)
@@ -118,7 +125,7 @@ EXPORTS = [
     "search_exhaustive_complete", "search_exhaustive_states_explored", "search_state_dump",
     "pcagb_last_error", "pcagb_default_opts", "pcagb_engine_create", "pcagb_engine_destroy",
     "pcagb_solve", "pcagb_solve_batch", "pcagb_solve_batch_cb", "pcagb_solve_ordered",
-    "pcagb_complete",
+    "pcagb_complete", "pcagb_record",
     "pcagb_num_candidates",
     "pcagb_engine_stream", "pcagb_device_memory",
     "pcagb_solve_small_noalloc", "pcagb_noalloc_last_error",
@@ -163,6 +170,8 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
                                  P(ctypes.c_uint16), P(ctypes.c_int), ctypes.c_int], ctypes.c_int),
         "pcagb_complete": ([ctypes.c_void_p, P(SearchCtx), P(SearchState), ctypes.c_int,
                             P(ctypes.c_uint16), P(ctypes.c_int), P(ctypes.c_uint64)], ctypes.c_int),
+        "pcagb_record": ([ctypes.c_void_p, P(TaskSpec), ctypes.c_int, ctypes.c_uint32, ctypes.c_int,
+                          ctypes.c_char_p, P(RecordStats)], ctypes.c_int),
         "pcagb_num_candidates": ([ctypes.c_uint8], ctypes.c_int),
         "pcagb_engine_stream": ([ctypes.c_void_p], ctypes.c_void_p),
         "pcagb_device_memory": ([ctypes.c_int, P(ctypes.c_size_t), P(ctypes.c_size_t)],
@@ -459,6 +468,19 @@ class Engine:
     def stream(self) -> int:
         """cudaStream_t of the engine, as an integer handle."""
         return self.lib.pcagb_engine_stream(self.h) or 0
+
+    def record(self, task: TaskSpec, out_dir: str, max_depth: int = 4, task_id: int = 0,
+               neg_stride: int = 8) -> dict:
+        """The reference's recording pass (`enumerate --record`) from the GPU
+        levels: writes states_<id>.bin / edges_<id>.bin into out_dir and
+        returns the counts ({} fields of pcagb_record_stats_t); nothing is
+        written when no program of kernel depth <= max_depth exists."""
+        st = RecordStats()
+        rc = self.lib.pcagb_record(self.h, ctypes.byref(task), max_depth, task_id, neg_stride,
+                                   os.fsencode(out_dir), ctypes.byref(st))
+        if rc < 0:
+            raise EngineError(f"record failed ({rc}): {self.lib.pcagb_last_error().decode()}")
+        return {name: getattr(st, name) for name, _ in RecordStats._fields_}
 
     def complete(self, ctx: SearchCtx, state: SearchState, max_depth: int):
         insns = (ctypes.c_uint16 * 16)()

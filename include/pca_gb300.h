@@ -331,6 +331,20 @@ typedef struct {
 int  pcagb_record(pcagb_engine_t *e, const task_spec_t *task, int max_depth, uint32_t task_id,
                   int neg_stride, const char *dir, pcagb_record_stats_t *stats);
 
+/* The reference solver's branch mode (its default, without --no-branch;
+ * tools/enumerate.c:204-455): kernels may use CMP, forward BR (cond 1..6,
+ * offsets up to the end of the kernel), DIV and MOD besides the branchless
+ * set, with the reference's candidate rules and its pruner (key: registers
+ * and flags of every test after the partial program; BR children never
+ * pruned; first child in depth-first order kept), exact here. Every level
+ * of each depth is built on the engine's stream, so the per-depth counters
+ * (tried, pruned_cum) are the reference's, up to the 100th solution at the
+ * optimal depth as its walk stops there; the first sol_cap programs in
+ * depth-first order are returned. Errors: see pcagb_branch_last_error. */
+int  pcagb_solve_branch(pcagb_engine_t *e, const task_spec_t *task, int max_depth,
+                        pcagb_result_t *res, uint16_t *sol_progs, int *sol_lens, int sol_cap);
+const char *pcagb_branch_last_error(void);
+
 /* The CUDA stream (cudaStream_t) every kernel of this engine runs on, so a
  * caller can time a solve with events on that stream. */
 void *pcagb_engine_stream(pcagb_engine_t *e);

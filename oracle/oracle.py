@@ -47,6 +47,9 @@ def lib():
         L.orc_enumerate.argtypes = [P(TaskSpec), ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                     P(ctypes.c_uint16), P(ctypes.c_int), P(OrcResult)]
         L.orc_enumerate.restype = ctypes.c_int
+        L.orc_enumerate_branch.argtypes = [P(TaskSpec), ctypes.c_int, ctypes.c_int,
+                                           P(ctypes.c_uint16), P(ctypes.c_int), P(OrcResult)]
+        L.orc_enumerate_branch.restype = ctypes.c_int
         L.orc_enumerate_sample.argtypes = [P(TaskSpec), ctypes.c_int, ctypes.c_int,
                                            ctypes.c_double, P(ctypes.c_double), P(ctypes.c_uint64)]
         L.orc_enumerate_sample.restype = ctypes.c_uint64
@@ -83,6 +86,21 @@ def enumerate_task(task, max_depth: int, mode: int = REF32, sol_cap: int = -1):
     r = OrcResult()
     if L.orc_enumerate(ctypes.byref(task), max_depth, mode, sol_cap, progs, lens,
                        ctypes.byref(r)) != 0:
+        raise RuntimeError("oracle rejected the task")
+    out = [[progs[i * 16 + j] for j in range(lens[i])] for i in range(r.num_solutions)]
+    return r, out
+
+
+def enumerate_branch(task, max_depth: int, mode: int = REF32):
+    """Iterative deepening of the reference's branch mode (CMP, forward BR,
+    DIV, MOD) with its walk stopping at the 100th solution; mode REF32 (the
+    reference's 32-bit pruner) or EXACT. Returns (OrcResult, [programs])."""
+    L = lib()
+    progs = (ctypes.c_uint16 * (16 * 100))()
+    lens = (ctypes.c_int * 100)()
+    r = OrcResult()
+    if L.orc_enumerate_branch(ctypes.byref(task), max_depth, mode, progs, lens,
+                              ctypes.byref(r)) != 0:
         raise RuntimeError("oracle rejected the task")
     out = [[progs[i * 16 + j] for j in range(lens[i])] for i in range(r.num_solutions)]
     return r, out

@@ -777,6 +777,180 @@ static double since(const struct timespec *t0)
     return (double)(t.tv_sec - t0->tv_sec) + 1e-9 * (double)(t.tv_nsec - t0->tv_nsec);
 }
 
+/* ---- branch mode (tools/enumerate.c:204-286, 405-455, 624-662) --------- */
+
+/* Candidates of a position (tools/enumerate.c:204-260): ALU ops with DIV and
+   MOD, CMP, forward BR (cond 1..6, offset 1..kernel_depth - pos - 1), LDI,
+   ADDI, in the reference's order. */
+static int gen_branch_candidates(uint16_t *out, int max, uint8_t live, int pos, int kdepth)
+{
+    static const uint8_t alu[] = {OP_ADD, OP_SUB, OP_MUL, OP_DIV, OP_MOD,
+                                  OP_AND, OP_OR, OP_XOR, OP_SHL, OP_SHR, OP_ASR};
+    static const int commut[] = {1, 0, 1, 0, 0, 1, 1, 1, 0, 0, 0};
+    int n = 0;
+    for (int oi = 0; oi < 11; oi++) {
+        const int op = alu[oi];
+        for (int rd = 1; rd < 8 && n < max; rd++)
+            for (int rs = 0; rs < 8 && n < max; rs++) {
+                if (rs && !(live >> rs & 1)) continue;
+                for (int rt = commut[oi] ? rs : 0; rt < 8 && n < max; rt++) {
+                    if (rt && !(live >> rt & 1)) continue;
+                    if (rs == 0 && rt == 0) continue;
+                    if (op == OP_ADD && rs == rd && rt == 0) continue;
+                    if (op == OP_ADD && rt == rd && rs == 0) continue;
+                    if (op == OP_SUB && rs == rd && rt == 0) continue;
+                    if (op == OP_MUL && (rs == 0 || rt == 0)) continue;
+                    if ((op == OP_DIV || op == OP_MOD) && rt == 0) continue;
+                    if ((op == OP_SHL || op == OP_SHR || op == OP_ASR) && rt == 0) continue;
+                    out[n++] = ENC_R(op, rd, rs, rt);
+                }
+            }
+    }
+    for (int rd = 0; rd < 8 && n < max; rd++) {
+        if (rd && !(live >> rd & 1)) continue;
+        for (int rs = 0; rs < 8 && n < max; rs++) {
+            if (rs && !(live >> rs & 1)) continue;
+            if ((rd == 0 && rs == 0) || rd == rs) continue;
+            out[n++] = ENC_R(OP_CMP, rd, rs, 0);
+        }
+    }
+    const int mf = kdepth - pos - 1;
+    for (int cond = 1; cond <= 6 && mf > 0; cond++)
+        for (int off = 1; off <= mf && n < max; off++) out[n++] = ENC_I(OP_BR, cond, (uint8_t)off);
+    for (int rd = 1; rd < 8 && n < max; rd++)
+        for (int i = 0; i < 12 && n < max; i++) out[n++] = ENC_I(OP_LDI, rd, LDI_VALS[i]);
+    for (int rd = 1; rd < 8 && n < max; rd++) {
+        if (!(live >> rd & 1)) continue;
+        for (int i = 0; i < 6 && n < max; i++) out[n++] = ENC_I(OP_ADDI, rd, (uint8_t)ADDI_VALS[i]);
+    }
+    return n;
+}
+
+typedef struct {
+    const orc_task_t *task;
+    int mode, num_inputs;
+    uint16_t program[256];
+    uint16_t *sol_progs;
+    int *sol_lens;
+    int num_solutions;
+    uint64_t tried, pruned;
+    ref_oep_t ref;
+    exact_set_t ex[ORC_MAX_DEPTH];
+} bsolver_t;
+
+static void branch_try_output(bsolver_t *s, uint8_t live, int kend)
+{
+    if (s->num_solutions >= 100) return;
+    for (int r = 1; r < 8; r++) {
+        if (!(live >> r & 1)) continue;
+        s->program[kend] = ENC_I(OP_OUT, r, s->task->output_ports[0]);
+        s->program[kend + 1] = ENC_R(OP_HLT, 0, 0, 0);
+        s->tried++;
+        if (orc_task_evaluate(s->task, s->program, kend + 2) == s->task->num_tests) {
+            if (s->sol_progs && s->num_solutions < 100) {
+                memset(s->sol_progs + (size_t)s->num_solutions * 16, 0, 32);
+                memcpy(s->sol_progs + (size_t)s->num_solutions * 16, s->program, (size_t)(kend + 2) * 2);
+                s->sol_lens[s->num_solutions] = kend + 2;
+            }
+            s->num_solutions++;
+        }
+    }
+}
+
+static void branch_dfs(bsolver_t *s, int pos, int kdepth, uint8_t live)
+{
+    if (s->num_solutions >= 100) return;
+    const int kstart = s->num_inputs;
+    if (pos == kdepth) {
+        branch_try_output(s, live, kstart + kdepth);
+        return;
+    }
+    uint16_t cands[4096];
+    const int nc = gen_branch_candidates(cands, 4096, live, pos, kdepth);
+    const int ppos = kstart + pos;
+    for (int i = 0; i < nc; i++) {
+        if (s->num_solutions >= 100) return;
+        s->program[ppos] = cands[i];
+        const uint8_t op = I_OP(cands[i]), rd = I_RD(cands[i]);
+        uint8_t nl = live;
+        if (op != OP_CMP && op != OP_BR && rd != 0) nl |= (uint8_t)(1u << rd);
+        if (s->mode != ORC_OEP_NONE && op != OP_BR) {
+            /* the partial program, HLT appended, on every test (100 cycles) */
+            const int plen = ppos + 1;
+            s->program[plen] = ENC_R(OP_HLT, 0, 0, 0);
+            uint32_t h = 2166136261u;
+            uint8_t key[ORC_MAX_TESTS * 17];
+            size_t kn = 0;
+            for (int t = 0; t < s->task->num_tests; t++) {
+                orc_vm_t vm;
+                memset(&vm, 0, sizeof vm);
+                memcpy(vm.prog, s->program, (size_t)(plen + 1) * 2);
+                for (int p = 0; p < s->task->num_inputs; p++)
+                    vm.ports[s->task->input_ports[p]] = s->task->tests[t].in[p];
+                while (vm.status == 0 && vm.cycles < 100) vm_step(&vm);
+                for (int r = 0; r < 8; r++) {
+                    h ^= vm.r[r] & 0xFF; h *= 16777619u;
+                    h ^= vm.r[r] >> 8;   h *= 16777619u;
+                    memcpy(key + kn, &vm.r[r], 2);
+                    kn += 2;
+                }
+                h ^= vm.flags; h *= 16777619u;
+                key[kn++] = vm.flags;
+            }
+            int seen;
+            if (s->mode == ORC_OEP_REF32) seen = ref_oep_check_insert(&s->ref, pos, h);
+            else seen = exact_insert_raw(&s->ex[pos], key, kn, bytes_hash(key, kn));
+            if (seen) {
+                s->pruned++;
+                continue;
+            }
+        }
+        s->tried++;
+        branch_dfs(s, pos + 1, kdepth, nl);
+    }
+}
+
+int orc_enumerate_branch(const orc_task_t *task, int max_depth, int oep_mode,
+                         uint16_t *sol_progs, int *sol_lens, orc_result_t *res)
+{
+    memset(res, 0, sizeof *res);
+    res->optimal_depth = -1;
+    if (task->num_outputs != 1 || task->num_tests > ORC_MAX_TESTS || max_depth < 0 ||
+        task->num_inputs + max_depth + 2 > 16)
+        return -1;
+    bsolver_t *s = calloc(1, sizeof *s);
+    if (!s) return -1;
+    s->task = task;
+    s->mode = oep_mode == ORC_OEP_REF32 || oep_mode == ORC_OEP_NONE ? oep_mode : ORC_OEP_EXACT;
+    s->num_inputs = task->num_inputs;
+    s->sol_progs = sol_progs;
+    s->sol_lens = sol_lens;
+    uint8_t live0 = 0;
+    for (int i = 0; i < task->num_inputs; i++) {
+        s->program[i] = ENC_I(OP_IN, i + 1, task->input_ports[i]);
+        live0 |= (uint8_t)(1u << (i + 1));
+    }
+    for (int K = 0; K <= max_depth; K++) {
+        const uint64_t tried0 = s->tried;
+        ref_oep_clear(&s->ref);
+        for (int d = 0; d < ORC_MAX_DEPTH; d++) exact_clear(&s->ex[d]);
+        branch_dfs(s, 0, K, live0);
+        res->tried[K] = s->tried - tried0;
+        res->pruned_cum[K] = s->pruned;
+        res->sols_at[K] = s->num_solutions;
+        if (s->num_solutions > 0) {
+            res->optimal_depth = K;
+            break;
+        }
+    }
+    res->num_solutions = s->num_solutions < 100 ? s->num_solutions : 100;
+    res->total_solutions = (uint64_t)s->num_solutions;
+    ref_oep_free(&s->ref);
+    for (int d = 0; d < ORC_MAX_DEPTH; d++) exact_free(&s->ex[d]);
+    free(s);
+    return 0;
+}
+
 /* Work item k = (root candidate k / 4096, level-1 candidate k % 4096): the
  * thread steps both instructions (counting them as the reference does) and
  * runs the reference DFS below, with its own 32-bit OEP tables kept across

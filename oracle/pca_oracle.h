@@ -112,6 +112,18 @@ int  orc_enumerate(const orc_task_t *task, int max_depth, int oep_mode,
                    int sol_cap, uint16_t *sol_progs, int *sol_lens,
                    orc_result_t *res);
 
+/* Iterative deepening of the reference's branch mode, its default without
+ * --no-branch (tools/enumerate.c:204-260 candidates with CMP, forward BR,
+ * DIV and MOD; :262-286 output check; :405-455 search; :624-662 driver):
+ * every candidate re-runs the partial program on the VM for every test (100
+ * cycles) and is pruned when its registers and flags were seen at that
+ * position, BR candidates excepted. oep_mode: ORC_OEP_REF32 (the
+ * reference's 32-bit FNV-1a key in its 2^20-slot tables), ORC_OEP_EXACT
+ * (the same key compared exactly) or ORC_OEP_NONE. The walk stops at the
+ * 100th solution of a depth, as the reference's does. */
+int  orc_enumerate_branch(const orc_task_t *task, int max_depth, int oep_mode,
+                          uint16_t *sol_progs, int *sol_lens, orc_result_t *res);
+
 /* CPU throughput baseline: the reference algorithm (REF32 pruner) at one
  * fixed kernel depth on nthreads POSIX threads. Work items are the
  * (root candidate, level-1 candidate) pairs, handed out in DFS order from a

@@ -12,12 +12,12 @@
  * instructions (kernel depth K)", "Found N distinct program(s) at this
  * length.") and the same exit code (0 iff a program was found).
  *
- * The search runs on the GPU engine and is branchless: branch mode (CMP/BR)
- * is not implemented, so the reference's default without --no-branch is
- * refused with exit code 2. With OEP on, the pruner is exact (key
- * regs+flags, DFS-first representative, full-state compare); the printed
- * programs are the reference's (its DFS-first program per final state, at
- * most 100). --count builds every level with the pruner so the per-depth
+ * The search runs on the GPU. Without --no-branch it is the reference's
+ * branch mode (CMP, forward BR, DIV, MOD; pcagb_solve_branch) with its
+ * per-depth counters; with --no-branch the branchless engine. With OEP on,
+ * the pruner is exact (key regs+flags, DFS-first representative,
+ * full-state compare); the printed programs are the reference's (its
+ * DFS-first program per final state, at most 100). --count builds every level with the pruner so the per-depth
  * counters are the reference's exact-pruner counters; without it the search
  * builds levels only as deep as HBM allows and enumerates the rest, and the
  * counters are this engine's.
@@ -91,15 +91,56 @@ int main(int argc, char **argv)
     if (task_load(argv[1], &task) < 0) return 1;
     task_print(&task);
     printf("\n");
-    if (!no_branch) {
-        fprintf(stderr, "enumerate: branch mode (CMP/BR) is not implemented on the GPU engine; "
-                        "pass --no-branch\n");
+    if (!no_branch && no_oep) {
+        fprintf(stderr, "enumerate: branch mode without the pruner (--no-oep) is not supported\n");
         return 2;
     }
     pcagb_engine_t *e = nullptr;
-    if (pcagb_engine_create(0, 0, &e) != PCAGB_OK) {
+    /* branch mode keeps its levels outside the engine's arena */
+    if (pcagb_engine_create(0, no_branch ? 0 : ((size_t)1 << 30), &e) != PCAGB_OK) {
         fprintf(stderr, "enumerate: %s\n", pcagb_last_error());
         return 1;
+    }
+    if (!no_branch) {
+        printf("Enumerating programs (max kernel depth %d, branches on, OEP on)...\n\n", max_depth);
+        const int bcap = 100;
+        std::vector<uint16_t> bprogs(bcap * 16);
+        std::vector<int> blens(bcap);
+        pcagb_result_t br;
+        auto b0 = std::chrono::steady_clock::now();
+        int brc = pcagb_solve_branch(e, &task, max_depth, &br, bprogs.data(), blens.data(), bcap);
+        double bsecs = std::chrono::duration<double>(std::chrono::steady_clock::now() - b0).count();
+        if (brc != PCAGB_OK) {
+            fprintf(stderr, "enumerate: %s\n", pcagb_branch_last_error());
+            pcagb_engine_destroy(e);
+            return 1;
+        }
+        const int blast = br.optimal_depth >= 0 ? br.optimal_depth : max_depth;
+        uint64_t btotal = 0;
+        for (int k = 0; k <= blast; k++) {
+            printf("--- kernel depth %d (total program length %d) ---\n", k, task.num_inputs + k + 2);
+            btotal += br.tried[k];
+            const int found = k == br.optimal_depth ? (int)br.total_solutions : 0;
+            printf("  candidates: %llu  (%.1f M/sec)\n", (unsigned long long)br.tried[k],
+                   bsecs > 0 ? br.tried[k] / bsecs / 1e6 : 0.0);
+            printf("  OEP pruned: %llu\n", (unsigned long long)br.pruned_cum[k]);
+            printf("  solutions found: %d (total: %d)\n", found, found);
+            printf("  elapsed: %.2f sec\n\n", bsecs);
+            if (found)
+                for (int i = 0; i < br.stored; i++) print_solution(task, &bprogs[i * 16], blens[i], i);
+        }
+        if (br.optimal_depth < 0) {
+            printf("\nNo solutions found up to kernel depth %d.\n", max_depth);
+            pcagb_engine_destroy(e);
+            return 1;
+        }
+        printf("\nOptimal solution length: %d instructions (kernel depth %d)\n",
+               task.num_inputs + br.optimal_depth + 2, br.optimal_depth);
+        printf("Found %d distinct program(s) at this length.\n", (int)br.total_solutions);
+        printf("\nTotal: %llu candidates in %.2f sec (OEP pruned: %llu)\n", (unsigned long long)btotal,
+               bsecs, (unsigned long long)br.pruned_cum[blast]);
+        pcagb_engine_destroy(e);
+        return 0;
     }
     printf("Enumerating programs (max kernel depth %d, branches off, OEP %s, search_state)...\n\n",
            max_depth, no_oep ? "off" : "on");

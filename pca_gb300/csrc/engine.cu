@@ -1382,6 +1382,11 @@ thread_local uint64_t t_last_explored = 0;
 
 }  // namespace
 
+/* For the branch-mode solver (branch.cu), which runs on the engine's stream
+   and device but keeps its own levels. */
+cudaStream_t pcagb_internal_stream(pcagb_engine_t *e) { return e->stream; }
+int pcagb_internal_device(pcagb_engine_t *e) { return e->device; }
+
 extern "C" {
 
 const char *pcagb_last_error(void) { return g_err.c_str(); }

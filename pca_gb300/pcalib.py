@@ -125,7 +125,7 @@ EXPORTS = [
     "search_exhaustive_complete", "search_exhaustive_states_explored", "search_state_dump",
     "pcagb_last_error", "pcagb_default_opts", "pcagb_engine_create", "pcagb_engine_destroy",
     "pcagb_solve", "pcagb_solve_batch", "pcagb_solve_batch_cb", "pcagb_solve_ordered",
-    "pcagb_complete", "pcagb_record",
+    "pcagb_complete", "pcagb_record", "pcagb_solve_branch", "pcagb_branch_last_error",
     "pcagb_num_candidates",
     "pcagb_engine_stream", "pcagb_device_memory",
     "pcagb_solve_small_noalloc", "pcagb_noalloc_last_error",
@@ -172,6 +172,9 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
                             P(ctypes.c_uint16), P(ctypes.c_int), P(ctypes.c_uint64)], ctypes.c_int),
         "pcagb_record": ([ctypes.c_void_p, P(TaskSpec), ctypes.c_int, ctypes.c_uint32, ctypes.c_int,
                           ctypes.c_char_p, P(RecordStats)], ctypes.c_int),
+        "pcagb_solve_branch": ([ctypes.c_void_p, P(TaskSpec), ctypes.c_int, P(SolveResult),
+                                P(ctypes.c_uint16), P(ctypes.c_int), ctypes.c_int], ctypes.c_int),
+        "pcagb_branch_last_error": ([], ctypes.c_char_p),
         "pcagb_num_candidates": ([ctypes.c_uint8], ctypes.c_int),
         "pcagb_engine_stream": ([ctypes.c_void_p], ctypes.c_void_p),
         "pcagb_device_memory": ([ctypes.c_int, P(ctypes.c_size_t), P(ctypes.c_size_t)],
@@ -468,6 +471,27 @@ class Engine:
     def stream(self) -> int:
         """cudaStream_t of the engine, as an integer handle."""
         return self.lib.pcagb_engine_stream(self.h) or 0
+
+    def solve_branch(self, task: TaskSpec, max_depth: int = 4, sol_cap: int = 100) -> Solution:
+        """Branch mode (CMP / forward BR / DIV / MOD): the reference solver's
+        default search, with its per-depth counters and its first programs."""
+        r = SolveResult()
+        cap = max(sol_cap, 1)
+        progs = (ctypes.c_uint16 * (16 * cap))()
+        lens = (ctypes.c_int * cap)()
+        rc = self.lib.pcagb_solve_branch(self.h, ctypes.byref(task), max_depth, ctypes.byref(r),
+                                         progs, lens, cap)
+        if rc != 0:
+            raise EngineError(f"branch solve failed ({rc}): "
+                              f"{self.lib.pcagb_branch_last_error().decode()}")
+        sol = Solution(optimal_depth=r.optimal_depth, total_solutions=r.total_solutions)
+        sol.seconds = r.seconds
+        for i in range(r.stored):
+            sol.programs.append([progs[i * 16 + j] for j in range(lens[i])])
+        last = r.optimal_depth if r.optimal_depth >= 0 else max_depth
+        sol.tried = [r.tried[k] for k in range(last + 1)]
+        sol.pruned_cum = [r.pruned_cum[k] for k in range(last + 1)]
+        return sol
 
     def record(self, task: TaskSpec, out_dir: str, max_depth: int = 4, task_id: int = 0,
                neg_stride: int = 8) -> dict:

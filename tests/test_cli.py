@@ -26,8 +26,8 @@ def run(args):
     return subprocess.run(args, capture_output=True, text=True, timeout=600)
 
 
-def test_branch_mode_is_refused(tmp_path):
-    r = run([os.path.join(LIB, "enumerate"), write_task(tmp_path, ENUM[0]), "-d", "2"])
+def test_branch_mode_without_pruner_is_refused(tmp_path):
+    r = run([os.path.join(LIB, "enumerate"), write_task(tmp_path, ENUM[0]), "-d", "2", "--no-oep"])
     assert r.returncode == 2
     assert "branch mode" in r.stderr
 

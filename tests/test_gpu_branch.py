@@ -1,0 +1,82 @@
+"""Branch mode (the reference solver's default: CMP, forward BR, DIV, MOD)
+on the GPU against the reference's own runs (tests/golden/
+make_branch_golden.py): the same optimal length, the same printed programs
+in the same order, and the same per-depth "candidates" and cumulative "OEP
+pruned" counters (its walk stops at the 100th solution of the optimal depth,
+and so do the counters here). The reference keys its pruner on 32 bits in a
+table of 2^20 slots per depth; on tasks whose levels outgrow the table it
+misses prunes, keeps duplicate states and prints other programs, so
+counters and programs are compared where its levels stay small, the optimal
+length everywhere (with every program here checked by the VM). On depths
+up to 2 every result also equals the CPU restatement of the walk with the
+exact pruner (oracle.enumerate_branch), which with the reference's 32-bit
+keys reproduces the reference's own numbers (tests/test_oracle_branch.py);
+where the two pruners differ, the reference merged distinct states."""
+import json
+import os
+import subprocess
+
+import pytest
+
+from conftest import load_golden, spec_from_json
+
+pytestmark = pytest.mark.gpu
+
+BRANCH = load_golden("ref_enumerate_branch.json")
+
+
+def small(fx):
+    # levels well inside the reference's 2^20-slot tables
+    return max(fx["candidates"] or [0]) < 200000
+
+
+@pytest.mark.parametrize("fx", BRANCH, ids=lambda f: f"task{f['index']}")
+def test_branch_mode_matches_reference(engine, fx):
+    task = spec_from_json(fx["task"])
+    sol = engine.solve_branch(task, max_depth=fx["max_depth"], sol_cap=100)
+    want = fx["optimal_depth"] if fx["optimal_depth"] is not None else -1
+    assert sol.optimal_depth == want
+    if want < 0:
+        return
+    if fx["max_depth"] <= 2:
+        # the exact pruner's walk, restated on the CPU: equal everywhere
+        from oracle import oracle as O
+        r, progs = O.enumerate_branch(task, fx["max_depth"], O.EXACT)
+        assert r.optimal_depth == sol.optimal_depth
+        assert sol.programs == progs
+        assert sol.tried == [r.tried[k] for k in range(want + 1)]
+        assert sol.pruned_cum == [r.pruned_cum[k] for k in range(want + 1)]
+        if sol.tried == fx["candidates"]:
+            assert sol.pruned_cum == fx["pruned_cum"] and sol.programs == fx["programs"]
+        else:
+            # the reference's 32-bit keys merged distinct states (its
+            # restatement with those keys reproduces it)
+            assert sum(fx["candidates"]) < sum(sol.tried)
+    elif small(fx):
+        assert sol.programs == fx["programs"]
+        assert sol.tried == fx["candidates"]
+        assert sol.pruned_cum == fx["pruned_cum"]
+    else:
+        # the reference's saturated tables keep duplicate states, so it
+        # prints other representatives; every program here solves the task
+        from pca_gb300.pcalib import PCALib
+        lib = PCALib()
+        assert sol.programs
+        for prog in sol.programs:
+            assert len(prog) == fx["optimal_length"]
+            assert lib.evaluate(task, prog) == task.num_tests
+
+
+def test_branch_cli_report(tmp_path):
+    from pca_gb300.build import LIBDIR
+    fx = next(f for f in BRANCH if f["optimal_depth"] == 2 and small(f))
+    tp = tmp_path / "task.json"
+    tp.write_text(json.dumps(fx["task"]))
+    p = subprocess.run([os.path.join(LIBDIR, "enumerate"), str(tp), "-d", str(fx["max_depth"])],
+                       capture_output=True, text=True, timeout=300)
+    assert p.returncode == 0, p.stderr
+    assert "branches on, OEP on" in p.stdout
+    assert f"Optimal solution length: {fx['optimal_length']} instructions" in p.stdout
+    assert f"Found {fx['found']} distinct program(s)" in p.stdout
+    for k, c in enumerate(fx["candidates"]):
+        assert f"  candidates: {c}  " in p.stdout

@@ -56,7 +56,7 @@ def parse():
     ap.add_argument("--hbm-gb", type=float, default=0.0,
                     help="engine arena size in GB (0: 60%% of free HBM)")
     ap.add_argument("--workload", default="power2",
-                    choices=["power2", "batched", "served", "guided"],
+                    choices=["power2", "batched", "served", "guided", "branch"],
                     help="power2: the headline solve (default); batched: 1,000 synthetic "
                          "tasks plain vs batched; served: Poisson arrivals, served vs plain; "
                          "guided: value-ordered vs DFS-ordered search")
@@ -352,6 +352,39 @@ def run_guided(args):
     print(json.dumps(line), flush=True)
 
 
+def run_branch(args):
+    """Branch mode (CMP, forward BR, DIV, MOD) on the reference's own task
+    files at their documented optimal lengths: time to the proven optimum
+    per task (every shorter depth searched completely). The task specs come
+    from the committed fixture of the reference's tasks."""
+    from pca_gb300.pcalib import Engine, task_from_dict
+    fixture = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden",
+                           "ref_published.json")
+    eng = Engine(0, 1 << 30)
+    rows = []
+    for t in json.load(open(fixture)):
+        if t["name"] == "saturating_add":
+            continue
+        task = task_from_dict(t["task"])
+        K = t["published_length"] - task.num_inputs - 2
+        eng.solve_branch(task, max_depth=K)  # warm-up
+        t0 = time.perf_counter()
+        s = eng.solve_branch(task, max_depth=K)
+        dt = time.perf_counter() - t0
+        rows.append({"task": t["name"], "published_length": t["published_length"],
+                     "found_length": s.optimal_depth + task.num_inputs + 2
+                     if s.optimal_depth >= 0 else None, "seconds": dt,
+                     "candidates": int(sum(s.tried))})
+    total = sum(r["seconds"] for r in rows)
+    line = {"metric": "branch-mode time to proven optimal (sum over the reference's tasks)",
+            "value": total, "unit": "s", "higher_is_better": False, "n_gpus": 1,
+            "data": "the reference's task files", "config": {"workload": "branch mode, "
+            "reference tasks at their documented optimal lengths (is_power2 7, max 7, abs 6, ...)"},
+            "all_lengths_match": all(r["found_length"] == r["published_length"] for r in rows),
+            "tasks": rows}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -359,7 +392,8 @@ def main():
     if args.workload != "power2":
         from pca_gb300.build import build_engine
         build_engine()
-        return {"batched": run_batched, "served": run_served, "guided": run_guided}[args.workload](args)
+        return {"batched": run_batched, "served": run_served, "guided": run_guided,
+                "branch": run_branch}[args.workload](args)
     rank, world, local = dist_env()
     import torch
     from pca_gb300.build import build_engine

@@ -343,6 +343,14 @@ int  pcagb_record(pcagb_engine_t *e, const task_spec_t *task, int max_depth, uin
  * depth-first order are returned. Errors: see pcagb_branch_last_error. */
 int  pcagb_solve_branch(pcagb_engine_t *e, const task_spec_t *task, int max_depth,
                         pcagb_result_t *res, uint16_t *sol_progs, int *sol_lens, int sol_cap);
+/* The same with the size rule of the last position explicit: when a depth's
+ * last position has more than last_level_max_children children (default
+ * 2^26), its level is not built; the solving children are found directly
+ * and kept when they are the depth-first first of their key (the same
+ * programs), and that depth's counters are the engine's (split_used = K-1). */
+int  pcagb_solve_branch_ex(pcagb_engine_t *e, const task_spec_t *task, int max_depth,
+                           uint64_t last_level_max_children, pcagb_result_t *res,
+                           uint16_t *sol_progs, int *sol_lens, int sol_cap);
 const char *pcagb_branch_last_error(void);
 
 /* The CUDA stream (cudaStream_t) every kernel of this engine runs on, so a

@@ -48,6 +48,9 @@ constexpr int kOpDiv = 0x05, kOpMod = 0x06, kOpCmp = 0x0D, kOpBr = 0x13;
 constexpr uint8_t kFault = 255;
 constexpr int kWarps = 8;
 constexpr int kBThreads = 32 * kWarps;
+/* Last-position children above which the last level is not built (its
+   table alone would take 16 bytes per child). */
+constexpr uint64_t kMaterializeMax = 1ull << 26;
 
 std::string g_berr;
 void set_berr(const char *fmt, ...)
@@ -504,6 +507,129 @@ __global__ void k_bleaf(BDev P, int T, const uint32_t *target, uint8_t *mask)
     }
 }
 
+/* ---- the last position without its level ------------------------------------ */
+
+/* A solving child of the last position: its linear child index (depth-first
+   order), key, parent, candidate and the registers it solves for. */
+struct BSol {
+    uint64_t L;
+    uint64_t key;
+    uint32_t q;
+    uint16_t c;
+    uint8_t mask;
+    uint8_t pad;
+};
+
+/* One warp per parent, one lane per last-position candidate: the output
+   check of every complete kernel without materializing the last level. A
+   register other than the written one solves when the parent's column
+   already matches on every test; the written one when its new column does;
+   a test that faults (here or before) fails every register. */
+template <int TP>
+__global__ void __launch_bounds__(kBThreads)
+k_bsuffix(BDev P, BTab tab, int T, uint32_t p, const uint32_t *target, BSol *out,
+          unsigned long long *count, uint64_t cap)
+{
+    const int lane = threadIdx.x & 31;
+    const uint64_t nw = (uint64_t)gridDim.x * kWarps;
+    for (uint64_t q = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < P.n; q += nw) {
+        uint32_t pm = 0;
+        bool faulted = false;
+        for (int r = 1; r < 8; r++) {
+            bool good = true;
+            if (lane < T) good = P.regs[(q * 8 + r) * TP + lane] == target[lane];
+            if (__all_sync(0xFFFFFFFFu, good)) pm |= 1u << r;
+        }
+        if (lane < T) faulted = P.skip[q * TP + lane] == kFault;
+        if (__any_sync(0xFFFFFFFFu, faulted)) continue;
+        const uint32_t live = P.live[q];
+        const uint32_t m = (live >> 1) & 127u;
+        const uint32_t nc = bcount(tab, m);
+        for (uint32_t c0 = 0; c0 < nc; c0 += 32) {
+            const uint32_t c = c0 + lane;
+            if (c >= nc) continue;
+            const uint32_t insn = bcand(tab, m, c);
+            const uint32_t op = insn >> 11, rdi = (insn >> 8) & 7u;
+            const uint32_t wr = (op != (uint32_t)kOpCmp && op != (uint32_t)kOpBr && rdi != 0) ? rdi : 0u;
+            bool match = wr != 0, fault = false;
+            for (int t = 0; t < T; t++) {
+                uint32_t R[8];
+#pragma unroll
+                for (int r = 0; r < 8; r++) R[r] = P.regs[(q * 8 + r) * TP + t];
+                uint32_t v = 0, f, sk;
+                const uint32_t rd = bexec(insn, p, R, P.flags[q * TP + t], P.skip[q * TP + t], &v, &f, &sk);
+                if (sk == kFault) fault = true;
+                if (wr) match &= (rd == wr ? v : R[wr]) == target[t];
+            }
+            if (fault) continue;
+            const uint32_t clive = live | (wr ? 1u << wr : 0u);
+            uint32_t mask = pm & clive & ~(1u << wr);
+            if (match) mask |= 1u << wr;
+            mask &= 0xFEu;
+            if (!mask) continue;
+            const unsigned long long i = atomicAdd(count, 1ull);
+            if (i < cap) {
+                BSol s;
+                s.L = P.child_off[q] + c;
+                s.key = child_key<TP>(P, q, insn, p, T);
+                s.q = (uint32_t)q;
+                s.c = (uint16_t)c;
+                s.mask = (uint8_t)mask;
+                s.pad = 0;
+                out[i] = s;
+            }
+        }
+    }
+}
+
+/* Second pass: the depth-first-first child of each solving key. slots holds
+   the solving keys (open addressing, 0 = empty); first[slot] gets the
+   minimum linear child index among all children with that key. */
+template <int TP>
+__global__ void __launch_bounds__(kBThreads)
+k_bfirst(BDev P, BTab tab, int T, uint32_t p, const unsigned long long *slots, uint64_t smask,
+         unsigned long long *first)
+{
+    const int lane = threadIdx.x & 31;
+    const uint64_t nw = (uint64_t)gridDim.x * kWarps;
+    for (uint64_t q = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < P.n; q += nw) {
+        const uint32_t m = (P.live[q] >> 1) & 127u;
+        const uint32_t nc = bcount(tab, m);
+        for (uint32_t c = lane; c < nc; c += 32) {
+            const uint32_t insn = bcand(tab, m, c);
+            if ((insn >> 11) == (uint32_t)kOpBr) continue;
+            const uint64_t key = child_key<TP>(P, q, insn, p, T) | 1ull;
+            uint64_t i = key & smask;
+            for (uint64_t probes = 0; probes <= smask; probes++) {
+                const unsigned long long s = slots[i];
+                if (s == 0) break;
+                if (s == key) {
+                    atomicMin(&first[i], (unsigned long long)(P.child_off[q] + c));
+                    break;
+                }
+                i = (i + 1) & smask;
+            }
+        }
+    }
+}
+
+/* Pairs of last-position children (parent, candidate) compared in full,
+   one warp per pair: eq[i] = 1 when equal in registers and flags. */
+template <int TP>
+__global__ void k_bpairs_equal(BDev P, BTab tab, int T, uint32_t p, const uint4 *pairs, uint64_t n,
+                               uint8_t *eq)
+{
+    const int lane = threadIdx.x & 31;
+    const uint64_t nw = (uint64_t)gridDim.x * (blockDim.x >> 5);
+    for (uint64_t i = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < n; i += nw) {
+        const uint4 pr = pairs[i];
+        const uint32_t ia = bcand(tab, (P.live[pr.x] >> 1) & 127u, pr.y);
+        const uint32_t ib = bcand(tab, (P.live[pr.z] >> 1) & 127u, pr.w);
+        const bool e = bchild_equal<TP>(P, pr.x, ia, pr.z, ib, p, T, lane);
+        if (lane == 0) eq[i] = e ? 1 : 0;
+    }
+}
+
 /* ---- host driver ----------------------------------------------------------- */
 
 struct BranchRun {
@@ -579,7 +705,9 @@ int blaunch(BranchRun &b)
 
 /* Expand level P (position p of a depth-K pass) into C. Fills the number of
    generated children. */
-int build_blevel(BranchRun &b, BLevel &P, uint32_t p, int mf, BLevel &C)
+/* Children of every state of P at a position with mf forward offsets:
+   P.child_off (exclusive scan) and P.children. */
+int count_bchildren(BranchRun &b, BLevel &P, int mf)
 {
     const BTab tab = b.tab(mf);
     P.child_off = b.alloc<uint64_t>(P.n + 1);
@@ -608,6 +736,15 @@ int build_blevel(BranchRun &b, BLevel &P, uint32_t p, int mf, BLevel &C)
                  (unsigned long long)total);
         return PCAGB_ENOMEM;
     }
+    return PCAGB_OK;
+}
+
+int build_blevel(BranchRun &b, BLevel &P, uint32_t p, int mf, BLevel &C)
+{
+    const BTab tab = b.tab(mf);
+    int rc = P.child_off ? PCAGB_OK : count_bchildren(b, P, mf);
+    if (rc) return rc;
+    const uint64_t total = P.children;
     const uint64_t words = (total + 31) / 32;
     uint64_t slots = 1024;
     while (slots < 2 * total) slots <<= 1;
@@ -682,6 +819,158 @@ int fetch_links(BranchRun &b, const BLevel &L, HostLevel &H, bool links)
     return PCAGB_OK;
 }
 
+/* The last position of a depth-K pass without building level K: solving
+ * children from k_bsuffix; a child counts only if it is the depth-first
+ * first of its key (the pruner would have dropped it otherwise), found by a
+ * second pass over all children (k_bfirst) and checked by full compares.
+ * Returns the number of solutions found (0 = none at this depth). */
+int64_t branch_suffix(BranchRun &b, const BranchTables &bt, std::vector<BLevel> &lv, int K,
+                      const task_spec_t *task, pcagb_result_t *res, uint16_t *sol_progs,
+                      int *sol_lens, int cap)
+{
+    BLevel &P = lv[K - 1];
+    const BTab tab = b.tab(0);
+    const uint32_t p = (uint32_t)(K - 1);
+    const uint64_t kCap = 1ull << 22;
+    BSol *d_sol = b.alloc<BSol>(kCap);
+    unsigned long long *d_cnt = b.alloc<unsigned long long>(1);
+    if (!d_sol || !d_cnt) { set_berr("device memory exhausted"); return PCAGB_ENOMEM; }
+    BCK(cudaMemsetAsync(d_cnt, 0, 8, b.st));
+    if (b.TP == 16)
+        k_bsuffix<16><<<b.grid(4), kBThreads, 0, b.st>>>(bdev(P), tab, b.T, p, b.d_target, d_sol, d_cnt, kCap);
+    else
+        k_bsuffix<32><<<b.grid(4), kBThreads, 0, b.st>>>(bdev(P), tab, b.T, p, b.d_target, d_sol, d_cnt, kCap);
+    int rc = blaunch(b);
+    if (rc) return rc;
+    unsigned long long cnt = 0;
+    BCK(cudaMemcpyAsync(&cnt, d_cnt, 8, cudaMemcpyDeviceToHost, b.st));
+    BCK(cudaStreamSynchronize(b.st));
+    if (cnt > kCap) {
+        set_berr("%llu solving children at depth %d: more than the last-position buffer holds",
+                 (unsigned long long)cnt, K);
+        return PCAGB_ELIMIT;
+    }
+    if (cnt == 0) return 0;
+    std::vector<BSol> sol(cnt);
+    BCK(cudaMemcpyAsync(sol.data(), d_sol, cnt * sizeof(BSol), cudaMemcpyDeviceToHost, b.st));
+    BCK(cudaStreamSynchronize(b.st));
+    b.d2h += cnt * sizeof(BSol) + 8;
+    /* the depth-first first child of every solving key */
+    uint64_t slots = 1024;
+    while (slots < 2 * cnt) slots <<= 1;
+    std::vector<unsigned long long> hs(slots, 0);
+    auto slot_of = [&](uint64_t key) {
+        const uint64_t k = key | 1ull;
+        uint64_t i = k & (slots - 1);
+        while (hs[i] && hs[i] != k) i = (i + 1) & (slots - 1);
+        return i;
+    };
+    for (const BSol &x : sol) hs[slot_of(x.key)] = x.key | 1ull;
+    unsigned long long *d_slots = b.alloc<unsigned long long>(slots);
+    unsigned long long *d_first = b.alloc<unsigned long long>(slots);
+    if (!d_slots || !d_first) { set_berr("device memory exhausted"); return PCAGB_ENOMEM; }
+    BCK(cudaMemcpyAsync(d_slots, hs.data(), slots * 8, cudaMemcpyHostToDevice, b.st));
+    BCK(cudaMemsetAsync(d_first, 0xFF, slots * 8, b.st));
+    if (b.TP == 16)
+        k_bfirst<16><<<b.grid(4), kBThreads, 0, b.st>>>(bdev(P), tab, b.T, p, d_slots, slots - 1, d_first);
+    else
+        k_bfirst<32><<<b.grid(4), kBThreads, 0, b.st>>>(bdev(P), tab, b.T, p, d_slots, slots - 1, d_first);
+    rc = blaunch(b);
+    if (rc) return rc;
+    std::vector<unsigned long long> first(slots);
+    std::vector<uint64_t> coff(P.n + 1);
+    BCK(cudaMemcpyAsync(first.data(), d_first, slots * 8, cudaMemcpyDeviceToHost, b.st));
+    BCK(cudaMemcpyAsync(coff.data(), P.child_off, (P.n + 1) * 8, cudaMemcpyDeviceToHost, b.st));
+    BCK(cudaStreamSynchronize(b.st));
+    b.d2h += slots * 8 + (P.n + 1) * 8;
+    /* a solving child that is not the first of its key is dropped when the
+       first is equal to it in full (a 64-bit key collision would stop here) */
+    std::vector<uint4> pairs;
+    std::vector<size_t> pair_of;
+    std::vector<uint8_t> keep(cnt, 1);
+    for (size_t i = 0; i < cnt; i++) {
+        const uint64_t f = first[slot_of(sol[i].key)];
+        if (f == sol[i].L) continue;
+        const uint64_t q = (uint64_t)(std::upper_bound(coff.begin(), coff.end(), f) - coff.begin()) - 1;
+        pairs.push_back(make_uint4(sol[i].q, sol[i].c, (uint32_t)q, (uint32_t)(f - coff[q])));
+        pair_of.push_back(i);
+    }
+    if (!pairs.empty()) {
+        uint4 *d_pairs = b.alloc<uint4>(pairs.size());
+        uint8_t *d_eq = b.alloc<uint8_t>(pairs.size());
+        if (!d_pairs || !d_eq) { set_berr("device memory exhausted"); return PCAGB_ENOMEM; }
+        BCK(cudaMemcpyAsync(d_pairs, pairs.data(), pairs.size() * sizeof(uint4), cudaMemcpyHostToDevice, b.st));
+        if (b.TP == 16)
+            k_bpairs_equal<16><<<b.grid(2), 256, 0, b.st>>>(bdev(P), tab, b.T, p, d_pairs, pairs.size(), d_eq);
+        else
+            k_bpairs_equal<32><<<b.grid(2), 256, 0, b.st>>>(bdev(P), tab, b.T, p, d_pairs, pairs.size(), d_eq);
+        rc = blaunch(b);
+        if (rc) return rc;
+        std::vector<uint8_t> eq(pairs.size());
+        BCK(cudaMemcpyAsync(eq.data(), d_eq, pairs.size(), cudaMemcpyDeviceToHost, b.st));
+        BCK(cudaStreamSynchronize(b.st));
+        for (size_t j = 0; j < pairs.size(); j++) {
+            if (!eq[j]) {
+                set_berr("64-bit key collision between distinct children at depth %d", K);
+                return PCAGB_ELIMIT;
+            }
+            keep[pair_of[j]] = 0;
+        }
+    }
+    std::vector<std::pair<uint64_t, int>> order;  /* (L, register) in depth-first order */
+    std::vector<size_t> idx;
+    for (size_t i = 0; i < cnt; i++)
+        if (keep[i]) idx.push_back(i);
+    std::sort(idx.begin(), idx.end(), [&](size_t a, size_t c) { return sol[a].L < sol[c].L; });
+    uint64_t found = 0;
+    for (size_t i : idx) found += __builtin_popcount(sol[i].mask);
+    if (found == 0) return 0;
+    /* programs: prefix links of levels 1..K-1, then the last candidate */
+    std::vector<HostLevel> H(K);
+    for (int d = 0; d < K; d++) {
+        rc = fetch_links(b, lv[d], H[d], d > 0);
+        if (rc) return rc;
+    }
+    /* the reference's walk stops at the leaf that brings its count to 100 */
+    int stored = 0;
+    uint64_t listed = 0;
+    for (size_t i : idx) {
+        for (int r = 1; r < 8; r++) {
+            if (!(sol[i].mask >> r & 1u)) continue;
+            listed++;
+            if (stored >= cap || !sol_progs) continue;
+            std::vector<uint16_t> kern(K);
+            BTab last{bt.pre_off.data(), bt.post_off.data(), bt.pre.data(), bt.post.data(), 0};
+            kern[K - 1] = bcand(last, (H[K - 1].live[sol[i].q] >> 1) & 127u, sol[i].c);
+            uint64_t s = sol[i].q;
+            for (int d = K - 1; d >= 1; d--) {
+                const uint32_t par = H[d].parent[s];
+                BTab ht{bt.pre_off.data(), bt.post_off.data(), bt.pre.data(), bt.post.data(), K - d};
+                kern[d - 1] = bcand(ht, (H[d - 1].live[par] >> 1) & 127u, H[d].cidx[s]);
+                s = par;
+            }
+            uint16_t prog[16] = {0};
+            int n = 0;
+            for (int q = 0; q < task->num_inputs; q++)
+                prog[n++] = (uint16_t)PCA_ENC_I(PCA_OP_IN, q + 1, task->input_ports[q]);
+            for (uint16_t w : kern) prog[n++] = w;
+            prog[n++] = (uint16_t)PCA_ENC_I(PCA_OP_OUT, r, task->output_ports[0]);
+            prog[n++] = (uint16_t)PCA_ENC_R(PCA_OP_HLT, 0, 0, 0);
+            if (task_evaluate(task, prog, n) != task->num_tests) {
+                set_berr("internal: a branch-mode solution failed the VM re-check");
+                return PCAGB_ELIMIT;
+            }
+            memcpy(sol_progs + (size_t)stored * 16, prog, sizeof prog);
+            if (sol_lens) sol_lens[stored] = n;
+            stored++;
+        }
+        if (listed >= 100) break;
+    }
+    res->stored = stored;
+    res->total_solutions = listed;
+    return (int64_t)listed;
+}
+
 }  // namespace
 
 /* Internal accessors of engine.cu. */
@@ -694,6 +983,14 @@ const char *pcagb_branch_last_error(void) { return g_berr.c_str(); }
 
 int pcagb_solve_branch(pcagb_engine_t *e, const task_spec_t *task, int max_depth,
                        pcagb_result_t *res, uint16_t *sol_progs, int *sol_lens, int sol_cap)
+{
+    return pcagb_solve_branch_ex(e, task, max_depth, kMaterializeMax, res, sol_progs, sol_lens,
+                                 sol_cap);
+}
+
+int pcagb_solve_branch_ex(pcagb_engine_t *e, const task_spec_t *task, int max_depth,
+                          uint64_t last_level_max_children, pcagb_result_t *res,
+                          uint16_t *sol_progs, int *sol_lens, int sol_cap)
 {
     if (!e || !task || !res) { set_berr("null argument"); return PCAGB_EINVAL; }
     memset(res, 0, sizeof *res);
@@ -763,12 +1060,39 @@ int pcagb_solve_branch(pcagb_engine_t *e, const task_spec_t *task, int max_depth
         BCK(cudaMemcpyAsync(lv[0].parent, &zero, 4, cudaMemcpyHostToDevice, b.st));
         BCK(cudaMemcpyAsync(lv[0].cidx, &zero, 2, cudaMemcpyHostToDevice, b.st));
         uint64_t tried = 0, pruned = 0;
+        bool unbuilt_last = false;
         for (int d = 0; d < K; d++) {
             const int mf = K - d - 1;
+            if (d == K - 1) {
+                int rc = count_bchildren(b, lv[d], mf);
+                if (rc) return rc;
+                if (lv[d].children > last_level_max_children) {
+                    unbuilt_last = true;
+                    break;
+                }
+            }
             int rc = build_blevel(b, lv[d], (uint32_t)d, mf, lv[d + 1]);
             if (rc) return rc;
             tried += lv[d + 1].n;
             pruned += lv[d].children - lv[d + 1].n;
+        }
+        if (unbuilt_last) {
+            /* the engine's counters for this depth: states built plus the
+               last position's children (the reference's walk is not
+               replayed without the last level) */
+            res->split_used = K - 1;
+            res->tried[K] = tried + lv[K - 1].children;
+            res->pruned_cum[K] = pruned_cum + pruned;
+            res->candidates[K] = res->tried[K];
+            res->level_children[K] = lv[K - 1].children;
+            const int64_t got = branch_suffix(b, bt, lv, K, task, res, sol_progs, sol_lens, cap);
+            if (got < 0) return (int)got;
+            pruned_cum += pruned;
+            if (got > 0) {
+                res->optimal_depth = K;
+                break;
+            }
+            continue;
         }
         res->level_children[K] = K ? lv[K - 1].children : 1;
         res->level_survivors[K] = lv[K].n;

@@ -125,7 +125,8 @@ EXPORTS = [
     "search_exhaustive_complete", "search_exhaustive_states_explored", "search_state_dump",
     "pcagb_last_error", "pcagb_default_opts", "pcagb_engine_create", "pcagb_engine_destroy",
     "pcagb_solve", "pcagb_solve_batch", "pcagb_solve_batch_cb", "pcagb_solve_ordered",
-    "pcagb_complete", "pcagb_record", "pcagb_solve_branch", "pcagb_branch_last_error",
+    "pcagb_complete", "pcagb_record", "pcagb_solve_branch", "pcagb_solve_branch_ex",
+    "pcagb_branch_last_error",
     "pcagb_num_candidates",
     "pcagb_engine_stream", "pcagb_device_memory",
     "pcagb_solve_small_noalloc", "pcagb_noalloc_last_error",
@@ -174,6 +175,9 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
                           ctypes.c_char_p, P(RecordStats)], ctypes.c_int),
         "pcagb_solve_branch": ([ctypes.c_void_p, P(TaskSpec), ctypes.c_int, P(SolveResult),
                                 P(ctypes.c_uint16), P(ctypes.c_int), ctypes.c_int], ctypes.c_int),
+        "pcagb_solve_branch_ex": ([ctypes.c_void_p, P(TaskSpec), ctypes.c_int, ctypes.c_uint64,
+                                   P(SolveResult), P(ctypes.c_uint16), P(ctypes.c_int), ctypes.c_int],
+                                  ctypes.c_int),
         "pcagb_branch_last_error": ([], ctypes.c_char_p),
         "pcagb_num_candidates": ([ctypes.c_uint8], ctypes.c_int),
         "pcagb_engine_stream": ([ctypes.c_void_p], ctypes.c_void_p),
@@ -258,6 +262,28 @@ class PCALib:
         buf = ctypes.create_string_buffer(64)
         self.lib.pca_disasm(insn, buf, 64)
         return buf.value.decode()
+
+
+def task_from_dict(d: dict) -> "TaskSpec":
+    """A task spec from the task JSON's fields (tasks/spec.c:80-184: name,
+    max_cycles, input_ports, output_ports, tests[{in, out}], values masked to
+    16 bits, at most 32 tests)."""
+    s = TaskSpec()
+    s.name = str(d.get("name", "")).encode()[:63]
+    s.max_cycles = int(d.get("max_cycles", 1000))
+    s.num_inputs = len(d["input_ports"])
+    for i, p in enumerate(d["input_ports"]):
+        s.input_ports[i] = p
+    s.num_outputs = len(d["output_ports"])
+    for i, p in enumerate(d["output_ports"]):
+        s.output_ports[i] = p
+    for t, tc in enumerate(d["tests"][:32]):
+        for i, v in enumerate(tc["in"]):
+            s.tests[t].inputs[i] = v & 0xFFFF
+        for i, v in enumerate(tc["out"]):
+            s.tests[t].outputs[i] = v & 0xFFFF
+    s.num_tests = min(len(d["tests"]), 32)
+    return s
 
 
 def make_task(name, inputs, outputs, max_cycles=100, input_ports=None) -> TaskSpec:
@@ -472,15 +498,23 @@ class Engine:
         """cudaStream_t of the engine, as an integer handle."""
         return self.lib.pcagb_engine_stream(self.h) or 0
 
-    def solve_branch(self, task: TaskSpec, max_depth: int = 4, sol_cap: int = 100) -> Solution:
+    def solve_branch(self, task: TaskSpec, max_depth: int = 4, sol_cap: int = 100,
+                     last_level_max_children: int | None = None) -> Solution:
         """Branch mode (CMP / forward BR / DIV / MOD): the reference solver's
-        default search, with its per-depth counters and its first programs."""
+        default search, with its per-depth counters and its first programs.
+        last_level_max_children: above it a depth's last level is not built
+        (None = the library's default)."""
         r = SolveResult()
         cap = max(sol_cap, 1)
         progs = (ctypes.c_uint16 * (16 * cap))()
         lens = (ctypes.c_int * cap)()
-        rc = self.lib.pcagb_solve_branch(self.h, ctypes.byref(task), max_depth, ctypes.byref(r),
-                                         progs, lens, cap)
+        if last_level_max_children is None:
+            rc = self.lib.pcagb_solve_branch(self.h, ctypes.byref(task), max_depth,
+                                             ctypes.byref(r), progs, lens, cap)
+        else:
+            rc = self.lib.pcagb_solve_branch_ex(self.h, ctypes.byref(task), max_depth,
+                                                last_level_max_children, ctypes.byref(r), progs,
+                                                lens, cap)
         if rc != 0:
             raise EngineError(f"branch solve failed ({rc}): "
                               f"{self.lib.pcagb_branch_last_error().decode()}")
@@ -491,6 +525,7 @@ class Engine:
         last = r.optimal_depth if r.optimal_depth >= 0 else max_depth
         sol.tried = [r.tried[k] for k in range(last + 1)]
         sol.pruned_cum = [r.pruned_cum[k] for k in range(last + 1)]
+        sol.split_used = r.split_used
         return sol
 
     def record(self, task: TaskSpec, out_dir: str, max_depth: int = 4, task_id: int = 0,

@@ -80,3 +80,39 @@ def test_branch_cli_report(tmp_path):
     assert f"Found {fx['found']} distinct program(s)" in p.stdout
     for k, c in enumerate(fx["candidates"]):
         assert f"  candidates: {c}  " in p.stdout
+
+
+@pytest.mark.parametrize("fx", [f for f in BRANCH if f["optimal_depth"] in (1, 2)][::3],
+                         ids=lambda f: f"task{f['index']}")
+def test_unbuilt_last_level_gives_same_programs(engine, fx):
+    """Without building the last level (solving children found directly, the
+    pruner's choice replayed by a second pass), the optimal length and the
+    printed programs are the same."""
+    task = spec_from_json(fx["task"])
+    full = engine.solve_branch(task, max_depth=fx["max_depth"])
+    direct = engine.solve_branch(task, max_depth=fx["max_depth"], last_level_max_children=0)
+    assert direct.optimal_depth == full.optimal_depth
+    assert direct.programs == full.programs
+    assert direct.split_used == full.optimal_depth - 1
+
+
+PUBLISHED = load_golden("ref_published.json")
+
+
+@pytest.mark.parametrize("t", [t for t in PUBLISHED if t["name"] != "saturating_add"],
+                         ids=lambda t: t["name"])
+def test_published_branch_mode_lengths(engine, t):
+    """The reference's documented optimal lengths of its own task files in
+    branch mode (negate/double/square 4, add 5, abs/relu 6, max 7, is_power2
+    7), found and proven here (every shorter depth searched completely); the
+    programs pass the VM."""
+    from pca_gb300.pcalib import PCALib
+    task = spec_from_json(t["task"])
+    K = t["published_length"] - task.num_inputs - 2
+    sol = engine.solve_branch(task, max_depth=K)
+    assert sol.optimal_depth == K
+    lib = PCALib()
+    assert sol.programs
+    for prog in sol.programs:
+        assert len(prog) == t["published_length"]
+        assert lib.evaluate(task, prog) == task.num_tests

@@ -226,7 +226,11 @@ int fetch_hist(pcagb_engine *e, Level &L)
 {
     const size_t nh = (size_t)e->ntasks * 128;
     CK(cudaMemsetAsync(e->d_hist, 0, nh * sizeof(unsigned long long), e->stream));
-    k_task_hist<<<e->grid(2), 256, 0, e->stream>>>(L.live, L.task, L.n, e->d_hist);
+    if (nh <= 4096)
+        k_task_hist_smem<<<e->grid(2), 256, nh * sizeof(uint32_t), e->stream>>>(
+            L.live, L.task, L.n, (uint32_t)nh, e->d_hist);
+    else
+        k_task_hist<<<e->grid(2), 256, 0, e->stream>>>(L.live, L.task, L.n, e->d_hist);
     int rc = check_launch(e);
     if (rc) return rc;
     L.hist.assign(nh, 0);

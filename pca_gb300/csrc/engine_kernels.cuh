@@ -530,6 +530,30 @@ __global__ void k_task_hist(const uint8_t *live, const uint16_t *task, uint64_t 
     }
 }
 
+/* The same with a per-block histogram in shared memory (nbins u32 counters,
+   nbins = tasks x 128 <= 4096), flushed with one global atomic per nonzero
+   bin: a level's states crowd a few bins, and per-warp global atomics on
+   them serialize. */
+__global__ void k_task_hist_smem(const uint8_t *live, const uint16_t *task, uint64_t n,
+                                 uint32_t nbins, unsigned long long *hist)
+{
+    extern __shared__ uint32_t sh_hist[];
+    for (uint32_t b = threadIdx.x; b < nbins; b += blockDim.x) sh_hist[b] = 0;
+    __syncthreads();
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    const uint64_t n_round = (n + 31) & ~31ull;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_round; i += stride) {
+        const bool valid = i < n;
+        const uint32_t key = valid ? (uint32_t)task[i] * 128u + ((live[i] >> 1) & 127u) : ~0u;
+        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, key);
+        if (valid && (threadIdx.x & 31) == __ffs(peers) - 1 && key < nbins)
+            atomicAdd(&sh_hist[key], (uint32_t)__popc(peers));
+    }
+    __syncthreads();
+    for (uint32_t b = threadIdx.x; b < nbins; b += blockDim.x)
+        if (sh_hist[b]) atomicAdd(&hist[b], (unsigned long long)sh_hist[b]);
+}
+
 /* ---- solutions ----------------------------------------------------------- */
 
 struct SolBuf {

@@ -475,38 +475,43 @@ k_materialize(LevelDev P, TaskDev task, const uint32_t *bitmap, const uint64_t *
         const uint32_t base = c_cand_off[m], nc = c_cand_off[m + 1] - base;
         const uint64_t off = P.child_off[q];
         for (uint32_t c0 = 0; c0 < nc; c0 += 32) {
-            uint32_t c = c0 + lane;
+            /* each lane settles its own candidate (kept?, rank, micro-op and
+               the child's links) so the per-child loop below needs no
+               global load */
+            const uint32_t c = c0 + lane;
             bool keep = false;
+            uint64_t rank = 0;
+            uint32_t u = 0;
             if (c < nc) {
-                uint64_t L = off + c;
-                keep = (bitmap[L >> 5] >> (L & 31)) & 1u;
+                const uint64_t L = off + c;
+                const uint32_t wv = bitmap[L >> 5];
+                keep = (wv >> (L & 31)) & 1u;
+                if (keep) {
+                    rank = word_off[L >> 5] + __popc(wv & ((1u << (L & 31)) - 1u));
+                    u = c_cand_uop[base + c];
+                    C.live[rank] = (uint8_t)(live | (1u << UOP_RD(u)));
+                    C.task[rank] = (uint16_t)tid;
+                    C.parent[rank] = (uint32_t)q;
+                    C.cidx[rank] = (uint16_t)c;
+                }
             }
             uint32_t bal = __ballot_sync(0xFFFFFFFFu, keep);
             while (bal) {
                 const int j = __ffs(bal) - 1;
                 bal &= bal - 1;
-                const uint32_t cj = c0 + j;
-                const uint64_t L = off + cj;
-                const uint32_t wv = bitmap[L >> 5];
-                const uint64_t rank = word_off[L >> 5] + __popc(wv & ((1u << (L & 31)) - 1u));
-                const uint32_t u = c_cand_uop[base + cj];
-                const uint32_t op = UOP_OP(u), rd = UOP_RD(u);
+                const uint64_t rk = __shfl_sync(0xFFFFFFFFu, rank, j);
+                const uint32_t uj = __shfl_sync(0xFFFFFFFFu, u, j);
+                const uint32_t op = UOP_OP(uj), rd = UOP_RD(uj);
                 if (lane < TPC) {
-                    uint32_t a = ws.R[UOP_A(u)][lane], b = ws.R[UOP_B(u)][lane];
-                    uint32_t res = pca_alu(op, a, b, UOP_IMM(u));
-                    uint32_t f = pca_alu_flags(op, a, b, UOP_IMM(u), res, ws.F[lane]);
+                    uint32_t a = ws.R[UOP_A(uj)][lane], b = ws.R[UOP_B(uj)][lane];
+                    uint32_t res = pca_alu(op, a, b, UOP_IMM(uj));
+                    uint32_t f = pca_alu_flags(op, a, b, UOP_IMM(uj), res, ws.F[lane]);
                     if (lane >= T) { res = 0; f = 0; }
-                    uint16_t *dst = C.regs + rank * 8 * TPC + lane;
+                    uint16_t *dst = C.regs + rk * 8 * TPC + lane;
 #pragma unroll
                     for (uint32_t r = 0; r < 8; r++)
                         dst[r * TPC] = (uint16_t)(r == rd ? res : ws.R[r][lane]);
-                    C.flags[rank * TPC + lane] = (uint8_t)f;
-                }
-                if (lane == 0) {
-                    C.live[rank] = (uint8_t)(live | (1u << rd));
-                    C.task[rank] = (uint16_t)tid;
-                    C.parent[rank] = (uint32_t)q;
-                    C.cidx[rank] = (uint16_t)cj;
+                    C.flags[rk * TPC + lane] = (uint8_t)f;
                 }
             }
         }

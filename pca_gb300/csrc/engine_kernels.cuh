@@ -252,23 +252,21 @@ __device__ __forceinline__ void child_hashes_any(uint32_t op, const WarpState<TP
 }
 
 /* Exact compare of child A (the warp's parent in shared memory + micro-op
-   uA) with child B (parent qB of the level in HBM + candidate cB), the whole
+   uA) with child B (parent qB of the level in HBM + micro-op uB), the whole
    warp cooperating: lane t rebuilds test t of both children (every register,
-   the flags) and __all_sync decides. All lanes must call it. */
+   the flags) and __all_sync decides. The requesting lane has already checked
+   the task and (when it is part of the key) the live mask. All lanes must
+   call it. */
 template <int TPC>
-__device__ bool warp_child_equal(const LevelDev &P, const TaskDev &task, const WarpState<TPC> &A,
-                                 uint64_t qA, uint32_t tid, int T, uint32_t liveA, uint32_t uA,
-                                 uint64_t qB, uint32_t cB, int lane)
+__device__ bool warp_child_equal(const LevelDev &P, const WarpState<TPC> &A, uint64_t qA, int T,
+                                 uint32_t uA, uint64_t qB, uint32_t uB, int lane)
 {
-    const uint32_t rdA = UOP_RD(uA);
+    const uint32_t rdA = UOP_RD(uA), rdB = UOP_RD(uB);
+    bool ok = true;
     if (qB == qA) {
         /* same parent (about a fifth of the duplicates): only the written
            columns and the flags can differ, and the parent is in shared
            memory */
-        const uint32_t uB = c_cand_uop[c_cand_off[(liveA >> 1) & 127u] + cB];
-        const uint32_t rdB = UOP_RD(uB);
-        if (task.key_live && ((liveA | (1u << rdA)) != (liveA | (1u << rdB)))) return false;
-        bool ok = true;
         if (lane < T) {
             const uint32_t a1 = A.R[UOP_A(uA)][lane], b1 = A.R[UOP_B(uA)][lane];
             const uint32_t resA = pca_alu(UOP_OP(uA), a1, b1, UOP_IMM(uA));
@@ -286,12 +284,6 @@ __device__ bool warp_child_equal(const LevelDev &P, const TaskDev &task, const W
         }
         return __all_sync(0xFFFFFFFFu, ok);
     }
-    if (P.task[qB] != tid) return false;
-    const uint32_t liveB = P.live[qB];
-    const uint32_t uB = c_cand_uop[c_cand_off[(liveB >> 1) & 127u] + cB];
-    const uint32_t rdB = UOP_RD(uB);
-    if (task.key_live && ((liveA | (1u << rdA)) != (liveB | (1u << rdB)))) return false;
-    bool ok = true;
     if (lane < T) {
         const uint16_t *RB = P.regs + qB * 8 * TPC + lane;
         const uint32_t a1 = A.R[UOP_A(uA)][lane], b1 = A.R[UOP_B(uA)][lane];
@@ -367,16 +359,33 @@ k_expand_insert(LevelDev P, TaskDev task, unsigned long long *table, uint64_t tm
                     }
                     if (!done) needcmp = (s >> 40) == (mine >> 40);
                 }
+                /* a tag match first settles the stored child's task, live
+                   mask and micro-op in its own lane (all lanes at once);
+                   only a match on those takes a warp-wide compare */
+                uint64_t qB = 0;
+                uint32_t uB = 0;
+                if (needcmp) {
+                    const uint64_t oref = (s & kRefMask) - 1;
+                    qB = oref >> 12;
+                    uint32_t liveB = live;
+                    if (qB != q) {
+                        const uint32_t tB = P.task[qB];
+                        liveB = P.live[qB];
+                        needcmp = tB == tid;
+                    }
+                    uB = c_cand_uop[c_cand_off[(liveB >> 1) & 127u] + (uint32_t)(oref & 4095)];
+                    if (task.key_live && (live | (1u << rd)) != (liveB | (1u << UOP_RD(uB))))
+                        needcmp = false;
+                }
                 uint32_t req = __ballot_sync(0xFFFFFFFFu, needcmp);
                 bool eq = false;
                 while (req) {
                     const int j = __ffs(req) - 1;
                     req &= req - 1;
                     const uint32_t uj = __shfl_sync(0xFFFFFFFFu, u, j);
-                    const unsigned long long sj = __shfl_sync(0xFFFFFFFFu, s, j);
-                    const uint64_t oref = (sj & kRefMask) - 1;
-                    const bool e = warp_child_equal<TPC>(P, task, ws, q, tid, T, live, uj,
-                                                         oref >> 12, (uint32_t)(oref & 4095), lane);
+                    const uint32_t ubj = __shfl_sync(0xFFFFFFFFu, uB, j);
+                    const uint64_t qbj = __shfl_sync(0xFFFFFFFFu, qB, j);
+                    const bool e = warp_child_equal<TPC>(P, ws, q, T, uj, qbj, ubj, lane);
                     if (lane == j) eq = e;
                 }
                 if (!done) {

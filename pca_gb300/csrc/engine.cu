@@ -1117,6 +1117,12 @@ int engine_init(pcagb_engine *e, int device, size_t budget)
     CK(cudaEventCreate(&e->ev2));
     CK(cudaEventCreate(&e->ev3));
     {
+        /* the insert kernel keeps each warp's children in shared memory:
+           its occupancy needs the largest shared-memory carveout */
+        cudaFuncSetAttribute(k_expand_insert<32>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             cudaSharedmemCarveoutMaxShared);
+        cudaFuncSetAttribute(k_expand_insert<16>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             cudaSharedmemCarveoutMaxShared);
         int nb = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_expand_insert<32>, kThreads, 0) ==
                 cudaSuccess && nb > 0)

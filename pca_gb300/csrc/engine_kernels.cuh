@@ -122,8 +122,8 @@ __device__ __forceinline__ uint64_t task_final(uint32_t task)
     return fmix64(0x9E3779B97F4A7C15ull * (task + 1));
 }
 
-template <int TPC>
-__device__ __forceinline__ uint64_t hash_column(const uint32_t *col)
+template <int TPC, typename E>
+__device__ __forceinline__ uint64_t hash_column(const E *col)
 {
     uint64_t h = 0x243F6A8885A308D3ull;
 #pragma unroll
@@ -172,6 +172,32 @@ __device__ __forceinline__ void load_state(WarpState<TPC> &ws, const uint16_t *r
 
 /* ---- level expansion: insert every child into the exact table ------------ */
 
+/* One warp's shared memory in the insert kernel: its parent (16-bit columns,
+   a row stride of TPC + 2 halves so that lanes reading different operand
+   columns of one test hit different banks) and the new column and flags of
+   each lane's child in the current chunk, which the warp-wide compares read
+   instead of recomputing them. */
+template <int TPC>
+struct InsertState {
+    uint64_t colh[8];           /* colh[r] = col_final(r, hash(col r)), r >= 1 */
+    uint64_t flagsA[TPC / 16][32]; /* [word][lane]: the lane's child flags, 4 bits a test */
+    uint16_t R[8][TPC + 2];
+    uint16_t colA[TPC][33];     /* [test][lane]: odd stride, a test row per lane is conflict free */
+    uint8_t F[TPC];
+};
+
+template <int TPC>
+__device__ __forceinline__ void load_insert_state(InsertState<TPC> &ws, const uint16_t *regs,
+                                                  const uint8_t *flags, uint64_t q, int lane)
+{
+    if (lane < TPC) {
+        const uint16_t *src = regs + q * 8 * TPC + lane;
+#pragma unroll
+        for (int r = 0; r < 8; r++) ws.R[r][lane] = src[r * TPC];
+        ws.F[lane] = flags[q * TPC + lane];
+    }
+}
+
 /* The op is a template parameter here: a warp expands a run of candidates
    that share one op, so the switch is resolved at compile time and the
    lanes never diverge on it. */
@@ -203,12 +229,14 @@ __device__ __forceinline__ uint32_t flags_t(uint32_t a, uint32_t b, uint32_t imm
 }
 
 /* Hash of the child's new column (chain over 4 tests per word) and of its
-   flags (16 tests per word), tests >= T contributing zeros. The loop over
-   word groups is kept rolled: eleven op variants of a fully unrolled loop
-   overflow the instruction cache. */
+   flags (16 tests per word), tests >= T contributing zeros; the column and
+   the flags are also left in the warp's shared memory for the compares. The
+   loop over word groups is kept rolled: eleven op variants of a fully
+   unrolled loop overflow the instruction cache. */
 template <int TPC, int OP>
-__device__ __forceinline__ void child_hashes(const WarpState<TPC> &ws, uint32_t ra, uint32_t rb,
-                                             uint32_t imm, int T, uint64_t &h, uint64_t &hf)
+__device__ __forceinline__ void child_hashes(InsertState<TPC> &ws, uint32_t ra, uint32_t rb,
+                                             uint32_t imm, int T, int lane, uint64_t &h,
+                                             uint64_t &hf)
 {
     h = 0x243F6A8885A308D3ull;
     hf = 0x13198A2E03707344ull;
@@ -223,54 +251,58 @@ __device__ __forceinline__ void child_hashes(const WarpState<TPC> &ws, uint32_t 
             uint32_t res = alu_t<OP>(a, b, imm);
             uint32_t f = flags_t<OP>(a, b, imm, res, ws.F[t]);
             if (t >= T) { res = 0; f = 0; }
+            ws.colA[t][lane] = (uint16_t)res;
             w |= (uint64_t)res << (16 * j);
             wf |= (uint64_t)f << (4 * (t & 15));
         }
         h = chain(h, w);
-        if ((t0 & 15) == 12) { hf = chain(hf, wf); wf = 0; }
+        if ((t0 & 15) == 12) {
+            hf = chain(hf, wf);
+            ws.flagsA[t0 >> 4][lane] = wf;
+            wf = 0;
+        }
     }
 }
 
 template <int TPC>
-__device__ __forceinline__ void child_hashes_any(uint32_t op, const WarpState<TPC> &ws, uint32_t ra,
-                                                 uint32_t rb, uint32_t imm, int T, uint64_t &h,
-                                                 uint64_t &hf)
+__device__ __forceinline__ void child_hashes_any(uint32_t op, InsertState<TPC> &ws, uint32_t ra,
+                                                 uint32_t rb, uint32_t imm, int T, int lane,
+                                                 uint64_t &h, uint64_t &hf)
 {
     switch (op) {
-    case PCA_OP_ADD: child_hashes<TPC, PCA_OP_ADD>(ws, ra, rb, imm, T, h, hf); break;
-    case PCA_OP_SUB: child_hashes<TPC, PCA_OP_SUB>(ws, ra, rb, imm, T, h, hf); break;
-    case PCA_OP_MUL: child_hashes<TPC, PCA_OP_MUL>(ws, ra, rb, imm, T, h, hf); break;
-    case PCA_OP_AND: child_hashes<TPC, PCA_OP_AND>(ws, ra, rb, imm, T, h, hf); break;
-    case PCA_OP_OR: child_hashes<TPC, PCA_OP_OR>(ws, ra, rb, imm, T, h, hf); break;
-    case PCA_OP_XOR: child_hashes<TPC, PCA_OP_XOR>(ws, ra, rb, imm, T, h, hf); break;
-    case PCA_OP_SHL: child_hashes<TPC, PCA_OP_SHL>(ws, ra, rb, imm, T, h, hf); break;
-    case PCA_OP_SHR: child_hashes<TPC, PCA_OP_SHR>(ws, ra, rb, imm, T, h, hf); break;
-    case PCA_OP_ASR: child_hashes<TPC, PCA_OP_ASR>(ws, ra, rb, imm, T, h, hf); break;
-    case PCA_OP_LDI: child_hashes<TPC, PCA_OP_LDI>(ws, ra, rb, imm, T, h, hf); break;
-    default: child_hashes<TPC, PCA_OP_ADDI>(ws, ra, rb, imm, T, h, hf); break;
+    case PCA_OP_ADD: child_hashes<TPC, PCA_OP_ADD>(ws, ra, rb, imm, T, lane, h, hf); break;
+    case PCA_OP_SUB: child_hashes<TPC, PCA_OP_SUB>(ws, ra, rb, imm, T, lane, h, hf); break;
+    case PCA_OP_MUL: child_hashes<TPC, PCA_OP_MUL>(ws, ra, rb, imm, T, lane, h, hf); break;
+    case PCA_OP_AND: child_hashes<TPC, PCA_OP_AND>(ws, ra, rb, imm, T, lane, h, hf); break;
+    case PCA_OP_OR: child_hashes<TPC, PCA_OP_OR>(ws, ra, rb, imm, T, lane, h, hf); break;
+    case PCA_OP_XOR: child_hashes<TPC, PCA_OP_XOR>(ws, ra, rb, imm, T, lane, h, hf); break;
+    case PCA_OP_SHL: child_hashes<TPC, PCA_OP_SHL>(ws, ra, rb, imm, T, lane, h, hf); break;
+    case PCA_OP_SHR: child_hashes<TPC, PCA_OP_SHR>(ws, ra, rb, imm, T, lane, h, hf); break;
+    case PCA_OP_ASR: child_hashes<TPC, PCA_OP_ASR>(ws, ra, rb, imm, T, lane, h, hf); break;
+    case PCA_OP_LDI: child_hashes<TPC, PCA_OP_LDI>(ws, ra, rb, imm, T, lane, h, hf); break;
+    default: child_hashes<TPC, PCA_OP_ADDI>(ws, ra, rb, imm, T, lane, h, hf); break;
     }
 }
 
-/* Exact compare of child A (the warp's parent in shared memory + micro-op
-   uA) with child B (parent qB of the level in HBM + micro-op uB), the whole
-   warp cooperating: lane t rebuilds test t of both children (every register,
-   the flags) and __all_sync decides. The requesting lane has already checked
-   the task and (when it is part of the key) the live mask. All lanes must
-   call it. */
+/* Exact compare of child A (lane jA's child of the warp's parent, its new
+   column and flags in shared memory, micro-op uA) with child B (parent qB of
+   the level in HBM + micro-op uB), the whole warp cooperating: lane t
+   rebuilds test t of child B (every register, the flags) and __all_sync
+   decides. The requesting lane has already checked the task and (when it is
+   part of the key) the live mask. All lanes must call it. */
 template <int TPC>
-__device__ bool warp_child_equal(const LevelDev &P, const WarpState<TPC> &A, uint64_t qA, int T,
-                                 uint32_t uA, uint64_t qB, uint32_t uB, int lane)
+__device__ bool warp_child_equal(const LevelDev &P, const InsertState<TPC> &A, uint64_t qA, int T,
+                                 int jA, uint32_t uA, uint64_t qB, uint32_t uB, int lane)
 {
     const uint32_t rdA = UOP_RD(uA), rdB = UOP_RD(uB);
     bool ok = true;
-    if (qB == qA) {
-        /* same parent (about a fifth of the duplicates): only the written
-           columns and the flags can differ, and the parent is in shared
-           memory */
-        if (lane < T) {
-            const uint32_t a1 = A.R[UOP_A(uA)][lane], b1 = A.R[UOP_B(uA)][lane];
-            const uint32_t resA = pca_alu(UOP_OP(uA), a1, b1, UOP_IMM(uA));
-            const uint32_t fA = pca_alu_flags(UOP_OP(uA), a1, b1, UOP_IMM(uA), resA, A.F[lane]);
+    if (lane < T) {
+        const uint32_t resA = A.colA[lane][jA];
+        const uint32_t fA = (uint32_t)(A.flagsA[lane >> 4][jA] >> (4 * (lane & 15))) & 15u;
+        if (qB == qA) {
+            /* same parent (about a fifth of the duplicates): only the written
+               columns and the flags can differ, and the parent is in shared
+               memory */
             const uint32_t a2 = A.R[UOP_A(uB)][lane], b2 = A.R[UOP_B(uB)][lane];
             const uint32_t resB = pca_alu(UOP_OP(uB), a2, b2, UOP_IMM(uB));
             const uint32_t fB = pca_alu_flags(UOP_OP(uB), a2, b2, UOP_IMM(uB), resB, A.F[lane]);
@@ -281,24 +313,19 @@ __device__ bool warp_child_equal(const LevelDev &P, const WarpState<TPC> &A, uin
                 ok &= resA == A.R[rdA][lane];   /* B keeps the parent's rdA column */
                 ok &= resB == A.R[rdB][lane];   /* A keeps the parent's rdB column */
             }
-        }
-        return __all_sync(0xFFFFFFFFu, ok);
-    }
-    if (lane < T) {
-        const uint16_t *RB = P.regs + qB * 8 * TPC + lane;
-        const uint32_t a1 = A.R[UOP_A(uA)][lane], b1 = A.R[UOP_B(uA)][lane];
-        const uint32_t resA = pca_alu(UOP_OP(uA), a1, b1, UOP_IMM(uA));
-        const uint32_t fA = pca_alu_flags(UOP_OP(uA), a1, b1, UOP_IMM(uA), resA, A.F[lane]);
-        const uint32_t a2 = RB[UOP_A(uB) * TPC], b2 = RB[UOP_B(uB) * TPC];
-        const uint32_t resB = pca_alu(UOP_OP(uB), a2, b2, UOP_IMM(uB));
-        const uint32_t fB = pca_alu_flags(UOP_OP(uB), a2, b2, UOP_IMM(uB), resB,
-                                          P.flags[qB * TPC + lane]);
-        ok = fA == fB;
+        } else {
+            const uint16_t *RB = P.regs + qB * 8 * TPC + lane;
+            const uint32_t a2 = RB[UOP_A(uB) * TPC], b2 = RB[UOP_B(uB) * TPC];
+            const uint32_t resB = pca_alu(UOP_OP(uB), a2, b2, UOP_IMM(uB));
+            const uint32_t fB = pca_alu_flags(UOP_OP(uB), a2, b2, UOP_IMM(uB), resB,
+                                              P.flags[qB * TPC + lane]);
+            ok = fA == fB;
 #pragma unroll
-        for (uint32_t r = 1; r < 8; r++) {
-            const uint32_t vA = r == rdA ? resA : A.R[r][lane];
-            const uint32_t vB = r == rdB ? resB : (uint32_t)RB[r * TPC];
-            ok &= vA == vB;
+            for (uint32_t r = 1; r < 8; r++) {
+                const uint32_t vA = r == rdA ? resA : (uint32_t)A.R[r][lane];
+                const uint32_t vB = r == rdB ? resB : (uint32_t)RB[r * TPC];
+                ok &= vA == vB;
+            }
         }
     }
     return __all_sync(0xFFFFFFFFu, ok);
@@ -311,16 +338,16 @@ __global__ void __launch_bounds__(kThreads, 8)
 k_expand_insert(LevelDev P, TaskDev task, unsigned long long *table, uint64_t tmask,
                 uint32_t *status)
 {
-    __shared__ WarpState<TPC> sws[kWarpsPerBlock];
+    __shared__ InsertState<TPC> sws[kWarpsPerBlock];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    WarpState<TPC> &ws = sws[wib];
+    InsertState<TPC> &ws = sws[wib];
     const uint64_t nw = (uint64_t)gridDim.x * kWarpsPerBlock;
     for (uint64_t q = (uint64_t)blockIdx.x * kWarpsPerBlock + wib; q < P.n; q += nw) {
         const uint32_t tid = P.task[q];
         if (!task.active[tid]) continue;
         const int T = task.T[tid];
         __syncwarp();
-        load_state<TPC>(ws, P.regs, P.flags, q, lane);
+        load_insert_state<TPC>(ws, P.regs, P.flags, q, lane);
         const uint32_t live = P.live[q];
         __syncwarp();
         if (lane >= 1 && lane < 8) ws.colh[lane] = col_final(lane, hash_column<TPC>(ws.R[lane]));
@@ -337,7 +364,9 @@ k_expand_insert(LevelDev P, TaskDev task, unsigned long long *table, uint64_t tm
             const uint32_t u = c_cand_uop[base + c];
             const uint32_t op = UOP_OP(u), rd = UOP_RD(u);
             uint64_t h, hf;
-            child_hashes_any<TPC>(op, ws, UOP_A(u), UOP_B(u), UOP_IMM(u), T, h, hf);
+            __syncwarp();   /* the previous chunk's compares are done with colA */
+            child_hashes_any<TPC>(op, ws, UOP_A(u), UOP_B(u), UOP_IMM(u), T, lane, h, hf);
+            __syncwarp();
             uint64_t H = regsum - ws.colh[rd] + col_final(rd, h) + hf;
             if (task.key_live) H += live_final(live | (1u << rd));
             const uint64_t ref = (q << 12) | c;
@@ -385,7 +414,7 @@ k_expand_insert(LevelDev P, TaskDev task, unsigned long long *table, uint64_t tm
                     const uint32_t uj = __shfl_sync(0xFFFFFFFFu, u, j);
                     const uint32_t ubj = __shfl_sync(0xFFFFFFFFu, uB, j);
                     const uint64_t qbj = __shfl_sync(0xFFFFFFFFu, qB, j);
-                    const bool e = warp_child_equal<TPC>(P, ws, q, T, uj, qbj, ubj, lane);
+                    const bool e = warp_child_equal<TPC>(P, ws, q, T, j, uj, qbj, ubj, lane);
                     if (lane == j) eq = e;
                 }
                 if (!done) {

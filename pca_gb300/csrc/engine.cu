@@ -63,6 +63,12 @@ static void set_err(const char *fmt, ...)
     } while (0)
 
 constexpr int kMaxBatch = 8192;
+/* slots of the pinned host buffer */
+constexpr int kPinStatus = 0, kPinSurvivors = 1, kPinTotal = 2, kPinCount = 3, kPinFirst = 4,
+              kPinHist = 64;
+/* A level whose children fit in this many bytes of states is written into
+   space for all of them, so its build needs one host round trip. */
+constexpr uint64_t kOneSyncBytes = 64ull << 20;
 
 struct Level {
     uint64_t n = 0;
@@ -118,6 +124,10 @@ struct pcagb_engine {
     uint8_t *d_task_active = nullptr;
     uint16_t *d_task_io = nullptr;           /* [kMaxBatch][3][32] in0, in1, target */
     unsigned long long *d_hist = nullptr;    /* [kMaxBatch][128] */
+    /* pinned host mirror of the small results (kPin* slots) and of d_hist:
+       device-to-host reads of these never wait on their own */
+    unsigned long long *h_pin = nullptr;
+    std::vector<uint8_t> h_active;           /* host copy of d_task_active */
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
     int occ_insert = 4, occ_suffix = 8, occ_mat = 4;   /* resident blocks per SM */
     uint64_t launches = 0;
@@ -179,10 +189,15 @@ int check_launch(pcagb_engine *e)
     return PCAGB_OK;
 }
 
-/* Exclusive scan of a[0..n) in place; returns the total in *total. */
+/* Exclusive scan of a[0..n) in place; returns the total in *total, or,
+   with total null, only enqueues the scan (scanning n + 1 entries whose last
+   is 0 leaves the total on the device, in a[n]). */
 int exclusive_scan(pcagb_engine *e, uint64_t *a, uint64_t n, uint64_t *total)
 {
-    if (n == 0) { *total = 0; return PCAGB_OK; }
+    if (n == 0) {
+        if (total) *total = 0;
+        return PCAGB_OK;
+    }
     uint64_t nb = (n + kScanBlock - 1) / kScanBlock;
     size_t saved = e->top;
     uint64_t *sums = (uint64_t *)e->alloc_top((nb + 1) * sizeof(uint64_t));
@@ -191,8 +206,12 @@ int exclusive_scan(pcagb_engine *e, uint64_t *a, uint64_t n, uint64_t *total)
     int rc = check_launch(e);
     if (rc) return rc;
     if (nb == 1) {
-        CK(e_copy(e, total, sums, sizeof(uint64_t), cudaMemcpyDeviceToHost, e->stream));
-        CK(cudaStreamSynchronize(e->stream));
+        if (total) {
+            CK(e_copy(e, &e->h_pin[kPinTotal], sums, sizeof(uint64_t), cudaMemcpyDeviceToHost,
+                      e->stream));
+            CK(cudaStreamSynchronize(e->stream));
+            *total = e->h_pin[kPinTotal];
+        }
     } else {
         rc = exclusive_scan(e, sums, nb, total);
         if (rc) return rc;
@@ -222,29 +241,48 @@ int alloc_level(pcagb_engine *e, Level &L, uint64_t n)
     return PCAGB_OK;
 }
 
-int fetch_hist(pcagb_engine *e, Level &L)
+/* Enqueue the level's (task, mask) histogram and its copy into the pinned
+   buffer; take_hist reads it after the stream has been synchronised. With
+   n_dev set, L.n is an upper bound and the device holds the count. */
+int enqueue_hist(pcagb_engine *e, const Level &L, const unsigned long long *n_dev)
 {
     const size_t nh = (size_t)e->ntasks * 128;
     CK(cudaMemsetAsync(e->d_hist, 0, nh * sizeof(unsigned long long), e->stream));
     if (nh <= 4096)
         k_task_hist_smem<<<e->grid(2), 256, nh * sizeof(uint32_t), e->stream>>>(
-            L.live, L.task, L.n, (uint32_t)nh, e->d_hist);
+            L.live, L.task, L.n, n_dev, (uint32_t)nh, e->d_hist);
     else
-        k_task_hist<<<e->grid(2), 256, 0, e->stream>>>(L.live, L.task, L.n, e->d_hist);
+        k_task_hist<<<e->grid(2), 256, 0, e->stream>>>(L.live, L.task, L.n, n_dev, e->d_hist);
     int rc = check_launch(e);
     if (rc) return rc;
-    L.hist.assign(nh, 0);
-    CK(e_copy(e, L.hist.data(), e->d_hist, nh * sizeof(uint64_t), cudaMemcpyDeviceToHost,
+    CK(e_copy(e, e->h_pin + kPinHist, e->d_hist, nh * sizeof(uint64_t), cudaMemcpyDeviceToHost,
               e->stream));
-    CK(cudaStreamSynchronize(e->stream));
     return PCAGB_OK;
+}
+
+void take_hist(pcagb_engine *e, Level &L)
+{
+    const size_t nh = (size_t)e->ntasks * 128;
+    L.hist.assign(e->h_pin + kPinHist, e->h_pin + kPinHist + nh);
+}
+
+/* log2 of the slices each parent's candidates are cut into, so that a
+   level of few parents still gives every resident warp work (up to 32
+   slices; 1 slice once the parents alone fill the grid) */
+uint32_t split_log2(uint64_t parents, int grid)
+{
+    const uint64_t warps = (uint64_t)grid * kWarpsPerBlock;
+    uint32_t l = 0;
+    while (l < 5 && (parents << (l + 1)) <= warps) l++;
+    return l;
 }
 
 template <int TPC>
 int launch_expand(pcagb_engine *e, const Level &P, unsigned long long *table, uint64_t tmask)
 {
-    k_expand_insert<TPC><<<e->grid(e->occ_insert), kThreads, 0, e->stream>>>(
-        view(P), e->td, table, tmask, e->d_status);
+    const int g = e->grid(e->occ_insert);
+    k_expand_insert<TPC><<<g, kThreads, 0, e->stream>>>(view(P), e->td, table, tmask,
+                                                        e->d_status, split_log2(P.n, g));
     return check_launch(e);
 }
 
@@ -253,15 +291,24 @@ int launch_materialize(pcagb_engine *e, const Level &P, const uint32_t *bitmap,
                        const uint64_t *word_off, Level &C)
 {
     LevelOut out{C.regs, C.flags, C.live, C.task, C.parent, C.cidx};
-    k_materialize<TPC><<<e->grid(e->occ_mat), kThreads, 0, e->stream>>>(view(P), e->td, bitmap,
-                                                                         word_off, out);
+    const int g = e->grid(e->occ_mat);
+    k_materialize<TPC><<<g, kThreads, 0, e->stream>>>(view(P), e->td, bitmap, word_off, out,
+                                                      split_log2(P.n, g));
     return check_launch(e);
 }
 
 /* Build level d+1 from level d for the active tasks. Returns PCAGB_ENOMEM
- * (and leaves the arena as it was) when the level does not fit. */
+ * (and leaves the arena as it was) when the level does not fit.
+ *
+ * The child count comes from the parent level's histogram on the host (the
+ * same sum the device scan forms), so nothing waits before the insert. A
+ * level whose children's states fit in kOneSyncBytes is materialised into
+ * space for every child and its survivor count, status, scan total and
+ * histogram come back in one round trip; a larger level reads the survivor
+ * count first and allocates exactly. */
 int build_level(pcagb_engine *e, int d)
 {
+    const GenTables &gt = gen_tables();
     Level &P = e->levels[d];
     const size_t bottom0 = e->bottom, top0 = e->top;
     auto fail = [&](int rc) {
@@ -278,12 +325,18 @@ int build_level(pcagb_engine *e, int d)
                                                           P.child_off);
         int rc = check_launch(e);
         if (rc) return rc;
-        rc = exclusive_scan(e, P.child_off, P.n + 1, &P.children);
+        rc = exclusive_scan(e, P.child_off, P.n + 1, nullptr);
         if (rc) return fail(rc);
+        uint64_t c = 0;
+        for (size_t i = 0; i < P.hist.size(); i++)
+            if (e->h_active[i >> 7]) c += P.hist[i] * (uint64_t)gt.nc((int)(i & 127));
+        P.children = c;
     }
     const uint64_t children = P.children;
     if (children >= (1ull << 38)) return fail(PCAGB_ENOMEM);
     const uint64_t words = (children + 31) / 32;
+    const uint64_t state_bytes = 8ull * 2 * e->TPC + e->TPC + 1 + 2 + 4 + 2;
+    const bool one_sync = children * state_bytes <= kOneSyncBytes;
 
     cudaEventRecord(e->ev0, e->stream);
     uint32_t *bitmap = (uint32_t *)e->alloc_top(words * 4 + 4);
@@ -311,42 +364,72 @@ int build_level(pcagb_engine *e, int d)
                                                   e->d_small + 2);
         rc = check_launch(e);
         if (rc) return rc;
-        uint32_t status = 0;
-        CK(e_copy(e, &status, e->d_status, 4, cudaMemcpyDeviceToHost, e->stream));
-        CK(e_copy(e, &survivors, e->d_small + 2, 8, cudaMemcpyDeviceToHost, e->stream));
-        CK(cudaStreamSynchronize(e->stream));
-        if (status) {
-            set_err("expansion of level %d hit a device limit (status %u)", d + 1, status);
-            return PCAGB_ELIMIT;
+        CK(e_copy(e, &e->h_pin[kPinStatus], e->d_status, 4, cudaMemcpyDeviceToHost, e->stream));
+        CK(e_copy(e, &e->h_pin[kPinSurvivors], e->d_small + 2, 8, cudaMemcpyDeviceToHost,
+                  e->stream));
+        if (!one_sync) {
+            CK(cudaStreamSynchronize(e->stream));
+            if ((uint32_t)e->h_pin[kPinStatus]) {
+                set_err("expansion of level %d hit a device limit (status %u)", d + 1,
+                        (uint32_t)e->h_pin[kPinStatus]);
+                return PCAGB_ELIMIT;
+            }
+            survivors = e->h_pin[kPinSurvivors];
         }
-        float ims = 0;
-        cudaEventElapsedTime(&ims, e->ev2, e->ev3);
-        e->ms_insert += ims;
         e->insert_launches++;
         e->insert_children += children;
     }
     uint64_t *word_off = (uint64_t *)e->alloc_top((words + 1) * sizeof(uint64_t));
     if (!word_off) return fail(PCAGB_ENOMEM);
+    CK(cudaMemsetAsync(word_off + words, 0, sizeof(uint64_t), e->stream));
     k_popc<<<e->grid(2), 256, 0, e->stream>>>(bitmap, words, word_off);
     int rc = check_launch(e);
     if (rc) return rc;
-    uint64_t total = 0;
-    rc = exclusive_scan(e, word_off, words, &total);
+    rc = exclusive_scan(e, word_off, words + 1, nullptr);
     if (rc) return fail(rc);
-    if (total != survivors) {
-        set_err("internal: bitmap holds %llu winners, table %llu", (unsigned long long)total,
-                (unsigned long long)survivors);
-        return PCAGB_ELIMIT;
+    CK(e_copy(e, &e->h_pin[kPinTotal], word_off + words, 8, cudaMemcpyDeviceToHost, e->stream));
+    if (!one_sync) {
+        /* the winners' ranks must stay inside the level about to be sized */
+        CK(cudaStreamSynchronize(e->stream));
+        if (e->h_pin[kPinTotal] != survivors) {
+            set_err("internal: bitmap holds %llu winners, table %llu",
+                    (unsigned long long)e->h_pin[kPinTotal], (unsigned long long)survivors);
+            return PCAGB_ELIMIT;
+        }
     }
     Level C;
-    if (survivors >= (1ull << 28)) return fail(PCAGB_ENOMEM);
-    if (alloc_level(e, C, survivors) != PCAGB_OK) return fail(PCAGB_ENOMEM);
+    /* one round trip: space for every child (the ranks of the marked
+       children are below their count, whatever the table did) */
+    const uint64_t space = one_sync ? children : survivors;
+    if (space >= (1ull << 28)) return fail(PCAGB_ENOMEM);
+    if (alloc_level(e, C, space) != PCAGB_OK) return fail(PCAGB_ENOMEM);
     rc = e->TPC == 16 ? launch_materialize<16>(e, P, bitmap, word_off, C)
                       : launch_materialize<32>(e, P, bitmap, word_off, C);
     if (rc) return rc;
     cudaEventRecord(e->ev1, e->stream);
-    rc = fetch_hist(e, C);
+    rc = enqueue_hist(e, C, one_sync && !e->no_oep ? e->d_small + 2 : nullptr);
     if (rc) return rc;
+    CK(cudaStreamSynchronize(e->stream));
+    if (one_sync && !e->no_oep) {
+        if ((uint32_t)e->h_pin[kPinStatus]) {
+            set_err("expansion of level %d hit a device limit (status %u)", d + 1,
+                    (uint32_t)e->h_pin[kPinStatus]);
+            return fail(PCAGB_ELIMIT);
+        }
+        survivors = e->h_pin[kPinSurvivors];
+        if (e->h_pin[kPinTotal] != survivors) {
+            set_err("internal: bitmap holds %llu winners, table %llu",
+                    (unsigned long long)e->h_pin[kPinTotal], (unsigned long long)survivors);
+            return fail(PCAGB_ELIMIT);
+        }
+        C.n = survivors;
+    }
+    take_hist(e, C);
+    if (!e->no_oep) {
+        float ims = 0;
+        cudaEventElapsedTime(&ims, e->ev2, e->ev3);
+        e->ms_insert += ims;
+    }
     float ms = 0;
     cudaEventElapsedTime(&ms, e->ev0, e->ev1);
     e->ms_expand += ms;
@@ -442,11 +525,11 @@ int run_stage(pcagb_engine *e, int S, int K, std::vector<TaskRun> &runs, bool fi
             rc = check_launch(e);
             if (rc) return rc;
             if (so && so->stop_at_first) {
-                unsigned long long hits = 0;
-                CK(e_copy(e, &hits, e->d_small, 8, cudaMemcpyDeviceToHost, e->stream));
+                CK(e_copy(e, &e->h_pin[kPinCount], e->d_small, 8, cudaMemcpyDeviceToHost,
+                          e->stream));
                 cudaEventRecord(e->ev1, e->stream);
                 CK(cudaStreamSynchronize(e->stream));
-                if (hits) {
+                if (e->h_pin[kPinCount]) {
                     so->prefixes_to_first = R.begin + R.count;
                     cudaEventElapsedTime(&so->ms_to_first, e->ev0, e->ev1);
                     break;
@@ -458,25 +541,16 @@ int run_stage(pcagb_engine *e, int S, int K, std::vector<TaskRun> &runs, bool fi
         return PCAGB_ENOMEM;
     }
     cudaEventRecord(e->ev1, e->stream);
-    unsigned long long nrec = 0, first = 0;
-    CK(e_copy(e, &nrec, e->d_small, 8, cudaMemcpyDeviceToHost, e->stream));
-    CK(e_copy(e, &first, e->d_small + 1, 8, cudaMemcpyDeviceToHost, e->stream));
+    CK(e_copy(e, &e->h_pin[kPinCount], e->d_small, 16, cudaMemcpyDeviceToHost, e->stream));
     CK(cudaStreamSynchronize(e->stream));
+    const unsigned long long nrec = e->h_pin[kPinCount], first = e->h_pin[kPinFirst];
     float ms = 0;
     cudaEventElapsedTime(&ms, e->ev0, e->ev1);
     e->ms_suffix += ms;
     e->suffix_launches++;
     if (s >= 1 && !(so && so->stop_at_first)) {
         /* value-class evaluations of this stage, for the autotuner */
-        std::vector<uint64_t> g(128);
-        for (int m = 0; m < 128; m++) g[m] = gt.nvc(m);
-        for (int step = 1; step < s; step++) {
-            std::vector<uint64_t> g2(128, 0);
-            for (int m = 0; m < 128; m++)
-                for (uint32_t i = gt.cand_off[m]; i < gt.cand_off[m + 1]; i++)
-                    g2[m] += g[(m | (1u << (UOP_RD(gt.cand_uop[i]) - 1))) & 127];
-            g.swap(g2);
-        }
+        const std::vector<uint64_t> &g = gt.ev[s];
         uint64_t evals = 0;
         for (size_t i = 0; i < L.hist.size(); i++) evals += L.hist[i] * g[i & 127];
         if (evals > 10000000ull)
@@ -688,15 +762,7 @@ int autotune_split(pcagb_engine *e, int K, const std::vector<uint8_t> &active)
     const int lo = std::max(0, K - 3);
     if (hi <= D) return std::max(hi, lo);
     auto evals_from = [&](int S, int s) {
-        std::vector<uint64_t> g(128);
-        for (int m = 0; m < 128; m++) g[m] = gt.nvc(m);
-        for (int step = 1; step < s; step++) {
-            std::vector<uint64_t> g2(128, 0);
-            for (int m = 0; m < 128; m++)
-                for (uint32_t i = gt.cand_off[m]; i < gt.cand_off[m + 1]; i++)
-                    g2[m] += g[(m | (1u << (UOP_RD(gt.cand_uop[i]) - 1))) & 127];
-            g.swap(g2);
-        }
+        const std::vector<uint64_t> &g = gt.ev[s];
         double ev = 0;
         const Level &L = e->levels[S];
         for (size_t i = 0; i < L.hist.size(); i++)
@@ -718,13 +784,27 @@ int autotune_split(pcagb_engine *e, int K, const std::vector<uint8_t> &active)
         if (S <= D) {
             ms = evals_from(S, K - S) * e->t_eval_ms;
         } else {
-            /* build D+1..S from D, then the suffix from S */
+            /* build D+1..S from D, then the suffix from S. A build that would
+               not fit the arena (its table, bitmap and ranks, plus the new
+               level sized at 1.5x the measured dedup ratio) is not chosen:
+               it would only find that out after its insert. */
             double kids = children_of(D), build = 0, states_scale = 1.0;
+            double parents = (double)e->levels[D].n, held = 0;
+            const double state_bytes = 16.0 * e->TPC + e->TPC + 9;
+            const double free_b = (double)(e->top - e->bottom);
+            bool fits = true;
             for (int d = D + 1; d <= S; d++) {
                 build += kids * e->t_child_ms + e->t_build_fixed_ms;
+                double slots = 1024;
+                while (slots < 2 * kids) slots *= 2;
+                const double states = kids * std::min(1.0, 1.5 * e->dedup_ratio);
+                held += (parents + 1) * 8 + states * state_bytes;
+                if (held + slots * 8 + kids / 32 * 12 > free_b) fits = false;
                 states_scale *= e->dedup_ratio;
+                parents = kids * e->dedup_ratio;
                 kids *= e->dedup_ratio * 800.0;  /* ~children per state deeper down */
             }
+            if (!fits) continue;
             ms = build + evals_from(D, K - D) * states_scale * e->t_eval_ms;
         }
         if (ms < best_ms) { best_ms = ms; best = S; }
@@ -930,11 +1010,8 @@ int run_batch(pcagb_engine *e, std::vector<TaskRun> &runs, const pcagb_opts_t &o
         if (runs[i].done) notify(i);
     std::vector<uint8_t> active(nt, 0);
     std::vector<uint64_t> pruned_cum(nt, 0);
-    std::vector<uint64_t> nc_w(128), nvc_w(128), ones(128, 1);
-    for (int m = 0; m < 128; m++) {
-        nc_w[m] = gt.nc(m);
-        nvc_w[m] = gt.nvc(m);
-    }
+    std::vector<uint64_t> nc_w(128), ones(128, 1);
+    for (int m = 0; m < 128; m++) nc_w[m] = gt.nc(m);
     for (int K = 1; K <= maxK; K++) {
         int nact = 0;
         for (int i = 0; i < nt; i++) {
@@ -949,6 +1026,7 @@ int run_batch(pcagb_engine *e, std::vector<TaskRun> &runs, const pcagb_opts_t &o
         }
         if (!nact) break;
         CK(e_copy(e, e->d_task_active, active.data(), nt, cudaMemcpyHostToDevice, e->stream));
+        e->h_active = active;
         int S_target = o.count_levels ? K : K - 1;
         if (o.split_depth >= 0) S_target = std::min(S_target, o.split_depth);
         else if (o.first_only && !o.count_levels) S_target = autotune_split(e, K, active);
@@ -973,14 +1051,7 @@ int run_batch(pcagb_engine *e, std::vector<TaskRun> &runs, const pcagb_opts_t &o
             return PCAGB_ENOMEM;
         }
         /* evaluations: value classes scanned at the last position */
-        std::vector<uint64_t> g(nvc_w);
-        for (int step = 1; step < s; step++) {
-            std::vector<uint64_t> g2(128, 0);
-            for (int m = 0; m < 128; m++)
-                for (uint32_t i = gt.cand_off[m]; i < gt.cand_off[m + 1]; i++)
-                    g2[m] += g[(m | (1u << (UOP_RD(gt.cand_uop[i]) - 1))) & 127];
-            g.swap(g2);
-        }
+        const std::vector<uint64_t> &g = gt.ev[std::max(s, 1)];
         const Level &LS = e->levels[S];
         for (int i = 0; i < nt; i++) {
             if (!active[i]) continue;
@@ -1153,6 +1224,7 @@ int engine_init(pcagb_engine *e, int device, size_t budget)
     CK(cudaMalloc(&e->d_task_active, kMaxBatch));
     CK(cudaMalloc(&e->d_task_io, (size_t)kMaxBatch * 3 * 32 * 2));
     CK(cudaMalloc(&e->d_hist, (size_t)kMaxBatch * 128 * sizeof(unsigned long long)));
+    CK(cudaMallocHost(&e->h_pin, (kPinHist + (size_t)kMaxBatch * 128) * sizeof(unsigned long long)));
     return PCAGB_OK;
 }
 
@@ -1444,6 +1516,7 @@ void pcagb_engine_destroy(pcagb_engine_t *e)
     cudaFree(e->d_task_active);
     cudaFree(e->d_task_io);
     cudaFree(e->d_hist);
+    if (e->h_pin) cudaFreeHost(e->h_pin);
     for (cudaEvent_t ev : {e->ev0, e->ev1, e->ev2, e->ev3})
         if (ev) cudaEventDestroy(ev);
     if (e->stream) cudaStreamDestroy(e->stream);

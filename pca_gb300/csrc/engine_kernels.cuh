@@ -337,13 +337,19 @@ __device__ bool warp_child_equal(const LevelDev &P, const InsertState<TPC> &A, u
 template <int TPC>
 __global__ void __launch_bounds__(kThreads, 6)
 k_expand_insert(LevelDev P, TaskDev task, unsigned long long *table, uint64_t tmask,
-                uint32_t *status)
+                uint32_t *status, uint32_t split_log2)
 {
     __shared__ InsertState<TPC> sws[kWarpsPerBlock];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     InsertState<TPC> &ws = sws[wib];
     const uint64_t nw = (uint64_t)gridDim.x * kWarpsPerBlock;
-    for (uint64_t q = (uint64_t)blockIdx.x * kWarpsPerBlock + wib; q < P.n; q += nw) {
+    const uint32_t split = 1u << split_log2;
+    /* a work item is a parent (split 1) or one of `split` slices of its
+       chunk list: small levels spread each parent over several warps */
+    for (uint64_t it = (uint64_t)blockIdx.x * kWarpsPerBlock + wib; it < (P.n << split_log2);
+         it += nw) {
+        const uint64_t q = it >> split_log2;
+        const uint32_t g = (uint32_t)it & (split - 1);
         const uint32_t tid = P.task[q];
         if (!task.active[tid]) continue;
         const int T = task.T[tid];
@@ -358,7 +364,10 @@ k_expand_insert(LevelDev P, TaskDev task, unsigned long long *table, uint64_t tm
         for (int r = 1; r < 8; r++) regsum += ws.colh[r];
         const uint32_t m = (live >> 1) & 127u;
         const uint32_t base = c_cand_off[m];
-        for (uint32_t k = c_chunk_off[m]; k < c_chunk_off[m + 1]; k++) {
+        const uint32_t k0 = c_chunk_off[m], k1 = c_chunk_off[m + 1];
+        const uint32_t per = (k1 - k0 + split - 1) >> split_log2;
+        const uint32_t ka = min(k1, k0 + g * per), kb = min(k1, ka + per);
+        for (uint32_t k = ka; k < kb; k++) {
             const uint32_t ch = c_chunks[k], start = ch >> 8, cnt = ch & 255u;
             const bool valid = (uint32_t)lane < cnt;
             const uint32_t c = start + (valid ? lane : 0);
@@ -496,13 +505,19 @@ __global__ void k_child_counts(const uint8_t *live, const uint16_t *task, const 
 template <int TPC>
 __global__ void __launch_bounds__(kThreads)
 k_materialize(LevelDev P, TaskDev task, const uint32_t *bitmap, const uint64_t *word_off,
-              LevelOut C)
+              LevelOut C, uint32_t split_log2)
 {
     __shared__ WarpState<TPC> sws[kWarpsPerBlock];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     WarpState<TPC> &ws = sws[wib];
     const uint64_t nw = (uint64_t)gridDim.x * kWarpsPerBlock;
-    for (uint64_t q = (uint64_t)blockIdx.x * kWarpsPerBlock + wib; q < P.n; q += nw) {
+    const uint32_t split = 1u << split_log2;
+    /* work items as in k_expand_insert: a parent, or a slice of its
+       32-candidate groups */
+    for (uint64_t it = (uint64_t)blockIdx.x * kWarpsPerBlock + wib; it < (P.n << split_log2);
+         it += nw) {
+        const uint64_t q = it >> split_log2;
+        const uint32_t g = (uint32_t)it & (split - 1);
         const uint32_t tid = P.task[q];
         if (!task.active[tid]) continue;
         const int T = task.T[tid];
@@ -513,7 +528,10 @@ k_materialize(LevelDev P, TaskDev task, const uint32_t *bitmap, const uint64_t *
         const uint32_t m = (live >> 1) & 127u;
         const uint32_t base = c_cand_off[m], nc = c_cand_off[m + 1] - base;
         const uint64_t off = P.child_off[q];
-        for (uint32_t c0 = 0; c0 < nc; c0 += 32) {
+        const uint32_t groups = (nc + 31) >> 5;
+        const uint32_t per = (groups + split - 1) >> split_log2;
+        const uint32_t ga = min(groups, g * per), gb = min(groups, ga + per);
+        for (uint32_t c0 = ga * 32; c0 < gb * 32; c0 += 32) {
             /* each lane settles its own candidate (kept?, rank, micro-op and
                the child's links) so the per-child loop below needs no
                global load */
@@ -559,10 +577,12 @@ k_materialize(LevelDev P, TaskDev task, const uint32_t *bitmap, const uint64_t *
 
 /* hist[task][mask] += states of that task with that liveness mask. Lanes
    with the same key are counted by one atomic (states of a level are
-   grouped by task and mostly by mask). */
+   grouped by task and mostly by mask). With n_dev set, the level holds
+   min(n, *n_dev) states (n is then the space written, an upper bound). */
 __global__ void k_task_hist(const uint8_t *live, const uint16_t *task, uint64_t n,
-                            unsigned long long *hist)
+                            const unsigned long long *n_dev, unsigned long long *hist)
 {
+    if (n_dev && *n_dev < n) n = *n_dev;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     const uint64_t n_round = (n + 31) & ~31ull;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_round; i += stride) {
@@ -579,9 +599,11 @@ __global__ void k_task_hist(const uint8_t *live, const uint16_t *task, uint64_t 
    bin: a level's states crowd a few bins, and per-warp global atomics on
    them serialize. */
 __global__ void k_task_hist_smem(const uint8_t *live, const uint16_t *task, uint64_t n,
-                                 uint32_t nbins, unsigned long long *hist)
+                                 const unsigned long long *n_dev, uint32_t nbins,
+                                 unsigned long long *hist)
 {
     extern __shared__ uint32_t sh_hist[];
+    if (n_dev && *n_dev < n) n = *n_dev;
     for (uint32_t b = threadIdx.x; b < nbins; b += blockDim.x) sh_hist[b] = 0;
     __syncthreads();
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;

@@ -42,6 +42,10 @@ struct GenTables {
     /* f[s][m]: programs decided by s more instructions from mask m:
        f[1][m] = nc(m), f[s][m] = sum over candidates c of f[s-1][m | rd(c)] */
     std::vector<uint64_t> f[5];
+    /* ev[s][m]: value-class evaluations of a suffix of s instructions from
+       mask m: ev[1][m] = nvc(m), ev[s][m] = sum over candidates c of
+       ev[s-1][m | rd(c)] (the suffix kernels' unit of work) */
+    std::vector<uint64_t> ev[5];
     int max_nc = 0;
     int max_nvc = 0;
 

@@ -117,6 +117,17 @@ static GenTables build_tables()
             }
             t.f[s][m] = sum;
         }
+    for (int s = 0; s < 5; s++) t.ev[s].assign(128, 0);
+    for (int m = 0; m < 128; m++) t.ev[1][m] = t.vc_off[m + 1] - t.vc_off[m];
+    for (int s = 2; s < 5; s++)
+        for (int m = 0; m < 128; m++) {
+            uint64_t sum = 0;
+            for (uint32_t i = t.cand_off[m]; i < t.cand_off[m + 1]; i++) {
+                uint32_t rd = UOP_RD(t.cand_uop[i]);
+                sum += t.ev[s - 1][(m | (1u << (rd - 1))) & 127];
+            }
+            t.ev[s][m] = sum;
+        }
     return t;
 }
 

@@ -29,6 +29,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <mutex>
 #include <string>
 #include <unordered_set>
@@ -78,6 +79,7 @@ struct Level {
     uint16_t *task = nullptr;
     uint32_t *parent = nullptr;
     uint16_t *cidx = nullptr;
+    uint8_t *rdl = nullptr;         /* register each state's last instruction wrote */
     uint64_t *child_off = nullptr;  /* set when this level is expanded */
     uint64_t children = 0;
     std::vector<uint64_t> hist;     /* [task][128] states per liveness mask */
@@ -225,7 +227,7 @@ int exclusive_scan(pcagb_engine *e, uint64_t *a, uint64_t n, uint64_t *total)
 
 LevelDev view(const Level &L)
 {
-    return LevelDev{L.regs, L.flags, L.live, L.task, L.child_off, L.n};
+    return LevelDev{L.regs, L.flags, L.live, L.task, L.child_off, L.n, L.rdl};
 }
 
 int alloc_level(pcagb_engine *e, Level &L, uint64_t n)
@@ -237,7 +239,9 @@ int alloc_level(pcagb_engine *e, Level &L, uint64_t n)
     L.task = (uint16_t *)e->alloc_bottom(n * 2);
     L.parent = (uint32_t *)e->alloc_bottom(n * 4);
     L.cidx = (uint16_t *)e->alloc_bottom(n * 2);
-    if (!L.regs || !L.flags || !L.live || !L.task || !L.parent || !L.cidx) return PCAGB_ENOMEM;
+    L.rdl = (uint8_t *)e->alloc_bottom(n);
+    if (!L.regs || !L.flags || !L.live || !L.task || !L.parent || !L.cidx || !L.rdl)
+        return PCAGB_ENOMEM;
     return PCAGB_OK;
 }
 
@@ -290,7 +294,7 @@ template <int TPC>
 int launch_materialize(pcagb_engine *e, const Level &P, const uint32_t *bitmap,
                        const uint64_t *word_off, Level &C)
 {
-    LevelOut out{C.regs, C.flags, C.live, C.task, C.parent, C.cidx};
+    LevelOut out{C.regs, C.flags, C.live, C.task, C.parent, C.cidx, C.rdl};
     const int g = e->grid(e->occ_mat);
     k_materialize<TPC><<<g, kThreads, 0, e->stream>>>(view(P), e->td, bitmap, word_off, out,
                                                       split_log2(P.n, g));
@@ -335,7 +339,7 @@ int build_level(pcagb_engine *e, int d)
     const uint64_t children = P.children;
     if (children >= (1ull << 38)) return fail(PCAGB_ENOMEM);
     const uint64_t words = (children + 31) / 32;
-    const uint64_t state_bytes = 8ull * 2 * e->TPC + e->TPC + 1 + 2 + 4 + 2;
+    const uint64_t state_bytes = 8ull * 2 * e->TPC + e->TPC + 1 + 2 + 4 + 2 + 1;
     const bool one_sync = children * state_bytes <= kOneSyncBytes;
 
     cudaEventRecord(e->ev0, e->stream);
@@ -478,102 +482,30 @@ struct StageOrder {
     float ms_to_first = 0;
 };
 
-/* Run the last stage at depth K from level S (suffix depth K-S, or the leaf
- * check when K == S) for the active tasks; appends each task's raw
- * solutions in DFS order. */
-int run_stage(pcagb_engine *e, int S, int K, std::vector<TaskRun> &runs, bool first_only,
-              StageOrder *so = nullptr)
+/* Turn solving records r0..r1 of the stage at depth K from level S into
+ * the tasks' raw solutions (kept sorted in DFS order). `first` is the
+ * packed DFS-first key, used instead of the records for one task in
+ * first-only mode. */
+int take_records(pcagb_engine *e, int S, int K, std::vector<TaskRun> &runs, bool first_only,
+                 uint64_t r0, uint64_t r1, unsigned long long first)
 {
     const GenTables &gt = gen_tables();
-    Level &L = e->levels[S];
+    const Level &L = e->levels[S];
     const int s = K - S;
-    CK(cudaMemsetAsync(e->d_small, 0, 8, e->stream));
-    CK(cudaMemsetAsync(e->d_small + 1, 0xFF, 8, e->stream));
-    SolBuf sb{e->d_small, e->d_sol, e->sol_cap, e->d_small + 1};
-    cudaEventRecord(e->ev0, e->stream);
-    const bool t16 = e->TPC == 16;
-    const int g = e->grid(e->occ_suffix);
-    int rc = PCAGB_OK;
-    if (s == 0) {
-        if (t16) k_leaf<16><<<e->grid(4), 256, 0, e->stream>>>(view(L), e->td, sb);
-        else k_leaf<32><<<e->grid(4), 256, 0, e->stream>>>(view(L), e->td, sb);
-        rc = check_launch(e);
-        if (rc) return rc;
-    } else if (s <= 3) {
-        int ncmax = 0;
-        for (size_t i = 0; i < L.hist.size(); i++)
-            if (L.hist[i]) ncmax = std::max(ncmax, gt.nc((int)(i & 127)));
-        const uint32_t chunk = s == 1 ? 1 : s == 2 ? 16 : 1;
-        const uint32_t cpp =
-            s == 1 ? 1 : std::max(1u, (uint32_t)((ncmax + chunk - 1) / chunk));
-        /* ordered stages start with `chunk` prefixes per launch and double
-           it after every launch without a solution, so a stage that has to
-           be searched completely takes O(log n) launches */
-        uint64_t step = so && so->chunk ? so->chunk : std::max<uint64_t>(L.n, 1);
-        for (uint64_t b0 = 0; b0 < L.n; b0 += step, step = so && so->chunk ? step * 2 : step) {
-            const PrefixRange R{so ? so->order : nullptr, b0, std::min(step, L.n - b0)};
-            if (s == 1) {
-                if (t16) k_suffix<16, 1><<<g, kThreads, 0, e->stream>>>(view(L), e->td, sb, 1, 1, R);
-                else k_suffix<32, 1><<<g, kThreads, 0, e->stream>>>(view(L), e->td, sb, 1, 1, R);
-            } else if (s == 2) {
-                if (t16) k_suffix<16, 2><<<g, kThreads, 0, e->stream>>>(view(L), e->td, sb, cpp, chunk, R);
-                else k_suffix<32, 2><<<g, kThreads, 0, e->stream>>>(view(L), e->td, sb, cpp, chunk, R);
-            } else {
-                if (t16) k_suffix<16, 3><<<g, kThreads, 0, e->stream>>>(view(L), e->td, sb, cpp, chunk, R);
-                else k_suffix<32, 3><<<g, kThreads, 0, e->stream>>>(view(L), e->td, sb, cpp, chunk, R);
-            }
-            rc = check_launch(e);
-            if (rc) return rc;
-            if (so && so->stop_at_first) {
-                CK(e_copy(e, &e->h_pin[kPinCount], e->d_small, 8, cudaMemcpyDeviceToHost,
-                          e->stream));
-                cudaEventRecord(e->ev1, e->stream);
-                CK(cudaStreamSynchronize(e->stream));
-                if (e->h_pin[kPinCount]) {
-                    so->prefixes_to_first = R.begin + R.count;
-                    cudaEventElapsedTime(&so->ms_to_first, e->ev0, e->ev1);
-                    break;
-                }
-            }
-        }
-    } else {
-        set_err("suffix depth %d not supported (split too shallow)", s);
-        return PCAGB_ENOMEM;
-    }
-    cudaEventRecord(e->ev1, e->stream);
-    CK(e_copy(e, &e->h_pin[kPinCount], e->d_small, 16, cudaMemcpyDeviceToHost, e->stream));
-    CK(cudaStreamSynchronize(e->stream));
-    const unsigned long long nrec = e->h_pin[kPinCount], first = e->h_pin[kPinFirst];
-    float ms = 0;
-    cudaEventElapsedTime(&ms, e->ev0, e->ev1);
-    e->ms_suffix += ms;
-    e->suffix_launches++;
-    if (s >= 1 && !(so && so->stop_at_first)) {
-        /* value-class evaluations of this stage, for the autotuner */
-        const std::vector<uint64_t> &g = gt.ev[s];
-        uint64_t evals = 0;
-        for (size_t i = 0; i < L.hist.size(); i++) evals += L.hist[i] * g[i & 127];
-        if (evals > 10000000ull)
-            e->t_eval_ms = 0.7 * e->t_eval_ms + 0.3 * (ms / (double)evals);
-    }
-    if (!nrec) return PCAGB_OK;
-
-    /* Fetch the records (or, for one task in first-only mode, just the
-       DFS-first one rebuilt from its packed key) and their prefix paths. */
     std::vector<ulonglong2> rec;
     if (first_only && e->ntasks == 1) {
         const uint64_t m1 = (first >> 24) & 4095, m2 = (first >> 12) & 4095, fc = first & 4095;
         /* low 16 bits with bit 15 set: a candidate index, not a class */
         rec.push_back(make_ulonglong2(first >> 36, (m1 << 32) | (m2 << 16) | (0x8000u | fc)));
     } else {
-        if (nrec > e->sol_cap) {
-            set_err("%llu solving records exceed the buffer of %llu", (unsigned long long)nrec,
+        if (r1 > e->sol_cap) {
+            set_err("%llu solving records exceed the buffer of %llu", (unsigned long long)r1,
                     (unsigned long long)e->sol_cap);
             return PCAGB_ELIMIT;
         }
-        rec.resize(nrec);
-        CK(e_copy(e, rec.data(), e->d_sol, nrec * sizeof(ulonglong2), cudaMemcpyDeviceToHost,
-                  e->stream));
+        rec.resize(r1 - r0);
+        CK(e_copy(e, rec.data(), e->d_sol + r0, rec.size() * sizeof(ulonglong2),
+                  cudaMemcpyDeviceToHost, e->stream));
         CK(cudaStreamSynchronize(e->stream));
     }
     std::vector<uint16_t> paths(rec.size() * SEARCH_MAX_DEPTH, 0);
@@ -596,15 +528,17 @@ int run_stage(pcagb_engine *e, int S, int K, std::vector<TaskRun> &runs, bool fi
         }
         G.task = L.task;
         k_gather_paths<<<64, 256, 0, e->stream>>>(G, S, d_rec, rec.size(), d_paths, d_task);
-        rc = check_launch(e);
+        int rc = check_launch(e);
         if (rc) return rc;
         CK(e_copy(e, paths.data(), d_paths, paths.size() * 2, cudaMemcpyDeviceToHost, e->stream));
         CK(e_copy(e, rtask.data(), d_task, rtask.size() * 2, cudaMemcpyDeviceToHost, e->stream));
         CK(cudaStreamSynchronize(e->stream));
         e->top = top0;
     }
+    std::vector<uint8_t> touched(runs.size(), 0);
     for (size_t i = 0; i < rec.size(); i++) {
         TaskRun &tr = runs[rtask[i]];
+        touched[rtask[i]] = 1;
         tr.nrec++;
         RawSol base;
         uint32_t mask = (tr.root.live >> 1) & 127u;
@@ -645,11 +579,155 @@ int run_stage(pcagb_engine *e, int S, int K, std::vector<TaskRun> &runs, bool fi
             tr.sols.push_back(r);
         }
     }
-    for (TaskRun &tr : runs)
-        if (!tr.sols.empty())
-            std::sort(tr.sols.begin(), tr.sols.end(),
+    for (size_t t = 0; t < runs.size(); t++)
+        if (touched[t])
+            std::sort(runs[t].sols.begin(), runs[t].sols.end(),
                       [](const RawSol &a, const RawSol &b) { return a.key < b.key; });
     return PCAGB_OK;
+}
+
+/* Run the last stage at depth K from level S (suffix depth K-S, or the leaf
+ * check when K == S) for the active tasks; appends each task's raw
+ * solutions in DFS order.
+ *
+ * With several active tasks and `on_tasks` given, the suffix stage runs as
+ * consecutive launches over groups of whole tasks (a level holds its tasks'
+ * states task after task), each group about 1.5 ms of work, and calls
+ * on_tasks(lo, hi) once tasks lo..hi-1 are searched at this depth, their
+ * solutions taken: a batch's tasks are decided one group after another
+ * instead of all at the end of the stage. */
+int run_stage(pcagb_engine *e, int S, int K, std::vector<TaskRun> &runs, bool first_only,
+              StageOrder *so = nullptr,
+              const std::function<void(int, int)> *on_tasks = nullptr)
+{
+    const GenTables &gt = gen_tables();
+    Level &L = e->levels[S];
+    const int s = K - S;
+    CK(cudaMemsetAsync(e->d_small, 0, 8, e->stream));
+    CK(cudaMemsetAsync(e->d_small + 1, 0xFF, 8, e->stream));
+    SolBuf sb{e->d_small, e->d_sol, e->sol_cap, e->d_small + 1};
+    cudaEventRecord(e->ev0, e->stream);
+    const bool t16 = e->TPC == 16;
+    const int g = e->grid(e->occ_suffix);
+    int rc = PCAGB_OK;
+    uint64_t taken = 0;  /* records already turned into solutions */
+    if (s == 0) {
+        if (t16) k_leaf<16><<<e->grid(4), 256, 0, e->stream>>>(view(L), e->td, sb);
+        else k_leaf<32><<<e->grid(4), 256, 0, e->stream>>>(view(L), e->td, sb);
+        rc = check_launch(e);
+        if (rc) return rc;
+    } else if (s <= 3) {
+        int ncmax = 0;
+        for (size_t i = 0; i < L.hist.size(); i++)
+            if (L.hist[i]) ncmax = std::max(ncmax, gt.nc((int)(i & 127)));
+        const uint32_t chunk = s == 1 ? 1 : s == 2 ? 16 : 1;
+        const uint32_t cpp =
+            s == 1 ? 1 : std::max(1u, (uint32_t)((ncmax + chunk - 1) / chunk));
+        auto launch = [&](const PrefixRange &R) {
+            if (s == 1) {
+                if (t16) k_suffix<16, 1><<<g, kThreads, 0, e->stream>>>(view(L), e->td, sb, 1, 1, R);
+                else k_suffix<32, 1><<<g, kThreads, 0, e->stream>>>(view(L), e->td, sb, 1, 1, R);
+            } else if (s == 2) {
+                if (t16) k_suffix<16, 2><<<g, kThreads, 0, e->stream>>>(view(L), e->td, sb, cpp, chunk, R);
+                else k_suffix<32, 2><<<g, kThreads, 0, e->stream>>>(view(L), e->td, sb, cpp, chunk, R);
+            } else {
+                if (t16) k_suffix<16, 3><<<g, kThreads, 0, e->stream>>>(view(L), e->td, sb, cpp, chunk, R);
+                else k_suffix<32, 3><<<g, kThreads, 0, e->stream>>>(view(L), e->td, sb, cpp, chunk, R);
+            }
+            return check_launch(e);
+        };
+        /* task groups of the progressive mode: [first task, end task) with
+           the level range they occupy */
+        struct Group { int t0, t1; uint64_t b0, b1; };
+        std::vector<Group> groups;
+        if (!so && on_tasks && e->ntasks > 1) {
+            const int nt = e->ntasks;
+            const double per_group = 1.5 / std::max(e->t_eval_ms, 1e-12);
+            int nact = 0;
+            for (int t = 0; t < nt; t++) nact += e->h_active[t] ? 1 : 0;
+            if (nact > 1) {
+                uint64_t off = 0, gb0 = 0;
+                int gt0 = 0;
+                double acc = 0;
+                for (int t = 0; t < nt; t++) {
+                    uint64_t cnt = 0, ev = 0;
+                    for (int m = 0; m < 128; m++) {
+                        cnt += L.hist[(size_t)t * 128 + m];
+                        ev += L.hist[(size_t)t * 128 + m] * gt.ev[s][m];
+                    }
+                    off += cnt;
+                    if (e->h_active[t]) acc += (double)ev;
+                    if (acc >= per_group || t == nt - 1) {
+                        groups.push_back({gt0, t + 1, gb0, off});
+                        gt0 = t + 1;
+                        gb0 = off;
+                        acc = 0;
+                    }
+                }
+                if (off != L.n) groups.clear();   /* histogram and level disagree: one launch */
+            }
+        }
+        if (groups.size() > 1) {
+            for (const Group &G : groups) {
+                if (G.b1 > G.b0) {
+                    rc = launch(PrefixRange{nullptr, G.b0, G.b1 - G.b0});
+                    if (rc) return rc;
+                }
+                CK(e_copy(e, &e->h_pin[kPinCount], e->d_small, 8, cudaMemcpyDeviceToHost,
+                          e->stream));
+                CK(cudaStreamSynchronize(e->stream));
+                const uint64_t cnt = e->h_pin[kPinCount];
+                if (cnt > taken) {
+                    rc = take_records(e, S, K, runs, first_only, taken, cnt, 0);
+                    if (rc) return rc;
+                    taken = cnt;
+                }
+                (*on_tasks)(G.t0, G.t1);
+            }
+        } else {
+            /* ordered stages start with `chunk` prefixes per launch and
+               double it after every launch without a solution, so a stage
+               that has to be searched completely takes O(log n) launches */
+            uint64_t step = so && so->chunk ? so->chunk : std::max<uint64_t>(L.n, 1);
+            for (uint64_t b0 = 0; b0 < L.n; b0 += step, step = so && so->chunk ? step * 2 : step) {
+                const PrefixRange R{so ? so->order : nullptr, b0, std::min(step, L.n - b0)};
+                rc = launch(R);
+                if (rc) return rc;
+                if (so && so->stop_at_first) {
+                    CK(e_copy(e, &e->h_pin[kPinCount], e->d_small, 8, cudaMemcpyDeviceToHost,
+                              e->stream));
+                    cudaEventRecord(e->ev1, e->stream);
+                    CK(cudaStreamSynchronize(e->stream));
+                    if (e->h_pin[kPinCount]) {
+                        so->prefixes_to_first = R.begin + R.count;
+                        cudaEventElapsedTime(&so->ms_to_first, e->ev0, e->ev1);
+                        break;
+                    }
+                }
+            }
+        }
+    } else {
+        set_err("suffix depth %d not supported (split too shallow)", s);
+        return PCAGB_ENOMEM;
+    }
+    cudaEventRecord(e->ev1, e->stream);
+    CK(e_copy(e, &e->h_pin[kPinCount], e->d_small, 16, cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    const unsigned long long nrec = e->h_pin[kPinCount], first = e->h_pin[kPinFirst];
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e->ev0, e->ev1);
+    e->ms_suffix += ms;
+    e->suffix_launches++;
+    if (s >= 1 && !(so && so->stop_at_first)) {
+        /* value-class evaluations of this stage, for the autotuner */
+        const std::vector<uint64_t> &g = gt.ev[s];
+        uint64_t evals = 0;
+        for (size_t i = 0; i < L.hist.size(); i++) evals += L.hist[i] * g[i & 127];
+        if (evals > 10000000ull)
+            e->t_eval_ms = 0.7 * e->t_eval_ms + 0.3 * (ms / (double)evals);
+    }
+    if (nrec <= taken) return PCAGB_OK;
+    return take_records(e, S, K, runs, first_only, taken, nrec, first);
 }
 
 /* Host-side step for the reference-key dedup of the solving leaves
@@ -790,7 +868,7 @@ int autotune_split(pcagb_engine *e, int K, const std::vector<uint8_t> &active)
                it would only find that out after its insert. */
             double kids = children_of(D), build = 0, states_scale = 1.0;
             double parents = (double)e->levels[D].n, held = 0;
-            const double state_bytes = 16.0 * e->TPC + e->TPC + 9;
+            const double state_bytes = 16.0 * e->TPC + e->TPC + 10;
             const double free_b = (double)(e->top - e->bottom);
             bool fits = true;
             for (int d = D + 1; d <= S; d++) {
@@ -972,6 +1050,7 @@ int run_batch(pcagb_engine *e, std::vector<TaskRun> &runs, const pcagb_opts_t &o
         CK(e_copy(e, L0.task, task.data(), nt * 2, cudaMemcpyHostToDevice, e->stream));
         CK(e_copy(e, L0.parent, parent.data(), nt * 4, cudaMemcpyHostToDevice, e->stream));
         CK(e_copy(e, L0.cidx, cidx.data(), nt * 2, cudaMemcpyHostToDevice, e->stream));
+        CK(cudaMemsetAsync(L0.rdl, 0, nt, e->stream));
     }
     e->levels.push_back(std::move(L0));
 
@@ -1083,10 +1162,12 @@ int run_batch(pcagb_engine *e, std::vector<TaskRun> &runs, const pcagb_opts_t &o
             so.stop_at_first = true;
             sop = &so;
         }
-        int rc = run_stage(e, S, K, runs, o.first_only != 0, sop);
-        if (rc) return rc;
-        for (int i = 0; i < nt; i++) {
-            if (!active[i]) continue;
+        /* a task searched at depth K: its counters, and done when it has
+           solutions or K is its last depth */
+        std::vector<uint8_t> finished(nt, 0);
+        auto finish = [&](int i) {
+            if (!active[i] || finished[i]) return;
+            finished[i] = 1;
             TaskRun &tr = runs[i];
             /* the reference's counters (exact when every level up to K is built) */
             uint64_t tried = 0, pruned = 0;
@@ -1108,8 +1189,18 @@ int run_batch(pcagb_engine *e, std::vector<TaskRun> &runs, const pcagb_opts_t &o
                 tr.res.total_solutions =
                     s == 0 || (o.first_only && nt == 1) ? tr.nrec : tr.sols.size();
                 notify(i);
+            } else if (K >= tr.max_depth) {
+                tr.done = true;
+                tr.t_done = elapsed();
+                notify(i);
             }
-        }
+        };
+        const std::function<void(int, int)> on_tasks = [&](int lo, int hi) {
+            for (int i = lo; i < hi; i++) finish(i);
+        };
+        int rc = run_stage(e, S, K, runs, o.first_only != 0, sop, sop ? nullptr : &on_tasks);
+        if (rc) return rc;
+        for (int i = 0; i < nt; i++) finish(i);
     }
     const double total = elapsed();
     for (TaskRun &tr : runs) {
@@ -1153,8 +1244,18 @@ int ensure_device_tables(int device)
             if (!seen[v]) { seen[v] = true; first[gt.vc_off[m] + v] = (uint16_t)c; }
         }
     }
-    uint32_t *cand_uop = nullptr, *vc_uop = nullptr, *chunks = nullptr;
-    uint16_t *vc_first = nullptr;
+    uint32_t *cand_uop = nullptr, *vc_uop = nullptr, *chunks = nullptr, *vcr_off = nullptr;
+    uint16_t *vc_first = nullptr, *vcr = nullptr;
+    CK(cudaMalloc(&vcr_off, gt.vcr_off.size() * 4));
+    CK(cudaMalloc(&vcr, std::max<size_t>(gt.vcr.size(), 1) * 2));
+    CK(cudaMemcpy(vcr_off, gt.vcr_off.data(), gt.vcr_off.size() * 4, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(vcr, gt.vcr.data(), gt.vcr.size() * 2, cudaMemcpyHostToDevice));
+    {
+        const uint32_t *vo = vcr_off;
+        const uint16_t *vr = vcr;
+        CK(cudaMemcpyToSymbol(c_vcr_off, &vo, sizeof vo));
+        CK(cudaMemcpyToSymbol(c_vcr, &vr, sizeof vr));
+    }
     CK(cudaMalloc(&cand_uop, gt.cand_uop.size() * 4));
     CK(cudaMalloc(&vc_uop, gt.vc_uop.size() * 4));
     CK(cudaMalloc(&vc_first, first.size() * 2));

@@ -59,6 +59,8 @@ __constant__ const uint32_t *c_vc_uop;
 __constant__ const uint16_t *c_vc_first;   /* first candidate index per class */
 __constant__ uint32_t c_chunk_off[129];    /* op-uniform runs of candidates */
 __constant__ const uint32_t *c_chunks;
+__constant__ const uint32_t *c_vcr_off;    /* [mask*8 + r]: classes reading r */
+__constant__ const uint16_t *c_vcr;
 
 /* Per-task parameters of a batch: device arrays indexed by task id. A
    state's task id travels with it through the levels; states of different
@@ -77,6 +79,7 @@ struct LevelDev {
     const uint16_t *task;   /* [n] */
     const uint64_t *child_off; /* [n+1] */
     uint64_t n;
+    const uint8_t *rdl;     /* [n] register the state's last instruction wrote (0: root) */
 };
 
 struct LevelOut {
@@ -86,6 +89,7 @@ struct LevelOut {
     uint16_t *task;
     uint32_t *parent;
     uint16_t *cidx;
+    uint8_t *rdl;
 };
 
 /* ---- hashing (a multiply-rotate chain; the table compares full states, so
@@ -547,6 +551,7 @@ k_materialize(LevelDev P, TaskDev task, const uint32_t *bitmap, const uint64_t *
                     rank = word_off[L >> 5] + __popc(wv & ((1u << (L & 31)) - 1u));
                     u = c_cand_uop[base + c];
                     C.live[rank] = (uint8_t)(live | (1u << UOP_RD(u)));
+                    C.rdl[rank] = (uint8_t)UOP_RD(u);
                     C.task[rank] = (uint16_t)tid;
                     C.parent[rank] = (uint32_t)q;
                     C.cidx[rank] = (uint16_t)c;
@@ -664,26 +669,47 @@ __global__ void k_leaf(LevelDev P, TaskDev task, SolBuf S)
 
 /* Scan the value classes of mask m against the warp's state, with operand
  * registers remapped: a register equal to rd2 reads spare column 9, else a
- * register equal to rd1 reads column 8 (rd = 8 means "none"). */
+ * register equal to rd1 reads column 8 (rd = 8 means "none").
+ *
+ * need1 / need2 (0 = none): registers the last instruction must read. At a
+ * depth K reached only after depth K-1 was searched without a solution,
+ * every instruction of a solving program feeds a later one: an instruction
+ * whose value nothing reads could be dropped, leaving a solving program of
+ * K-1 instructions in the same candidate space. So the last instruction
+ * reads the register the one before it wrote (need1), and need2 names an
+ * earlier write nothing else read. Only classes that read need1 are
+ * scanned, from the per-register class lists; the solutions are the same. */
 template <int TPC>
 __device__ __forceinline__ void scan_last(const WarpState<TPC> &ws, int T,
                                           uint32_t m, uint32_t rd1, uint32_t rd2, uint32_t tgt,
                                           uint32_t tgt0, uint32_t tgt1, int lane,
-                                          const SolBuf &S, uint64_t q, uint32_t m1, uint32_t m2)
+                                          const SolBuf &S, uint64_t q, uint32_t m1, uint32_t m2,
+                                          uint32_t need1, uint32_t need2)
 {
-    const uint32_t vbase = c_vc_off[m], nvc = c_vc_off[m + 1] - vbase;
+    const uint32_t vbase = c_vc_off[m];
+    const uint16_t *list = nullptr;
+    uint32_t nvc;
+    if (need1) {
+        const uint32_t l0 = c_vcr_off[m * 8 + need1];
+        list = c_vcr + l0;
+        nvc = c_vcr_off[m * 8 + need1 + 1] - l0;
+    } else {
+        nvc = c_vc_off[m + 1] - vbase;
+    }
     for (uint32_t b0 = 0; b0 < nvc; b0 += 32) {
         const uint32_t i = b0 + lane;
-        uint32_t u = 0;
+        uint32_t u = 0, ci = 0;
         bool pass = false;
         if (i < nvc) {
             /* first two tests per lane; survivors are checked on all tests below */
-            u = c_vc_uop[vbase + i];
+            ci = list ? (uint32_t)list[i] : i;
+            u = c_vc_uop[vbase + ci];
             uint32_t ra = UOP_A(u), rb = UOP_B(u);
+            const bool reads2 = !need2 || ra == need2 || rb == need2;
             ra = ra == rd2 ? 9u : ra == rd1 ? 8u : ra;
             rb = rb == rd2 ? 9u : rb == rd1 ? 8u : rb;
             const uint32_t op = UOP_OP(u), imm = UOP_IMM(u);
-            pass = pca_alu(op, ws.R[ra][0], ws.R[rb][0], imm) == tgt0 &&
+            pass = reads2 && pca_alu(op, ws.R[ra][0], ws.R[rb][0], imm) == tgt0 &&
                    (T < 2 || pca_alu(op, ws.R[ra][1], ws.R[rb][1], imm) == tgt1);
         }
         uint32_t bal = __ballot_sync(0xFFFFFFFFu, pass);
@@ -691,14 +717,36 @@ __device__ __forceinline__ void scan_last(const WarpState<TPC> &ws, int T,
             const int j = __ffs(bal) - 1;
             bal &= bal - 1;
             const uint32_t uj = __shfl_sync(0xFFFFFFFFu, u, j);
+            const uint32_t cj = __shfl_sync(0xFFFFFFFFu, ci, j);
             uint32_t ra = UOP_A(uj), rb = UOP_B(uj);
             ra = ra == rd2 ? 9u : ra == rd1 ? 8u : ra;
             rb = rb == rd2 ? 9u : rb == rd1 ? 8u : rb;
             bool ok = true;
             if (lane < T) ok = pca_alu(UOP_OP(uj), ws.R[ra][lane], ws.R[rb][lane], UOP_IMM(uj)) == tgt;
             if (__all_sync(0xFFFFFFFFu, ok) && lane == 0)
-                record_solution(S, q, m1, m2, b0 + j, c_vc_first[vbase + b0 + j]);
+                record_solution(S, q, m1, m2, cj, c_vc_first[vbase + cj]);
         }
+    }
+}
+
+/* Reads: does micro-op u read register r (1..7)? */
+__device__ __forceinline__ bool uop_reads(uint32_t u, uint32_t r)
+{
+    return UOP_A(u) == r || UOP_B(u) == r;
+}
+
+/* The suffix kernels' view of a prefix: only its live columns (no operand
+   of a candidate reads anything else; column 0 is zeroed once per warp)
+   and no flags (no branchless op reads them). */
+template <int TPC>
+__device__ __forceinline__ void load_live_cols(WarpState<TPC> &ws, const uint16_t *regs,
+                                               uint64_t q, uint32_t live, int lane)
+{
+    if (lane < TPC) {
+        const uint16_t *src = regs + q * 8 * TPC + lane;
+#pragma unroll
+        for (int r = 1; r < 8; r++)
+            if ((live >> r) & 1u) ws.R[r][lane] = src[r * TPC];
     }
 }
 
@@ -743,6 +791,7 @@ k_suffix(LevelDev P, TaskDev task, SolBuf S, uint32_t chunks_per_prefix, uint32_
     uint64_t loaded = ~0ull;
     uint32_t cur_task = ~0u, tgt = 0, tgt0 = 0, tgt1 = 0;
     int T = 0;
+    if (lane < TPC) ws.R[0][lane] = 0;
     for (uint64_t it = (uint64_t)blockIdx.x * kWarpsPerBlock + wib; it < items; it += nw) {
         const uint64_t qi = it / chunks_per_prefix;
         const uint32_t ck = (uint32_t)(it - qi * chunks_per_prefix);
@@ -760,13 +809,16 @@ k_suffix(LevelDev P, TaskDev task, SolBuf S, uint32_t chunks_per_prefix, uint32_
         const uint32_t live = P.live[q];
         if (q != loaded) {
             __syncwarp();
-            load_state<TPC>(ws, P.regs, P.flags, q, lane);
+            load_live_cols<TPC>(ws, P.regs, q, live, lane);
             loaded = q;
             __syncwarp();
         }
         const uint32_t m0 = (live >> 1) & 127u;
+        /* the prefix's last write (0 at a root): some later instruction
+           must read it (the rule scan_last states) */
+        const uint32_t w0 = P.rdl[q];
         if (SD == 1) {
-            scan_last<TPC>(ws, T, m0, 8, 8, tgt, tgt0, tgt1, lane, S, q, 0, 0);
+            scan_last<TPC>(ws, T, m0, 8, 8, tgt, tgt0, tgt1, lane, S, q, 0, 0, w0, 0);
             continue;
         }
         const uint32_t cb0 = c_cand_off[m0], nc0 = c_cand_off[m0 + 1] - cb0;
@@ -774,6 +826,10 @@ k_suffix(LevelDev P, TaskDev task, SolBuf S, uint32_t chunks_per_prefix, uint32_
         for (uint32_t i1 = lo; i1 < hi; i1++) {
             const uint32_t u1 = c_cand_uop[cb0 + i1];
             const uint32_t rd1 = UOP_RD(u1);
+            /* w0 still unread after u1: overwritten (dead, skip) or owed by
+               a later instruction */
+            const uint32_t owe0 = w0 && !uop_reads(u1, w0) ? w0 : 0u;
+            if (owe0 && rd1 == owe0) continue;
             __syncwarp();
             if (lane < TPC)
                 ws.R[8][lane] = lane < T ? pca_alu(UOP_OP(u1), ws.R[UOP_A(u1)][lane],
@@ -782,13 +838,21 @@ k_suffix(LevelDev P, TaskDev task, SolBuf S, uint32_t chunks_per_prefix, uint32_
             __syncwarp();
             const uint32_t m1 = (m0 | (1u << (rd1 - 1))) & 127u;
             if (SD == 2) {
-                scan_last<TPC>(ws, T, m1, rd1, 8, tgt, tgt0, tgt1, lane, S, q, i1, 0);
+                scan_last<TPC>(ws, T, m1, rd1, 8, tgt, tgt0, tgt1, lane, S, q, i1, 0, rd1, owe0);
                 continue;
             }
             const uint32_t cb1 = c_cand_off[m1], nc1 = c_cand_off[m1 + 1] - cb1;
             for (uint32_t i2 = 0; i2 < nc1; i2++) {
                 const uint32_t u2 = c_cand_uop[cb1 + i2];
                 const uint32_t rd2 = UOP_RD(u2);
+                /* writes still owed a read after u2 (u1's and maybe w0's);
+                   one overwritten unread is dead, and the last instruction
+                   reads rd2 and at most one more register */
+                const uint32_t owe1 = uop_reads(u2, rd1) ? 0u : rd1;
+                const uint32_t owe0b = owe0 && !uop_reads(u2, owe0) ? owe0 : 0u;
+                if ((owe1 && rd2 == owe1) || (owe0b && rd2 == owe0b)) continue;
+                if (owe1 && owe0b) continue;   /* three registers to read */
+                const uint32_t need2 = owe1 ? owe1 : owe0b;
                 uint32_t ra = UOP_A(u2), rb = UOP_B(u2);
                 ra = ra == rd1 ? 8u : ra;
                 rb = rb == rd1 ? 8u : rb;
@@ -800,7 +864,7 @@ k_suffix(LevelDev P, TaskDev task, SolBuf S, uint32_t chunks_per_prefix, uint32_
                 __syncwarp();
                 const uint32_t m2 = (m1 | (1u << (rd2 - 1))) & 127u;
                 scan_last<TPC>(ws, T, m2, rd2 == rd1 ? 8u : rd1, rd2, tgt, tgt0, tgt1, lane, S,
-                               q, i1, i2);
+                               q, i1, i2, rd2, need2);
             }
         }
     }

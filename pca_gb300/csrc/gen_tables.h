@@ -46,6 +46,10 @@ struct GenTables {
        mask m: ev[1][m] = nvc(m), ev[s][m] = sum over candidates c of
        ev[s-1][m | rd(c)] (the suffix kernels' unit of work) */
     std::vector<uint64_t> ev[5];
+    /* the value classes of mask m that read register r (1..7): class
+       indices (within the mask's list) vcr[vcr_off[m*8+r] .. vcr_off[m*8+r+1]) */
+    std::vector<uint32_t> vcr_off;     /* size 128*8+1 */
+    std::vector<uint16_t> vcr;
     int max_nc = 0;
     int max_nvc = 0;
 

@@ -117,6 +117,17 @@ static GenTables build_tables()
             }
             t.f[s][m] = sum;
         }
+    t.vcr_off.assign(128 * 8 + 1, 0);
+    for (int m = 0; m < 128; m++)
+        for (uint32_t r = 0; r < 8; r++) {
+            t.vcr_off[m * 8 + r] = (uint32_t)t.vcr.size();
+            if (r == 0) continue;
+            for (uint32_t i = t.vc_off[m]; i < t.vc_off[m + 1]; i++) {
+                const uint32_t u = t.vc_uop[i];
+                if (UOP_A(u) == r || UOP_B(u) == r) t.vcr.push_back((uint16_t)(i - t.vc_off[m]));
+            }
+        }
+    t.vcr_off[128 * 8] = (uint32_t)t.vcr.size();
     for (int s = 0; s < 5; s++) t.ev[s].assign(128, 0);
     for (int m = 0; m < 128; m++) t.ev[1][m] = t.vc_off[m + 1] - t.vc_off[m];
     for (int s = 2; s < 5; s++)

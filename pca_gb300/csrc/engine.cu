@@ -1244,16 +1244,21 @@ int ensure_device_tables(int device)
             if (!seen[v]) { seen[v] = true; first[gt.vc_off[m] + v] = (uint16_t)c; }
         }
     }
-    uint32_t *cand_uop = nullptr, *vc_uop = nullptr, *chunks = nullptr, *vcr_off = nullptr;
+    uint32_t *cand_uop = nullptr, *vc_uop = nullptr, *chunks = nullptr, *vcr_uop_d = nullptr;
     uint16_t *vc_first = nullptr, *vcr = nullptr;
-    CK(cudaMalloc(&vcr_off, gt.vcr_off.size() * 4));
-    CK(cudaMalloc(&vcr, std::max<size_t>(gt.vcr.size(), 1) * 2));
-    CK(cudaMemcpy(vcr_off, gt.vcr_off.data(), gt.vcr_off.size() * 4, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(vcr, gt.vcr.data(), gt.vcr.size() * 2, cudaMemcpyHostToDevice));
     {
-        const uint32_t *vo = vcr_off;
+        std::vector<uint32_t> vcr_uop(gt.vcr.size());
+        for (int m = 0; m < 128; m++)
+            for (uint32_t k = gt.vcr_off[m * 8]; k < gt.vcr_off[m * 8 + 8]; k++)
+                vcr_uop[k] = gt.vc_uop[gt.vc_off[m] + gt.vcr[k]];
+        CK(cudaMalloc(&vcr_uop_d, std::max<size_t>(vcr_uop.size(), 1) * 4));
+        CK(cudaMalloc(&vcr, std::max<size_t>(gt.vcr.size(), 1) * 2));
+        CK(cudaMemcpy(vcr_uop_d, vcr_uop.data(), vcr_uop.size() * 4, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(vcr, gt.vcr.data(), gt.vcr.size() * 2, cudaMemcpyHostToDevice));
+        const uint32_t *vu = vcr_uop_d;
         const uint16_t *vr = vcr;
-        CK(cudaMemcpyToSymbol(c_vcr_off, &vo, sizeof vo));
+        CK(cudaMemcpyToSymbol(c_vcr_off, gt.vcr_off.data(), gt.vcr_off.size() * 4));
+        CK(cudaMemcpyToSymbol(c_vcr_uop, &vu, sizeof vu));
         CK(cudaMemcpyToSymbol(c_vcr, &vr, sizeof vr));
     }
     CK(cudaMalloc(&cand_uop, gt.cand_uop.size() * 4));

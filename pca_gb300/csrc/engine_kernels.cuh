@@ -59,8 +59,9 @@ __constant__ const uint32_t *c_vc_uop;
 __constant__ const uint16_t *c_vc_first;   /* first candidate index per class */
 __constant__ uint32_t c_chunk_off[129];    /* op-uniform runs of candidates */
 __constant__ const uint32_t *c_chunks;
-__constant__ const uint32_t *c_vcr_off;    /* [mask*8 + r]: classes reading r */
-__constant__ const uint16_t *c_vcr;
+__constant__ uint32_t c_vcr_off[128 * 8 + 1]; /* [mask*8 + r]: classes reading r */
+__constant__ const uint32_t *c_vcr_uop;    /* their micro-ops */
+__constant__ const uint16_t *c_vcr;        /* their indices in the mask's class list */
 
 /* Per-task parameters of a batch: device arrays indexed by task id. A
    state's task id travels with it through the levels; states of different
@@ -687,23 +688,25 @@ __device__ __forceinline__ void scan_last(const WarpState<TPC> &ws, int T,
                                           uint32_t need1, uint32_t need2)
 {
     const uint32_t vbase = c_vc_off[m];
+    const uint32_t *uops;
     const uint16_t *list = nullptr;
     uint32_t nvc;
     if (need1) {
         const uint32_t l0 = c_vcr_off[m * 8 + need1];
+        uops = c_vcr_uop + l0;
         list = c_vcr + l0;
         nvc = c_vcr_off[m * 8 + need1 + 1] - l0;
     } else {
+        uops = c_vc_uop + vbase;
         nvc = c_vc_off[m + 1] - vbase;
     }
     for (uint32_t b0 = 0; b0 < nvc; b0 += 32) {
         const uint32_t i = b0 + lane;
-        uint32_t u = 0, ci = 0;
+        uint32_t u = 0;
         bool pass = false;
         if (i < nvc) {
             /* first two tests per lane; survivors are checked on all tests below */
-            ci = list ? (uint32_t)list[i] : i;
-            u = c_vc_uop[vbase + ci];
+            u = uops[i];
             uint32_t ra = UOP_A(u), rb = UOP_B(u);
             const bool reads2 = !need2 || ra == need2 || rb == need2;
             ra = ra == rd2 ? 9u : ra == rd1 ? 8u : ra;
@@ -717,14 +720,15 @@ __device__ __forceinline__ void scan_last(const WarpState<TPC> &ws, int T,
             const int j = __ffs(bal) - 1;
             bal &= bal - 1;
             const uint32_t uj = __shfl_sync(0xFFFFFFFFu, u, j);
-            const uint32_t cj = __shfl_sync(0xFFFFFFFFu, ci, j);
             uint32_t ra = UOP_A(uj), rb = UOP_B(uj);
             ra = ra == rd2 ? 9u : ra == rd1 ? 8u : ra;
             rb = rb == rd2 ? 9u : rb == rd1 ? 8u : rb;
             bool ok = true;
             if (lane < T) ok = pca_alu(UOP_OP(uj), ws.R[ra][lane], ws.R[rb][lane], UOP_IMM(uj)) == tgt;
-            if (__all_sync(0xFFFFFFFFu, ok) && lane == 0)
+            if (__all_sync(0xFFFFFFFFu, ok) && lane == 0) {
+                const uint32_t cj = list ? (uint32_t)list[b0 + j] : b0 + j;
                 record_solution(S, q, m1, m2, cj, c_vc_first[vbase + cj]);
+            }
         }
     }
 }
@@ -792,20 +796,22 @@ k_suffix(LevelDev P, TaskDev task, SolBuf S, uint32_t chunks_per_prefix, uint32_
     uint32_t cur_task = ~0u, tgt = 0, tgt0 = 0, tgt1 = 0;
     int T = 0;
     if (lane < TPC) ws.R[0][lane] = 0;
+    bool cur_active = false;
     for (uint64_t it = (uint64_t)blockIdx.x * kWarpsPerBlock + wib; it < items; it += nw) {
-        const uint64_t qi = it / chunks_per_prefix;
-        const uint32_t ck = (uint32_t)(it - qi * chunks_per_prefix);
+        const uint64_t qi = SD == 1 ? it : it / chunks_per_prefix;
+        const uint32_t ck = SD == 1 ? 0u : (uint32_t)(it - qi * chunks_per_prefix);
         const uint64_t q = R.order ? (uint64_t)R.order[R.begin + qi] : R.begin + qi;
         if (q >= P.n) continue;  /* orders are checked on the host; never index outside */
         const uint32_t tid = P.task[q];
-        if (!task.active[tid]) continue;
         if (tid != cur_task) {
             cur_task = tid;
+            cur_active = task.active[tid] != 0;
             T = task.T[tid];
             tgt = lane < T ? task.target[tid * 32 + lane] : 0u;
             tgt0 = task.target[tid * 32];
             tgt1 = task.target[tid * 32 + 1];
         }
+        if (!cur_active) continue;
         const uint32_t live = P.live[q];
         if (q != loaded) {
             __syncwarp();

@@ -797,9 +797,59 @@ k_suffix(LevelDev P, TaskDev task, SolBuf S, uint32_t chunks_per_prefix, uint32_
     int T = 0;
     if (lane < TPC) ws.R[0][lane] = 0;
     bool cur_active = false;
+    if constexpr (SD == 1) {
+        /* one prefix per item, software-pipelined: the next prefix's
+           links and columns are loaded while this one's classes are scanned
+           (the scan is short, and waiting on those loads bounded the loop) */
+        uint64_t nq = ~0ull;
+        uint32_t ntid = 0, nlive = 0, nw0 = 0, ncol[7];
+        auto fetch = [&](uint64_t i) {
+            nq = ~0ull;
+            if (i >= items) return;
+            const uint64_t q = R.order ? (uint64_t)R.order[R.begin + i] : R.begin + i;
+            if (q >= P.n) return;  /* orders are checked on the host; never index outside */
+            nq = q;
+            ntid = P.task[q];
+            nlive = P.live[q];
+            nw0 = P.rdl[q];
+            const uint16_t *src = P.regs + q * 8 * TPC + (lane < TPC ? lane : 0);
+#pragma unroll
+            for (int r = 1; r < 8; r++) ncol[r - 1] = src[r * TPC];
+        };
+        uint64_t it = (uint64_t)blockIdx.x * kWarpsPerBlock + wib;
+        fetch(it);
+        for (; it < items; it += nw) {
+            const uint64_t q = nq;
+            const uint32_t tid = ntid, live = nlive, w0 = nw0;
+            if (q != ~0ull) {
+                __syncwarp();
+                if (lane < TPC) {
+#pragma unroll
+                    for (int r = 1; r < 8; r++) ws.R[r][lane] = ncol[r - 1];
+                }
+                __syncwarp();
+            }
+            fetch(it + nw);
+            if (q == ~0ull) continue;
+            if (tid != cur_task) {
+                cur_task = tid;
+                cur_active = task.active[tid] != 0;
+                T = task.T[tid];
+                tgt = lane < T ? task.target[tid * 32 + lane] : 0u;
+                tgt0 = task.target[tid * 32];
+                tgt1 = task.target[tid * 32 + 1];
+            }
+            if (!cur_active) continue;
+            /* w0: the prefix's last write (0 at a root); some later
+               instruction must read it (the rule scan_last states) */
+            scan_last<TPC>(ws, T, (live >> 1) & 127u, 8, 8, tgt, tgt0, tgt1, lane, S, q, 0, 0, w0,
+                           0);
+        }
+        return;
+    }
     for (uint64_t it = (uint64_t)blockIdx.x * kWarpsPerBlock + wib; it < items; it += nw) {
-        const uint64_t qi = SD == 1 ? it : it / chunks_per_prefix;
-        const uint32_t ck = SD == 1 ? 0u : (uint32_t)(it - qi * chunks_per_prefix);
+        const uint64_t qi = it / chunks_per_prefix;
+        const uint32_t ck = (uint32_t)(it - qi * chunks_per_prefix);
         const uint64_t q = R.order ? (uint64_t)R.order[R.begin + qi] : R.begin + qi;
         if (q >= P.n) continue;  /* orders are checked on the host; never index outside */
         const uint32_t tid = P.task[q];
@@ -823,10 +873,6 @@ k_suffix(LevelDev P, TaskDev task, SolBuf S, uint32_t chunks_per_prefix, uint32_
         /* the prefix's last write (0 at a root): some later instruction
            must read it (the rule scan_last states) */
         const uint32_t w0 = P.rdl[q];
-        if (SD == 1) {
-            scan_last<TPC>(ws, T, m0, 8, 8, tgt, tgt0, tgt1, lane, S, q, 0, 0, w0, 0);
-            continue;
-        }
         const uint32_t cb0 = c_cand_off[m0], nc0 = c_cand_off[m0 + 1] - cb0;
         const uint32_t lo = ck * chunk, hi = min(nc0, lo + chunk);
         for (uint32_t i1 = lo; i1 < hi; i1++) {

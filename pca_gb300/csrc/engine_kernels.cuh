@@ -781,9 +781,11 @@ struct PrefixRange {
 
 /* Suffix enumeration of depth SD (1..3) from the prefixes of level P in
  * range R whose task is active. Work item = (prefix, chunk of first-suffix
- * candidates); for SD = 1 the chunk is the whole prefix. */
+ * candidates); for SD = 1 the chunk is the whole prefix. At SD = 1 five
+ * CTAs per SM (48 registers) measured fastest: four at 64 registers hide
+ * less latency, six spill the prefetched columns. */
 template <int TPC, int SD>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, SD == 1 ? 5 : 1)
 k_suffix(LevelDev P, TaskDev task, SolBuf S, uint32_t chunks_per_prefix, uint32_t chunk,
          PrefixRange R)
 {

@@ -308,20 +308,24 @@ def run_guided(args):
     ev = taskgen.synthetic_batch(2000, seed=202)
     sols = eng.solve_batch(ev, max_depth=4, sol_cap=1, first_only=True)
     sel = [t for t, s in zip(ev, sols) if s.optimal_depth in (3, 4)]
-    vo = ValueOrder(net)
+    vo = ValueOrder(net, sample=4096)
     orders = (("dfs", lambda v: None), ("random", RandomOrder(1)), ("value", vo),
               ("value_every_stage", ValueOrder(net, min_states=1, gain=0.0)))
+    # dfs, random and value orders run with the engine's automatic split
+    # (stages it expects to be cheap run plain); value_every_stage orders
+    # every stage from level 2, to measure the ordering itself
+    split = {"dfs": -1, "random": -1, "value": -1, "value_every_stage": 2}
     for t in sel[:3]:  # warm-up (lazy kernel loading)
         eng.solve(t, max_depth=4, sol_cap=1, first_only=True)
         for name, fn in orders:
-            eng.solve_ordered(t, fn, chunk=256, max_depth=4, split_depth=2)
+            eng.solve_ordered(t, fn, chunk=256, max_depth=4, split_depth=split[name])
     vo.score_ms = 0.0
     res = {"plain": [], "dfs": [], "random": [], "value": [], "value_every_stage": []}
     for t in sel:
         p = eng.solve(t, max_depth=4, sol_cap=1, first_only=True)
         res["plain"].append((1.0, None, p.seconds))
         for name, fn in orders:
-            s = eng.solve_ordered(t, fn, chunk=256, max_depth=4, split_depth=2)
+            s = eng.solve_ordered(t, fn, chunk=256, max_depth=4, split_depth=split[name])
             assert s.optimal_depth == p.optimal_depth
             res[name].append((s.prefixes_to_first / max(s.prefixes_at_optimal, 1), s.ms_to_first,
                               s.seconds))
@@ -343,7 +347,10 @@ def run_guided(args):
                 summ["value_every_stage"]["mean_fraction_to_first"]
                 / summ["dfs"]["mean_fraction_to_first"],
             "config": {"workload": f"{len(sel)} held-out synthetic tasks with optimal kernel depth "
-                                   "3-4; ordered solves from split level 2, first launch 256 "
+                                   "3-4; ordered solves with the engine's automatic split (stages "
+                                   "predicted under 2 ms run plain; value ranks a 4,096-prefix "
+                                   "random sample, the rest follows at random), value_every_stage "
+                                   "scores whole levels from split level 2; first launch 256 "
                                    "prefixes, doubling",
                        "train_tasks_used": used, "train_states": ds.n,
                        "params": net.n_params(), "epochs": 10},
@@ -496,11 +503,12 @@ def main():
     line["kernels_ms_per_step"]["expand_total"] = None
     # Roofline of the suffix kernel: integer-issue bound. Peak = one warp
     # instruction per SM sub-partition per clock at the measured max clock.
-    # Achieved = this run's value-class evaluations per second of suffix-kernel
-    # time x the kernel's warp instructions per evaluation, measured by ncu
-    # (profiles/k_suffix_is_power2_t32_k4.md: 2.20e9 instructions for the
-    # depth-4 launch's 7.30e8 evaluations).
-    inst_per_eval = 2203637570 / 7.30e8
+    # Achieved = this run's value-class evaluations of the full candidate
+    # space per second of suffix-kernel time x the kernel's warp instructions
+    # per such evaluation, measured by ncu (profiles/k_suffix_is_power2_t32_k4.md:
+    # 1.50e9 instructions for the depth-4 launch, whose full space is 7.30e8
+    # evaluations; the kernel scans only the classes that can solve).
+    inst_per_eval = 1496436129 / 7.30e8
     peak_issue = sms * 4 * sm_max * 1e6
     achieved_issue = suffix_evals_per_s * inst_per_eval
     line["roofline"] = {
@@ -508,7 +516,7 @@ def main():
         "bound": "int_issue", "unit": "Gwarp-inst/s",
         "achieved": achieved_issue / 1e9, "peak": peak_issue / 1e9,
         "frac": achieved_issue / peak_issue,
-        "traffic": 2888440000 + 3394560,
+        "traffic": 2735593000 + 3713024,
         "evaluations_per_s": suffix_evals_per_s,
         "peak_source": f"{sms} SMs x 4 issue slots x sm_max_mhz from MEASURED_PEAKS.json ({pk_kind})",
         "ncu": "profiles/k_suffix_is_power2_t32_k4.md",

@@ -70,6 +70,9 @@ constexpr int kPinStatus = 0, kPinSurvivors = 1, kPinTotal = 2, kPinCount = 3, k
 /* A level whose children fit in this many bytes of states is written into
    space for all of them, so its build needs one host round trip. */
 constexpr uint64_t kOneSyncBytes = 64ull << 20;
+/* ordered solves with an automatic split (see run_batch) */
+constexpr double kOrderMinStageMs = 2.0;
+constexpr double kOrderStageShare = 0.1;
 
 struct Level {
     uint64_t n = 0;
@@ -831,14 +834,16 @@ typedef void (*done_fn)(int task, void *user);
  *   builds(D+1..S) + evals(S, K-S) x ms per evaluation,
  * with evals of a level not built yet extrapolated from the deepest built
  * level D: evals(S, K-S) ~ evals(D, K-D) x dedup_ratio^(S-D). The cheapest
- * S within the HBM budget (max_feasible) wins. */
-int autotune_split(pcagb_engine *e, int K, const std::vector<uint8_t> &active)
+ * S within the HBM budget (max_feasible) wins. stage_scale weights the
+ * stage term (an ordered stage that stops at its first solution is expected
+ * to run a fraction of it); *pred_ms receives the winner's predicted time. */
+int autotune_split(pcagb_engine *e, int K, const std::vector<uint8_t> &active,
+                   double stage_scale = 1.0, double *pred_ms = nullptr)
 {
     const GenTables &gt = gen_tables();
     const int D = (int)e->levels.size() - 1;
     const int hi = std::min(K - 1, e->max_feasible);
     const int lo = std::max(0, K - 3);
-    if (hi <= D) return std::max(hi, lo);
     auto evals_from = [&](int S, int s) {
         const std::vector<uint64_t> &g = gt.ev[s];
         double ev = 0;
@@ -854,13 +859,19 @@ int autotune_split(pcagb_engine *e, int K, const std::vector<uint8_t> &active)
             if (active[i >> 7]) c += (double)L.hist[i] * gt.nc((int)(i & 127));
         return c;
     };
+    if (hi <= D) {
+        const int S = std::max(hi, lo);
+        if (pred_ms)
+            *pred_ms = K - S <= 3 ? evals_from(S, K - S) * e->t_eval_ms * stage_scale : 1e300;
+        return S;
+    }
     int best = -1;
     double best_ms = 1e300;
     for (int S = std::max(lo, 0); S <= hi; S++) {
         if (K - S > 3) continue;
         double ms;
         if (S <= D) {
-            ms = evals_from(S, K - S) * e->t_eval_ms;
+            ms = evals_from(S, K - S) * e->t_eval_ms * stage_scale;
         } else {
             /* build D+1..S from D, then the suffix from S. A build that would
                not fit the arena (its table, bitmap and ranks, plus the new
@@ -883,10 +894,11 @@ int autotune_split(pcagb_engine *e, int K, const std::vector<uint8_t> &active)
                 kids *= e->dedup_ratio * 800.0;  /* ~children per state deeper down */
             }
             if (!fits) continue;
-            ms = build + evals_from(D, K - D) * states_scale * e->t_eval_ms;
+            ms = build + evals_from(D, K - D) * states_scale * e->t_eval_ms * stage_scale;
         }
         if (ms < best_ms) { best_ms = ms; best = S; }
     }
+    if (pred_ms) *pred_ms = best_ms;
     return best < 0 ? std::max(hi, lo) : best;
 }
 
@@ -1107,8 +1119,26 @@ int run_batch(pcagb_engine *e, std::vector<TaskRun> &runs, const pcagb_opts_t &o
         CK(e_copy(e, e->d_task_active, active.data(), nt, cudaMemcpyHostToDevice, e->stream));
         e->h_active = active;
         int S_target = o.count_levels ? K : K - 1;
-        if (o.split_depth >= 0) S_target = std::min(S_target, o.split_depth);
-        else if (o.first_only && !o.count_levels) S_target = autotune_split(e, K, active);
+        /* an ordered solve with an automatic split orders only the stages
+           worth it: a stage the autotuner expects to finish in under
+           kOrderMinStageMs runs plain from its cheapest level; the others
+           start from the level that minimises builds + a tenth of the stage
+           (the share an ordered stage is expected to run) */
+        bool ordered_stage = ord != nullptr;
+        if (o.split_depth >= 0) {
+            S_target = std::min(S_target, o.split_depth);
+        } else if (ord && !o.count_levels) {
+            double plain_ms = 0;
+            const int Sp = autotune_split(e, K, active, 1.0, &plain_ms);
+            if (plain_ms < kOrderMinStageMs) {
+                S_target = Sp;
+                ordered_stage = false;
+            } else {
+                S_target = autotune_split(e, K, active, kOrderStageShare);
+            }
+        } else if (o.first_only && !o.count_levels) {
+            S_target = autotune_split(e, K, active);
+        }
         while ((int)e->levels.size() - 1 < S_target &&
                (int)e->levels.size() - 1 < e->max_feasible) {
             const int d = (int)e->levels.size() - 1;
@@ -1146,7 +1176,7 @@ int run_batch(pcagb_engine *e, std::vector<TaskRun> &runs, const pcagb_opts_t &o
         }
         StageOrder so;
         StageOrder *sop = nullptr;
-        if (ord && s >= 1) {
+        if (ordered_stage && s >= 1) {
             double evals = 0;
             for (int i = 0; i < nt; i++)
                 if (active[i]) evals += (double)runs[i].res.evaluations[K];
@@ -1198,7 +1228,10 @@ int run_batch(pcagb_engine *e, std::vector<TaskRun> &runs, const pcagb_opts_t &o
         const std::function<void(int, int)> on_tasks = [&](int lo, int hi) {
             for (int i = lo; i < hi; i++) finish(i);
         };
-        int rc = run_stage(e, S, K, runs, o.first_only != 0, sop, sop ? nullptr : &on_tasks);
+        /* a plain stage of an ordered solve keeps only the DFS-first
+           solution, as a first-only solve does */
+        const bool stage_first_only = o.first_only != 0 || (ord && !ordered_stage);
+        int rc = run_stage(e, S, K, runs, stage_first_only, sop, sop ? nullptr : &on_tasks);
         if (rc) return rc;
         for (int i = 0; i < nt; i++) finish(i);
     }

@@ -170,14 +170,23 @@ class ValueOrder:
     (stages at several depths reuse its order). Stages keep DFS order when
     scoring would cost more than it can save: levels below `min_states`,
     and stages the engine expects to finish in less than `gain` x the
-    scoring time (fixed_ms + n / states_per_ms)."""
+    scoring time (fixed_ms + scored states / states_per_ms).
+
+    With `sample` set, a level larger than it is scored on a uniform random
+    sample of that many prefixes: the order is the sample by decreasing
+    score, then every other prefix in random order. The first correct
+    program usually sits in the first few percent of a good order, so the
+    ranked sample decides the first launches at a fraction of the scoring
+    cost; the order stays a permutation of the whole level."""
 
     def __init__(self, net: ValueNet, chunk_states=1 << 20, min_states=4096, gain=2.0,
-                 fixed_ms=0.25, states_per_ms=1.0e5):
+                 fixed_ms=0.25, states_per_ms=1.0e5, sample=None, seed=0):
         self.net = net
         self.chunk_states = chunk_states
         self.min_states = min_states
         self.gain, self.fixed_ms, self.states_per_ms = gain, fixed_ms, states_per_ms
+        self.sample = sample
+        self.gen = torch.Generator(device=net.dev).manual_seed(seed)
         self.score_ms = 0.0
         self._cache = {}
 
@@ -186,8 +195,9 @@ class ValueOrder:
         if n < self.min_states:
             return None
         key = (view.regs, n, view.depth)
+        scored = n if not self.sample else min(n, self.sample)
         if key not in self._cache and \
-                view.est_stage_ms < self.gain * (self.fixed_ms + n / self.states_per_ms):
+                view.est_stage_ms < self.gain * (self.fixed_ms + scored / self.states_per_ms):
             return None
         if key in self._cache:
             return self._cache[key]
@@ -200,6 +210,14 @@ class ValueOrder:
             ntask = view.ntasks
             task_io = _device_view(view.task_io, ntask * 3 * 32, torch.int16, dev)
             task_T = _device_view(view.task_T, ntask, torch.int32, dev)
+            if scored < n:
+                order = self._sampled_order(view, n, scored, tp, task_io, task_T, dev)
+                ev1.record(stream)
+                ev1.synchronize()
+                self.net.check_status()
+                self.score_ms += ev0.elapsed_time(ev1)
+                self._cache = {key: order}
+                return order
             scores = torch.empty(n, device=dev, dtype=torch.float32)
             for b0 in range(0, n, self.chunk_states):
                 m = min(self.chunk_states, n - b0)
@@ -217,6 +235,22 @@ class ValueOrder:
         self.score_ms += ev0.elapsed_time(ev1)
         self._cache = {key: order}
         return order
+
+
+    def _sampled_order(self, view, n, m, tp, task_io, task_T, dev):
+        perm = torch.randperm(n, device=dev, generator=self.gen)
+        head = perm[:m]
+        regs = _device_view(view.regs, n * 8 * tp, torch.int16, dev).view(n, 8 * tp)
+        flags = _device_view(view.flags, n * tp, torch.uint8, dev).view(n, tp)
+        live = _device_view(view.live, n, torch.uint8, dev)
+        task = _device_view(view.task, n, torch.int16, dev)
+        depth = torch.full((m,), view.depth, device=dev, dtype=torch.uint8)
+        scores = self.net.forward_fused(regs.index_select(0, head).reshape(-1),
+                                        flags.index_select(0, head).reshape(-1),
+                                        live.index_select(0, head), task.index_select(0, head),
+                                        depth, tp, task_io, task_T)[:, 0]
+        ranked = head[torch.argsort(scores, descending=True, stable=True)]
+        return torch.cat([ranked, perm[m:]]).to(torch.int32)
 
 
 class RandomOrder:

@@ -47,13 +47,14 @@ def test_positive_labels_are_exact(engine):
     assert checked > 0
 
 
-@pytest.mark.parametrize("order", ["dfs", "random", "value"])
+@pytest.mark.parametrize("order", ["dfs", "random", "value", "value_sampled"])
 def test_ordered_solve_is_exact(engine, order):
     from pca_gb300.guided import RandomOrder, ValueOrder
     from pca_gb300.valuenet import ValueNet
     lib = PCALib()
     fn = {"dfs": lambda v: None, "random": RandomOrder(5),
-          "value": ValueOrder(ValueNet(seed=1), min_states=1, gain=0.0)}[order]
+          "value": ValueOrder(ValueNet(seed=1), min_states=1, gain=0.0),
+          "value_sampled": ValueOrder(ValueNet(seed=1), min_states=1, gain=0.0, sample=512)}[order]
     for task in pick(engine, 41, 300, (3, 4))[:6]:
         plain = engine.solve(task, max_depth=4, split_depth=2, sol_cap=1 << 14)
         got = engine.solve_ordered(task, fn, chunk=64, max_depth=4, split_depth=2, sol_cap=1 << 14)
@@ -62,6 +63,26 @@ def test_ordered_solve_is_exact(engine, order):
         for p in got.programs:
             assert lib.evaluate(task, p) == task.num_tests
         assert 0 < got.prefixes_to_first <= got.prefixes_at_optimal
+
+
+@pytest.mark.parametrize("order", ["dfs", "value"])
+def test_ordered_solve_auto_split_is_exact(engine, order):
+    """With an automatic split the engine runs a stage it expects to be
+    cheap plain (keeping its DFS-first solution) and orders the others;
+    either way the optimal depth and correct programs of the plain set come
+    back."""
+    from pca_gb300.guided import ValueOrder
+    from pca_gb300.valuenet import ValueNet
+    lib = PCALib()
+    fn = {"dfs": lambda v: None, "value": ValueOrder(ValueNet(seed=1), min_states=1, gain=0.0)}[order]
+    tasks = pick(engine, 41, 300, (3, 4))[:6] + pick(engine, 202, 800, (4,))[:2]
+    for task in tasks:
+        plain = engine.solve(task, max_depth=4, split_depth=2, sol_cap=1 << 14)
+        got = engine.solve_ordered(task, fn, chunk=64, max_depth=4, split_depth=-1, sol_cap=1 << 14)
+        assert got.optimal_depth == plain.optimal_depth
+        assert got.programs and set(map(tuple, got.programs)) <= set(map(tuple, plain.programs))
+        for p in got.programs:
+            assert lib.evaluate(task, p) == task.num_tests
 
 
 def test_trained_network_beats_dfs_order(engine):

@@ -293,7 +293,12 @@ typedef const uint32_t *(*pcagb_order_cb)(const pcagb_level_view_t *view, void *
  * launch of the optimal depth that holds a solution.
  * Exact: every depth below the optimum is still searched completely, so the
  * optimal depth is proven; only the order of work at the optimal depth
- * changes (its programs are those of the visited chunks). */
+ * changes (its programs are those of the visited chunks).
+ * opts->split_depth >= 0 starts every stage from that level and calls the
+ * callback for each. split_depth = -1 lets the engine choose: a stage it
+ * predicts to finish in under 2 ms runs plain from its cheapest level
+ * (no callback; its DFS-first solution is kept), the others start from the
+ * level that minimises level builds plus a tenth of the stage. */
 int  pcagb_solve_ordered(pcagb_engine_t *e, const task_spec_t *task, const pcagb_opts_t *opts,
                          pcagb_order_cb order, void *user, uint64_t chunk,
                          pcagb_result_t *res, uint16_t *sol_progs, int *sol_lens, int sol_cap);

@@ -83,6 +83,8 @@ struct Level {
     uint32_t *parent = nullptr;
     uint16_t *cidx = nullptr;
     uint8_t *rdl = nullptr;         /* register each state's last instruction wrote */
+    uint32_t *fcr = nullptr;        /* [n][8] rank of the first kept child writing r (set
+                                       when the level below is materialised) */
     uint64_t *child_off = nullptr;  /* set when this level is expanded */
     uint64_t children = 0;
     std::vector<uint64_t> hist;     /* [task][128] states per liveness mask */
@@ -230,7 +232,7 @@ int exclusive_scan(pcagb_engine *e, uint64_t *a, uint64_t n, uint64_t *total)
 
 LevelDev view(const Level &L)
 {
-    return LevelDev{L.regs, L.flags, L.live, L.task, L.child_off, L.n, L.rdl};
+    return LevelDev{L.regs, L.flags, L.live, L.task, L.child_off, L.n, L.rdl, L.parent};
 }
 
 int alloc_level(pcagb_engine *e, Level &L, uint64_t n)
@@ -285,11 +287,12 @@ uint32_t split_log2(uint64_t parents, int grid)
 }
 
 template <int TPC>
-int launch_expand(pcagb_engine *e, const Level &P, unsigned long long *table, uint64_t tmask)
+int launch_expand(pcagb_engine *e, const Level &P, const uint32_t *fcr_up,
+                  unsigned long long *table, uint64_t tmask)
 {
     const int g = e->grid(e->occ_insert);
     k_expand_insert<TPC><<<g, kThreads, 0, e->stream>>>(view(P), e->td, table, tmask,
-                                                        e->d_status, split_log2(P.n, g));
+                                                        e->d_status, split_log2(P.n, g), fcr_up);
     return check_launch(e);
 }
 
@@ -300,7 +303,7 @@ int launch_materialize(pcagb_engine *e, const Level &P, const uint32_t *bitmap,
     LevelOut out{C.regs, C.flags, C.live, C.task, C.parent, C.cidx, C.rdl};
     const int g = e->grid(e->occ_mat);
     k_materialize<TPC><<<g, kThreads, 0, e->stream>>>(view(P), e->td, bitmap, word_off, out,
-                                                      split_log2(P.n, g));
+                                                      split_log2(P.n, g), P.fcr);
     return check_launch(e);
 }
 
@@ -321,7 +324,10 @@ int build_level(pcagb_engine *e, int d)
     auto fail = [&](int rc) {
         e->bottom = bottom0;
         e->top = top0;
-        if (rc == PCAGB_ENOMEM) P.child_off = nullptr;
+        if (rc == PCAGB_ENOMEM) {
+            P.child_off = nullptr;
+            P.fcr = nullptr;
+        }
         return rc;
     };
     if (!P.child_off) {
@@ -339,6 +345,14 @@ int build_level(pcagb_engine *e, int d)
             if (e->h_active[i >> 7]) c += P.hist[i] * (uint64_t)gt.nc((int)(i & 127));
         P.children = c;
     }
+    if (!P.fcr && !e->no_oep) {
+        P.fcr = (uint32_t *)e->alloc_bottom(P.n * 8 * sizeof(uint32_t));
+        if (!P.fcr) return fail(PCAGB_ENOMEM);
+        CK(cudaMemsetAsync(P.fcr, 0xFF, P.n * 8 * sizeof(uint32_t), e->stream));
+    }
+    /* the dead-write rule of the insert kernel needs the first-child ranks
+       of the level above (unset at the root) */
+    const uint32_t *fcr_up = d >= 1 ? e->levels[d - 1].fcr : nullptr;
     const uint64_t children = P.children;
     if (children >= (1ull << 38)) return fail(PCAGB_ENOMEM);
     const uint64_t words = (children + 31) / 32;
@@ -363,8 +377,8 @@ int build_level(pcagb_engine *e, int d)
         CK(cudaMemsetAsync(bitmap, 0, words * 4 + 4, e->stream));
         CK(cudaMemsetAsync(e->d_small + 2, 0, 8, e->stream));
         cudaEventRecord(e->ev2, e->stream);
-        int rc = e->TPC == 16 ? launch_expand<16>(e, P, table, slots - 1)
-                              : launch_expand<32>(e, P, table, slots - 1);
+        int rc = e->TPC == 16 ? launch_expand<16>(e, P, fcr_up, table, slots - 1)
+                              : launch_expand<32>(e, P, fcr_up, table, slots - 1);
         if (rc) return rc;
         cudaEventRecord(e->ev3, e->stream);
         k_mark<<<e->grid(4), 256, 0, e->stream>>>(table, slots, P.child_off, bitmap,

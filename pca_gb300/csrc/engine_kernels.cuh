@@ -81,6 +81,7 @@ struct LevelDev {
     const uint64_t *child_off; /* [n+1] */
     uint64_t n;
     const uint8_t *rdl;     /* [n] register the state's last instruction wrote (0: root) */
+    const uint32_t *parent; /* [n] rank of the parent in the level above */
 };
 
 struct LevelOut {
@@ -152,6 +153,12 @@ __device__ __forceinline__ uint64_t hash_flags(const uint32_t *f)
         h = chain(h, w);
     }
     return h;
+}
+
+/* Reads: does micro-op u read register r (1..7)? */
+__device__ __forceinline__ bool uop_reads(uint32_t u, uint32_t r)
+{
+    return UOP_A(u) == r || UOP_B(u) == r;
 }
 
 /* ---- shared-memory view of one state per warp ---------------------------- */
@@ -342,7 +349,7 @@ __device__ bool warp_child_equal(const LevelDev &P, const InsertState<TPC> &A, u
 template <int TPC>
 __global__ void __launch_bounds__(kThreads, 6)
 k_expand_insert(LevelDev P, TaskDev task, unsigned long long *table, uint64_t tmask,
-                uint32_t *status, uint32_t split_log2)
+                uint32_t *status, uint32_t split_log2, const uint32_t *fcr_up)
 {
     __shared__ InsertState<TPC> sws[kWarpsPerBlock];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -372,12 +379,26 @@ k_expand_insert(LevelDev P, TaskDev task, unsigned long long *table, uint64_t tm
         const uint32_t k0 = c_chunk_off[m], k1 = c_chunk_off[m + 1];
         const uint32_t per = (k1 - k0 + split - 1) >> split_log2;
         const uint32_t ka = min(k1, k0 + g * per), kb = min(k1, ka + per);
+        /* Dead writes. Let q = P' + z with z writing w. A child y that is not
+           an LDI and overwrites w without reading it gives the same state
+           (registers, y's flags, live) for every kept sibling of q that also
+           wrote w, so only the first of them (fcr_up: the lowest-ranked kept
+           child of P' writing w) can hold the smallest ref, the DFS-first
+           representative; the others' such children are not inserted. The
+           table's winners, and so every level, are unchanged. */
+        uint32_t wdead = 0;
+        if (fcr_up) {
+            const uint32_t w = P.rdl[q];
+            if (w && fcr_up[(uint64_t)P.parent[q] * 8 + w] != (uint32_t)q) wdead = w;
+        }
         for (uint32_t k = ka; k < kb; k++) {
             const uint32_t ch = c_chunks[k], start = ch >> 8, cnt = ch & 255u;
-            const bool valid = (uint32_t)lane < cnt;
+            bool valid = (uint32_t)lane < cnt;
             const uint32_t c = start + (valid ? lane : 0);
             const uint32_t u = c_cand_uop[base + c];
             const uint32_t op = UOP_OP(u), rd = UOP_RD(u);
+            if (wdead && rd == wdead && op != PCA_OP_LDI && !uop_reads(u, wdead)) valid = false;
+            if (!__any_sync(0xFFFFFFFFu, valid)) continue;
             uint64_t h, hf;
             __syncwarp();   /* the previous chunk's compares are done with colA */
             child_hashes_any<TPC>(op, ws, UOP_A(u), UOP_B(u), UOP_IMM(u), T, lane, h, hf);
@@ -510,7 +531,7 @@ __global__ void k_child_counts(const uint8_t *live, const uint16_t *task, const 
 template <int TPC>
 __global__ void __launch_bounds__(kThreads)
 k_materialize(LevelDev P, TaskDev task, const uint32_t *bitmap, const uint64_t *word_off,
-              LevelOut C, uint32_t split_log2)
+              LevelOut C, uint32_t split_log2, uint32_t *fcr)
 {
     __shared__ WarpState<TPC> sws[kWarpsPerBlock];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -556,6 +577,8 @@ k_materialize(LevelDev P, TaskDev task, const uint32_t *bitmap, const uint64_t *
                     C.task[rank] = (uint16_t)tid;
                     C.parent[rank] = (uint32_t)q;
                     C.cidx[rank] = (uint16_t)c;
+                    /* first kept child of q per written register */
+                    if (fcr) atomicMin(&fcr[q * 8 + UOP_RD(u)], (uint32_t)rank);
                 }
             }
             uint32_t bal = __ballot_sync(0xFFFFFFFFu, keep);
@@ -731,12 +754,6 @@ __device__ __forceinline__ void scan_last(const WarpState<TPC> &ws, int T,
             }
         }
     }
-}
-
-/* Reads: does micro-op u read register r (1..7)? */
-__device__ __forceinline__ bool uop_reads(uint32_t u, uint32_t r)
-{
-    return UOP_A(u) == r || UOP_B(u) == r;
 }
 
 /* The suffix kernels' view of a prefix: only its live columns (no operand

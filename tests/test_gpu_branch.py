@@ -99,13 +99,12 @@ def test_unbuilt_last_level_gives_same_programs(engine, fx):
 PUBLISHED = load_golden("ref_published.json")
 
 
-@pytest.mark.parametrize("t", [t for t in PUBLISHED if t["name"] != "saturating_add"],
-                         ids=lambda t: t["name"])
+@pytest.mark.parametrize("t", PUBLISHED, ids=lambda t: t["name"])
 def test_published_branch_mode_lengths(engine, t):
     """The reference's documented optimal lengths of its own task files in
     branch mode (negate/double/square 4, add 5, abs/relu 6, max 7, is_power2
-    7), found and proven here (every shorter depth searched completely); the
-    programs pass the VM."""
+    7, saturating_add 8), found and proven here (every shorter depth searched
+    completely); the programs pass the VM."""
     from pca_gb300.pcalib import PCALib
     task = spec_from_json(t["task"])
     K = t["published_length"] - task.num_inputs - 2

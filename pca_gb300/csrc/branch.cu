@@ -37,6 +37,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/pca_gb300.h"
@@ -509,8 +510,11 @@ __global__ void k_bleaf(BDev P, int T, const uint32_t *target, uint8_t *mask)
 
 /* ---- the last position without its level ------------------------------------ */
 
-/* A solving child of the last position: its linear child index (depth-first
-   order), key, parent, candidate and the registers it solves for. */
+/* A child of the last position whose registers hold the target on every
+   test (live or not, faulted or not): its linear child index (depth-first
+   order), key, parent, candidate, and the registers it solves for (0 when
+   it faulted or the matching registers are not live: it cannot solve, but
+   it may be the depth-first first of a solving child's key). */
 struct BSol {
     uint64_t L;
     uint64_t key;
@@ -522,9 +526,13 @@ struct BSol {
 
 /* One warp per parent, one lane per last-position candidate: the output
    check of every complete kernel without materializing the last level. A
-   register other than the written one solves when the parent's column
-   already matches on every test; the written one when its new column does;
-   a test that faults (here or before) fails every register. */
+   register other than the written one holds the target when the parent's
+   column already does on every test; the written one when its new column
+   does; a test that faults (here or before) fails every register. Every
+   child whose registers hold the target is recorded, solving or not: a
+   child with the same state as a solving one holds the same registers, so
+   the records contain the depth-first first child of every solving state
+   (the one the pruner keeps) without a pass over all children. */
 template <int TP>
 __global__ void __launch_bounds__(kBThreads)
 k_bsuffix(BDev P, BTab tab, int T, uint32_t p, const uint32_t *target, BSol *out,
@@ -541,7 +549,7 @@ k_bsuffix(BDev P, BTab tab, int T, uint32_t p, const uint32_t *target, BSol *out
             if (__all_sync(0xFFFFFFFFu, good)) pm |= 1u << r;
         }
         if (lane < T) faulted = P.skip[q * TP + lane] == kFault;
-        if (__any_sync(0xFFFFFFFFu, faulted)) continue;
+        const bool pfault = __any_sync(0xFFFFFFFFu, faulted);
         const uint32_t live = P.live[q];
         const uint32_t m = (live >> 1) & 127u;
         const uint32_t nc = bcount(tab, m);
@@ -551,7 +559,10 @@ k_bsuffix(BDev P, BTab tab, int T, uint32_t p, const uint32_t *target, BSol *out
             const uint32_t insn = bcand(tab, m, c);
             const uint32_t op = insn >> 11, rdi = (insn >> 8) & 7u;
             const uint32_t wr = (op != (uint32_t)kOpCmp && op != (uint32_t)kOpBr && rdi != 0) ? rdi : 0u;
-            bool match = wr != 0, fault = false;
+            /* a register the child leaves as the parent's can hold the
+               target only where the parent's column does */
+            if (!(pm & ~(1u << wr) & 0xFEu) && !wr) continue;
+            bool match = wr != 0, fault = pfault;
             for (int t = 0; t < T; t++) {
                 uint32_t R[8];
 #pragma unroll
@@ -561,12 +572,12 @@ k_bsuffix(BDev P, BTab tab, int T, uint32_t p, const uint32_t *target, BSol *out
                 if (sk == kFault) fault = true;
                 if (wr) match &= (rd == wr ? v : R[wr]) == target[t];
             }
-            if (fault) continue;
+            uint32_t any = pm & ~(1u << wr);
+            if (match) any |= 1u << wr;
+            any &= 0xFEu;
+            if (!any) continue;
             const uint32_t clive = live | (wr ? 1u << wr : 0u);
-            uint32_t mask = pm & clive & ~(1u << wr);
-            if (match) mask |= 1u << wr;
-            mask &= 0xFEu;
-            if (!mask) continue;
+            const uint32_t mask = fault ? 0u : (any & clive);
             const unsigned long long i = atomicAdd(count, 1ull);
             if (i < cap) {
                 BSol s;
@@ -577,37 +588,6 @@ k_bsuffix(BDev P, BTab tab, int T, uint32_t p, const uint32_t *target, BSol *out
                 s.mask = (uint8_t)mask;
                 s.pad = 0;
                 out[i] = s;
-            }
-        }
-    }
-}
-
-/* Second pass: the depth-first-first child of each solving key. slots holds
-   the solving keys (open addressing, 0 = empty); first[slot] gets the
-   minimum linear child index among all children with that key. */
-template <int TP>
-__global__ void __launch_bounds__(kBThreads)
-k_bfirst(BDev P, BTab tab, int T, uint32_t p, const unsigned long long *slots, uint64_t smask,
-         unsigned long long *first)
-{
-    const int lane = threadIdx.x & 31;
-    const uint64_t nw = (uint64_t)gridDim.x * kWarps;
-    for (uint64_t q = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < P.n; q += nw) {
-        const uint32_t m = (P.live[q] >> 1) & 127u;
-        const uint32_t nc = bcount(tab, m);
-        for (uint32_t c = lane; c < nc; c += 32) {
-            const uint32_t insn = bcand(tab, m, c);
-            if ((insn >> 11) == (uint32_t)kOpBr) continue;
-            const uint64_t key = child_key<TP>(P, q, insn, p, T) | 1ull;
-            uint64_t i = key & smask;
-            for (uint64_t probes = 0; probes <= smask; probes++) {
-                const unsigned long long s = slots[i];
-                if (s == 0) break;
-                if (s == key) {
-                    atomicMin(&first[i], (unsigned long long)(P.child_off[q] + c));
-                    break;
-                }
-                i = (i + 1) & smask;
             }
         }
     }
@@ -821,9 +801,10 @@ int fetch_links(BranchRun &b, const BLevel &L, HostLevel &H, bool links)
 
 /* The last position of a depth-K pass without building level K: solving
  * children from k_bsuffix; a child counts only if it is the depth-first
- * first of its key (the pruner would have dropped it otherwise), found by a
- * second pass over all children (k_bfirst) and checked by full compares.
- * Returns the number of solutions found (0 = none at this depth). */
+ * first of its key (the pruner would have dropped it otherwise), the
+ * smallest child index among k_bsuffix's records with that key, checked by
+ * full compares. Returns the number of solutions found (0 = none at this
+ * depth). */
 int64_t branch_suffix(BranchRun &b, const BranchTables &bt, std::vector<BLevel> &lv, int K,
                       const task_spec_t *task, pcagb_result_t *res, uint16_t *sol_progs,
                       int *sol_lens, int cap)
@@ -855,44 +836,27 @@ int64_t branch_suffix(BranchRun &b, const BranchTables &bt, std::vector<BLevel> 
     BCK(cudaMemcpyAsync(sol.data(), d_sol, cnt * sizeof(BSol), cudaMemcpyDeviceToHost, b.st));
     BCK(cudaStreamSynchronize(b.st));
     b.d2h += cnt * sizeof(BSol) + 8;
-    /* the depth-first first child of every solving key */
-    uint64_t slots = 1024;
-    while (slots < 2 * cnt) slots <<= 1;
-    std::vector<unsigned long long> hs(slots, 0);
-    auto slot_of = [&](uint64_t key) {
-        const uint64_t k = key | 1ull;
-        uint64_t i = k & (slots - 1);
-        while (hs[i] && hs[i] != k) i = (i + 1) & (slots - 1);
-        return i;
-    };
-    for (const BSol &x : sol) hs[slot_of(x.key)] = x.key | 1ull;
-    unsigned long long *d_slots = b.alloc<unsigned long long>(slots);
-    unsigned long long *d_first = b.alloc<unsigned long long>(slots);
-    if (!d_slots || !d_first) { set_berr("device memory exhausted"); return PCAGB_ENOMEM; }
-    BCK(cudaMemcpyAsync(d_slots, hs.data(), slots * 8, cudaMemcpyHostToDevice, b.st));
-    BCK(cudaMemsetAsync(d_first, 0xFF, slots * 8, b.st));
-    if (b.TP == 16)
-        k_bfirst<16><<<b.grid(4), kBThreads, 0, b.st>>>(bdev(P), tab, b.T, p, d_slots, slots - 1, d_first);
-    else
-        k_bfirst<32><<<b.grid(4), kBThreads, 0, b.st>>>(bdev(P), tab, b.T, p, d_slots, slots - 1, d_first);
-    rc = blaunch(b);
-    if (rc) return rc;
-    std::vector<unsigned long long> first(slots);
-    std::vector<uint64_t> coff(P.n + 1);
-    BCK(cudaMemcpyAsync(first.data(), d_first, slots * 8, cudaMemcpyDeviceToHost, b.st));
-    BCK(cudaMemcpyAsync(coff.data(), P.child_off, (P.n + 1) * 8, cudaMemcpyDeviceToHost, b.st));
-    BCK(cudaStreamSynchronize(b.st));
-    b.d2h += slots * 8 + (P.n + 1) * 8;
+    /* the depth-first first child of every solving key: the smallest L
+       among the records with that key (every child equal to a solving one
+       is a record) */
+    std::unordered_map<uint64_t, size_t> first;
+    first.reserve(cnt * 2);
+    for (size_t i = 0; i < cnt; i++) {
+        auto it = first.find(sol[i].key);
+        if (it == first.end()) first.emplace(sol[i].key, i);
+        else if (sol[i].L < sol[it->second].L) it->second = i;
+    }
     /* a solving child that is not the first of its key is dropped when the
        first is equal to it in full (a 64-bit key collision would stop here) */
     std::vector<uint4> pairs;
     std::vector<size_t> pair_of;
-    std::vector<uint8_t> keep(cnt, 1);
+    std::vector<uint8_t> keep(cnt, 0);
     for (size_t i = 0; i < cnt; i++) {
-        const uint64_t f = first[slot_of(sol[i].key)];
-        if (f == sol[i].L) continue;
-        const uint64_t q = (uint64_t)(std::upper_bound(coff.begin(), coff.end(), f) - coff.begin()) - 1;
-        pairs.push_back(make_uint4(sol[i].q, sol[i].c, (uint32_t)q, (uint32_t)(f - coff[q])));
+        if (!sol[i].mask) continue;
+        keep[i] = 1;
+        const size_t f = first[sol[i].key];
+        if (f == i) continue;
+        pairs.push_back(make_uint4(sol[i].q, sol[i].c, sol[f].q, sol[f].c));
         pair_of.push_back(i);
     }
     if (!pairs.empty()) {
@@ -900,6 +864,7 @@ int64_t branch_suffix(BranchRun &b, const BranchTables &bt, std::vector<BLevel> 
         uint8_t *d_eq = b.alloc<uint8_t>(pairs.size());
         if (!d_pairs || !d_eq) { set_berr("device memory exhausted"); return PCAGB_ENOMEM; }
         BCK(cudaMemcpyAsync(d_pairs, pairs.data(), pairs.size() * sizeof(uint4), cudaMemcpyHostToDevice, b.st));
+        b.h2d += pairs.size() * sizeof(uint4);
         if (b.TP == 16)
             k_bpairs_equal<16><<<b.grid(2), 256, 0, b.st>>>(bdev(P), tab, b.T, p, d_pairs, pairs.size(), d_eq);
         else
@@ -909,6 +874,7 @@ int64_t branch_suffix(BranchRun &b, const BranchTables &bt, std::vector<BLevel> 
         std::vector<uint8_t> eq(pairs.size());
         BCK(cudaMemcpyAsync(eq.data(), d_eq, pairs.size(), cudaMemcpyDeviceToHost, b.st));
         BCK(cudaStreamSynchronize(b.st));
+        b.d2h += pairs.size();
         for (size_t j = 0; j < pairs.size(); j++) {
             if (!eq[j]) {
                 set_berr("64-bit key collision between distinct children at depth %d", K);

@@ -5,6 +5,7 @@
     python -m pca_gb300.profile_cases valuenet        # training and scoring kernels
     python -m pca_gb300.profile_cases orders          # k_check_perm
     python -m pca_gb300.profile_cases branch          # branch-mode kernels
+    python -m pca_gb300.profile_cases branch_saturating_add   # the same, two inputs, depth 4
 
 Each case runs its work `--reps` times (default 2) and prints one timing line
 per repetition (CUDA events); the device memory it holds stays below a few
@@ -128,26 +129,39 @@ def case_orders(reps: int):
         print(f"orders: K*={s.optimal_depth} {time.perf_counter() - t0:.4f} s", flush=True)
 
 
-def case_branch(reps: int):
-    """Branch mode on the reference's is_power2 task file (11 tests) to its
-    documented optimal length 7 (kernel depth 4): levels 1..3 built with the
-    exact pruner, the last position searched without its level."""
+def _branch_case(name: str, reps: int):
     import json
     import os
     from .pcalib import Engine, task_from_dict
     fx = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "tests",
                       "golden", "ref_published.json")
-    task = task_from_dict(next(t for t in json.load(open(fx)) if t["name"] == "is_power2")["task"])
+    spec = next(t for t in json.load(open(fx)) if t["name"] == name)
+    task = task_from_dict(spec["task"])
+    K = spec["published_length"] - task.num_inputs - 2
     eng = Engine(0, 1 << 30)
     for _ in range(reps):
         t0 = time.perf_counter()
-        s = eng.solve_branch(task, max_depth=4)
-        print(f"branch is_power2: length {s.optimal_depth + 3} in {time.perf_counter() - t0:.3f} s",
-              flush=True)
+        s = eng.solve_branch(task, max_depth=K)
+        print(f"branch {name}: length {s.optimal_depth + task.num_inputs + 2} in "
+              f"{time.perf_counter() - t0:.3f} s", flush=True)
+
+
+def case_branch(reps: int):
+    """Branch mode on the reference's is_power2 task file (11 tests) to its
+    documented optimal length 7 (kernel depth 4): levels 1..3 built with the
+    exact pruner, the last position searched without its level."""
+    _branch_case("is_power2", reps)
+
+
+def case_branch_saturating_add(reps: int):
+    """Branch mode on the reference's saturating_add task file (two inputs,
+    8 tests) to its documented optimal length 8 (kernel depth 4)."""
+    _branch_case("saturating_add", reps)
 
 
 CASES = {"engine_depths": case_engine_depths, "noalloc": case_noalloc,
-         "valuenet": case_valuenet, "orders": case_orders, "branch": case_branch}
+         "valuenet": case_valuenet, "orders": case_orders, "branch": case_branch,
+         "branch_saturating_add": case_branch_saturating_add}
 
 
 def main(argv=None):

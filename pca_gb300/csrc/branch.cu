@@ -538,7 +538,11 @@ __global__ void __launch_bounds__(kBThreads)
 k_bsuffix(BDev P, BTab tab, int T, uint32_t p, const uint32_t *target, BSol *out,
           unsigned long long *count, uint64_t cap)
 {
-    const int lane = threadIdx.x & 31;
+    __shared__ uint32_t sRall[kWarps][8][TP + 1];
+    __shared__ uint32_t sFall[kWarps][TP], sSall[kWarps][TP];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    uint32_t (&sR)[8][TP + 1] = sRall[wib];
+    uint32_t *sF = sFall[wib], *sS = sSall[wib];
     const uint64_t nw = (uint64_t)gridDim.x * kWarps;
     for (uint64_t q = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < P.n; q += nw) {
         uint32_t pm = 0;
@@ -550,6 +554,15 @@ k_bsuffix(BDev P, BTab tab, int T, uint32_t p, const uint32_t *target, BSol *out
         }
         if (lane < T) faulted = P.skip[q * TP + lane] == kFault;
         const bool pfault = __any_sync(0xFFFFFFFFu, faulted);
+        /* the parent in shared memory: every lane reads test t of it */
+        __syncwarp();
+        if (lane < TP) {
+#pragma unroll
+            for (int r = 0; r < 8; r++) sR[r][lane] = P.regs[(q * 8 + r) * TP + lane];
+            sF[lane] = P.flags[q * TP + lane];
+            sS[lane] = P.skip[q * TP + lane];
+        }
+        __syncwarp();
         const uint32_t live = P.live[q];
         const uint32_t m = (live >> 1) & 127u;
         const uint32_t nc = bcount(tab, m);
@@ -561,16 +574,20 @@ k_bsuffix(BDev P, BTab tab, int T, uint32_t p, const uint32_t *target, BSol *out
             const uint32_t wr = (op != (uint32_t)kOpCmp && op != (uint32_t)kOpBr && rdi != 0) ? rdi : 0u;
             /* a register the child leaves as the parent's can hold the
                target only where the parent's column does */
-            if (!(pm & ~(1u << wr) & 0xFEu) && !wr) continue;
+            const bool kept = (pm & ~(1u << wr) & 0xFEu) != 0;
+            if (!kept && !wr) continue;
             bool match = wr != 0, fault = pfault;
             for (int t = 0; t < T; t++) {
                 uint32_t R[8];
 #pragma unroll
-                for (int r = 0; r < 8; r++) R[r] = P.regs[(q * 8 + r) * TP + t];
+                for (int r = 0; r < 8; r++) R[r] = sR[r][t];
                 uint32_t v = 0, f, sk;
-                const uint32_t rd = bexec(insn, p, R, P.flags[q * TP + t], P.skip[q * TP + t], &v, &f, &sk);
+                const uint32_t rd = bexec(insn, p, R, sF[t], sS[t], &v, &f, &sk);
                 if (sk == kFault) fault = true;
                 if (wr) match &= (rd == wr ? v : R[wr]) == target[t];
+                /* nothing left to record once the written register missed
+                   and no other register holds the target */
+                if (!match && !kept) break;
             }
             uint32_t any = pm & ~(1u << wr);
             if (match) any |= 1u << wr;

@@ -83,6 +83,7 @@ struct Level {
     uint32_t *parent = nullptr;
     uint16_t *cidx = nullptr;
     uint8_t *rdl = nullptr;         /* register each state's last instruction wrote */
+    uint8_t *own = nullptr;         /* dead-able older writes (engine_kernels.cuh) */
     uint32_t *fcr = nullptr;        /* [n][8] rank of the first kept child writing r (set
                                        when the level below is materialised) */
     uint64_t *child_off = nullptr;  /* set when this level is expanded */
@@ -232,7 +233,7 @@ int exclusive_scan(pcagb_engine *e, uint64_t *a, uint64_t n, uint64_t *total)
 
 LevelDev view(const Level &L)
 {
-    return LevelDev{L.regs, L.flags, L.live, L.task, L.child_off, L.n, L.rdl, L.parent};
+    return LevelDev{L.regs, L.flags, L.live, L.task, L.child_off, L.n, L.rdl, L.parent, L.own};
 }
 
 int alloc_level(pcagb_engine *e, Level &L, uint64_t n)
@@ -245,7 +246,8 @@ int alloc_level(pcagb_engine *e, Level &L, uint64_t n)
     L.parent = (uint32_t *)e->alloc_bottom(n * 4);
     L.cidx = (uint16_t *)e->alloc_bottom(n * 2);
     L.rdl = (uint8_t *)e->alloc_bottom(n);
-    if (!L.regs || !L.flags || !L.live || !L.task || !L.parent || !L.cidx || !L.rdl)
+    L.own = (uint8_t *)e->alloc_bottom(n);
+    if (!L.regs || !L.flags || !L.live || !L.task || !L.parent || !L.cidx || !L.rdl || !L.own)
         return PCAGB_ENOMEM;
     return PCAGB_OK;
 }
@@ -297,13 +299,13 @@ int launch_expand(pcagb_engine *e, const Level &P, const uint32_t *fcr_up,
 }
 
 template <int TPC>
-int launch_materialize(pcagb_engine *e, const Level &P, const uint32_t *bitmap,
-                       const uint64_t *word_off, Level &C)
+int launch_materialize(pcagb_engine *e, const Level &P, const uint32_t *fcr_up,
+                       const uint32_t *bitmap, const uint64_t *word_off, Level &C)
 {
-    LevelOut out{C.regs, C.flags, C.live, C.task, C.parent, C.cidx, C.rdl};
+    LevelOut out{C.regs, C.flags, C.live, C.task, C.parent, C.cidx, C.rdl, C.own};
     const int g = e->grid(e->occ_mat);
     k_materialize<TPC><<<g, kThreads, 0, e->stream>>>(view(P), e->td, bitmap, word_off, out,
-                                                      split_log2(P.n, g), P.fcr);
+                                                      split_log2(P.n, g), P.fcr, fcr_up);
     return check_launch(e);
 }
 
@@ -356,7 +358,7 @@ int build_level(pcagb_engine *e, int d)
     const uint64_t children = P.children;
     if (children >= (1ull << 38)) return fail(PCAGB_ENOMEM);
     const uint64_t words = (children + 31) / 32;
-    const uint64_t state_bytes = 8ull * 2 * e->TPC + e->TPC + 1 + 2 + 4 + 2 + 1;
+    const uint64_t state_bytes = 8ull * 2 * e->TPC + e->TPC + 1 + 2 + 4 + 2 + 1 + 1;
     const bool one_sync = children * state_bytes <= kOneSyncBytes;
 
     cudaEventRecord(e->ev0, e->stream);
@@ -424,8 +426,8 @@ int build_level(pcagb_engine *e, int d)
     const uint64_t space = one_sync ? children : survivors;
     if (space >= (1ull << 28)) return fail(PCAGB_ENOMEM);
     if (alloc_level(e, C, space) != PCAGB_OK) return fail(PCAGB_ENOMEM);
-    rc = e->TPC == 16 ? launch_materialize<16>(e, P, bitmap, word_off, C)
-                      : launch_materialize<32>(e, P, bitmap, word_off, C);
+    rc = e->TPC == 16 ? launch_materialize<16>(e, P, fcr_up, bitmap, word_off, C)
+                      : launch_materialize<32>(e, P, fcr_up, bitmap, word_off, C);
     if (rc) return rc;
     cudaEventRecord(e->ev1, e->stream);
     rc = enqueue_hist(e, C, one_sync && !e->no_oep ? e->d_small + 2 : nullptr);
@@ -893,7 +895,7 @@ int autotune_split(pcagb_engine *e, int K, const std::vector<uint8_t> &active,
                it would only find that out after its insert. */
             double kids = children_of(D), build = 0, states_scale = 1.0;
             double parents = (double)e->levels[D].n, held = 0;
-            const double state_bytes = 16.0 * e->TPC + e->TPC + 10;
+            const double state_bytes = 16.0 * e->TPC + e->TPC + 11;
             const double free_b = (double)(e->top - e->bottom);
             bool fits = true;
             for (int d = D + 1; d <= S; d++) {
@@ -1077,6 +1079,7 @@ int run_batch(pcagb_engine *e, std::vector<TaskRun> &runs, const pcagb_opts_t &o
         CK(e_copy(e, L0.parent, parent.data(), nt * 4, cudaMemcpyHostToDevice, e->stream));
         CK(e_copy(e, L0.cidx, cidx.data(), nt * 2, cudaMemcpyHostToDevice, e->stream));
         CK(cudaMemsetAsync(L0.rdl, 0, nt, e->stream));
+        CK(cudaMemsetAsync(L0.own, 0, nt, e->stream));
     }
     e->levels.push_back(std::move(L0));
 

@@ -82,6 +82,7 @@ struct LevelDev {
     uint64_t n;
     const uint8_t *rdl;     /* [n] register the state's last instruction wrote (0: root) */
     const uint32_t *parent; /* [n] rank of the parent in the level above */
+    const uint8_t *own;     /* [n] registers whose last write is unread and dead-able (below) */
 };
 
 struct LevelOut {
@@ -92,6 +93,7 @@ struct LevelOut {
     uint32_t *parent;
     uint16_t *cidx;
     uint8_t *rdl;
+    uint8_t *own;
 };
 
 /* ---- hashing (a multiply-rotate chain; the table compares full states, so
@@ -159,6 +161,29 @@ __device__ __forceinline__ uint64_t hash_flags(const uint32_t *f)
 __device__ __forceinline__ bool uop_reads(uint32_t u, uint32_t r)
 {
     return UOP_A(u) == r || UOP_B(u) == r;
+}
+
+/* Dead writes. In a state's path, a write to register w that no later
+   instruction has read yet, made by an instruction z that is not the first
+   kept sibling writing w (the lowest-ranked kept child of z's parent that
+   writes w), is dead-able: a child y that is not an LDI and overwrites w
+   without reading it reaches a state (registers, y's flags, live) that the
+   same path with the first sibling in z's place reaches too, by a smaller
+   ref (every instruction after z is the same candidate under the same
+   liveness mask, and none reads w). Such a child is never the DFS-first
+   representative, so the insert kernel skips it and the table's winners,
+   and every level, are unchanged. A state keeps these registers in `own`
+   (writes older than its last instruction); its last write is dead-able
+   when the state is not the first kept sibling writing it (fcr_up, the
+   first-child ranks of the level above). */
+__device__ __forceinline__ uint32_t deadable_writes(const LevelDev &P, const uint32_t *fcr_up,
+                                                    uint64_t q)
+{
+    if (!fcr_up) return 0;
+    uint32_t W = P.own[q];
+    const uint32_t w = P.rdl[q];
+    if (w && fcr_up[(uint64_t)P.parent[q] * 8 + w] != (uint32_t)q) W |= 1u << w;
+    return W;
 }
 
 /* ---- shared-memory view of one state per warp ---------------------------- */
@@ -379,25 +404,14 @@ k_expand_insert(LevelDev P, TaskDev task, unsigned long long *table, uint64_t tm
         const uint32_t k0 = c_chunk_off[m], k1 = c_chunk_off[m + 1];
         const uint32_t per = (k1 - k0 + split - 1) >> split_log2;
         const uint32_t ka = min(k1, k0 + g * per), kb = min(k1, ka + per);
-        /* Dead writes. Let q = P' + z with z writing w. A child y that is not
-           an LDI and overwrites w without reading it gives the same state
-           (registers, y's flags, live) for every kept sibling of q that also
-           wrote w, so only the first of them (fcr_up: the lowest-ranked kept
-           child of P' writing w) can hold the smallest ref, the DFS-first
-           representative; the others' such children are not inserted. The
-           table's winners, and so every level, are unchanged. */
-        uint32_t wdead = 0;
-        if (fcr_up) {
-            const uint32_t w = P.rdl[q];
-            if (w && fcr_up[(uint64_t)P.parent[q] * 8 + w] != (uint32_t)q) wdead = w;
-        }
+        const uint32_t wdead = deadable_writes(P, fcr_up, q);
         for (uint32_t k = ka; k < kb; k++) {
             const uint32_t ch = c_chunks[k], start = ch >> 8, cnt = ch & 255u;
             bool valid = (uint32_t)lane < cnt;
             const uint32_t c = start + (valid ? lane : 0);
             const uint32_t u = c_cand_uop[base + c];
             const uint32_t op = UOP_OP(u), rd = UOP_RD(u);
-            if (wdead && rd == wdead && op != PCA_OP_LDI && !uop_reads(u, wdead)) valid = false;
+            if ((wdead >> rd & 1u) && op != PCA_OP_LDI && !uop_reads(u, rd)) valid = false;
             if (!__any_sync(0xFFFFFFFFu, valid)) continue;
             uint64_t h, hf;
             __syncwarp();   /* the previous chunk's compares are done with colA */
@@ -531,7 +545,7 @@ __global__ void k_child_counts(const uint8_t *live, const uint16_t *task, const 
 template <int TPC>
 __global__ void __launch_bounds__(kThreads)
 k_materialize(LevelDev P, TaskDev task, const uint32_t *bitmap, const uint64_t *word_off,
-              LevelOut C, uint32_t split_log2, uint32_t *fcr)
+              LevelOut C, uint32_t split_log2, uint32_t *fcr, const uint32_t *fcr_up)
 {
     __shared__ WarpState<TPC> sws[kWarpsPerBlock];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -554,6 +568,7 @@ k_materialize(LevelDev P, TaskDev task, const uint32_t *bitmap, const uint64_t *
         const uint32_t m = (live >> 1) & 127u;
         const uint32_t base = c_cand_off[m], nc = c_cand_off[m + 1] - base;
         const uint64_t off = P.child_off[q];
+        const uint32_t W = deadable_writes(P, fcr_up, q);
         const uint32_t groups = (nc + 31) >> 5;
         const uint32_t per = (groups + split - 1) >> split_log2;
         const uint32_t ga = min(groups, g * per), gb = min(groups, ga + per);
@@ -577,6 +592,9 @@ k_materialize(LevelDev P, TaskDev task, const uint32_t *bitmap, const uint64_t *
                     C.task[rank] = (uint16_t)tid;
                     C.parent[rank] = (uint32_t)q;
                     C.cidx[rank] = (uint16_t)c;
+                    /* a write read by u is used; the one u overwrites is gone */
+                    C.own[rank] = (uint8_t)(W & ~((1u << UOP_A(u)) | (1u << UOP_B(u)) |
+                                                  (1u << UOP_RD(u))));
                     /* first kept child of q per written register */
                     if (fcr) atomicMin(&fcr[q * 8 + UOP_RD(u)], (uint32_t)rank);
                 }

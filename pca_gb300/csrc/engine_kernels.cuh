@@ -82,7 +82,8 @@ struct LevelDev {
     uint64_t n;
     const uint8_t *rdl;     /* [n] register the state's last instruction wrote (0: root) */
     const uint32_t *parent; /* [n] rank of the parent in the level above */
-    const uint8_t *own;     /* [n] registers whose last write is unread and dead-able (below) */
+    const uint8_t *own;     /* [n] registers whose last write is unread and dead-able (below);
+                               bit 0: the last instruction is an LDI */
 };
 
 struct LevelOut {
@@ -180,10 +181,26 @@ __device__ __forceinline__ uint32_t deadable_writes(const LevelDev &P, const uin
                                                     uint64_t q)
 {
     if (!fcr_up) return 0;
-    uint32_t W = P.own[q];
+    uint32_t W = P.own[q] & 0xFEu;
     const uint32_t w = P.rdl[q];
     if (w && fcr_up[(uint64_t)P.parent[q] * 8 + w] != (uint32_t)q) W |= 1u << w;
     return W;
+}
+
+/* LDI swaps. When a state's last instruction is an LDI (bit 0 of `own`)
+   writing register y, a child x that neither reads nor writes y reaches the
+   state of the path with x and the LDI in the other order (the LDI keeps
+   the flags, so both end with x's). That path is the smaller ref when x
+   comes first in the generator's order: every ALU op precedes every LDI,
+   and an LDI precedes another when its register is lower. Such a child is
+   never the DFS-first representative; the insert kernel skips it. */
+__device__ __forceinline__ bool ldi_swap(uint32_t u, uint32_t last_ldi_reg)
+{
+    if (!last_ldi_reg) return false;
+    const uint32_t op = UOP_OP(u), rd = UOP_RD(u);
+    if (rd == last_ldi_reg || uop_reads(u, last_ldi_reg)) return false;
+    if (op == PCA_OP_LDI) return rd < last_ldi_reg;
+    return op != PCA_OP_ADDI;
 }
 
 /* ---- shared-memory view of one state per warp ---------------------------- */
@@ -405,6 +422,7 @@ k_expand_insert(LevelDev P, TaskDev task, unsigned long long *table, uint64_t tm
         const uint32_t per = (k1 - k0 + split - 1) >> split_log2;
         const uint32_t ka = min(k1, k0 + g * per), kb = min(k1, ka + per);
         const uint32_t wdead = deadable_writes(P, fcr_up, q);
+        const uint32_t wldi = fcr_up && (P.own[q] & 1u) ? P.rdl[q] : 0u;
         for (uint32_t k = ka; k < kb; k++) {
             const uint32_t ch = c_chunks[k], start = ch >> 8, cnt = ch & 255u;
             bool valid = (uint32_t)lane < cnt;
@@ -412,6 +430,7 @@ k_expand_insert(LevelDev P, TaskDev task, unsigned long long *table, uint64_t tm
             const uint32_t u = c_cand_uop[base + c];
             const uint32_t op = UOP_OP(u), rd = UOP_RD(u);
             if ((wdead >> rd & 1u) && op != PCA_OP_LDI && !uop_reads(u, rd)) valid = false;
+            if (ldi_swap(u, wldi)) valid = false;
             if (!__any_sync(0xFFFFFFFFu, valid)) continue;
             uint64_t h, hf;
             __syncwarp();   /* the previous chunk's compares are done with colA */
@@ -593,8 +612,9 @@ k_materialize(LevelDev P, TaskDev task, const uint32_t *bitmap, const uint64_t *
                     C.parent[rank] = (uint32_t)q;
                     C.cidx[rank] = (uint16_t)c;
                     /* a write read by u is used; the one u overwrites is gone */
-                    C.own[rank] = (uint8_t)(W & ~((1u << UOP_A(u)) | (1u << UOP_B(u)) |
-                                                  (1u << UOP_RD(u))));
+                    C.own[rank] = (uint8_t)((W & ~((1u << UOP_A(u)) | (1u << UOP_B(u)) |
+                                                   (1u << UOP_RD(u))) & 0xFEu) |
+                                            (UOP_OP(u) == PCA_OP_LDI ? 1u : 0u));
                     /* first kept child of q per written register */
                     if (fcr) atomicMin(&fcr[q * 8 + UOP_RD(u)], (uint32_t)rank);
                 }

@@ -145,7 +145,8 @@ struct pcagb_engine {
     /* autotuner: unit costs measured on this engine (running averages) */
     double t_child_ms = 2.5e-7;     /* device ms per child of a level build */
     double t_build_fixed_ms = 0.3;  /* device ms of a level build's fixed part */
-    double t_eval_ms = 4.0e-9;      /* device ms per value-class evaluation */
+    double t_eval_ms[4] = {0, 4.0e-9, 4.0e-9, 4.0e-9};  /* device ms per value-class
+                                                           evaluation, per suffix depth */
     double dedup_ratio = 0.35;      /* survivors / children of the last build */
 
     /* per batch */
@@ -661,7 +662,7 @@ int run_stage(pcagb_engine *e, int S, int K, std::vector<TaskRun> &runs, bool fi
         std::vector<Group> groups;
         if (!so && on_tasks && e->ntasks > 1) {
             const int nt = e->ntasks;
-            const double per_group = 1.5 / std::max(e->t_eval_ms, 1e-12);
+            const double per_group = 1.5 / std::max(e->t_eval_ms[s], 1e-12);
             int nact = 0;
             for (int t = 0; t < nt; t++) nact += e->h_active[t] ? 1 : 0;
             if (nact > 1) {
@@ -743,7 +744,7 @@ int run_stage(pcagb_engine *e, int S, int K, std::vector<TaskRun> &runs, bool fi
         uint64_t evals = 0;
         for (size_t i = 0; i < L.hist.size(); i++) evals += L.hist[i] * g[i & 127];
         if (evals > 10000000ull)
-            e->t_eval_ms = 0.7 * e->t_eval_ms + 0.3 * (ms / (double)evals);
+            e->t_eval_ms[s] = 0.7 * e->t_eval_ms[s] + 0.3 * (ms / (double)evals);
     }
     if (nrec <= taken) return PCAGB_OK;
     return take_records(e, S, K, runs, first_only, taken, nrec, first);
@@ -878,7 +879,8 @@ int autotune_split(pcagb_engine *e, int K, const std::vector<uint8_t> &active,
     if (hi <= D) {
         const int S = std::max(hi, lo);
         if (pred_ms)
-            *pred_ms = K - S <= 3 ? evals_from(S, K - S) * e->t_eval_ms * stage_scale : 1e300;
+            *pred_ms = K - S <= 3 && K - S >= 1
+                           ? evals_from(S, K - S) * e->t_eval_ms[K - S] * stage_scale : 1e300;
         return S;
     }
     int best = -1;
@@ -887,7 +889,7 @@ int autotune_split(pcagb_engine *e, int K, const std::vector<uint8_t> &active,
         if (K - S > 3) continue;
         double ms;
         if (S <= D) {
-            ms = evals_from(S, K - S) * e->t_eval_ms * stage_scale;
+            ms = evals_from(S, K - S) * e->t_eval_ms[K - S] * stage_scale;
         } else {
             /* build D+1..S from D, then the suffix from S. A build that would
                not fit the arena (its table, bitmap and ranks, plus the new
@@ -910,7 +912,7 @@ int autotune_split(pcagb_engine *e, int K, const std::vector<uint8_t> &active,
                 kids *= e->dedup_ratio * 800.0;  /* ~children per state deeper down */
             }
             if (!fits) continue;
-            ms = build + evals_from(D, K - D) * states_scale * e->t_eval_ms * stage_scale;
+            ms = build + evals_from(D, K - D) * states_scale * e->t_eval_ms[K - S] * stage_scale;
         }
         if (ms < best_ms) { best_ms = ms; best = S; }
     }
@@ -1199,7 +1201,7 @@ int run_batch(pcagb_engine *e, std::vector<TaskRun> &runs, const pcagb_opts_t &o
                 if (active[i]) evals += (double)runs[i].res.evaluations[K];
             pcagb_level_view_t lv{LS.regs, LS.flags, LS.live, LS.task, LS.n, e->TPC, S, K, nt,
                                   e->d_task_io, e->d_task_T, (void *)e->stream,
-                                  evals * e->t_eval_ms};
+                                  evals * e->t_eval_ms[s]};
             so.order = ord->cb ? ord->cb(&lv, ord->user) : nullptr;
             if (so.order) {
                 const int vrc = validate_order(e, so.order, LS.n);

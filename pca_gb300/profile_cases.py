@@ -1,6 +1,7 @@
 """Fixed small workloads, one per kernel family, for profiling under ncu.
 
     python -m pca_gb300.profile_cases engine_depths   # k_suffix<32, 2/3>, k_leaf
+    python -m pca_gb300.profile_cases suffix_depth2   # one k_suffix<32, 2> depth-4 stage
     python -m pca_gb300.profile_cases noalloc         # k_suffix_noalloc
     python -m pca_gb300.profile_cases valuenet        # training and scoring kernels
     python -m pca_gb300.profile_cases orders          # k_check_perm
@@ -40,6 +41,20 @@ def case_engine_depths(reps: int):
             s = eng.solve(task, max_depth=depth, split_depth=split, sol_cap=1, count_levels=split == 3)
             print(f"engine_depths split={split} depth={depth}: K*={s.optimal_depth} "
                   f"{time.perf_counter() - t0:.4f} s, suffix {s.gpu_ms_suffix:.3f} ms", flush=True)
+
+
+def case_suffix_depth2(reps: int):
+    """is_power2 (32 tests) to kernel depth 4 from level 2: the depth-4 stage
+    is one k_suffix<32, 2> launch (the fourth k_suffix launch of a solve)."""
+    from .pcalib import Engine
+    from .taskgen import is_power2_task
+    eng = Engine(0, 4 << 30)
+    task = is_power2_task()
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        s = eng.solve(task, max_depth=4, split_depth=2, sol_cap=1, first_only=True)
+        print(f"suffix_depth2: K*={s.optimal_depth} {time.perf_counter() - t0:.4f} s, "
+              f"suffix {s.gpu_ms_suffix:.3f} ms", flush=True)
 
 
 def case_noalloc(reps: int):
@@ -159,7 +174,8 @@ def case_branch_saturating_add(reps: int):
     _branch_case("saturating_add", reps)
 
 
-CASES = {"engine_depths": case_engine_depths, "noalloc": case_noalloc,
+CASES = {"engine_depths": case_engine_depths, "suffix_depth2": case_suffix_depth2,
+         "noalloc": case_noalloc,
          "valuenet": case_valuenet, "orders": case_orders, "branch": case_branch,
          "branch_saturating_add": case_branch_saturating_add}
 

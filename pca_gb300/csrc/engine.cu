@@ -1313,6 +1313,19 @@ int ensure_device_tables(int device)
         CK(cudaMemcpyToSymbol(c_vcr_uop, &vu, sizeof vu));
         CK(cudaMemcpyToSymbol(c_vcr, &vr, sizeof vr));
     }
+    {
+        uint32_t *pr = nullptr;
+        uint16_t *pr_cls = nullptr;
+        CK(cudaMalloc(&pr, std::max<size_t>(gt.pr.size(), 1) * 4));
+        CK(cudaMalloc(&pr_cls, std::max<size_t>(gt.pr_cls.size(), 1) * 2));
+        CK(cudaMemcpy(pr, gt.pr.data(), gt.pr.size() * 4, cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(pr_cls, gt.pr_cls.data(), gt.pr_cls.size() * 2, cudaMemcpyHostToDevice));
+        const uint32_t *pp = pr;
+        const uint16_t *pc = pr_cls;
+        CK(cudaMemcpyToSymbol(c_pr_off, gt.pr_off.data(), gt.pr_off.size() * 4));
+        CK(cudaMemcpyToSymbol(c_pr, &pp, sizeof pp));
+        CK(cudaMemcpyToSymbol(c_pr_cls, &pc, sizeof pc));
+    }
     CK(cudaMalloc(&cand_uop, gt.cand_uop.size() * 4));
     CK(cudaMalloc(&vc_uop, gt.vc_uop.size() * 4));
     CK(cudaMalloc(&vc_first, first.size() * 2));

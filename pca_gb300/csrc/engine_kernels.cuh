@@ -62,6 +62,9 @@ __constant__ const uint32_t *c_chunks;
 __constant__ uint32_t c_vcr_off[128 * 8 + 1]; /* [mask*8 + r]: classes reading r */
 __constant__ const uint32_t *c_vcr_uop;    /* their micro-ops */
 __constant__ const uint16_t *c_vcr;        /* their indices in the mask's class list */
+__constant__ uint32_t c_pr_off[128 * 8 + 1];  /* [mask*8 + r]: the same, by operand pair */
+__constant__ const uint32_t *c_pr;         /* a | b << 3 | opmask << 6 | imm << 16 */
+__constant__ const uint16_t *c_pr_cls;     /* [entry][10] class index per opmask bit */
 
 /* Per-task parameters of a batch: device arrays indexed by task id. A
    state's task id travels with it through the levels; states of different
@@ -729,6 +732,42 @@ __global__ void k_leaf(LevelDev P, TaskDev task, SolBuf S)
     }
 }
 
+/* Which of the ops of an operand-pair entry give t from (x, y): bit k < 9
+   for the ALU op kPairOps[k], bit 9 for x + e (an ADDI, e its immediate
+   sign-extended to 16 bits). Every op is evaluated, with no branch. */
+__device__ __forceinline__ uint32_t pair_hits(uint32_t x, uint32_t y, uint32_t e, uint32_t t)
+{
+    const uint32_t s = y & 15u;
+    uint32_t h = 0;
+    h |= (uint32_t)(((x + y) & 0xFFFFu) == t);
+    h |= (uint32_t)(((x - y) & 0xFFFFu) == t) << 1;
+    h |= (uint32_t)(((x * y) & 0xFFFFu) == t) << 2;
+    h |= (uint32_t)((x & y) == t) << 3;
+    h |= (uint32_t)((x | y) == t) << 4;
+    h |= (uint32_t)((x ^ y) == t) << 5;
+    h |= (uint32_t)(((x << s) & 0xFFFFu) == t) << 6;
+    h |= (uint32_t)((x >> s) == t) << 7;
+    h |= (uint32_t)((uint32_t)(uint16_t)((int16_t)(uint16_t)x >> s) == t) << 8;
+    h |= (uint32_t)(((x + e) & 0xFFFFu) == t) << 9;
+    return h;
+}
+
+__device__ __forceinline__ uint32_t pair_op(uint32_t k)
+{
+    switch (k) {
+    case 0: return PCA_OP_ADD;
+    case 1: return PCA_OP_SUB;
+    case 2: return PCA_OP_MUL;
+    case 3: return PCA_OP_AND;
+    case 4: return PCA_OP_OR;
+    case 5: return PCA_OP_XOR;
+    case 6: return PCA_OP_SHL;
+    case 7: return PCA_OP_SHR;
+    case 8: return PCA_OP_ASR;
+    default: return PCA_OP_ADDI;
+    }
+}
+
 /* Scan the value classes of mask m against the warp's state, with operand
  * registers remapped: a register equal to rd2 reads spare column 9, else a
  * register equal to rd1 reads column 8 (rd = 8 means "none").
@@ -749,18 +788,52 @@ __device__ __forceinline__ void scan_last(const WarpState<TPC> &ws, int T,
                                           uint32_t need1, uint32_t need2)
 {
     const uint32_t vbase = c_vc_off[m];
-    const uint32_t *uops;
-    const uint16_t *list = nullptr;
-    uint32_t nvc;
     if (need1) {
-        const uint32_t l0 = c_vcr_off[m * 8 + need1];
-        uops = c_vcr_uop + l0;
-        list = c_vcr + l0;
-        nvc = c_vcr_off[m * 8 + need1 + 1] - l0;
-    } else {
-        uops = c_vc_uop + vbase;
-        nvc = c_vc_off[m + 1] - vbase;
+        /* the classes reading need1, one operand pair (or ADDI) per lane,
+           every op of the pair evaluated on the first two tests at once */
+        const uint32_t p0 = c_pr_off[m * 8 + need1], np = c_pr_off[m * 8 + need1 + 1] - p0;
+        for (uint32_t b0 = 0; b0 < np; b0 += 32) {
+            const uint32_t i = b0 + lane;
+            uint32_t hits = 0, ra = 0, rb = 0, e = 0;
+            if (i < np) {
+                const uint32_t d = c_pr[p0 + i];
+                const uint32_t a = d & 7u, b = (d >> 3) & 7u;
+                if (!need2 || a == need2 || b == need2) {
+                    ra = a == rd2 ? 9u : a == rd1 ? 8u : a;
+                    rb = b == rd2 ? 9u : b == rd1 ? 8u : b;
+                    e = (uint32_t)(uint16_t)(int16_t)(int8_t)(uint8_t)(d >> 16);
+                    hits = pair_hits(ws.R[ra][0], ws.R[rb][0], e, tgt0) & (d >> 6) & 0x3FFu;
+                    if (T >= 2 && hits) hits &= pair_hits(ws.R[ra][1], ws.R[rb][1], e, tgt1);
+                }
+            }
+            uint32_t bal = __ballot_sync(0xFFFFFFFFu, hits != 0);
+            while (bal) {
+                const int j = __ffs(bal) - 1;
+                bal &= bal - 1;
+                uint32_t hj = __shfl_sync(0xFFFFFFFFu, hits, j);
+                const uint32_t aj = __shfl_sync(0xFFFFFFFFu, ra, j);
+                const uint32_t bj = __shfl_sync(0xFFFFFFFFu, rb, j);
+                const uint32_t ej = __shfl_sync(0xFFFFFFFFu, e, j);
+                while (hj) {
+                    const uint32_t k = (uint32_t)(__ffs(hj) - 1);
+                    hj &= hj - 1;
+                    bool ok = true;
+                    if (lane < T) {
+                        const uint32_t x = ws.R[aj][lane], y = ws.R[bj][lane];
+                        ok = (k == 9 ? ((x + ej) & 0xFFFFu) : pca_alu(pair_op(k), x, y, 0)) == tgt;
+                    }
+                    if (__all_sync(0xFFFFFFFFu, ok) && lane == 0) {
+                        const uint32_t cj = c_pr_cls[(uint64_t)(p0 + b0 + j) * 10 + k];
+                        record_solution(S, q, m1, m2, cj, c_vc_first[vbase + cj]);
+                    }
+                }
+            }
+        }
+        return;
     }
+    const uint32_t *uops = c_vc_uop + vbase;
+    const uint16_t *list = nullptr;
+    const uint32_t nvc = c_vc_off[m + 1] - vbase;
     for (uint32_t b0 = 0; b0 < nvc; b0 += 32) {
         const uint32_t i = b0 + lane;
         uint32_t u = 0;

@@ -24,6 +24,8 @@
 #include <stdint.h>
 #include <vector>
 
+#include "pca_isa.h"
+
 namespace pcagb {
 
 struct GenTables {
@@ -50,12 +52,24 @@ struct GenTables {
        indices (within the mask's list) vcr[vcr_off[m*8+r] .. vcr_off[m*8+r+1]) */
     std::vector<uint32_t> vcr_off;     /* size 128*8+1 */
     std::vector<uint16_t> vcr;
+    /* The same classes grouped by operand pair, for evaluating every op of
+       a pair at once: entry = a | b << 3 | opmask << 6 | imm << 16, where
+       opmask bit k < 9 is the ALU op kPairOps[k] on (a, b) and bit 9 an ADDI
+       on register a with immediate imm (an ADDI class per entry).
+       pr_cls[entry * 10 + k] = that class's index in the mask's list. */
+    std::vector<uint32_t> pr_off;      /* size 128*8+1 */
+    std::vector<uint32_t> pr;
+    std::vector<uint16_t> pr_cls;
     int max_nc = 0;
     int max_nvc = 0;
 
     int nc(int mask) const { return (int)(cand_off[mask + 1] - cand_off[mask]); }
     int nvc(int mask) const { return (int)(vc_off[mask + 1] - vc_off[mask]); }
 };
+
+/* The ALU ops of an operand-pair entry, by opmask bit. */
+static const uint32_t kPairOps[9] = {PCA_OP_ADD, PCA_OP_SUB, PCA_OP_MUL, PCA_OP_AND, PCA_OP_OR,
+                                     PCA_OP_XOR, PCA_OP_SHL, PCA_OP_SHR, PCA_OP_ASR};
 
 /* Built once (thread-safe, immutable afterwards). */
 const GenTables &gen_tables();

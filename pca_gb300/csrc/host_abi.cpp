@@ -128,6 +128,39 @@ static GenTables build_tables()
             }
         }
     t.vcr_off[128 * 8] = (uint32_t)t.vcr.size();
+    t.pr_off.assign(128 * 8 + 1, 0);
+    for (int m = 0; m < 128; m++)
+        for (uint32_t r = 0; r < 8; r++) {
+            t.pr_off[m * 8 + r] = (uint32_t)t.pr.size();
+            if (r == 0) continue;
+            const size_t first = t.pr.size();
+            for (uint32_t i = t.vc_off[m]; i < t.vc_off[m + 1]; i++) {
+                const uint32_t u = t.vc_uop[i], op = UOP_OP(u);
+                const uint32_t a = UOP_A(u), b = UOP_B(u);
+                if (a != r && b != r) continue;
+                const uint16_t ci = (uint16_t)(i - t.vc_off[m]);
+                if (op == PCA_OP_ADDI) {
+                    t.pr.push_back(a | (1u << 15) | (UOP_IMM(u) << 16));
+                    t.pr_cls.insert(t.pr_cls.end(), 10, 0xFFFF);
+                    t.pr_cls.back() = ci;
+                    continue;
+                }
+                int k = 0;
+                while (k < 9 && kPairOps[k] != op) k++;
+                if (k == 9) continue;  /* LDI reads no register */
+                size_t e = first;
+                while (e < t.pr.size() &&
+                       ((t.pr[e] & 63u) != (a | (b << 3)) || (t.pr[e] >> 15 & 1u)))
+                    e++;
+                if (e == t.pr.size()) {
+                    t.pr.push_back(a | (b << 3));
+                    t.pr_cls.insert(t.pr_cls.end(), 10, 0xFFFF);
+                }
+                t.pr[e] |= 1u << (6 + k);
+                t.pr_cls[e * 10 + k] = ci;
+            }
+        }
+    t.pr_off[128 * 8] = (uint32_t)t.pr.size();
     for (int s = 0; s < 5; s++) t.ev[s].assign(128, 0);
     for (int m = 0; m < 128; m++) t.ev[1][m] = t.vc_off[m + 1] - t.vc_off[m];
     for (int s = 2; s < 5; s++)

@@ -507,9 +507,9 @@ def main():
     # Achieved = this run's value-class evaluations of the full candidate
     # space per second of suffix-kernel time x the kernel's warp instructions
     # per such evaluation, measured by ncu (profiles/k_suffix_is_power2_t32_k4.md:
-    # 1.50e9 instructions for the depth-4 launch, whose full space is 7.30e8
+    # 1.26e9 instructions for the depth-4 launch, whose full space is 7.30e8
     # evaluations; the kernel scans only the classes that can solve).
-    inst_per_eval = 1496436129 / 7.30e8
+    inst_per_eval = 1255101666 / 7.30e8
     peak_issue = sms * 4 * sm_max * 1e6
     achieved_issue = suffix_evals_per_s * inst_per_eval
     line["roofline"] = {
@@ -517,7 +517,7 @@ def main():
         "bound": "int_issue", "unit": "Gwarp-inst/s",
         "achieved": achieved_issue / 1e9, "peak": peak_issue / 1e9,
         "frac": achieved_issue / peak_issue,
-        "traffic": 2735593000 + 3713024,
+        "traffic": 2735377000 + 3757056,
         "evaluations_per_s": suffix_evals_per_s,
         "peak_source": f"{sms} SMs x 4 issue slots x sm_max_mhz from MEASURED_PEAKS.json ({pk_kind})",
         "ncu": "profiles/k_suffix_is_power2_t32_k4.md",

@@ -1330,7 +1330,14 @@ int ensure_device_tables(int device)
     CK(cudaMalloc(&vc_uop, gt.vc_uop.size() * 4));
     CK(cudaMalloc(&vc_first, first.size() * 2));
     CK(cudaMalloc(&chunks, gt.chunks.size() * 4));
-    CK(cudaMemcpy(cand_uop, gt.cand_uop.data(), gt.cand_uop.size() * 4, cudaMemcpyHostToDevice));
+    {
+        /* bit 31 of a device micro-op marks a candidate whose child is an
+           earlier sibling's state (cand_dupe); the field macros ignore it */
+        std::vector<uint32_t> cu_flagged(gt.cand_uop);
+        for (size_t i = 0; i < cu_flagged.size(); i++)
+            if (gt.cand_dupe[i]) cu_flagged[i] |= 1u << 31;
+        CK(cudaMemcpy(cand_uop, cu_flagged.data(), cu_flagged.size() * 4, cudaMemcpyHostToDevice));
+    }
     CK(cudaMemcpy(vc_uop, gt.vc_uop.data(), gt.vc_uop.size() * 4, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(vc_first, first.data(), first.size() * 2, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(chunks, gt.chunks.data(), gt.chunks.size() * 4, cudaMemcpyHostToDevice));

@@ -54,7 +54,7 @@ constexpr uint32_t kStatusRefOverflow = 2u;
 /* Candidate tables, uploaded once per device. */
 __constant__ uint32_t c_cand_off[129];
 __constant__ uint32_t c_vc_off[129];
-__constant__ const uint32_t *c_cand_uop;
+__constant__ const uint32_t *c_cand_uop;   /* bit 31: a same-state duplicate of an earlier candidate */
 __constant__ const uint32_t *c_vc_uop;
 __constant__ const uint16_t *c_vc_first;   /* first candidate index per class */
 __constant__ uint32_t c_chunk_off[129];    /* op-uniform runs of candidates */
@@ -434,6 +434,7 @@ k_expand_insert(LevelDev P, TaskDev task, unsigned long long *table, uint64_t tm
             const uint32_t op = UOP_OP(u), rd = UOP_RD(u);
             if ((wdead >> rd & 1u) && op != PCA_OP_LDI && !uop_reads(u, rd)) valid = false;
             if (ldi_swap(u, wldi)) valid = false;
+            if (u >> 31) valid = false;   /* an earlier sibling's state (same value and flags) */
             if (!__any_sync(0xFFFFFFFFu, valid)) continue;
             uint64_t h, hf;
             __syncwarp();   /* the previous chunk's compares are done with colA */

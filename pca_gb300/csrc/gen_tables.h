@@ -57,6 +57,11 @@ struct GenTables {
        opmask bit k < 9 is the ALU op kPairOps[k] on (a, b) and bit 9 an ADDI
        on register a with immediate imm (an ADDI class per entry).
        pr_cls[entry * 10 + k] = that class's index in the mask's list. */
+    /* cand_dupe[i]: candidate i writes the same value and flags as an
+       earlier candidate of its mask on every state (copies of one register
+       with its Z/N flags, zero with Z, zero with Z and C); a child by it is
+       that sibling's state and never its representative */
+    std::vector<uint8_t> cand_dupe;
     std::vector<uint32_t> pr_off;      /* size 128*8+1 */
     std::vector<uint32_t> pr;
     std::vector<uint16_t> pr_cls;

@@ -10,6 +10,7 @@
 #include "gen_tables.h"
 #include "pca_isa.h"
 
+#include <algorithm>
 #include <cctype>
 #include <cstdio>
 #include <cstdlib>
@@ -128,6 +129,33 @@ static GenTables build_tables()
             }
         }
     t.vcr_off[128 * 8] = (uint32_t)t.vcr.size();
+    /* same-value-and-flags families among one mask's candidates:
+       copy of x (ADD rd,r0,x; AND rd,x,x; OR rd,r0,x; OR rd,x,x; XOR rd,r0,x:
+       value x, flags Z/N of x), zero with Z (AND rd,r0,x; XOR rd,x,x;
+       SHL/SHR/ASR rd,r0,x) and zero with Z and C (SUB rd,x,x), x >= 1 */
+    t.cand_dupe.assign(t.cand_uop.size(), 0);
+    for (int m = 0; m < 128; m++) {
+        std::vector<uint32_t> seen;
+        for (uint32_t i = t.cand_off[m]; i < t.cand_off[m + 1]; i++) {
+            const uint32_t u = t.cand_uop[i], op = UOP_OP(u), rd = UOP_RD(u);
+            const uint32_t a = UOP_A(u), b = UOP_B(u);
+            uint32_t key = 0;
+            if ((op == PCA_OP_ADD || op == PCA_OP_OR || op == PCA_OP_XOR) && a == 0 && b >= 1)
+                key = 1u << 16 | rd << 8 | b;                       /* copy of b */
+            else if ((op == PCA_OP_AND || op == PCA_OP_OR) && a == b && a >= 1)
+                key = 1u << 16 | rd << 8 | a;                       /* copy of a */
+            else if ((op == PCA_OP_AND || op == PCA_OP_SHL || op == PCA_OP_SHR ||
+                      op == PCA_OP_ASR) && a == 0 && b >= 1)
+                key = 2u << 16 | rd << 8;                           /* zero, Z */
+            else if (op == PCA_OP_XOR && a == b && a >= 1)
+                key = 2u << 16 | rd << 8;                           /* zero, Z */
+            else if (op == PCA_OP_SUB && a == b && a >= 1)
+                key = 3u << 16 | rd << 8;                           /* zero, Z and C */
+            if (!key) continue;
+            if (std::find(seen.begin(), seen.end(), key) != seen.end()) t.cand_dupe[i] = 1;
+            else seen.push_back(key);
+        }
+    }
     t.pr_off.assign(128 * 8 + 1, 0);
     for (int m = 0; m < 128; m++)
         for (uint32_t r = 0; r < 8; r++) {

@@ -143,9 +143,11 @@ struct pcagb_engine {
     uint64_t insert_launches = 0, suffix_launches = 0, insert_children = 0;
     float ms_insert = 0;
     /* autotuner: unit costs measured on this engine (running averages) */
-    double t_child_ms = 2.5e-7;     /* device ms per child of a level build */
-    double t_build_fixed_ms = 0.3;  /* device ms of a level build's fixed part */
-    double t_eval_ms[4] = {0, 4.0e-9, 4.0e-9, 4.0e-9};  /* device ms per value-class
+    /* starting values: this engine's costs measured on a GB300 (one- and
+       two-input depth-4 searches); every solve refines them */
+    double t_child_ms = 1.8e-7;     /* device ms per child of a level build */
+    double t_build_fixed_ms = 0.08; /* device ms of a level build's fixed part */
+    double t_eval_ms[4] = {0, 1.8e-9, 1.4e-9, 1.3e-9};  /* device ms per value-class
                                                            evaluation, per suffix depth */
     double dedup_ratio = 0.35;      /* survivors / children of the last build */
 
@@ -177,6 +179,39 @@ struct pcagb_engine {
 };
 
 namespace {
+
+/* Unit costs the engines of one device have measured (the autotuner's
+   model), shared so that a new engine, e.g. a server's slot, starts from
+   what earlier engines measured on the same GPU instead of the defaults. */
+struct CostModel {
+    bool set = false;
+    double t_child_ms = 0, t_build_fixed_ms = 0, t_eval_ms[4] = {0, 0, 0, 0}, dedup_ratio = 0;
+};
+std::mutex g_cost_mu;
+CostModel g_cost[64];
+
+void load_costs(pcagb_engine *e)
+{
+    std::lock_guard<std::mutex> lk(g_cost_mu);
+    if (e->device < 0 || e->device >= 64 || !g_cost[e->device].set) return;
+    const CostModel &c = g_cost[e->device];
+    e->t_child_ms = c.t_child_ms;
+    e->t_build_fixed_ms = c.t_build_fixed_ms;
+    for (int i = 0; i < 4; i++) e->t_eval_ms[i] = c.t_eval_ms[i];
+    e->dedup_ratio = c.dedup_ratio;
+}
+
+void store_costs(const pcagb_engine *e)
+{
+    std::lock_guard<std::mutex> lk(g_cost_mu);
+    if (e->device < 0 || e->device >= 64) return;
+    CostModel &c = g_cost[e->device];
+    c.t_child_ms = e->t_child_ms;
+    c.t_build_fixed_ms = e->t_build_fixed_ms;
+    for (int i = 0; i < 4; i++) c.t_eval_ms[i] = e->t_eval_ms[i];
+    c.dedup_ratio = e->dedup_ratio;
+    c.set = true;
+}
 
 /* every host<->device copy of a solve goes through here and is counted */
 cudaError_t e_copy(pcagb_engine *e, void *dst, const void *src, size_t n, cudaMemcpyKind kind,
@@ -1271,6 +1306,7 @@ int run_batch(pcagb_engine *e, std::vector<TaskRun> &runs, const pcagb_opts_t &o
         tr.res.seconds = tr.t_done;
     }
     for (int i = 0; i < nt; i++) notify(i);
+    store_costs(e);
     return PCAGB_OK;
 }
 
@@ -1359,6 +1395,7 @@ int engine_init(pcagb_engine *e, int device, size_t budget)
 {
     CK(cudaSetDevice(device));
     e->device = device;
+    load_costs(e);
     CK(cudaDeviceGetAttribute(&e->sms, cudaDevAttrMultiProcessorCount, device));
     CK(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
     CK(cudaEventCreate(&e->ev0));

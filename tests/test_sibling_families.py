@@ -78,3 +78,81 @@ def test_family_members_reach_the_first_members_state():
                     assert got.live == ref.live
                     checked += 1
     assert checked > 1000
+
+
+LDI, ADDI = 0x10, 0x12
+
+
+def reads(w, r):
+    op, rd, a, b = fields(w)
+    if op == LDI:
+        return False
+    if op == ADDI:
+        return rd == r
+    return a == r or b == r
+
+
+def random_state(live, T, rng):
+    s = SearchState()
+    s.live = live
+    for t in range(T):
+        for r in range(1, 8):
+            s.regs[t][r] = rng.getrandbits(16) if (live >> r) & 1 else 0
+        s.flags[t] = rng.getrandbits(4)
+    return s
+
+
+def same(a, b, T):
+    return all(list(a.regs[t]) == list(b.regs[t]) and a.flags[t] == b.flags[t] for t in range(T)) \
+        and a.live == b.live
+
+
+def test_ldi_swap_and_dead_write_reach_the_same_state():
+    """The insert kernel's two ordering rules, on the host: an LDI of
+    register y and an instruction x that neither reads nor writes y give the
+    same state in either order; two writes z, z' of register w followed by an
+    instruction that is not an LDI and overwrites w without reading it give
+    the same state."""
+    lib = PCALib()
+    from pca_gb300.taskgen import synthetic_task
+    task = synthetic_task(3, 2)[0]
+    ctx = lib.init_ctx(task)
+    T = task.num_tests
+    rng = random.Random(9)
+    swaps = dead = 0
+    for mask in range(0, 128, 3):
+        live = (mask << 1) | 2
+        cands = lib.gen_candidates(random_state(live, T, rng))
+        ldis = [w for w in cands if fields(w)[0] == LDI]
+        others = [w for w in cands if fields(w)[0] != LDI]
+        for _ in range(40):
+            src = random_state(live, T, rng)
+            y = rng.choice(ldis)
+            ry = fields(y)[1]
+            x = rng.choice(others)
+            if fields(x)[1] == ry or reads(x, ry) or fields(x)[0] == ADDI:
+                continue
+            a = lib.step(ctx, lib.step(ctx, src, y), x)
+            b = lib.step(ctx, lib.step(ctx, src, x), y)
+            if a is None or b is None:
+                continue
+            assert same(a, b, T), (hex(y), hex(x))
+            swaps += 1
+        for _ in range(40):
+            src = random_state(live, T, rng)
+            z1, z2 = rng.choice(cands), rng.choice(cands)
+            w = fields(z1)[1]
+            if fields(z2)[1] != w:
+                continue
+            s1, s2 = lib.step(ctx, src, z1), lib.step(ctx, src, z2)
+            if s1 is None or s2 is None:
+                continue
+            follow = [u for u in lib.gen_candidates(s1)
+                      if fields(u)[1] == w and fields(u)[0] != LDI and not reads(u, w)]
+            if not follow:
+                continue
+            u = rng.choice(follow)
+            a, b = lib.step(ctx, s1, u), lib.step(ctx, s2, u)
+            assert a is not None and b is not None and same(a, b, T), (hex(z1), hex(z2), hex(u))
+            dead += 1
+    assert swaps > 200 and dead > 200

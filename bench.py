@@ -358,6 +358,10 @@ def run_guided(args):
                        "params": net.n_params(), "epochs": 10},
             "label_seconds": t_label, "train_seconds": t_train, "train_loss": losses,
             "orders": summ, "value_scoring_ms_per_task": vo.score_ms / max(len(sel), 1)}
+    for _, fn in orders:
+        if isinstance(fn, ValueOrder):
+            fn.close()
+    torch.cuda.synchronize()
     print(json.dumps(line), flush=True)
 
 

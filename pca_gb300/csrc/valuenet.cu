@@ -23,6 +23,8 @@
  */
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
+
+#include <algorithm>
 #include <stdint.h>
 
 #include <cmath>
@@ -354,7 +356,76 @@ int launch_ok()
 
 }  // namespace
 
+/* Where a sampled ranking reads its states: kept in device memory so that
+ * a captured CUDA graph of the ranking replays on any level. Sample i is
+ * state (a * i + b) mod n, with a coprime to n: the map is a bijection of
+ * 0..n-1, so the sample and the rest of the order partition the level. */
+struct SampleSrc {
+    const uint16_t *regs;
+    const uint8_t *flags;
+    const uint8_t *live;
+    const uint16_t *task;
+    unsigned long long n, a, b;
+    unsigned int depth, pad;
+};
+
+__device__ __forceinline__ unsigned long long sample_pos(const SampleSrc &S, unsigned long long i)
+{
+    return (S.a * i + S.b) % S.n;
+}
+
+/* Copy sample i's state (registers, flags, live, task) into row i. */
+__global__ void k_gather_sample(const SampleSrc *src, uint16_t *regs, uint8_t *flags, uint8_t *live,
+                                uint16_t *task, uint8_t *depth, int m, int TP)
+{
+    const SampleSrc S = *src;
+    if (S.n == 0) return;   /* no level: nothing to read (and no modulus) */
+    for (int i = blockIdx.x; i < m; i += gridDim.x) {
+        const unsigned long long p = sample_pos(S, (unsigned long long)i);
+        for (int k = threadIdx.x; k < 8 * TP; k += blockDim.x)
+            regs[(size_t)i * 8 * TP + k] = S.regs[p * 8 * TP + k];
+        for (int k = threadIdx.x; k < TP; k += blockDim.x)
+            flags[(size_t)i * TP + k] = S.flags[p * TP + k];
+        if (threadIdx.x == 0) {
+            live[i] = S.live[p];
+            task[i] = S.task[p];
+            depth[i] = (uint8_t)S.depth;
+        }
+    }
+}
+
+/* The order: the sample by rank (ranked[i] = sample index), then every
+   other state in sample-map order. */
+__global__ void k_compose_order(const SampleSrc *src, const long long *ranked, int m,
+                                uint32_t *order)
+{
+    const SampleSrc S = *src;
+    if (S.n == 0) return;
+    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < S.n;
+         i += (unsigned long long)gridDim.x * blockDim.x)
+        order[i] = (uint32_t)sample_pos(S, i < (unsigned long long)m ? (unsigned long long)ranked[i] : i);
+}
+
 extern "C" {
+
+int pcagb_vnet_gather_sample(const void *src, uint16_t *regs, uint8_t *flags, uint8_t *live,
+                             uint16_t *task, uint8_t *depth, int m, int TP, void *stream)
+{
+    if (m <= 0) return PCAGB_OK;
+    k_gather_sample<<<std::min(m, 4096), 128, 0, (cudaStream_t)stream>>>(
+        (const SampleSrc *)src, regs, flags, live, task, depth, m, TP);
+    return launch_ok();
+}
+
+int pcagb_vnet_compose_order(const void *src, const long long *ranked, int m, uint32_t *order,
+                             unsigned long long n, void *stream)
+{
+    if (n == 0) return PCAGB_OK;
+    const unsigned blocks = (unsigned)std::min<unsigned long long>((n + 255) / 256, 4096);
+    k_compose_order<<<blocks, 256, 0, (cudaStream_t)stream>>>((const SampleSrc *)src, ranked, m,
+                                                             order);
+    return launch_ok();
+}
 
 int pcagb_vnet_gemm_nt(const void *A, const void *B, const float *bias, void *C_bf16,
                        float *C_f32, int M, int N, int K, int lda, int ldb, int ldc, int relu,

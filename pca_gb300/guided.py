@@ -21,8 +21,11 @@ fallback and the judge.
 """
 from __future__ import annotations
 
+import atexit
 import ctypes
+import math
 import random
+import weakref
 
 import numpy as np
 import torch
@@ -172,12 +175,17 @@ class ValueOrder:
     and stages the engine expects to finish in less than `gain` x the
     scoring time (fixed_ms + scored states / states_per_ms).
 
-    With `sample` set, a level larger than it is scored on a uniform random
-    sample of that many prefixes: the order is the sample by decreasing
-    score, then every other prefix in random order. The first correct
-    program usually sits in the first few percent of a good order, so the
-    ranked sample decides the first launches at a fraction of the scoring
-    cost; the order stays a permutation of the whole level."""
+    With `sample` set, a level larger than it is scored on a sample of that
+    many prefixes spread over it (prefix (a * i + b) mod n for sample i, a
+    coprime to n, a and b drawn per level): the order is the sample by
+    decreasing score, then every other prefix in the same map's order (a
+    permutation of the whole level). The first correct program usually sits
+    in the first few percent of a good order, so the ranked sample decides
+    the first launches at a fraction of the scoring cost. The ranking (the
+    gather of the sample, the fused encoder, the trunk and the sort) is a
+    CUDA graph captured once per test width and task table and replayed on
+    the engine's stream; the level's addresses reach it through a small
+    device buffer, so one replay and one order kernel serve any level."""
 
     def __init__(self, net: ValueNet, chunk_states=1 << 20, min_states=4096, gain=2.0,
                  fixed_ms=0.25, states_per_ms=1.0e5, sample=None, seed=0):
@@ -186,9 +194,20 @@ class ValueOrder:
         self.min_states = min_states
         self.gain, self.fixed_ms, self.states_per_ms = gain, fixed_ms, states_per_ms
         self.sample = sample
-        self.gen = torch.Generator(device=net.dev).manual_seed(seed)
+        self.rng = random.Random(seed)
         self.score_ms = 0.0
         self._cache = {}
+        self._graphs = {}
+        _LIVE_ORDERS.add(self)
+
+    def close(self):
+        """Release the captured ranking graphs and their buffers (also done
+        for every live ValueOrder when the interpreter exits, while the CUDA
+        context still exists)."""
+        self._cache = {}
+        for G in self._graphs.values():
+            G.pop("graph", None)
+        self._graphs = {}
 
     def __call__(self, view):
         n = view.n
@@ -211,10 +230,12 @@ class ValueOrder:
             task_io = _device_view(view.task_io, ntask * 3 * 32, torch.int16, dev)
             task_T = _device_view(view.task_T, ntask, torch.int32, dev)
             if scored < n:
-                order = self._sampled_order(view, n, scored, tp, task_io, task_T, dev)
+                status, order = self._sampled_order(view, n, scored, tp, task_io, task_T, dev,
+                                                    stream)
                 ev1.record(stream)
                 ev1.synchronize()
-                self.net.check_status()
+                if int(status.item()):
+                    raise RuntimeError("fused encoder aborted (barrier wait timed out)")
                 self.score_ms += ev0.elapsed_time(ev1)
                 self._cache = {key: order}
                 return order
@@ -237,20 +258,91 @@ class ValueOrder:
         return order
 
 
-    def _sampled_order(self, view, n, m, tp, task_io, task_T, dev):
-        perm = torch.randperm(n, device=dev, generator=self.gen)
-        head = perm[:m]
-        regs = _device_view(view.regs, n * 8 * tp, torch.int16, dev).view(n, 8 * tp)
-        flags = _device_view(view.flags, n * tp, torch.uint8, dev).view(n, tp)
-        live = _device_view(view.live, n, torch.uint8, dev)
-        task = _device_view(view.task, n, torch.int16, dev)
-        depth = torch.full((m,), view.depth, device=dev, dtype=torch.uint8)
-        scores = self.net.forward_fused(regs.index_select(0, head).reshape(-1),
-                                        flags.index_select(0, head).reshape(-1),
-                                        live.index_select(0, head), task.index_select(0, head),
-                                        depth, tp, task_io, task_T)[:, 0]
-        ranked = head[torch.argsort(scores, descending=True, stable=True)]
-        return torch.cat([ranked, perm[m:]]).to(torch.int32)
+    def _ranking_graph(self, m, tp, task_io, task_T, dev):
+        """The sampled ranking captured as a CUDA graph for m samples of
+        width tp against one task table."""
+        gkey = (m, tp, task_io.data_ptr(), task_T.data_ptr())
+        if gkey in self._graphs:
+            return self._graphs[gkey]
+        lib = self.net.lib
+        G = {"src": torch.zeros(8, device=dev, dtype=torch.int64),
+             "src_host": torch.zeros(8, dtype=torch.int64),
+             "regs": torch.zeros(m * 8 * tp, device=dev, dtype=torch.int16),
+             "flags": torch.zeros(m * tp, device=dev, dtype=torch.uint8),
+             "live": torch.zeros(m, device=dev, dtype=torch.uint8),
+             "task": torch.zeros(m, device=dev, dtype=torch.int16),
+             "depth": torch.zeros(m, device=dev, dtype=torch.uint8)}
+
+        def body():
+            st = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+            rc = lib.pcagb_vnet_gather_sample(
+                ctypes.c_void_p(G["src"].data_ptr()), ctypes.c_void_p(G["regs"].data_ptr()),
+                ctypes.c_void_p(G["flags"].data_ptr()), ctypes.c_void_p(G["live"].data_ptr()),
+                ctypes.c_void_p(G["task"].data_ptr()), ctypes.c_void_p(G["depth"].data_ptr()),
+                m, tp, st)
+            if rc != 0:
+                raise RuntimeError(f"sample gather failed ({rc})")
+            n_before = len(self.net._status)
+            logits = self.net.forward_fused(G["regs"], G["flags"], G["live"], G["task"], G["depth"],
+                                            tp, task_io, task_T)
+            G["status"] = self.net._status.pop()
+            assert len(self.net._status) == n_before
+            G["ranked"] = torch.argsort(logits[:, 0], descending=True, stable=True)
+
+        # the warm-up and capture runs read the sample buffers themselves, a
+        # valid level of m states (sample i = state i)
+        G["src"].copy_(torch.tensor([G["regs"].data_ptr(), G["flags"].data_ptr(),
+                                     G["live"].data_ptr(), G["task"].data_ptr(), m, 1, 0, 0],
+                                    dtype=torch.int64))
+        side = torch.cuda.Stream(device=dev)
+        side.wait_stream(torch.cuda.current_stream(dev))
+        with torch.cuda.stream(side):
+            body()   # allocations and lazy initialisation outside the capture
+        torch.cuda.current_stream(dev).wait_stream(side)
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph, stream=side):
+            body()
+        G["graph"] = graph
+        self._graphs[gkey] = G
+        return G
+
+    def _sampled_order(self, view, n, m, tp, task_io, task_T, dev, stream):
+        G = self._ranking_graph(m, tp, task_io, task_T, dev)
+        a = 0
+        for p in _MAP_PRIMES[self.rng.randrange(len(_MAP_PRIMES)):] + _MAP_PRIMES:
+            if math.gcd(p % n, n) == 1:
+                a = p % n
+                break
+        G["src_host"].numpy()[:] = (view.regs, view.flags, view.live, view.task, n, a,
+                                    self.rng.randrange(n), view.depth)
+        G["src"].copy_(G["src_host"])   # 64 bytes, ordered on the engine's stream
+        G["graph"].replay()
+        order = torch.empty(n, device=dev, dtype=torch.int32)
+        rc = self.net.lib.pcagb_vnet_compose_order(
+            ctypes.c_void_p(G["src"].data_ptr()), ctypes.c_void_p(G["ranked"].data_ptr()), m,
+            ctypes.c_void_p(order.data_ptr()), n, ctypes.c_void_p(stream.cuda_stream))
+        if rc != 0:
+            raise RuntimeError(f"order composition failed ({rc})")
+        return G["status"], order
+
+
+# Graph memory freed after the CUDA context is gone aborts the process, so
+# the graphs of every live ValueOrder are released at interpreter exit.
+_LIVE_ORDERS = weakref.WeakSet()
+
+
+@atexit.register
+def _release_graphs():
+    for vo in list(_LIVE_ORDERS):
+        vo.close()
+    if torch.cuda.is_initialized():
+        torch.cuda.synchronize()
+
+
+# multipliers of the sample map: primes, so a level size shares no factor
+# with one of them unless it is a multiple of it
+_MAP_PRIMES = [1000003, 1000033, 1000037, 1000039, 1000081, 1000099, 1000117, 1000121,
+               1000133, 1000151, 1000159, 1000171, 1000183, 1000187, 1000193, 1000199]
 
 
 class RandomOrder:

@@ -43,6 +43,8 @@ def _lib():
         "pcagb_vnet_to_bf16": [vp, vp, sz, vp],
         "pcagb_vnet_encode_pool_tc": [vp, vp, vp, vp, vp, vp, vp, vp, vp, i, i, vp, vp, vp, vp,
                                       vp],
+        "pcagb_vnet_gather_sample": [vp, vp, vp, vp, vp, vp, i, i, vp],
+        "pcagb_vnet_compose_order": [vp, vp, i, vp, ctypes.c_ulonglong, vp],
     }
     for name, args in sigs.items():
         fn = getattr(lib, name)

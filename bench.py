@@ -351,7 +351,8 @@ def run_guided(args):
             "config": {"workload": f"{len(sel)} held-out synthetic tasks with optimal kernel depth "
                                    "3-4; ordered solves with the engine's automatic split (stages "
                                    "predicted under 2 ms run plain; value ranks a 4,096-prefix "
-                                   "random sample, the rest follows at random), value_every_stage "
+                                   "sample spread over the level by a CUDA-graph replay, the rest "
+                                   "follows in the sample map's order), value_every_stage "
                                    "scores whole levels from split level 2; first launch 256 "
                                    "prefixes, doubling",
                        "train_tasks_used": used, "train_states": ds.n,

@@ -1063,7 +1063,7 @@ int run_batch(pcagb_engine *e, std::vector<TaskRun> &runs, const pcagb_opts_t &o
     e->TPC = maxT <= 16 ? 16 : 32;
     e->no_oep = o.oep_mode == PCAGB_OEP_NONE;
     e->td = TaskDev{e->d_task_T, e->d_task_target, e->d_task_active,
-                    o.oep_mode == PCAGB_OEP_EXACT_LIVE};
+                    o.oep_mode == PCAGB_OEP_EXACT_LIVE, o.oep_mode != PCAGB_OEP_NONE};
     CK(cudaSetDevice(e->device));
     CK(cudaMemsetAsync(e->d_status, 0, 4, e->stream));
     {

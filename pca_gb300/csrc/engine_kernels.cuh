@@ -74,6 +74,8 @@ struct TaskDev {
     const uint32_t *target;    /* [task][32] expected outputs */
     const uint8_t *active;     /* task still searched at the current depth */
     int key_live;              /* OEP key includes live */
+    int dedup_mid;             /* OEP on: a suffix's middle instruction that
+                                  repeats an earlier sibling's state is skipped */
 };
 
 struct LevelDev {
@@ -1010,6 +1012,10 @@ k_suffix(LevelDev P, TaskDev task, SolBuf S, uint32_t chunks_per_prefix, uint32_
         const uint32_t lo = ck * chunk, hi = min(nc0, lo + chunk);
         for (uint32_t i1 = lo; i1 < hi; i1++) {
             const uint32_t u1 = c_cand_uop[cb0 + i1];
+            /* a middle writing the same value and flags as an earlier
+               sibling leads to the states that sibling leads to: under OEP
+               its subtree is the pruned duplicate (never the DFS-first) */
+            if (task.dedup_mid && (u1 >> 31)) continue;
             const uint32_t rd1 = UOP_RD(u1);
             /* w0 still unread after u1: overwritten (dead, skip) or owed by
                a later instruction */
@@ -1029,6 +1035,7 @@ k_suffix(LevelDev P, TaskDev task, SolBuf S, uint32_t chunks_per_prefix, uint32_
             const uint32_t cb1 = c_cand_off[m1], nc1 = c_cand_off[m1 + 1] - cb1;
             for (uint32_t i2 = 0; i2 < nc1; i2++) {
                 const uint32_t u2 = c_cand_uop[cb1 + i2];
+                if (task.dedup_mid && (u2 >> 31)) continue;
                 const uint32_t rd2 = UOP_RD(u2);
                 /* writes still owed a read after u2 (u1's and maybe w0's);
                    one overwritten unread is dead, and the last instruction

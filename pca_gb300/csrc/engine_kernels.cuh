@@ -19,19 +19,24 @@
  * key), so a hash collision can never merge two different states. Among
  * equal states the smallest ref wins (atomicCAS loop), which is the first
  * child in the reference's DFS order -- the representative the reference's
- * DFS pruner keeps (tools/enumerate.c:379-384).
+ * DFS pruner keeps (tools/enumerate.c:379-384). Children that can never be
+ * that representative are not inserted at all: same-state siblings of an
+ * earlier candidate (bit 31 of the device micro-op), children overwriting a
+ * dead-able unread write (deadable_writes) and LDI swaps (ldi_swap); each
+ * has an equal state with a smaller ref, so the winners do not change.
  *
  * The winners are then marked in a bitmap indexed by the child's linear
  * index (child_off[parent] + candidate), ranked by a scan, and written out
  * in that order, so every level stays in DFS order.
  *
  * Suffix kernels: one warp per prefix state. The last instruction's value
- * does not depend on its destination (except ADDI), so the lanes scan the
- * value classes of the prefix's live mask on test 0, and each survivor is
- * checked on all tests at once, lane t taking test t, with __ballot_sync /
- * __all_sync deciding. Suffix depths 2 and 3 enumerate the middle
- * instructions in the warp, keeping the new columns in spare shared-memory
- * columns 8 and 9.
+ * does not depend on its destination (except ADDI), so only value classes
+ * are evaluated, and only those that read the last write (the read rule in
+ * scan_last): one lane per operand pair, every op of the pair evaluated on
+ * the first two tests at once, each survivor checked on all tests by the
+ * warp (lane t taking test t, __all_sync deciding). Suffix depths 2 and 3
+ * enumerate the middle instructions in the warp, keeping the new columns in
+ * spare shared-memory columns 8 and 9.
  */
 #pragma once
 

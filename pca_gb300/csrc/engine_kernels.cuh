@@ -154,20 +154,6 @@ __device__ __forceinline__ uint64_t hash_column(const E *col)
     return h;
 }
 
-template <int TPC>
-__device__ __forceinline__ uint64_t hash_flags(const uint32_t *f)
-{
-    uint64_t h = 0x13198A2E03707344ull;
-#pragma unroll
-    for (int t = 0; t < TPC; t += 16) {
-        uint64_t w = 0;
-#pragma unroll
-        for (int k = 0; k < 16; k++) w |= (uint64_t)f[t + k] << (4 * k);
-        h = chain(h, w);
-    }
-    return h;
-}
-
 /* Reads: does micro-op u read register r (1..7)? */
 __device__ __forceinline__ bool uop_reads(uint32_t u, uint32_t r)
 {

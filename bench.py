@@ -438,6 +438,7 @@ def main():
     dev_ms, wall_s, cands, evals = [], [], 0, 0
     launches, h2d, d2h = 0, 0, 0
     insert_ms, insert_n, insert_children, suffix_ms, suffix_n = 0.0, 0, 0, 0.0, 0
+    expand_ms = 0.0
     sol = None
     for _ in range(args.steps):
         flush.fill_(1)  # L2 flush between timed steps (256 MB > 126 MB L2)
@@ -458,6 +459,7 @@ def main():
         h2d += sol.h2d_bytes
         d2h += sol.d2h_bytes
         insert_ms += sol.gpu_ms_insert
+        expand_ms += sol.gpu_ms_expand
         insert_n += sol.insert_launches
         insert_children += sol.insert_children
         suffix_ms += sol.gpu_ms_suffix
@@ -503,10 +505,10 @@ def main():
                 "h2d_bytes_per_step": h2d // args.steps, "d2h_bytes_per_step": d2h // args.steps},
         "gpu_launches": launches,
         "clocks": clocks,
+        # expand_total: every level build (insert, mark, scan, materialise)
         "kernels_ms_per_step": {"suffix": suffix_ms / args.steps, "insert": insert_ms / args.steps,
-                                "expand_total": sum([]) if False else None},
+                                "expand_total": expand_ms / args.steps},
     }
-    line["kernels_ms_per_step"]["expand_total"] = None
     # Roofline of the suffix kernel: integer-issue bound. Peak = one warp
     # instruction per SM sub-partition per clock at the measured max clock.
     # Achieved = this run's value-class evaluations of the full candidate

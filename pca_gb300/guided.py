@@ -30,8 +30,8 @@ import weakref
 import numpy as np
 import torch
 
-from .pcalib import PCALib, SearchState
-from .valuenet import ROWS, ValueNet
+from .pcalib import PCALib
+from .valuenet import ValueNet
 
 
 def _state_arrays(states, T):

@@ -6,7 +6,7 @@ import pytest
 
 from conftest import load_golden, spec_from_json
 from pca_gb300 import taskgen
-from pca_gb300.pcalib import OEP_EXACT, OEP_EXACT_LIVE
+from pca_gb300.pcalib import OEP_EXACT
 
 pytestmark = pytest.mark.gpu
 

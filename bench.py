@@ -155,6 +155,18 @@ def dist_env():
     return rank, world, local
 
 
+def reduce_over_ranks(t_dev: float, t_wall: float, cands: float, device) -> tuple:
+    """Replica aggregation over the process group: the slowest rank's device
+    and wall times (MAX) and the candidates every rank decided (SUM)."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([t_dev, t_wall], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    c = torch.tensor([float(cands)], dtype=torch.float64, device=device)
+    dist.all_reduce(c)
+    return float(t[0]), float(t[1]), float(c[0])
+
+
 def run_reference(args):
     """Reference arm: the reference's CPU solver algorithm on the host cores."""
     rank, world, _ = dist_env()
@@ -471,12 +483,7 @@ def main():
     t_dev = sum(dev_ms) / 1000.0
     t_wall = sum(wall_s)
     if world > 1:
-        t = torch.tensor([t_dev, t_wall], dtype=torch.float64, device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_dev, t_wall = float(t[0]), float(t[1])
-        c = torch.tensor([cands], dtype=torch.float64, device=f"cuda:{local}")
-        dist.all_reduce(c)
-        total_cands = float(c[0])
+        t_dev, t_wall, total_cands = reduce_over_ranks(t_dev, t_wall, cands, f"cuda:{local}")
     else:
         total_cands = float(cands)
     if rank != 0:
@@ -488,7 +495,6 @@ def main():
     # suffix kernel: value classes evaluated per second against the issue
     # roofline (one warp instruction per SM sub-partition per clock)
     suffix_evals_per_s = evals / (suffix_ms / 1000.0) if suffix_ms > 0 else 0.0
-    insert_gbs = 0.0
     line = {
         "metric": METRIC, "value": total_cands / t_dev, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": max(3, args.warmup),
@@ -508,6 +514,8 @@ def main():
         # expand_total: every level build (insert, mark, scan, materialise)
         "kernels_ms_per_step": {"suffix": suffix_ms / args.steps, "insert": insert_ms / args.steps,
                                 "expand_total": expand_ms / args.steps},
+        "launches_per_step": {"insert": insert_n / args.steps, "suffix": suffix_n / args.steps},
+        "children_inserted_per_step": insert_children // args.steps,
     }
     # Roofline of the suffix kernel: integer-issue bound. Peak = one warp
     # instruction per SM sub-partition per clock at the measured max clock.

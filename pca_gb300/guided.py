@@ -17,7 +17,7 @@ order, chunk by chunk, and stops the optimal depth's stage at the first
 chunk with a correct program. Depths below the optimum are searched
 completely in any order, so the optimal depth stays proven: the network
 reorders work, it never prunes. DFS order (the plain engine) is the
-fallback and the judge.
+fallback, and its answers are the ones an ordered solve must reproduce.
 """
 from __future__ import annotations
 

@@ -308,11 +308,7 @@ class ValueOrder:
 
     def _sampled_order(self, view, n, m, tp, task_io, task_T, dev, stream):
         G = self._ranking_graph(m, tp, task_io, task_T, dev)
-        a = 0
-        for p in _MAP_PRIMES[self.rng.randrange(len(_MAP_PRIMES)):] + _MAP_PRIMES:
-            if math.gcd(p % n, n) == 1:
-                a = p % n
-                break
+        a = map_multiplier(n, self.rng.randrange(len(_MAP_PRIMES)))
         G["src_host"].numpy()[:] = (view.regs, view.flags, view.live, view.task, n, a,
                                     self.rng.randrange(n), view.depth)
         G["src"].copy_(G["src_host"])   # 64 bytes, ordered on the engine's stream
@@ -343,6 +339,19 @@ def _release_graphs():
 # with one of them unless it is a multiple of it
 _MAP_PRIMES = [1000003, 1000033, 1000037, 1000039, 1000081, 1000099, 1000117, 1000121,
                1000133, 1000151, 1000159, 1000171, 1000183, 1000187, 1000193, 1000199]
+
+
+def map_multiplier(n: int, start: int = 0) -> int:
+    """The multiplier a of the sample map i -> (a*i + b) mod n: the first of
+    the primes (from index `start`, wrapping) that is coprime to n, reduced
+    mod n, so the map is a permutation of 0..n-1 for any b. A level size
+    divisible by all sixteen primes (over 10^95) is out of reach."""
+    if n < 1:
+        raise ValueError(f"sample map over {n} prefixes")
+    for p in _MAP_PRIMES[start:] + _MAP_PRIMES[:start]:
+        if math.gcd(p, n) == 1:
+            return p % n
+    raise ValueError(f"no multiplier coprime to {n}")
 
 
 class RandomOrder:

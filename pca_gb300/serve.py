@@ -11,7 +11,9 @@ when its batch ends. An answer is the task's proven optimal depth and its
 first optimal program in DFS order, which does not depend on the batch it
 ran in or the split level the engine's autotuner chose; a solve's state
 (levels, OEP tables, test order) lives only in its batch's arena and is
-keyed by task, so each result is the same alone and in the mix.
+keyed by task, so each result is the same alone and in the mix. A solve
+that fails (an engine error) hands its exception to every request of the
+batch still open (Request.error); the worker goes on with the next batch.
 
 `replay(trace)` drives a server from an arrival trace ((seconds, task)
 pairs, e.g. taskgen.poisson_stream) in real time and returns per-request
@@ -38,6 +40,7 @@ class Request:
     finish: float = 0.0
     solution: Solution | None = None
     batch_size: int = 0
+    error: Exception | None = None   # the engine's error, when the solve failed
 
     @property
     def latency(self) -> float:
@@ -46,10 +49,16 @@ class Request:
 
 class Server:
     def __init__(self, slots: int = 4, max_batch: int = 256, max_depth: int = 4, device: int = 0,
-                 hbm_fraction: float = 0.8, sol_cap: int = 16, oep_mode: int = OEP_EXACT_LIVE):
-        free, _ = device_memory(device)
-        budget = int(free * hbm_fraction / max(1, slots))
-        self.engines = [Engine(device, budget) for _ in range(slots)]
+                 hbm_fraction: float = 0.8, sol_cap: int = 16, oep_mode: int = OEP_EXACT_LIVE,
+                 engine_factory=None):
+        if engine_factory is None:
+            free, _ = device_memory(device)
+            budget = int(free * hbm_fraction / max(1, slots))
+
+            def engine_factory():
+                return Engine(device, budget)
+        # engine_factory() -> an object with Engine's solve_batch and close
+        self.engines = [engine_factory() for _ in range(slots)]
         self.max_batch = max_batch
         self.max_depth = max_depth
         self.sol_cap = sol_cap
@@ -105,8 +114,16 @@ class Server:
                 r.batch_size = len(batch)
                 r.done.set()
 
-            eng.solve_batch([r.task for r in batch], max_depth=depth, oep_mode=self.oep_mode,
-                            sol_cap=self.sol_cap, on_done=deliver, first_only=True)
+            try:
+                eng.solve_batch([r.task for r in batch], max_depth=depth, oep_mode=self.oep_mode,
+                                sol_cap=self.sol_cap, on_done=deliver, first_only=True)
+            except Exception as exc:  # noqa: BLE001 -- handed to the requests it leaves open
+                for r in batch:
+                    if not r.done.is_set():
+                        r.error = exc
+                        r.finish = self.now()
+                        r.batch_size = len(batch)
+                        r.done.set()
 
     def close(self):
         self._stop = True
@@ -122,9 +139,10 @@ class SerialServer(Server):
     served (the reference's one-task-per-run model, on the GPU)."""
 
     def __init__(self, max_depth: int = 4, device: int = 0, hbm_fraction: float = 0.8,
-                 sol_cap: int = 16, oep_mode: int = OEP_EXACT_LIVE):
+                 sol_cap: int = 16, oep_mode: int = OEP_EXACT_LIVE, engine_factory=None):
         super().__init__(slots=1, max_batch=1, max_depth=max_depth, device=device,
-                         hbm_fraction=hbm_fraction, sol_cap=sol_cap, oep_mode=oep_mode)
+                         hbm_fraction=hbm_fraction, sol_cap=sol_cap, oep_mode=oep_mode,
+                         engine_factory=engine_factory)
 
 
 def replay(server: Server, trace, max_depth: int | None = None) -> list[Request]:
@@ -143,6 +161,8 @@ def replay(server: Server, trace, max_depth: int | None = None) -> list[Request]
 
 
 def latency_summary(reqs: list[Request]) -> dict:
+    """Latency percentiles (time-to-proven-optimal), throughput and the
+    count of failed requests over a replayed trace."""
     lat = sorted(r.latency for r in reqs)
 
     def pct(p):
@@ -156,5 +176,6 @@ def latency_summary(reqs: list[Request]) -> dict:
     return {"requests": len(reqs), "p50_s": pct(50), "p99_s": pct(99), "max_s": lat[-1],
             "mean_s": sum(lat) / len(lat),
             "proven_optimal": sum(1 for r in reqs if r.solution and r.solution.optimal_depth >= 0),
+            "failed": sum(1 for r in reqs if r.error is not None),
             "span_s": span, "candidates": cands,
             "candidates_per_s": cands / span if span > 0 else 0.0}

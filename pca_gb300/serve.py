@@ -14,6 +14,7 @@ ran in or the split level the engine's autotuner chose; a solve's state
 keyed by task, so each result is the same alone and in the mix. A solve
 that fails (an engine error) hands its exception to every request of the
 batch still open (Request.error); the worker goes on with the next batch.
+`close()` stops new submissions and answers every request queued before it.
 
 `replay(trace)` drives a server from an arrival trace ((seconds, task)
 pairs, e.g. taskgen.poisson_stream) in real time and returns per-request
@@ -25,6 +26,7 @@ from __future__ import annotations
 import queue
 import threading
 import time
+import warnings
 from dataclasses import dataclass, field
 
 from .pcalib import Engine, OEP_EXACT_LIVE, Solution, device_memory
@@ -78,7 +80,10 @@ class Server:
 
     def submit(self, rid: int, task, max_depth: int | None = None) -> Request:
         r = Request(rid, task, self.now(), self.max_depth if max_depth is None else max_depth)
-        self.q.put(r)
+        with self._lock:
+            if self._stop:
+                raise RuntimeError("the server is closed")
+            self.q.put(r)
         return r
 
     def _take_batch(self) -> list[Request]:
@@ -98,10 +103,10 @@ class Server:
         return batch
 
     def _worker(self, eng: Engine):
-        while not self._stop:
+        while True:
             batch = self._take_batch()
             if not batch:
-                self.q.put(None)
+                self.q.put(None)   # the end marker, for the other workers
                 return
             with self._lock:
                 self.batches.append(len(batch))
@@ -125,12 +130,19 @@ class Server:
                         r.batch_size = len(batch)
                         r.done.set()
 
-    def close(self):
-        self._stop = True
-        self.q.put(None)
-        for t in self.threads:
-            t.join(timeout=60)
-        for e in self.engines:
+    def close(self, timeout: float = 60.0):
+        """Take no new requests, answer those already queued, and free the
+        engines. A worker still inside a solve after `timeout` seconds keeps
+        its engine (freeing it under the solve would crash the process)."""
+        with self._lock:
+            self._stop = True
+            self.q.put(None)
+        for t, e in zip(self.threads, self.engines):
+            t.join(timeout=timeout)
+            if t.is_alive():
+                warnings.warn(f"serving worker still busy after {timeout:g} s; its engine is "
+                              "left open", RuntimeWarning)
+                continue
             e.close()
 
 

@@ -119,3 +119,31 @@ def test_close_stops_every_worker():
     srv.close()
     assert all(not t.is_alive() for t in srv.threads)
     assert all(r.done.is_set() for r in reqs)
+
+
+def test_close_answers_queued_requests_and_refuses_new_ones():
+    srv = Server(slots=1, max_batch=2, engine_factory=lambda: FakeEngine(delay=0.05))
+    reqs = [srv.submit(i, i) for i in range(7)]   # queued behind a busy slot
+    srv.close()
+    assert all(r.done.is_set() and r.solution == answer(r.task) for r in reqs)
+    assert sum(srv.batches) == 7 and max(srv.batches) <= 2
+    try:
+        srv.submit(99, 1)
+    except RuntimeError:
+        pass
+    else:
+        raise AssertionError("a closed server took a request")
+
+
+def test_close_keeps_the_engine_of_a_worker_still_solving():
+    import warnings
+
+    eng = FakeEngine(delay=1.0)
+    srv = Server(slots=1, engine_factory=lambda: eng)
+    r = srv.submit(0, 3)
+    time.sleep(0.05)
+    with warnings.catch_warnings(record=True) as w:
+        warnings.simplefilter("always")
+        srv.close(timeout=0.1)
+    assert not eng.closed and any(issubclass(x.category, RuntimeWarning) for x in w)
+    assert r.done.wait(5) and r.solution == answer(3)

@@ -208,18 +208,6 @@ struct WarpState {
     uint64_t colh[8];         /* colh[r] = col_final(r, hash(col r)), r >= 1 */
 };
 
-template <int TPC>
-__device__ __forceinline__ void load_state(WarpState<TPC> &ws, const uint16_t *regs,
-                                           const uint8_t *flags, uint64_t q, int lane)
-{
-    if (lane < TPC) {
-        const uint16_t *src = regs + q * 8 * TPC + lane;
-#pragma unroll
-        for (int r = 0; r < 8; r++) ws.R[r][lane] = src[r * TPC];
-        ws.F[lane] = flags[q * TPC + lane];
-    }
-}
-
 /* ---- level expansion: insert every child into the exact table ------------ */
 
 /* One warp's shared memory in the insert kernel: its parent (16-bit columns,
@@ -557,15 +545,40 @@ __global__ void k_child_counts(const uint8_t *live, const uint16_t *task, const 
     }
 }
 
-/* Write the marked children of each parent, in rank (DFS) order. */
+/* One warp's shared memory in the materialisation: the parent's register
+   block in the level's own layout (8 columns of TPC tests) and the current
+   child's new column and flags, from which each lane writes one 16-byte
+   piece of the child. */
+template <int TPC>
+struct MatState {
+    __align__(16) uint16_t PR[8 * TPC];
+    __align__(16) uint16_t CB[TPC];
+    __align__(16) uint8_t FB[TPC];
+};
+
+/* Write the marked children of each parent, in rank (DFS) order. A child's
+   register block (8 x TPC halves) is written as TPC 16-byte pieces, one per
+   lane, and its flags as TPC/16 pieces: lane t first computes the new value
+   and flags of test t into shared memory, then lane L copies piece L from
+   the parent's block, or from the new column when the piece lies in the
+   written register's column. Level blocks start on 256-byte boundaries (the
+   arena's allocation unit) and a state's block is 256 or 512 bytes, so
+   every piece is 16-byte aligned. */
 template <int TPC>
 __global__ void __launch_bounds__(kThreads)
 k_materialize(LevelDev P, TaskDev task, const uint32_t *bitmap, const uint64_t *word_off,
               LevelOut C, uint32_t split_log2, uint32_t *fcr, const uint32_t *fcr_up)
 {
-    __shared__ WarpState<TPC> sws[kWarpsPerBlock];
+    static_assert(TPC == 16 || TPC == 32, "a state holds 16 or 32 tests");
+    constexpr int kPieces = 8 * TPC * 2 / 16;   /* = TPC: lanes 0..TPC-1 */
+    constexpr int kFlagPieces = TPC / 16;
+    constexpr int kPiecesPerCol = TPC / 8;
+    __shared__ MatState<TPC> sms[kWarpsPerBlock];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    WarpState<TPC> &ws = sws[wib];
+    MatState<TPC> &ms = sms[wib];
+    const uint32_t my_col = (uint32_t)lane / kPiecesPerCol;   /* column of piece `lane` */
+    const uint4 *my_new = reinterpret_cast<const uint4 *>(ms.CB) + lane % kPiecesPerCol;
+    const uint4 *my_old = reinterpret_cast<const uint4 *>(ms.PR) + lane;
     const uint64_t nw = (uint64_t)gridDim.x * kWarpsPerBlock;
     const uint32_t split = 1u << split_log2;
     /* work items as in k_expand_insert: a parent, or a slice of its
@@ -578,7 +591,10 @@ k_materialize(LevelDev P, TaskDev task, const uint32_t *bitmap, const uint64_t *
         if (!task.active[tid]) continue;
         const int T = task.T[tid];
         __syncwarp();
-        load_state<TPC>(ws, P.regs, P.flags, q, lane);
+        if (lane < kPieces)
+            reinterpret_cast<uint4 *>(ms.PR)[lane] =
+                reinterpret_cast<const uint4 *>(P.regs + q * 8 * TPC)[lane];
+        const uint32_t pf = lane < TPC ? P.flags[q * TPC + lane] : 0u;
         const uint32_t live = P.live[q];
         __syncwarp();
         const uint32_t m = (live >> 1) & 127u;
@@ -624,16 +640,22 @@ k_materialize(LevelDev P, TaskDev task, const uint32_t *bitmap, const uint64_t *
                 const uint32_t uj = __shfl_sync(0xFFFFFFFFu, u, j);
                 const uint32_t op = UOP_OP(uj), rd = UOP_RD(uj);
                 if (lane < TPC) {
-                    uint32_t a = ws.R[UOP_A(uj)][lane], b = ws.R[UOP_B(uj)][lane];
+                    const uint32_t a = ms.PR[UOP_A(uj) * TPC + lane];
+                    const uint32_t b = ms.PR[UOP_B(uj) * TPC + lane];
                     uint32_t res = pca_alu(op, a, b, UOP_IMM(uj));
-                    uint32_t f = pca_alu_flags(op, a, b, UOP_IMM(uj), res, ws.F[lane]);
+                    uint32_t f = pca_alu_flags(op, a, b, UOP_IMM(uj), res, pf);
                     if (lane >= T) { res = 0; f = 0; }
-                    uint16_t *dst = C.regs + rk * 8 * TPC + lane;
-#pragma unroll
-                    for (uint32_t r = 0; r < 8; r++)
-                        dst[r * TPC] = (uint16_t)(r == rd ? res : ws.R[r][lane]);
-                    C.flags[rk * TPC + lane] = (uint8_t)f;
+                    ms.CB[lane] = (uint16_t)res;
+                    ms.FB[lane] = (uint8_t)f;
                 }
+                __syncwarp();
+                if (lane < kPieces)
+                    reinterpret_cast<uint4 *>(C.regs + rk * 8 * TPC)[lane] =
+                        *(my_col == rd ? my_new : my_old);
+                if (lane < kFlagPieces)
+                    reinterpret_cast<uint4 *>(C.flags + rk * TPC)[lane] =
+                        reinterpret_cast<const uint4 *>(ms.FB)[lane];
+                __syncwarp();
             }
         }
     }

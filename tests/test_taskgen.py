@@ -35,3 +35,41 @@ def test_batches_deterministic():
     assert [bytes(x) for x in a] == [bytes(x) for x in b]
     s = taskgen.poisson_stream(100)
     assert all(s[i][0] < s[i + 1][0] for i in range(99))
+
+
+def test_served_stream_rate_and_length_mix():
+    s = taskgen.poisson_stream(4000, rate=50.0, seed=5)
+    gaps = [b[0] - a[0] for a, b in zip(s, s[1:])]
+    assert abs(sum(gaps) / len(gaps) - 1 / 50.0) < 0.1 / 50.0
+    lengths = [int(t.name.decode().rsplit("len", 1)[1]) for _, t in s]
+    want = {4: 0.30, 5: 0.30, 6: 0.25, 7: 0.10, 8: 0.05}
+    for L, p in want.items():
+        assert abs(lengths.count(L) / len(lengths) - p) < 0.03, (L, lengths.count(L))
+    assert set(lengths) == set(want)
+
+
+def test_batched_lengths_and_shapes():
+    tasks = taskgen.synthetic_batch(600, seed=9)
+    lengths = [int(t.name.decode().rsplit("len", 1)[1]) for t in tasks]
+    assert set(lengths) == set(range(3, 9))
+    assert all(abs(lengths.count(L) / 600 - 1 / 6) < 0.06 for L in range(3, 9))
+    assert {t.num_inputs for t in tasks} == {1, 2}
+    assert min(t.num_tests for t in tasks) == 16 and max(t.num_tests for t in tasks) == 32
+    assert {int(t.name.decode().rsplit("len", 1)[1]) for t in taskgen.deep_tasks(60)} == {8, 9, 10}
+
+
+def test_program_generator_distribution():
+    import random
+    rng = random.Random(0)
+    ops, regs, small, imms = {}, set(), 0, 0
+    for _ in range(3000):
+        for op, rd, rs, rt, imm in taskgen.random_program(rng, 1):
+            ops[op] = ops.get(op, 0) + 1
+            regs |= {rd, rs, rt} if op not in ("LDI", "ADDI") else {rd}
+            if op in ("LDI", "ADDI"):
+                imms += 1
+                small += imm < 16
+    assert set(ops) == set(taskgen.BRANCHLESS_OPS)
+    assert all(abs(c / 3000 - 1 / 11) < 0.03 for c in ops.values())
+    assert regs == set(range(1, 8))
+    assert 0.45 < small / imms < 0.6   # half small immediates, plus uniform ones below 16

@@ -430,12 +430,23 @@ class Engine:
                 setattr(sol, name, [arr2[k] for k in range(min(last + 1, MAXD))])
             return sol
 
+        errors = []
         if on_done is None:
             rc = self.lib.pcagb_solve_batch(self.h, arr, n, ctypes.byref(o), res, progs, lens, cap)
         else:
-            cb = DONE_CB(lambda i, rp, _u: on_done(i, convert(i, rp.contents)))
+            def done(i, rp, _user):
+                # ctypes would print and drop an exception raised here: keep
+                # the first one and raise it once the batch returns
+                try:
+                    on_done(i, convert(i, rp.contents))
+                except BaseException as exc:  # noqa: BLE001 - re-raised after the batch
+                    errors.append(exc)
+
+            cb = DONE_CB(done)
             rc = self.lib.pcagb_solve_batch_cb(self.h, arr, n, ctypes.byref(o), res, progs, lens,
                                                cap, cb, None)
+        if errors:
+            raise errors[0]
         if rc != 0:
             raise EngineError(f"batch solve failed ({rc}): {self.lib.pcagb_last_error().decode()}")
         return [convert(i, res[i]) for i in range(n)]

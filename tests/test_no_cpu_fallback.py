@@ -1,7 +1,8 @@
 """No entry point falls back to the CPU: on a machine without a CUDA device
-the engine refuses to start (PCAGB_ENODEV, with a message), and the
-GPU-backed search_exhaustive_complete returns that error instead of
-searching on the host. Skipped where a device is present."""
+the engine refuses to start (PCAGB_ENODEV, with a message), the solver
+command lines exit with an error, and the GPU-backed
+search_exhaustive_complete returns that error instead of searching on the
+host. Skipped where a device is present."""
 import ctypes
 
 import pytest
@@ -41,3 +42,20 @@ def test_exhaustive_completion_does_not_search_on_the_host(lib):
                                         ctypes.byref(n))
     assert rc == PCAGB_ENODEV and n.value == 0
     assert lib.search_exhaustive_states_explored() == 0
+
+
+def test_solver_command_lines_refuse_without_a_device(lib, tmp_path):
+    import json
+    import os
+    import subprocess
+
+    from conftest import REPO, load_golden
+    fx = load_golden("ref_enumerate.json")[0]
+    path = tmp_path / "task.json"
+    path.write_text(json.dumps(fx["task"]))
+    bindir = os.path.join(REPO, "pca_gb300", "_lib")
+    for args in (["enumerate", str(path), "-d", "2"], ["gpu_hybrid", str(path), "2"]):
+        r = subprocess.run([os.path.join(bindir, args[0])] + args[1:], capture_output=True,
+                           text=True, timeout=60)
+        assert r.returncode == 1 and "no CUDA device" in r.stderr, (args[0], r.stderr)
+        assert "Optimal solution length" not in r.stdout

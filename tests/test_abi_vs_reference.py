@@ -1,0 +1,95 @@
+"""The libpca half of libpcagb.so against the reference's own libpca.so built
+from its sources (oracle/_ref; skipped where the reference tree is absent):
+search_state_step on every one of the 65,536 instruction words from states
+reached by random walks (legal or not, the written state byte for byte),
+the two FNV-1a hashes and the leaf outputs of the states it produces, and
+the branchless generator for all 128 liveness masks."""
+import ctypes
+import os
+import random
+
+import pytest
+
+from conftest import REPO
+from pca_gb300 import taskgen
+from pca_gb300.pcalib import PCALib, SearchCtx, SearchState
+
+REF_LIB = os.path.join(REPO, "oracle", "_ref", "libpca.so")
+
+
+@pytest.fixture(scope="module")
+def ref():
+    if not os.path.exists(REF_LIB):
+        pytest.skip("the reference's libpca.so is not built here")
+    L = ctypes.CDLL(REF_LIB)
+    P = ctypes.POINTER
+    L.search_ctx_init.argtypes = [P(SearchCtx), ctypes.c_void_p]
+    L.search_ctx_init.restype = ctypes.c_int
+    L.search_state_init_root.argtypes = [P(SearchCtx), P(SearchState)]
+    L.search_state_init_root.restype = None
+    L.search_state_step.argtypes = [P(SearchCtx), P(SearchState), ctypes.c_uint16, P(SearchState)]
+    L.search_state_step.restype = ctypes.c_int
+    for name in ("search_state_oep_hash64", "search_state_key_hash64"):
+        getattr(L, name).argtypes = [P(SearchCtx), P(SearchState)]
+        getattr(L, name).restype = ctypes.c_uint64
+    L.search_state_leaf_outputs.argtypes = [P(SearchCtx), P(SearchState)]
+    L.search_state_leaf_outputs.restype = ctypes.c_uint8
+    L.search_gen_candidates_branchless.argtypes = [P(ctypes.c_uint16), ctypes.c_int, P(SearchState)]
+    L.search_gen_candidates_branchless.restype = ctypes.c_int
+    return L
+
+
+def _walk(lib, ctx, steps, rng):
+    s = lib.init_root(ctx)
+    for _ in range(steps):
+        s = lib.step(ctx, s, rng.choice(lib.gen_candidates(s)))
+    return s
+
+
+@pytest.mark.parametrize("task_kind,steps", [("negate", 0), ("negate", 2), ("two_input", 1),
+                                             ("two_input", 3)])
+def test_step_on_every_instruction_word(ref, task_kind, steps):
+    mine = PCALib()
+    if task_kind == "negate":
+        task = taskgen.negate_task(3)
+    else:
+        task, _ = taskgen.synthetic_task(50, 4)
+    assert task_kind == "negate" or task.num_inputs == 2
+    ctx = mine.init_ctx(task)
+    s = _walk(mine, ctx, steps, random.Random(steps))
+    a, b = SearchState(), SearchState()
+    size = ctypes.sizeof(SearchState)
+    legal = 0
+    for insn in range(1 << 16):
+        ctypes.memset(ctypes.byref(a), 0, size)
+        ctypes.memset(ctypes.byref(b), 0, size)
+        ra = mine.lib.search_state_step(ctypes.byref(ctx), ctypes.byref(s), insn, ctypes.byref(a))
+        rb = ref.search_state_step(ctypes.byref(ctx), ctypes.byref(s), insn, ctypes.byref(b))
+        assert ra == rb, hex(insn)
+        if ra != 1:
+            continue
+        legal += 1
+        assert bytes(a) == bytes(b), hex(insn)
+        if insn % 61 == 0:
+            for name in ("search_state_oep_hash64", "search_state_key_hash64",
+                         "search_state_leaf_outputs"):
+                assert getattr(mine.lib, name)(ctypes.byref(ctx), ctypes.byref(a)) == \
+                    getattr(ref, name)(ctypes.byref(ctx), ctypes.byref(b)), (name, hex(insn))
+    assert legal > 1000
+
+
+def test_generator_for_every_liveness_mask(ref):
+    mine = PCALib()
+    s = SearchState()
+    buf_a = (ctypes.c_uint16 * 4096)()
+    buf_b = (ctypes.c_uint16 * 4096)()
+    for m in range(128):
+        s.live = m << 1
+        na = mine.lib.search_gen_candidates_branchless(buf_a, 4096, ctypes.byref(s))
+        nb = ref.search_gen_candidates_branchless(buf_b, 4096, ctypes.byref(s))
+        assert na == nb and list(buf_a[:na]) == list(buf_b[:nb]), m
+    # a short buffer: the count and the prefix written agree
+    s.live = 0xFE
+    na = mine.lib.search_gen_candidates_branchless(buf_a, 100, ctypes.byref(s))
+    nb = ref.search_gen_candidates_branchless(buf_b, 100, ctypes.byref(s))
+    assert na == nb and list(buf_a[:min(na, 100)]) == list(buf_b[:min(nb, 100)])

@@ -93,3 +93,32 @@ def test_generator_for_every_liveness_mask(ref):
     na = mine.lib.search_gen_candidates_branchless(buf_a, 100, ctypes.byref(s))
     nb = ref.search_gen_candidates_branchless(buf_b, 100, ctypes.byref(s))
     assert na == nb and list(buf_a[:min(na, 100)]) == list(buf_b[:min(nb, 100)])
+
+
+def test_disassembler_on_every_instruction_word(ref):
+    mine = PCALib().lib
+    ref.pca_disasm.argtypes = [ctypes.c_uint16, ctypes.c_char_p, ctypes.c_size_t]
+    ref.pca_disasm.restype = None
+    a = ctypes.create_string_buffer(96)
+    b = ctypes.create_string_buffer(96)
+    for insn in range(1 << 16):
+        mine.pca_disasm(insn, a, 96)
+        ref.pca_disasm(insn, b, 96)
+        assert a.value == b.value, hex(insn)
+
+
+def test_task_evaluate_on_random_programs(ref):
+    from conftest import load_golden, spec_from_json
+    mine = PCALib().lib
+    ref.task_evaluate.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint16), ctypes.c_int]
+    ref.task_evaluate.restype = ctypes.c_int
+    rng = random.Random(7)
+    specs = [spec_from_json(f["task"]) for f in load_golden("ref_enumerate.json")[:10]]
+    for spec in specs:
+        for _ in range(300):
+            n = rng.randrange(1, 14)
+            words = [rng.randrange(1 << 16) for _ in range(n)]
+            prog = (ctypes.c_uint16 * n)(*words)
+            ra = mine.task_evaluate(ctypes.byref(spec), prog, n)
+            rb = ref.task_evaluate(ctypes.byref(spec), prog, n)
+            assert ra == rb, (spec.name, [hex(w) for w in words])

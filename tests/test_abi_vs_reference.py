@@ -122,3 +122,18 @@ def test_task_evaluate_on_random_programs(ref):
             ra = mine.task_evaluate(ctypes.byref(spec), prog, n)
             rb = ref.task_evaluate(ctypes.byref(spec), prog, n)
             assert ra == rb, (spec.name, [hex(w) for w in words])
+
+
+def test_exports_cover_the_reference_library(ref):
+    import shutil
+    import subprocess
+    from pca_gb300.pcalib import EXPORTS, load_library
+    if not shutil.which("nm"):
+        pytest.skip("nm is not installed")
+    out = subprocess.run(["nm", "-D", "--defined-only", REF_LIB], capture_output=True, text=True,
+                         check=True).stdout
+    ref_funcs = {line.split()[-1] for line in out.splitlines() if " T " in line}
+    lib = load_library()
+    assert all(hasattr(lib, name) for name in ref_funcs - {"pca_assemble", "pca_dump"})
+    # the two left out serve the reference's emulator command line only
+    assert ref_funcs - set(EXPORTS) == {"pca_assemble", "pca_dump"}

@@ -66,3 +66,24 @@ def test_cli_writes_the_files(tmp_path):
     assert corpus.main(argv) == 0
     got = {f: open(os.path.join(tmp_path, f)).read() for f in os.listdir(tmp_path)}
     assert got == GOLDEN[args]
+
+
+@pytest.mark.parametrize("argv", [["-n", "25", "-s", "7"],
+                                  ["-n", "20", "-s", "2024", "--min-len", "5", "--max-len", "9"],
+                                  ["-n", "15", "-s", "99", "--verify"]])
+def test_files_equal_live_reference(tmp_path, argv):
+    """The same against the reference's gen_tasks run live (oracle/_ref,
+    built from its sources; skipped where absent), for seeds and length
+    ranges outside the fixtures."""
+    import subprocess
+    ref_bin = os.path.join(os.path.dirname(HERE), "oracle", "_ref", "gen_tasks")
+    if not os.path.exists(ref_bin):
+        pytest.skip("the reference's gen_tasks is not built here")
+    ref_dir, my_dir = tmp_path / "ref", tmp_path / "mine"
+    ref_dir.mkdir()
+    my_dir.mkdir()
+    subprocess.run([ref_bin, str(ref_dir)] + argv, check=True, capture_output=True, timeout=300)
+    assert corpus.main([str(my_dir)] + argv) == 0
+    ref = {f: (ref_dir / f).read_bytes() for f in os.listdir(ref_dir)}
+    mine = {f: (my_dir / f).read_bytes() for f in os.listdir(my_dir)}
+    assert ref and mine == ref

@@ -137,3 +137,41 @@ def test_exports_cover_the_reference_library(ref):
     assert all(hasattr(lib, name) for name in ref_funcs - {"pca_assemble", "pca_dump"})
     # the two left out serve the reference's emulator command line only
     assert ref_funcs - set(EXPORTS) == {"pca_assemble", "pca_dump"}
+
+
+def test_serialize_and_dump_of_walked_states(ref, tmp_path):
+    mine = PCALib()
+    libc = ctypes.CDLL(None)
+    libc.fopen.restype = ctypes.c_void_p
+    libc.fopen.argtypes = [ctypes.c_char_p, ctypes.c_char_p]
+    libc.fclose.argtypes = [ctypes.c_void_p]
+    P = ctypes.POINTER
+    rec_size = 576
+    for lib in (mine.lib, ref):
+        lib.search_state_serialize.argtypes = [P(SearchCtx), P(SearchState), ctypes.c_uint32,
+                                               ctypes.c_uint16, ctypes.c_uint8, ctypes.c_uint8,
+                                               ctypes.c_int8, ctypes.c_void_p]
+        lib.search_state_serialize.restype = None
+        lib.search_state_dump.argtypes = [P(SearchCtx), P(SearchState), ctypes.c_void_p]
+        lib.search_state_dump.restype = None
+    rng = random.Random(3)
+    task, _ = taskgen.synthetic_task(1006, 4)
+    ctx = mine.init_ctx(task)
+    for walk in range(12):
+        s = _walk(mine, ctx, walk % 5, rng)
+        args = (rng.randrange(1 << 32), rng.randrange(1 << 16), rng.randrange(8), rng.randrange(2),
+                rng.randrange(-1, 6))
+        outs = []
+        for lib in (mine.lib, ref):
+            buf = ctypes.create_string_buffer(rec_size)
+            lib.search_state_serialize(ctypes.byref(ctx), ctypes.byref(s), *args, buf)
+            outs.append(buf.raw)
+        assert outs[0] == outs[1], walk
+        texts = []
+        for k, lib in enumerate((mine.lib, ref)):
+            path = str(tmp_path / f"dump{k}.txt").encode()
+            fp = libc.fopen(path, b"w")
+            lib.search_state_dump(ctypes.byref(ctx), ctypes.byref(s), fp)
+            libc.fclose(fp)
+            texts.append(open(path, "rb").read())
+        assert texts[0] == texts[1] and texts[0], walk

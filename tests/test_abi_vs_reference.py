@@ -175,3 +175,40 @@ def test_serialize_and_dump_of_walked_states(ref, tmp_path):
             libc.fclose(fp)
             texts.append(open(path, "rb").read())
         assert texts[0] == texts[1] and texts[0], walk
+
+
+def _stdout_of(fn):
+    """What fn() writes to the process's file descriptor 1."""
+    import os
+    import tempfile
+    libc = ctypes.CDLL(None)
+    libc.fflush(None)
+    with tempfile.TemporaryFile() as f:
+        saved = os.dup(1)
+        os.dup2(f.fileno(), 1)
+        try:
+            fn()
+            libc.fflush(None)
+        finally:
+            os.dup2(saved, 1)
+            os.close(saved)
+        f.seek(0)
+        return f.read()
+
+
+def test_printed_task_and_program_listing(ref):
+    from conftest import load_golden, spec_from_json
+    mine = PCALib().lib
+    ref.task_print.argtypes = [ctypes.c_void_p]
+    ref.pca_disasm_prog.argtypes = [ctypes.POINTER(ctypes.c_uint16), ctypes.c_int]
+    rng = random.Random(5)
+    for f in load_golden("ref_enumerate.json")[:8]:
+        spec = spec_from_json(f["task"])
+        a = _stdout_of(lambda: mine.task_print(ctypes.byref(spec)))
+        b = _stdout_of(lambda: ref.task_print(ctypes.byref(spec)))
+        assert a == b and a
+        words = [rng.randrange(1 << 16) for _ in range(rng.randrange(1, 20))]
+        prog = (ctypes.c_uint16 * len(words))(*words)
+        a = _stdout_of(lambda: mine.pca_disasm_prog(prog, len(words)))
+        b = _stdout_of(lambda: ref.pca_disasm_prog(prog, len(words)))
+        assert a == b and a

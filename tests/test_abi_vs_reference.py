@@ -212,3 +212,28 @@ def test_printed_task_and_program_listing(ref):
         a = _stdout_of(lambda: mine.pca_disasm_prog(prog, len(words)))
         b = _stdout_of(lambda: ref.pca_disasm_prog(prog, len(words)))
         assert a == b and a
+
+
+def test_vm_runs_random_programs_alike(ref):
+    mine = PCALib().lib
+    for lib in (mine, ref):
+        lib.pca_init.argtypes = [ctypes.c_void_p]
+        lib.pca_load.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint16), ctypes.c_size_t]
+        lib.pca_step.argtypes = [ctypes.c_void_p]
+        lib.pca_run.argtypes = [ctypes.c_void_p, ctypes.c_uint64]
+        lib.pca_run.restype = ctypes.c_int
+    rng = random.Random(11)
+    size = 8192   # larger than pca_vm_t; the tail stays zero in both
+    for _ in range(400):
+        words = [rng.randrange(1 << 16) for _ in range(rng.randrange(1, 40))]
+        prog = (ctypes.c_uint16 * len(words))(*words)
+        max_cycles = rng.randrange(1, 300)
+        vms = []
+        for lib in (mine, ref):
+            vm = ctypes.create_string_buffer(size)
+            lib.pca_init(vm)
+            lib.pca_load(vm, prog, len(words))
+            lib.pca_step(vm)
+            rc = lib.pca_run(vm, max_cycles)
+            vms.append((rc, vm.raw))
+        assert vms[0] == vms[1], [hex(w) for w in words]

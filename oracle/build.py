@@ -1,6 +1,7 @@
 """Build the CPU oracle (test infrastructure): oracle/_build/liborc.so and
 oracle/_build/oracle_enumerate, plus, where the reference tree exists on this
-machine, the reference's own CPU solver via oracle/build_ref.sh.
+machine ($PCA_REFERENCE_ROOT), the reference's own CPU solver via
+oracle/build_ref.sh.
 
     python oracle/build.py [--force]
 """
@@ -13,7 +14,8 @@ import sys
 
 ORACLE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(ORACLE, "_build")
-REFERENCE_ROOT = "/root/reference"
+# the reference tree, when this machine has one: $PCA_REFERENCE_ROOT
+REFERENCE_ROOT = os.environ.get("PCA_REFERENCE_ROOT", "")
 
 
 def _newer(target: str, deps: list[str]) -> bool:
@@ -42,7 +44,7 @@ def build_oracle(force: bool = False) -> str:
             raise RuntimeError("oracle build failed")
     with open(stamp, "w") as f:
         f.write(platform.machine() + "\n")
-    if os.path.isdir(REFERENCE_ROOT) and (
+    if REFERENCE_ROOT and os.path.isdir(REFERENCE_ROOT) and (
             force or not os.path.exists(os.path.join(ORACLE, "_ref", "enumerate"))):
         subprocess.run(["sh", os.path.join(ORACLE, "build_ref.sh"), REFERENCE_ROOT],
                        check=True, capture_output=True)

@@ -3,12 +3,12 @@
 # sources, in place, into oracle/_ref/ (git-ignored). Used only as a checker:
 # tests and golden-fixture generation compare against these outputs.
 #
-#   oracle/build_ref.sh [REFERENCE_ROOT]
+#   oracle/build_ref.sh REFERENCE_ROOT
 #
-# REFERENCE_ROOT defaults to /root/reference. Without it, this script exits 0
-# and builds nothing (the GPU machine has no reference tree).
+# REFERENCE_ROOT is the argument, else $PCA_REFERENCE_ROOT. Without a
+# reference tree there, this script exits 0 and builds nothing.
 set -e
-REF=${1:-/root/reference}
+REF=${1:-${PCA_REFERENCE_ROOT:-}}
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
 if [ ! -f "$REF/tools/enumerate.c" ]; then

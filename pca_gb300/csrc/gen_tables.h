@@ -72,6 +72,11 @@ struct GenTables {
     int nvc(int mask) const { return (int)(vc_off[mask + 1] - vc_off[mask]); }
 };
 
+/* Upper bound on the candidates of all 128 masks together (130,144 with the
+   current generator): fixed-size device tables are sized by it, and a CPU
+   test checks the generator stays within it. */
+constexpr uint32_t kMaxTableCandidates = 131072;
+
 /* The ALU ops of an operand-pair entry, by opmask bit. */
 static const uint32_t kPairOps[9] = {PCA_OP_ADD, PCA_OP_SUB, PCA_OP_MUL, PCA_OP_AND, PCA_OP_OR,
                                      PCA_OP_XOR, PCA_OP_SHL, PCA_OP_SHR, PCA_OP_ASR};

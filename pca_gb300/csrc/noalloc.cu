@@ -21,8 +21,10 @@
  *
  * Set-up: the first call on a device (with that device current) resolves the
  * scratch's device address with cudaGetSymbolAddress and uploads the
- * candidate tables with cudaMemcpyToSymbol; later calls on that device reuse
- * them. Make the first call on each device before any stream capture.
+ * candidate tables with cudaMemcpyToSymbol, and loads all three suffix
+ * kernels (CUDA would otherwise load each at its first launch, taking device
+ * memory then); later calls on that device reuse them. Make the first call
+ * on each device before any stream capture.
  *
  * Every call shares the one scratch array, which keeps the last call's
  * contents; each call clears the counters it needs before its kernels run.
@@ -42,7 +44,7 @@
 
 namespace {
 
-constexpr uint32_t kNaMaxCand = 131072;   /* >= all 128 masks' candidates */
+constexpr uint32_t kNaMaxCand = pcagb::kMaxTableCandidates;
 constexpr uint64_t kNaHeader = 4096;      /* counters + root state        */
 constexpr uint64_t kNaMaxRecords =
     (PCAGB_NOALLOC_SCRATCH_BYTES - kNaHeader) / sizeof(ulonglong2);
@@ -205,6 +207,13 @@ int na_setup(int dev, NaPtrs *out)
         err = cudaMemcpyToSymbol(g_na_vc_uop, gt.vc_uop.data(), gt.vc_uop.size() * 4);
     if (err == cudaSuccess) err = cudaMemcpyToSymbol(c_na_cand_off, gt.cand_off.data(), 129 * 4);
     if (err == cudaSuccess) err = cudaMemcpyToSymbol(c_na_vc_off, gt.vc_off.data(), 129 * 4);
+    /* CUDA loads a kernel lazily, at its first launch, and loading takes
+       device memory. Load all three suffix depths here, so that a later call
+       that first reaches a deeper kernel allocates nothing. */
+    cudaFuncAttributes fa;
+    if (err == cudaSuccess) err = cudaFuncGetAttributes(&fa, k_suffix_noalloc<1>);
+    if (err == cudaSuccess) err = cudaFuncGetAttributes(&fa, k_suffix_noalloc<2>);
+    if (err == cudaSuccess) err = cudaFuncGetAttributes(&fa, k_suffix_noalloc<3>);
     if (err != cudaSuccess) {
         na_set_err("no-allocation set-up on device %d failed: %s", dev, cudaGetErrorString(err));
         return PCAGB_ECUDA;

@@ -1,12 +1,12 @@
 """Fixed small workloads, one per kernel family, for profiling under ncu.
 
-    python -m pca_gb300.profile_cases engine_depths   # k_suffix<32, 2/3>, k_leaf
-    python -m pca_gb300.profile_cases suffix_depth2   # one k_suffix<32, 2> depth-4 stage
-    python -m pca_gb300.profile_cases noalloc         # k_suffix_noalloc
-    python -m pca_gb300.profile_cases valuenet        # training and scoring kernels
-    python -m pca_gb300.profile_cases orders          # k_check_perm
-    python -m pca_gb300.profile_cases branch          # branch-mode kernels
-    python -m pca_gb300.profile_cases branch_saturating_add   # the same, two inputs, depth 4
+    python profile_cases.py engine_depths   # k_suffix<32, 2/3>, k_leaf
+    python profile_cases.py suffix_depth2   # one k_suffix<32, 2> depth-4 stage
+    python profile_cases.py noalloc         # k_suffix_noalloc
+    python profile_cases.py valuenet        # training and scoring kernels
+    python profile_cases.py orders          # k_check_perm
+    python profile_cases.py branch          # branch-mode kernels
+    python profile_cases.py branch_saturating_add   # the same, two inputs, depth 4
 
 Each case runs its work `--reps` times (default 2) and prints one timing line
 per repetition (CUDA events); the device memory it holds stays below a few

@@ -15,7 +15,7 @@ their outputs as JSON next to this script:
 
 Task specs are embedded in the fixtures, so tests need no reference tree.
 
-    python tests/golden/make_golden.py [REFERENCE_ROOT]
+    python tests/golden/make_golden.py REFERENCE_ROOT   (or PCA_REFERENCE_ROOT set)
 """
 from __future__ import annotations
 
@@ -36,7 +36,9 @@ sys.path.insert(0, REPO)
 from pca_gb300.pcalib import SearchCtx, SearchState, TaskSpec  # noqa: E402
 from pca_gb300 import taskgen  # noqa: E402
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PCA_REFERENCE_ROOT", "")
+if not REF:
+    sys.exit("usage: make_golden.py REFERENCE_ROOT (or set PCA_REFERENCE_ROOT)")
 REF_BIN = os.path.join(REPO, "oracle", "_ref", "enumerate")
 REF_LIB = os.path.join(REPO, "oracle", "_ref", "libpca.so")
 

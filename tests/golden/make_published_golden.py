@@ -6,7 +6,7 @@ branch mode (README.md:41-51 and the comments of Makefile:66-77): negate,
 double, square 4; add 5; abs, relu 6; max 7; saturating_add 8; is_power2 7.
 The task specs are read from the reference's tasks/*.json.
 
-    python tests/golden/make_published_golden.py [REFERENCE_ROOT]
+    python tests/golden/make_published_golden.py REFERENCE_ROOT   (or PCA_REFERENCE_ROOT set)
 """
 from __future__ import annotations
 
@@ -20,7 +20,9 @@ PUBLISHED = {"negate": 4, "double": 4, "square": 4, "add": 5, "abs": 6, "relu": 
 
 
 def main(ref=None):
-    ref = ref or "/root/reference"
+    ref = ref or os.environ.get("PCA_REFERENCE_ROOT", "")
+    if not ref:
+        sys.exit("usage: make_published_golden.py REFERENCE_ROOT (or set PCA_REFERENCE_ROOT)")
     out = []
     for name, length in PUBLISHED.items():
         task = json.load(open(os.path.join(ref, "tasks", name + ".json")))

@@ -125,7 +125,12 @@ def test_bad_orders_are_refused(engine, kind):
         if kind == "raises":
             raise Boom()
         if kind == "short":
-            return torch.arange(max(n - 1, 0), dtype=torch.int32, device="cuda")
+            # n - 1 entries; the word after them (inside the same allocation,
+            # so an allocation-granular range check cannot see the shortfall)
+            # repeats entry 0, so reading n entries finds a duplicate
+            buf = torch.arange(n + 1, dtype=torch.int32, device="cuda")
+            buf[max(n - 1, 0)] = 0
+            return buf[:max(n - 1, 0)]
         if kind == "float":
             return torch.arange(n, dtype=torch.float32, device="cuda")
         o = torch.arange(n, dtype=torch.int32, device="cuda")

@@ -79,6 +79,19 @@ def test_generator_tables_match_oracle():
         assert L.lib.pcagb_num_candidates(live) == len(O.gen_candidates(live))
 
 
+def test_fixed_device_tables_hold_every_candidate():
+    """The no-allocation solve keeps the candidates of all 128 liveness
+    masks in fixed-size device arrays of kMaxTableCandidates entries: the
+    generator must stay within that bound."""
+    L = PCALib()
+    total = sum(L.lib.pcagb_num_candidates(m << 1) for m in range(128))
+    src = open(os.path.join(REPO, "pca_gb300", "csrc", "gen_tables.h")).read()
+    bound = int(re.search(r"kMaxTableCandidates\s*=\s*(\d+)", src).group(1))
+    assert total <= bound
+    assert "pcagb::kMaxTableCandidates" in open(
+        os.path.join(REPO, "pca_gb300", "csrc", "noalloc.cu")).read()
+
+
 def test_step_matches_oracle_on_random_states():
     """Random register files and flags, every opcode word class."""
     L = PCALib()

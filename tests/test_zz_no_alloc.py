@@ -106,3 +106,40 @@ def test_repeated_call_allocates_no_device_memory(lib):
     torch.cuda.synchronize()
     free1, _ = torch.cuda.mem_get_info()
     assert free1 == free0
+
+
+FRESH_PROCESS = r"""
+import ctypes, sys
+sys.path.insert(0, sys.argv[1])
+from pca_gb300 import taskgen
+from pca_gb300.pcalib import device_memory, load_library
+lib = load_library()
+
+def call(task, depth):
+    opt, total = ctypes.c_int(-9), ctypes.c_uint64(0)
+    rc = lib.pcagb_solve_small_noalloc(ctypes.byref(task), depth, None, ctypes.byref(opt),
+                                       ctypes.byref(total), None, None, 0)
+    assert rc >= 0, lib.pcagb_noalloc_last_error().decode()
+    return opt.value
+
+assert call(taskgen.negate_task(1), 3) == 1       # first call: only the depth-1 kernel runs
+free0, _ = device_memory(0, lib)
+assert call(taskgen.is_power2_task(1), 3) == -1   # depths 1, 2 and 3 all run
+free1, _ = device_memory(0, lib)
+print(free0, free1)
+"""
+
+
+def test_first_shallow_call_then_deeper_call_allocates_nothing():
+    """In a fresh process whose first call is decided at kernel depth 1, a
+    later call that runs the depth-2 and depth-3 kernels for the first time
+    still takes no device memory: the set-up loaded every kernel."""
+    import os
+    import subprocess
+    import sys
+    repo = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, "-c", FRESH_PROCESS, repo], capture_output=True,
+                       text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    free0, free1 = map(int, r.stdout.split()[-2:])
+    assert free1 == free0

@@ -36,9 +36,36 @@ REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, REPO)
 
 METRIC = "verified candidates/s"
-UNIT = "candidates/s"
+UNIT = "candidates decided/s"
 WORKLOAD = ("is_power2, 32 tests, branchless, IDDFS to kernel depth 4 "
             "(program length 7), split depth 3")
+CANDIDATES = ("candidates as the reference's enumerator counts them (tools/enumerate.c:316-402 "
+              "'tried': every generated child of every kept state, at every position); the GPU "
+              "decides the last position's candidates by value classes (evaluations_run_per_s "
+              "counts the class evaluations its kernels execute)")
+
+# The suffix kernel's capture (profiles/k_suffix_is_power2_t32_k4.md): warp
+# instructions of the depth-4 launch, valid for the kernel source it was
+# taken from (SHA-256 of pca_gb300/csrc/engine_kernels.cuh, first 16 hex).
+SUFFIX_CAPTURE = {"inst": 1255101666, "ms": 1.501504, "source_sha16": "6ff4384c1f782676",
+                  "file": "profiles/k_suffix_is_power2_t32_k4.md"}
+# The insert kernel's capture (profiles/k_expand_insert_is_power2_t32_level3.md):
+# DRAM bytes read + written by the level-3 launch (99.6% of a solve's children).
+INSERT_CAPTURE = {"dram_bytes": 558502144 + 170077440, "source_sha16": "6ff4384c1f782676",
+                  "file": "profiles/k_expand_insert_is_power2_t32_level3.md"}
+
+
+def kernel_source_sha16() -> str:
+    import hashlib
+    with open(os.path.join(REPO, "pca_gb300", "csrc", "engine_kernels.cuh"), "rb") as f:
+        return hashlib.sha256(f.read()).hexdigest()[:16]
+
+
+def bench_config(args, world: int) -> dict:
+    """The workload's config, the same dict in both arms."""
+    return {"workload": WORKLOAD, "seed": args.seed, "max_kernel_depth": args.max_depth,
+            "split_depth": args.split, "oep": "exact regs+flags+live",
+            "l2": "flushed between steps (256 MB write)", "parallelism": f"replicas x{world}"}
 
 
 def parse():
@@ -53,6 +80,12 @@ def parse():
     ap.add_argument("--cpu-budget", type=float, default=12.0,
                     help="seconds of CPU work in the cpu_baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-proof", action="store_true",
+                    help="skip the time-to-proven-optimal runs after the timed region")
+    ap.add_argument("--proof-depth", type=int, default=5,
+                    help="kernel depth the headline task's IDDFS continues to after the timing")
+    ap.add_argument("--c3-tasks", type=int, default=100,
+                    help="synthetic tasks scanned for the CPU/GPU time-to-proven comparison")
     ap.add_argument("--hbm-gb", type=float, default=0.0,
                     help="engine arena size in GB (0: 60%% of free HBM)")
     ap.add_argument("--workload", default="power2",
@@ -61,6 +94,8 @@ def parse():
                          "tasks plain vs batched; served: Poisson arrivals, served vs plain; "
                          "guided: value-ordered vs DFS-ordered search")
     ap.add_argument("--rate", type=float, default=50.0, help="served: arrivals per second")
+    ap.add_argument("--sat-rate", type=float, default=1000.0,
+                    help="served: a saturating arrival rate, measured too")
     ap.add_argument("--requests", type=int, default=200, help="served: number of requests")
     ap.add_argument("--tasks", type=int, default=1000, help="batched: number of tasks")
     ap.add_argument("--source", default="synthetic", choices=["synthetic", "reference"],
@@ -148,6 +183,170 @@ def cpu_baseline(task, depth: int, budget: float):
                        f"{n} candidates")}
 
 
+def reference_binary():
+    """The reference's own enumerate, compiled on this machine from its
+    sources by oracle/build_ref.sh (None when it was not built here)."""
+    import platform
+    exe = os.path.join(REPO, "oracle", "_ref", "enumerate")
+    stamp = os.path.join(REPO, "oracle", "_ref", ".machine")
+    if not (os.path.exists(exe) and os.path.exists(stamp)):
+        return None
+    with open(stamp) as f:
+        return exe if f.read().strip() == platform.machine() else None
+
+
+def task_file(task, directory: str, name: str) -> str:
+    """Write a task as the reference's task JSON (tasks/spec.c:80-184)."""
+    n_in = task.num_inputs
+    d = {"name": task.name.decode(), "max_cycles": task.max_cycles,
+         "input_ports": [task.input_ports[i] for i in range(n_in)],
+         "output_ports": [task.output_ports[0]],
+         "tests": [{"in": [task.tests[t].inputs[i] for i in range(n_in)],
+                    "out": [task.tests[t].outputs[0]]} for t in range(task.num_tests)]}
+    path = os.path.join(directory, name + ".json")
+    with open(path, "w") as f:
+        json.dump(d, f)
+    return path
+
+
+def run_reference_binary(exe: str, path: str, depth: int):
+    """(seconds, kernel depth or -1, candidates) of the reference's
+    `enumerate <task> -d depth --no-branch`."""
+    import re
+    t0 = time.perf_counter()
+    out = subprocess.run([exe, path, "-d", str(depth), "--no-branch"], capture_output=True,
+                         text=True, timeout=3600).stdout
+    dt = time.perf_counter() - t0
+    m = re.search(r"kernel depth (\d+)\)", out)
+    cands = sum(int(x) for x in re.findall(r"  candidates: (\d+) ", out))
+    return dt, int(m.group(1)) if m else -1, cands
+
+
+def insert_roofline(sol, T: int, insert_ms: float, hbm_gbs: float, pk_kind: str) -> dict:
+    """k_expand_insert against HBM. Algorithmic bytes of a level build (the
+    OEP kernel's unit of work): per child an 8-byte slot probe, per child
+    that is not a new state a 17*T-byte compare of the state it equals, per
+    parent a 17*T-byte read of its state. Summed over the solve's builds
+    (levels 1..split) and divided by the insert launches' device time."""
+    S = len(sol.level_survivors) - 1
+    byts = 0
+    for d in range(1, S + 1):
+        kids, kept, parents = sol.level_children[d], sol.level_survivors[d], sol.level_survivors[d - 1]
+        if kids == 0:
+            continue
+        byts += kids * 8 + (kids - kept) * 17 * T + parents * 17 * T
+    achieved = byts / (insert_ms / 1000.0) / 1e9 if insert_ms > 0 else 0.0
+    fresh = kernel_source_sha16() == INSERT_CAPTURE["source_sha16"]
+    return {"kernel": "k_expand_insert<32> (exact OEP insert of levels 1..3)", "bound": "hbm",
+            "achieved": achieved, "peak": hbm_gbs, "unit": "GB/s", "frac": achieved / hbm_gbs,
+            "traffic": INSERT_CAPTURE["dram_bytes"] if fresh else None,
+            "algorithmic_bytes_per_solve": byts, "insert_ms_per_solve": insert_ms,
+            "peak_source": f"hbm_gbs of MEASURED_PEAKS.json ({pk_kind}); frac of measured",
+            "traffic_note": ("DRAM bytes of the level-3 launch from one ncu capture "
+                             f"({INSERT_CAPTURE['file']}); null when the kernel source changed "
+                             "since that capture"),
+            "bytes_model": "per child 8 B slot + per duplicate 17*T B compare + per parent 17*T B"}
+
+
+def suffix_roofline(suffix_ms: float, peak_issue: float, evals_run_per_s: float) -> dict:
+    """k_suffix<32,1> against the integer-issue roofline (one warp
+    instruction per SM sub-partition per clock): the warp instructions of its
+    ncu capture over the live launch time, valid while the kernel source is
+    the captured one."""
+    fresh = kernel_source_sha16() == SUFFIX_CAPTURE["source_sha16"]
+    out = {"kernel": "k_suffix<32,1> (last instruction over value classes)",
+           "bound": "int_issue", "unit": "Gwarp-inst/s", "peak": peak_issue / 1e9,
+           "evaluations_run_per_s": evals_run_per_s, "ncu": SUFFIX_CAPTURE["file"]}
+    if fresh and suffix_ms > 0:
+        ach = SUFFIX_CAPTURE["inst"] / (suffix_ms / 1000.0)
+        out.update({"achieved": ach / 1e9, "frac": ach / peak_issue,
+                    "frac_in_capture": SUFFIX_CAPTURE["inst"] / (SUFFIX_CAPTURE["ms"] / 1000.0)
+                    / peak_issue})
+    else:
+        out.update({"achieved": None, "frac": None,
+                    "note": "kernel source changed since the capture: no instruction count"})
+    return out
+
+
+def proof_and_time_to_optimal(eng, task, args) -> dict:
+    """Time to a proven optimum, outside the timed region.
+
+    is_power2_full: the headline task's IDDFS continued past kernel depth 4
+    (up to --proof-depth), split 3: the proven optimal depth and program.
+    is_power2_k3 / synthetic_k3: configurations the CPU finishes, timed on
+    both sides: the headline task to kernel depth 3, and the synthetic tasks
+    of the batched workload whose optimum is within kernel depth 3, on the
+    GPU (one at a time and batched) and by the reference algorithm on every
+    host core (one task per core; the oracle port of tools/enumerate.c, and
+    the reference's own enumerate where it was compiled here)."""
+    import concurrent.futures as cf
+    import tempfile
+    from oracle import oracle as O
+    from pca_gb300 import taskgen
+    out = {}
+    cores = os.cpu_count() or 1
+    if args.proof_depth > args.max_depth:
+        t0 = time.perf_counter()
+        s = eng.solve(task, max_depth=args.proof_depth, split_depth=args.split, sol_cap=64)
+        dt = time.perf_counter() - t0
+        out["is_power2_full"] = {
+            "max_kernel_depth": args.proof_depth, "optimal_depth": s.optimal_depth,
+            "program_length": s.optimal_depth + task.num_inputs + 2 if s.optimal_depth >= 0 else None,
+            "first_program": s.programs[0] if s.programs else None,
+            "programs_at_optimal": s.total_solutions, "seconds": dt,
+            "gpu_ms_suffix": s.gpu_ms_suffix, "evaluations_run": s.evaluations_run,
+            "candidates_decided": int(sum(s.candidates))}
+    # the headline task to kernel depth 3
+    gpu = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        g = eng.solve(task, max_depth=3, split_depth=args.split, sol_cap=16)
+        gpu.append(time.perf_counter() - t0)
+    port_s = 0.0
+    for K in (2, 3):
+        _, secs, _ = O.sample_throughput(task, K, cores, 1e9)
+        port_s += secs
+    row = {"gpu_s": statistics.median(gpu), "gpu_optimal_depth": g.optimal_depth,
+           "cpu_port_all_cores_s": port_s, "cores": cores}
+    exe = reference_binary()
+    with tempfile.TemporaryDirectory() as tmp:
+        if exe:
+            dt, k, _ = run_reference_binary(exe, task_file(task, tmp, "is_power2"), 3)
+            row.update({"cpu_reference_1_core_s": dt, "cpu_reference_optimal_depth": k})
+        out["is_power2_k3"] = row
+        if args.c3_tasks <= 0:
+            return out
+        tasks = taskgen.synthetic_batch(args.c3_tasks, seed=7)
+        first = eng.solve_batch(tasks, max_depth=3, first_only=True, sol_cap=1)
+        sel = [t for t, r in zip(tasks, first) if r.optimal_depth >= 0]
+        t0 = time.perf_counter()
+        plain = [eng.solve(t, max_depth=3, first_only=True, sol_cap=1) for t in sel]
+        t_plain = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        batch = eng.solve_batch(sel, max_depth=3, first_only=True, sol_cap=1)
+        t_batch = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        with cf.ThreadPoolExecutor(cores) as ex:
+            port = list(ex.map(lambda t: O.enumerate_task(t, 3, O.REF32)[0].optimal_depth, sel))
+        t_port = time.perf_counter() - t0
+        row = {"tasks": len(sel), "of": len(tasks), "gpu_plain_s": t_plain, "gpu_batched_s": t_batch,
+               "cpu_port_s": t_port, "cores": cores,
+               "depth_histogram": {str(k): sum(1 for r in batch if r.optimal_depth == k)
+                                   for k in range(4)},
+               "same_optimal_depth_port": sum(a.optimal_depth == b == c.optimal_depth
+                                              for a, b, c in zip(plain, port, batch))}
+        if exe:
+            paths = [task_file(t, tmp, f"c3_{i}") for i, t in enumerate(sel)]
+            t0 = time.perf_counter()
+            with cf.ThreadPoolExecutor(cores) as ex:
+                ref = list(ex.map(lambda p: run_reference_binary(exe, p, 3)[1], paths))
+            row["cpu_reference_s"] = time.perf_counter() - t0
+            row["same_optimal_depth_reference"] = sum(a.optimal_depth == b
+                                                      for a, b in zip(plain, ref))
+        out["synthetic_k3"] = row
+    return out
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -168,32 +367,67 @@ def reduce_over_ranks(t_dev: float, t_wall: float, cands: float, device) -> tupl
 
 
 def run_reference(args):
-    """Reference arm: the reference's CPU solver algorithm on the host cores."""
+    """Reference arm: the reference's CPU solver on every host core.
+
+    With the reference's own enumerate compiled on this machine (oracle/
+    build_ref.sh, from the sources staged in baseline/_ref), a step runs it
+    as one process per host core, each through the first passes of the
+    workload's iterative deepening (kernel depths 0..3 of the same task, the
+    passes that precede depth 4; the reference is single-threaded), and the
+    value is the candidates its counters report per second of wall time.
+    Otherwise the oracle's port of its algorithm samples the depth-4 pass on
+    every core for a bounded time per step."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
+    import concurrent.futures as cf
+    import tempfile
     from pca_gb300 import taskgen
     from oracle.build import build_oracle
     build_oracle()
     task = taskgen.is_power2_task(args.seed)
-    per_step = max(2.0, min(10.0, 150.0 / max(1, args.steps + args.warmup)))
-    from oracle import oracle as O
     cores = os.cpu_count() or 1
-    for _ in range(args.warmup):
-        O.sample_throughput(task, args.max_depth, cores, per_step)
+    exe = reference_binary()
     tot_n, tot_s = 0, 0.0
-    for _ in range(args.steps):
-        n, s, _ = O.sample_throughput(task, args.max_depth, cores, per_step)
-        tot_n += n
-        tot_s += s
+    if exe:
+        with tempfile.TemporaryDirectory() as tmp:
+            path = task_file(task, tmp, "is_power2")
+
+            def step():
+                t0 = time.perf_counter()
+                with cf.ThreadPoolExecutor(cores) as ex:
+                    runs = list(ex.map(lambda _: run_reference_binary(exe, path, 3), range(cores)))
+                return sum(r[2] for r in runs), time.perf_counter() - t0
+
+            for _ in range(args.warmup):
+                step()
+            for _ in range(args.steps):
+                n, s = step()
+                tot_n += n
+                tot_s += s
+        kind = "reference"
+        sample = (f"the reference's enumerate (compiled on this host) solving the workload's "
+                  f"task to kernel depth 3 (the IDDFS passes before depth 4), {cores} processes "
+                  f"at once per step")
+    else:
+        from oracle import oracle as O
+        per_step = max(2.0, min(10.0, 150.0 / max(1, args.steps + args.warmup)))
+        for _ in range(args.warmup):
+            O.sample_throughput(task, args.max_depth, cores, per_step)
+        for _ in range(args.steps):
+            n, s, _ = O.sample_throughput(task, args.max_depth, cores, per_step)
+            tot_n += n
+            tot_s += s
+        kind = "port"
+        sample = (f"kernel depth {args.max_depth} DFS of the workload over (root, level-1) "
+                  f"candidate pairs, {per_step:.0f} s per step on {cores} threads")
     v = tot_n / tot_s
-    sample = (f"kernel depth {args.max_depth} DFS of the workload over (root, level-1) candidate "
-              f"pairs, {per_step:.0f} s per step on {cores} threads")
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * tot_s / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u16",
-            "data": "synthetic", "config": {"workload": WORKLOAD, "seed": args.seed},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+            "data": "synthetic", "config": bench_config(args, world),
+            "candidates": CANDIDATES,
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": kind,
                              "sample": sample},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -269,30 +503,43 @@ def run_batched(args):
 
 def run_served(args):
     """Poisson arrivals of synthetic tasks (source length mix 4:30%, 5:30%,
-    6:25%, 7:10%, 8:5%), each proven optimal up to kernel depth 4: the
-    continuous-batching server vs one task at a time."""
+    6:25%, 7:10%, 8:5%), each proven optimal up to kernel depth 4, at the
+    configured rate and at a saturating one: the native server (admission by
+    free HBM, concurrent solves on their own streams, queued requests
+    batched), the slot server (fixed engines, one batch per slot) and one
+    task at a time."""
     from pca_gb300 import taskgen
-    from pca_gb300.serve import SerialServer, Server, latency_summary, replay
-    trace = taskgen.poisson_stream(args.requests, rate=args.rate, seed=11)
+    from pca_gb300.serve import NativeServer, SerialServer, Server, latency_summary, replay
+    makers = (("native", lambda: NativeServer(workers=8, max_batch=64, max_depth=4)),
+              ("slots", lambda: Server(slots=4, max_batch=256, max_depth=4)),
+              ("plain", lambda: SerialServer(max_depth=4)))
     out = {}
-    for name, make in (("served", lambda: Server(slots=4, max_batch=256, max_depth=4)),
-                       ("plain", lambda: SerialServer(max_depth=4))):
-        srv = make()
-        replay(srv, trace[:20])  # warm-up
-        srv.close()
-        srv = make()
-        reqs = replay(srv, trace)
-        srv.close()
-        out[name] = latency_summary(reqs)
-        out[name]["batches"] = len(srv.batches)
-    s, p = out["served"], out["plain"]
+    for rate in (args.rate, args.sat_rate):
+        trace = taskgen.poisson_stream(args.requests, rate=rate, seed=11)
+        row = {}
+        for name, make in makers:
+            srv = make()
+            replay(srv, trace[:20])  # warm-up
+            srv.close()
+            srv = make()
+            reqs = replay(srv, trace)
+            srv.close()
+            row[name] = latency_summary(reqs)
+            row[name]["solves"] = len(srv.batches)
+        for name in ("native", "slots"):
+            row[name]["p99_ratio_plain_over_this"] = (row["plain"]["p99_s"] / row[name]["p99_s"]
+                                                      if row[name]["p99_s"] else None)
+            row[name]["p50_ratio_plain_over_this"] = (row["plain"]["p50_s"] / row[name]["p50_s"]
+                                                      if row[name]["p50_s"] else None)
+        out[f"{rate:g}_req_per_s"] = row
+    s = out[f"{args.rate:g}_req_per_s"]["native"]
     line = {"metric": "p99 time-to-proven-optimal (served)", "value": s["p99_s"], "unit": "s",
             "higher_is_better": False, "n_gpus": 1, "data": "synthetic",
-            "config": {"workload": f"Poisson {args.rate:g} req/s, {args.requests} requests, "
-                                   "source length mix 4-8, kernel depth <= 4, 4 engine slots"},
-            "served": s, "plain": p,
-            "p99_ratio_plain_over_served": p["p99_s"] / s["p99_s"] if s["p99_s"] else None,
-            "p50_ratio_plain_over_served": p["p50_s"] / s["p50_s"] if s["p50_s"] else None}
+            "config": {"workload": f"Poisson {args.rate:g} req/s (and {args.sat_rate:g} req/s), "
+                                   f"{args.requests} requests, source length mix 4-8, kernel "
+                                   "depth <= 4; native: 8 workers, 1 GiB arenas from an 80% "
+                                   "pool, batches of up to 64; slots: 4 engines"},
+            "rates": out}
     print(json.dumps(line), flush=True)
 
 
@@ -447,7 +694,7 @@ def main():
         dist.barrier()
     sampler = ClockSampler(local)
     sampler.start()
-    dev_ms, wall_s, cands, evals = [], [], 0, 0
+    dev_ms, wall_s, cands, evals, evals_run = [], [], 0, 0, 0
     launches, h2d, d2h = 0, 0, 0
     insert_ms, insert_n, insert_children, suffix_ms, suffix_n = 0.0, 0, 0, 0.0, 0
     expand_ms = 0.0
@@ -467,6 +714,7 @@ def main():
         wall_s.append(t1 - t0)
         cands += sum(sol.candidates)
         evals += sum(sol.evaluations)
+        evals_run += sol.evaluations_run
         launches += sol.kernel_launches
         h2d += sol.h2d_bytes
         d2h += sol.d2h_bytes
@@ -492,21 +740,21 @@ def main():
     pk, pk_kind = peaks()
     sm_max = pk.get("sm_max_mhz", 2070.0)
     sms = torch.cuda.get_device_properties(local).multi_processor_count
-    # suffix kernel: value classes evaluated per second against the issue
-    # roofline (one warp instruction per SM sub-partition per clock)
-    suffix_evals_per_s = evals / (suffix_ms / 1000.0) if suffix_ms > 0 else 0.0
+    peak_issue = sms * 4 * sm_max * 1e6
+    evals_run_per_s = evals_run / (suffix_ms / 1000.0) if suffix_ms > 0 else 0.0
     line = {
         "metric": METRIC, "value": total_cands / t_dev, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": max(3, args.warmup),
         "ms_per_step": 1000.0 * t_dev / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u16", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "seed": args.seed, "max_kernel_depth": args.max_depth,
-                   "split_depth": args.split, "oep": "exact regs+flags+live",
-                   "l2": "flushed between steps (256 MB write)",
-                   "parallelism": f"replicas x{world}"},
+        "config": bench_config(args, world),
+        "candidates": CANDIDATES,
         "optimal_depth": sol.optimal_depth if sol else None,
         "candidates_per_step": cands // args.steps,
         "evaluations_per_step": evals // args.steps,
+        "evaluations_run_per_step": evals_run // args.steps,
+        "evaluations_per_s": evals / t_dev,
+        "evaluations_run_per_s": evals_run / t_dev,
         "e2e": {"value": total_cands / t_wall, "unit": UNIT,
                 "h2d_bytes_per_step": h2d // args.steps, "d2h_bytes_per_step": d2h // args.steps},
         "gpu_launches": launches,
@@ -517,28 +765,17 @@ def main():
         "launches_per_step": {"insert": insert_n / args.steps, "suffix": suffix_n / args.steps},
         "children_inserted_per_step": insert_children // args.steps,
     }
-    # Roofline of the suffix kernel: integer-issue bound. Peak = one warp
-    # instruction per SM sub-partition per clock at the measured max clock.
-    # Achieved = this run's value-class evaluations of the full candidate
-    # space per second of suffix-kernel time x the kernel's warp instructions
-    # per such evaluation, measured by ncu (profiles/k_suffix_is_power2_t32_k4.md:
-    # 1.26e9 instructions for the depth-4 launch, whose full space is 7.30e8
-    # evaluations; the kernel scans only the classes that can solve).
-    inst_per_eval = 1255101666 / 7.30e8
-    peak_issue = sms * 4 * sm_max * 1e6
-    achieved_issue = suffix_evals_per_s * inst_per_eval
-    line["roofline"] = {
-        "kernel": "k_suffix<32,1> (last instruction over value classes)",
-        "bound": "int_issue", "unit": "Gwarp-inst/s",
-        "achieved": achieved_issue / 1e9, "peak": peak_issue / 1e9,
-        "frac": achieved_issue / peak_issue,
-        "traffic": 2735377000 + 3757056,
-        "evaluations_per_s": suffix_evals_per_s,
-        "peak_source": f"{sms} SMs x 4 issue slots x sm_max_mhz from MEASURED_PEAKS.json ({pk_kind})",
-        "ncu": "profiles/k_suffix_is_power2_t32_k4.md",
-    }
+    # the dominant kernel (k_expand_insert, the exact OEP table) against HBM,
+    # and the suffix kernel against integer issue
+    line["roofline"] = insert_roofline(sol, task.num_tests, insert_ms / args.steps,
+                                       pk["hbm_gbs"], pk_kind)
+    line["roofline_suffix"] = suffix_roofline(suffix_ms / args.steps, peak_issue, evals_run_per_s)
+    line["roofline_suffix"]["peak_source"] = (f"{sms} SMs x 4 issue slots x sm_max_mhz of "
+                                              f"MEASURED_PEAKS.json ({pk_kind})")
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(task, args.max_depth, args.cpu_budget)
+    if not args.no_proof:
+        line["time_to_proven_optimal"] = proof_and_time_to_optimal(eng, task, args)
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()

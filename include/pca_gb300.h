@@ -188,7 +188,17 @@ typedef struct {
                            engine's autotuner (the answer does not depend on
                            it). 0: every program found at the optimal depth
                            from the deepest level that fits                  */
-    int reserved[6];
+    /* Launch choices of the suffix stages; 0 = chosen by the autotuner
+       from costs it measures. None changes an answer.                       */
+    int first_tests;    /* 1..3: tests a lane checks a value class on before
+                           the warp checks its survivors on every test       */
+    int suffix_chunk;   /* 1..64: first suffix instructions per work item of
+                           the depth-2 and depth-3 suffix kernels            */
+    int stage_launch;   /* first-only solves of one task: -1 = one launch per
+                           stage; n > 0 = a first launch of n prefixes in DFS
+                           order, doubling, stopping at the first launch that
+                           holds a solution                                  */
+    int reserved[3];
 } pcagb_opts_t;
 
 #define PCAGB_MAXD 17
@@ -222,7 +232,11 @@ typedef struct {
     uint64_t prefixes_at_optimal;
     uint64_t prefixes_to_first;
     double   ms_to_first;
-    int      reserved[2];
+    uint64_t evaluations_run;          /* value-class evaluations the suffix
+                                          kernels executed (a class of an
+                                          operand pair counts one); below
+                                          `evaluations`, which counts every
+                                          class of the candidate space       */
 } pcagb_result_t;
 
 const char *pcagb_last_error(void);
@@ -362,6 +376,26 @@ const char *pcagb_branch_last_error(void);
  * caller can time a solve with events on that stream. */
 void *pcagb_engine_stream(pcagb_engine_t *e);
 
+/* The autotuner's measured costs on this engine's device: device ms per
+ * value-class evaluation of each suffix depth (t_eval_ms) and per child of a
+ * level build, and for each suffix depth s the cost of each launch choice
+ * (first_tests 1..3 at [s][1..3], middle chunk choice c at [s][c] with
+ * chunk_choices[s][c] first instructions per work item) with the number of
+ * stages it was measured on; the host round trip of a chunked launch. */
+typedef struct {
+    double   t_eval_ms[4];
+    double   t_child_ms;
+    double   t_build_fixed_ms;
+    double   dedup_ratio;
+    double   first_tests_ms[4][4];
+    int      first_tests_n[4][4];
+    double   chunk_ms[4][4];
+    int      chunk_n[4][4];
+    uint32_t chunk_choices[4][4];
+    double   launch_rt_ms;
+} pcagb_tuning_t;
+int  pcagb_tuning(pcagb_engine_t *e, pcagb_tuning_t *out);
+
 /* Free and total device memory, for sizing engines (a server admits work by
  * free HBM). */
 int  pcagb_device_memory(int device, size_t *free_bytes, size_t *total_bytes);
@@ -392,6 +426,62 @@ int  pcagb_solve_small_noalloc(const task_spec_t *task, int max_depth, void *str
                                int *optimal_depth, uint64_t *total_solutions,
                                uint16_t *sol_progs, int *sol_lens, int sol_cap);
 const char *pcagb_noalloc_last_error(void);
+
+/* ---------------- Part 3: serving ---------------------------------------- */
+
+/* A solve server on one GPU (server.cu). The reference solves one task per
+ * process run (tools/enumerate.c, gpu/hybrid.cu:631-836) and has no serving
+ * loop; these entry points are what a request loop around that solver would
+ * bind. Requests of any input count, test count and depth are submitted as
+ * they arrive; a request is admitted as soon as a worker is idle and the
+ * device pool holds an arena slice for it (admission by free HBM, in
+ * arrival order), solves run concurrently on their own CUDA streams, queued
+ * requests found together share one batched solve, and each answer is
+ * stored the moment its task is decided. Every wait is on the host, with a
+ * timeout. */
+typedef struct pcagb_server pcagb_server_t;
+
+typedef struct {
+    int      device;
+    size_t   pool_bytes;   /* device pool for all solves; 0 = 80% of free memory */
+    size_t   arena_bytes;  /* the slice one solve reserves (a batch: up to four) */
+    int      workers;      /* solves that may run at once, each on its stream */
+    int      max_batch;    /* queued requests one solve may take together */
+    int      sol_cap;      /* programs kept per request */
+    pcagb_opts_t opts;     /* solve options (default: first_only) */
+} pcagb_server_config_t;
+
+typedef struct {
+    uint64_t queued;
+    uint64_t running_solves;
+    uint64_t max_running_solves;
+    uint64_t admitted;
+    uint64_t finished;
+    uint64_t batches;            /* solves run (a solve takes one or more requests) */
+    uint64_t pool_bytes;
+    uint64_t pool_used;
+    uint64_t pool_peak;
+    uint64_t pool_largest_free;
+} pcagb_server_stats_t;
+
+void pcagb_server_default_config(pcagb_server_config_t *cfg);
+int  pcagb_server_create(const pcagb_server_config_t *cfg, pcagb_server_t **out);
+/* Queue a solve of the task up to kernel depth max_depth; *id names it. */
+int  pcagb_server_submit(pcagb_server_t *s, const task_spec_t *task, int max_depth,
+                         uint64_t *id);
+/* The next finished request, in the order requests finish: 1 and *id, or 0
+ * when none finishes within timeout_s seconds. */
+int  pcagb_server_next(pcagb_server_t *s, double timeout_s, uint64_t *id);
+/* A finished request's result and first `cap` programs (then forgotten);
+ * times[0..3] = submitted, admitted, finished (seconds since the server
+ * started) and the number of requests its solve took. Returns 0, or the
+ * solve's error code (PCAGB_ENOMEM when the pool cannot hold one arena). */
+int  pcagb_server_collect(pcagb_server_t *s, uint64_t id, pcagb_result_t *res,
+                          uint16_t *sol_progs, int *sol_lens, int cap, double *times);
+int  pcagb_server_stats(pcagb_server_t *s, pcagb_server_stats_t *stats);
+/* Takes no new requests, solves the queued ones, then frees everything. */
+void pcagb_server_destroy(pcagb_server_t *s);
+const char *pcagb_server_last_error(void);
 
 #ifdef __cplusplus
 }

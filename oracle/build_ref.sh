@@ -25,4 +25,5 @@ gcc $CFLAGS -shared -fPIC -o "$OUT/libpca.so" \
 gcc $CFLAGS -o "$OUT/gen_tasks" \
     "$REF/src/vm.c" "$REF/src/asm.c" "$REF/src/search_state.c" \
     "$REF/tasks/spec.c" "$REF/tools/gen_tasks.c"
+uname -m > "$OUT/.machine"
 echo "build_ref: built $OUT/enumerate $OUT/libpca.so $OUT/gen_tasks"

@@ -47,6 +47,10 @@ def lib():
         L.orc_enumerate.argtypes = [P(TaskSpec), ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                     P(ctypes.c_uint16), P(ctypes.c_int), P(OrcResult)]
         L.orc_enumerate.restype = ctypes.c_int
+        L.orc_enumerate_split.argtypes = [P(TaskSpec), ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                          ctypes.c_int, ctypes.c_int, P(ctypes.c_uint16),
+                                          P(ctypes.c_int), P(OrcResult)]
+        L.orc_enumerate_split.restype = ctypes.c_int
         L.orc_enumerate_branch.argtypes = [P(TaskSpec), ctypes.c_int, ctypes.c_int,
                                            P(ctypes.c_uint16), P(ctypes.c_int), P(OrcResult)]
         L.orc_enumerate_branch.restype = ctypes.c_int
@@ -87,6 +91,26 @@ def enumerate_task(task, max_depth: int, mode: int = REF32, sol_cap: int = -1):
     if L.orc_enumerate(ctypes.byref(task), max_depth, mode, sol_cap, progs, lens,
                        ctypes.byref(r)) != 0:
         raise RuntimeError("oracle rejected the task")
+    out = [[progs[i * 16 + j] for j in range(lens[i])] for i in range(r.num_solutions)]
+    return r, out
+
+
+def enumerate_split(task, max_depth: int, split: int, mode: int = EXACT_LIVE,
+                    threads: int = 0, sol_cap: int = 1 << 16):
+    """Level-synchronous form of the IDDFS (oracle_levels.c): positions
+    1..min(K-1, split) deduplicated under `mode`, the rest enumerated without
+    pruning; every solving program at the first K with one is counted and the
+    first sol_cap are returned in depth-first order. threads = 0: every host
+    core. Returns (OrcResult, [programs])."""
+    L = lib()
+    n = max(sol_cap, 1)
+    progs = (ctypes.c_uint16 * (16 * n))()
+    lens = (ctypes.c_int * n)()
+    r = OrcResult()
+    nthreads = threads or (os.cpu_count() or 1)
+    if L.orc_enumerate_split(ctypes.byref(task), max_depth, split, mode, nthreads, sol_cap,
+                             progs, lens, ctypes.byref(r)) != 0:
+        raise RuntimeError("oracle rejected the task or ran out of host memory")
     out = [[progs[i * 16 + j] for j in range(lens[i])] for i in range(r.num_solutions)]
     return r, out
 

@@ -134,6 +134,20 @@ uint64_t orc_enumerate_sample(const orc_task_t *task, int depth, int nthreads,
                               double budget_s, double *seconds,
                               uint64_t *solutions);
 
+/* Level-synchronous, multi-threaded form of the branchless IDDFS
+ * (oracle_levels.c): for each K = 0..max_depth, the kept states of
+ * positions 1..S (S = min(K-1, split)) under oep_mode (NONE, EXACT or
+ * EXACT_LIVE; the first child in the reference's depth-first order keeps a
+ * key) and positions S+1..K without pruning; stops at the first K with a
+ * solution. Every solving (kernel, output register) at that K is counted in
+ * total_solutions and the first sol_cap are stored in depth-first order.
+ * tried[K] counts every generated child of positions 1..K; survivors and
+ * children hold levels 0..S. Returns 0, or -1 on bad arguments or when host
+ * memory runs out. */
+int  orc_enumerate_split(const orc_task_t *task, int max_depth, int split, int oep_mode,
+                         int nthreads, int sol_cap, uint16_t *sol_progs, int *sol_lens,
+                         orc_result_t *res);
+
 #ifdef __cplusplus
 }
 #endif

@@ -23,7 +23,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall"]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-Wextra"]
 
-CU_SOURCES = ["engine.cu", "noalloc.cu", "valuenet.cu", "valuenet_tc.cu", "branch.cu"]
+CU_SOURCES = ["engine.cu", "noalloc.cu", "valuenet.cu", "valuenet_tc.cu", "branch.cu", "server.cu"]
 CXX_SOURCES = ["host_abi.cpp"]
 CLI_SOURCES = {"enumerate": "cli_enumerate.cpp", "gpu_hybrid": "cli_gpu_hybrid.cpp"}
 

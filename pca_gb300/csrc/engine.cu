@@ -64,6 +64,8 @@ static void set_err(const char *fmt, ...)
     } while (0)
 
 constexpr int kMaxBatch = 8192;
+/* engine_init's budget for an engine whose arena each solve supplies */
+constexpr size_t kArenaExternal = ~size_t(0);
 /* slots of the pinned host buffer */
 constexpr int kPinStatus = 0, kPinSurvivors = 1, kPinTotal = 2, kPinCount = 3, kPinFirst = 4,
               kPinHist = 64;
@@ -84,6 +86,7 @@ struct Level {
     uint16_t *cidx = nullptr;
     uint8_t *rdl = nullptr;         /* register each state's last instruction wrote */
     uint8_t *own = nullptr;         /* dead-able older writes (engine_kernels.cuh) */
+    uint8_t *twin = nullptr;        /* later member of a flag-twin class (k_twins) */
     uint32_t *fcr = nullptr;        /* [n][8] rank of the first kept child writing r (set
                                        when the level below is materialised) */
     uint64_t *child_off = nullptr;  /* set when this level is expanded */
@@ -122,7 +125,8 @@ struct pcagb_engine {
     cudaStream_t stream = nullptr;
     char *arena = nullptr;
     size_t cap = 0, bottom = 0, top = 0;
-    unsigned long long *d_small = nullptr;   /* [0] sol count [1] first [2] count */
+    unsigned long long *d_small = nullptr;   /* [0] sol count [1] first [2] count
+                                                [3] value-class evaluations run */
     uint32_t *d_status = nullptr;
     ulonglong2 *d_sol = nullptr;
     uint64_t sol_cap = 1u << 20;
@@ -141,6 +145,7 @@ struct pcagb_engine {
     uint64_t launches = 0;
     uint64_t h2d = 0, d2h = 0;
     uint64_t insert_launches = 0, suffix_launches = 0, insert_children = 0;
+    uint64_t evals_run = 0;                  /* value-class evaluations the suffix kernels ran */
     float ms_insert = 0;
     /* autotuner: unit costs measured on this engine (running averages) */
     /* starting values: this engine's costs measured on a GB300 (one- and
@@ -150,6 +155,14 @@ struct pcagb_engine {
     double t_eval_ms[4] = {0, 1.8e-9, 1.4e-9, 1.3e-9};  /* device ms per value-class
                                                            evaluation, per suffix depth */
     double dedup_ratio = 0.35;      /* survivors / children of the last build */
+    /* launch choices of the suffix stages, with their measured costs (ms
+       per value-class evaluation, running averages; n = stages measured) */
+    double ft_ms[4][4] = {};        /* [suffix depth][tests checked per lane] */
+    int ft_n[4][4] = {};
+    double ck_ms[4][4] = {};        /* [suffix depth][index into kChunkChoices] */
+    int ck_n[4][4] = {};
+    double launch_rt_ms = 0.03;     /* host round trip of one launch of a chunked stage */
+    int force_ft = 0, force_chunk = 0;   /* per solve: pcagb_opts_t overrides */
 
     /* per batch */
     std::vector<Level> levels;
@@ -186,6 +199,8 @@ namespace {
 struct CostModel {
     bool set = false;
     double t_child_ms = 0, t_build_fixed_ms = 0, t_eval_ms[4] = {0, 0, 0, 0}, dedup_ratio = 0;
+    double ft_ms[4][4] = {}, ck_ms[4][4] = {}, launch_rt_ms = 0.03;
+    int ft_n[4][4] = {}, ck_n[4][4] = {};
 };
 std::mutex g_cost_mu;
 CostModel g_cost[64];
@@ -199,6 +214,11 @@ void load_costs(pcagb_engine *e)
     e->t_build_fixed_ms = c.t_build_fixed_ms;
     for (int i = 0; i < 4; i++) e->t_eval_ms[i] = c.t_eval_ms[i];
     e->dedup_ratio = c.dedup_ratio;
+    memcpy(e->ft_ms, c.ft_ms, sizeof c.ft_ms);
+    memcpy(e->ft_n, c.ft_n, sizeof c.ft_n);
+    memcpy(e->ck_ms, c.ck_ms, sizeof c.ck_ms);
+    memcpy(e->ck_n, c.ck_n, sizeof c.ck_n);
+    e->launch_rt_ms = c.launch_rt_ms;
 }
 
 void store_costs(const pcagb_engine *e)
@@ -210,6 +230,11 @@ void store_costs(const pcagb_engine *e)
     c.t_build_fixed_ms = e->t_build_fixed_ms;
     for (int i = 0; i < 4; i++) c.t_eval_ms[i] = e->t_eval_ms[i];
     c.dedup_ratio = e->dedup_ratio;
+    memcpy(c.ft_ms, e->ft_ms, sizeof c.ft_ms);
+    memcpy(c.ft_n, e->ft_n, sizeof c.ft_n);
+    memcpy(c.ck_ms, e->ck_ms, sizeof c.ck_ms);
+    memcpy(c.ck_n, e->ck_n, sizeof c.ck_n);
+    c.launch_rt_ms = e->launch_rt_ms;
     c.set = true;
 }
 
@@ -269,7 +294,8 @@ int exclusive_scan(pcagb_engine *e, uint64_t *a, uint64_t n, uint64_t *total)
 
 LevelDev view(const Level &L)
 {
-    return LevelDev{L.regs, L.flags, L.live, L.task, L.child_off, L.n, L.rdl, L.parent, L.own};
+    return LevelDev{L.regs, L.flags, L.live, L.task, L.child_off, L.n, L.rdl, L.parent, L.own,
+                    L.twin};
 }
 
 int alloc_level(pcagb_engine *e, Level &L, uint64_t n)
@@ -283,7 +309,9 @@ int alloc_level(pcagb_engine *e, Level &L, uint64_t n)
     L.cidx = (uint16_t *)e->alloc_bottom(n * 2);
     L.rdl = (uint8_t *)e->alloc_bottom(n);
     L.own = (uint8_t *)e->alloc_bottom(n);
-    if (!L.regs || !L.flags || !L.live || !L.task || !L.parent || !L.cidx || !L.rdl || !L.own)
+    L.twin = (uint8_t *)e->alloc_bottom(n);
+    if (!L.regs || !L.flags || !L.live || !L.task || !L.parent || !L.cidx || !L.rdl || !L.own ||
+        !L.twin)
         return PCAGB_ENOMEM;
     return PCAGB_OK;
 }
@@ -394,7 +422,7 @@ int build_level(pcagb_engine *e, int d)
     const uint64_t children = P.children;
     if (children >= (1ull << 38)) return fail(PCAGB_ENOMEM);
     const uint64_t words = (children + 31) / 32;
-    const uint64_t state_bytes = 8ull * 2 * e->TPC + e->TPC + 1 + 2 + 4 + 2 + 1 + 1;
+    const uint64_t state_bytes = 8ull * 2 * e->TPC + e->TPC + 1 + 2 + 4 + 2 + 1 + 1 + 1;
     const bool one_sync = children * state_bytes <= kOneSyncBytes;
 
     cudaEventRecord(e->ev0, e->stream);
@@ -407,6 +435,27 @@ int build_level(pcagb_engine *e, int d)
         if (rc) return rc;
     } else {
         if (P.n >= (1ull << 28)) return fail(PCAGB_ENOMEM);
+        /* mark the later flag twins of the parent level (k_twins); their
+           table lives on the scratch side only while the pass runs (stream
+           order keeps the space from being reused before it ends) */
+        CK(cudaMemsetAsync(P.twin, 0, P.n, e->stream));
+        if (P.n >= 2) {
+            const size_t top_tw = e->top;
+            uint64_t tslots = 1024;
+            while (tslots < 2 * P.n) tslots <<= 1;
+            unsigned long long *tt = (unsigned long long *)e->alloc_top(tslots * 8);
+            if (!tt) return fail(PCAGB_ENOMEM);
+            CK(cudaMemsetAsync(tt, 0, tslots * 8, e->stream));
+            if (e->TPC == 16)
+                k_twins<16><<<e->grid(4), 256, 0, e->stream>>>(view(P), e->td, tt, tslots - 1,
+                                                              P.twin, e->d_status);
+            else
+                k_twins<32><<<e->grid(4), 256, 0, e->stream>>>(view(P), e->td, tt, tslots - 1,
+                                                              P.twin, e->d_status);
+            const int rct = check_launch(e);
+            if (rct) return rct;
+            e->top = top_tw;
+        }
         uint64_t slots = 1024;
         while (slots < 2 * children) slots <<= 1;
         unsigned long long *table = (unsigned long long *)e->alloc_top(slots * 8);
@@ -641,6 +690,41 @@ int take_records(pcagb_engine *e, int S, int K, std::vector<TaskRun> &runs, bool
     return PCAGB_OK;
 }
 
+/* Middle-instruction chunks the depth-2 and depth-3 suffix kernels may take
+   per work item, by suffix depth (index 0 is unused). */
+constexpr uint32_t kChunkChoices[4][4] = {{1, 1, 1, 1}, {1, 1, 1, 1}, {4, 8, 16, 32}, {1, 2, 4, 8}};
+/* A stage is large enough to measure a launch choice on. */
+constexpr uint64_t kTuneMinEvals = 20000000ull;
+
+/* The option to use among n with measured costs ms[i] (n_meas[i] stages):
+   an unmeasured one first when exploring, else the cheapest measured; def
+   when none is measured. */
+int pick_option(const double *ms, const int *n_meas, int n, int def, bool explore)
+{
+    if (explore)
+        for (int i = 0; i < n; i++)
+            if (n_meas[i] == 0) return i;
+    int best = -1;
+    for (int i = 0; i < n; i++)
+        if (n_meas[i] > 0 && (best < 0 || ms[i] < ms[best])) best = i;
+    return best < 0 ? def : best;
+}
+
+void record_cost(double &ms, int &n, double v)
+{
+    ms = n == 0 ? v : 0.7 * ms + 0.3 * v;
+    n++;
+}
+
+template <int TPC, int SD>
+void launch_suffix(int ft, int g, cudaStream_t st, const LevelDev &L, const TaskDev &td,
+                   const SolBuf &sb, uint32_t cpp, uint32_t chunk, const PrefixRange &R)
+{
+    if (ft == 1) k_suffix<TPC, SD, 1><<<g, kThreads, 0, st>>>(L, td, sb, cpp, chunk, R);
+    else if (ft == 3) k_suffix<TPC, SD, 3><<<g, kThreads, 0, st>>>(L, td, sb, cpp, chunk, R);
+    else k_suffix<TPC, SD, 2><<<g, kThreads, 0, st>>>(L, td, sb, cpp, chunk, R);
+}
+
 /* Run the last stage at depth K from level S (suffix depth K-S, or the leaf
  * check when K == S) for the active tasks; appends each task's raw
  * solutions in DFS order.
@@ -660,7 +744,9 @@ int run_stage(pcagb_engine *e, int S, int K, std::vector<TaskRun> &runs, bool fi
     const int s = K - S;
     CK(cudaMemsetAsync(e->d_small, 0, 8, e->stream));
     CK(cudaMemsetAsync(e->d_small + 1, 0xFF, 8, e->stream));
-    SolBuf sb{e->d_small, e->d_sol, e->sol_cap, e->d_small + 1};
+    SolBuf sb{e->d_small, e->d_sol, e->sol_cap, e->d_small + 1, e->d_small + 3};
+    int tuned_ft = 0, tuned_ck = -1;   /* the launch choices this stage used */
+    bool stopped_early = false;
     cudaEventRecord(e->ev0, e->stream);
     const bool t16 = e->TPC == 16;
     const int g = e->grid(e->occ_suffix);
@@ -673,24 +759,50 @@ int run_stage(pcagb_engine *e, int S, int K, std::vector<TaskRun> &runs, bool fi
         if (rc) return rc;
     } else if (s <= 3) {
         int ncmax = 0;
+        uint64_t evals_pred = 0;
         for (size_t i = 0; i < L.hist.size(); i++)
-            if (L.hist[i]) ncmax = std::max(ncmax, gt.nc((int)(i & 127)));
-        const uint32_t chunk = s == 1 ? 1 : s == 2 ? 16 : 1;
+            if (L.hist[i]) {
+                ncmax = std::max(ncmax, gt.nc((int)(i & 127)));
+                if (e->h_active[i >> 7]) evals_pred += L.hist[i] * gt.ev[s][i & 127];
+            }
+        /* launch choices: forced by the caller, else the cheapest measured
+           (an unmeasured one is tried first on a stage large enough) */
+        const bool explore = evals_pred >= kTuneMinEvals && !so;
+        int ft = e->force_ft;
+        if (ft < 1 || ft > 3) ft = 1 + pick_option(&e->ft_ms[s][1], &e->ft_n[s][1], 3, 1, explore);
+        int ck = -1;
+        uint32_t chunk = 1;
+        if (s >= 2) {
+            if (e->force_chunk >= 1) {
+                chunk = (uint32_t)std::min(e->force_chunk, 64);
+            } else {
+                /* chunks are explored once the tests-per-lane choice is */
+                const bool ft_done = e->ft_n[s][1] && e->ft_n[s][2] && e->ft_n[s][3];
+                ck = pick_option(e->ck_ms[s], e->ck_n[s], 4, s == 2 ? 2 : 0, explore && ft_done);
+                chunk = kChunkChoices[s][ck];
+            }
+        }
         const uint32_t cpp =
             s == 1 ? 1 : std::max(1u, (uint32_t)((ncmax + chunk - 1) / chunk));
         auto launch = [&](const PrefixRange &R) {
+            const LevelDev V = view(L);
             if (s == 1) {
-                if (t16) k_suffix<16, 1><<<g, kThreads, 0, e->stream>>>(view(L), e->td, sb, 1, 1, R);
-                else k_suffix<32, 1><<<g, kThreads, 0, e->stream>>>(view(L), e->td, sb, 1, 1, R);
+                if (t16) launch_suffix<16, 1>(ft, g, e->stream, V, e->td, sb, 1, 1, R);
+                else launch_suffix<32, 1>(ft, g, e->stream, V, e->td, sb, 1, 1, R);
+                const int rc0 = check_launch(e);
+                if (rc0) return rc0;
+                k_count_evals<<<e->grid(2), 256, 0, e->stream>>>(V, e->td, R, sb);
             } else if (s == 2) {
-                if (t16) k_suffix<16, 2><<<g, kThreads, 0, e->stream>>>(view(L), e->td, sb, cpp, chunk, R);
-                else k_suffix<32, 2><<<g, kThreads, 0, e->stream>>>(view(L), e->td, sb, cpp, chunk, R);
+                if (t16) launch_suffix<16, 2>(ft, g, e->stream, V, e->td, sb, cpp, chunk, R);
+                else launch_suffix<32, 2>(ft, g, e->stream, V, e->td, sb, cpp, chunk, R);
             } else {
-                if (t16) k_suffix<16, 3><<<g, kThreads, 0, e->stream>>>(view(L), e->td, sb, cpp, chunk, R);
-                else k_suffix<32, 3><<<g, kThreads, 0, e->stream>>>(view(L), e->td, sb, cpp, chunk, R);
+                if (t16) launch_suffix<16, 3>(ft, g, e->stream, V, e->td, sb, cpp, chunk, R);
+                else launch_suffix<32, 3>(ft, g, e->stream, V, e->td, sb, cpp, chunk, R);
             }
             return check_launch(e);
         };
+        tuned_ft = ft;
+        tuned_ck = ck;
         /* task groups of the progressive mode: [first task, end task) with
            the level range they occupy */
         struct Group { int t0, t1; uint64_t b0, b1; };
@@ -749,13 +861,20 @@ int run_stage(pcagb_engine *e, int S, int K, std::vector<TaskRun> &runs, bool fi
                 rc = launch(R);
                 if (rc) return rc;
                 if (so && so->stop_at_first) {
+                    const auto h0 = std::chrono::steady_clock::now();
                     CK(e_copy(e, &e->h_pin[kPinCount], e->d_small, 8, cudaMemcpyDeviceToHost,
                               e->stream));
                     cudaEventRecord(e->ev1, e->stream);
                     CK(cudaStreamSynchronize(e->stream));
+                    /* the host side of a chunked launch: its wait beyond the
+                       device work is what the next launch pays in idle time */
+                    const double rt = std::chrono::duration<double, std::milli>(
+                                          std::chrono::steady_clock::now() - h0).count();
+                    e->launch_rt_ms = 0.9 * e->launch_rt_ms + 0.1 * std::min(rt, 1.0);
                     if (e->h_pin[kPinCount]) {
                         so->prefixes_to_first = R.begin + R.count;
                         cudaEventElapsedTime(&so->ms_to_first, e->ev0, e->ev1);
+                        stopped_early = R.begin + R.count < L.n;
                         break;
                     }
                 }
@@ -766,20 +885,29 @@ int run_stage(pcagb_engine *e, int S, int K, std::vector<TaskRun> &runs, bool fi
         return PCAGB_ENOMEM;
     }
     cudaEventRecord(e->ev1, e->stream);
-    CK(e_copy(e, &e->h_pin[kPinCount], e->d_small, 16, cudaMemcpyDeviceToHost, e->stream));
+    /* count, first key, (survivors), evaluations run so far in this solve */
+    CK(e_copy(e, &e->h_pin[kPinCount], e->d_small, 32, cudaMemcpyDeviceToHost, e->stream));
     CK(cudaStreamSynchronize(e->stream));
     const unsigned long long nrec = e->h_pin[kPinCount], first = e->h_pin[kPinFirst];
+    e->evals_run = e->h_pin[kPinCount + 3];
     float ms = 0;
     cudaEventElapsedTime(&ms, e->ev0, e->ev1);
     e->ms_suffix += ms;
     e->suffix_launches++;
-    if (s >= 1 && !(so && so->stop_at_first)) {
+    if (s >= 1 && !stopped_early && !(so && so->order)) {
         /* value-class evaluations of this stage, for the autotuner */
         const std::vector<uint64_t> &g = gt.ev[s];
         uint64_t evals = 0;
-        for (size_t i = 0; i < L.hist.size(); i++) evals += L.hist[i] * g[i & 127];
-        if (evals > 10000000ull)
-            e->t_eval_ms[s] = 0.7 * e->t_eval_ms[s] + 0.3 * (ms / (double)evals);
+        for (size_t i = 0; i < L.hist.size(); i++)
+            if (e->h_active[i >> 7]) evals += L.hist[i] * g[i & 127];
+        if (evals > 10000000ull) {
+            const double per = ms / (double)evals;
+            e->t_eval_ms[s] = 0.7 * e->t_eval_ms[s] + 0.3 * per;
+            if (evals >= kTuneMinEvals && s <= 3) {
+                if (tuned_ft >= 1) record_cost(e->ft_ms[s][tuned_ft], e->ft_n[s][tuned_ft], per);
+                if (tuned_ck >= 0) record_cost(e->ck_ms[s][tuned_ck], e->ck_n[s][tuned_ck], per);
+            }
+        }
     }
     if (nrec <= taken) return PCAGB_OK;
     return take_records(e, S, K, runs, first_only, taken, nrec, first);
@@ -932,7 +1060,7 @@ int autotune_split(pcagb_engine *e, int K, const std::vector<uint8_t> &active,
                it would only find that out after its insert. */
             double kids = children_of(D), build = 0, states_scale = 1.0;
             double parents = (double)e->levels[D].n, held = 0;
-            const double state_bytes = 16.0 * e->TPC + e->TPC + 11;
+            const double state_bytes = 16.0 * e->TPC + e->TPC + 12;
             const double free_b = (double)(e->top - e->bottom);
             bool fits = true;
             for (int d = D + 1; d <= S; d++) {
@@ -1051,6 +1179,9 @@ int run_batch(pcagb_engine *e, std::vector<TaskRun> &runs, const pcagb_opts_t &o
     e->launches = 0;
     e->h2d = e->d2h = 0;
     e->insert_launches = e->suffix_launches = e->insert_children = 0;
+    e->evals_run = 0;
+    e->force_ft = o.first_tests;
+    e->force_chunk = o.suffix_chunk;
     e->max_feasible = SEARCH_MAX_DEPTH;
     int maxT = 0, maxK = 0;
     for (TaskRun &tr : runs) {
@@ -1066,6 +1197,7 @@ int run_batch(pcagb_engine *e, std::vector<TaskRun> &runs, const pcagb_opts_t &o
                     o.oep_mode == PCAGB_OEP_EXACT_LIVE, o.oep_mode != PCAGB_OEP_NONE};
     CK(cudaSetDevice(e->device));
     CK(cudaMemsetAsync(e->d_status, 0, 4, e->stream));
+    CK(cudaMemsetAsync(e->d_small + 3, 0, 8, e->stream));
     {
         std::vector<int32_t> T(nt);
         std::vector<uint32_t> tgt((size_t)nt * 32, 0);
@@ -1117,6 +1249,7 @@ int run_batch(pcagb_engine *e, std::vector<TaskRun> &runs, const pcagb_opts_t &o
         CK(e_copy(e, L0.cidx, cidx.data(), nt * 2, cudaMemcpyHostToDevice, e->stream));
         CK(cudaMemsetAsync(L0.rdl, 0, nt, e->stream));
         CK(cudaMemsetAsync(L0.own, 0, nt, e->stream));
+        CK(cudaMemsetAsync(L0.twin, 0, nt, e->stream));
     }
     e->levels.push_back(std::move(L0));
 
@@ -1245,6 +1378,27 @@ int run_batch(pcagb_engine *e, std::vector<TaskRun> &runs, const pcagb_opts_t &o
             so.chunk = ord->chunk;
             so.stop_at_first = true;
             sop = &so;
+        } else if (s >= 1 && nt == 1 && o.first_only && !o.count_levels && !ord &&
+                   o.stage_launch >= 0) {
+            /* a first-only stage of one task in chunks of DFS order, stopping
+               at the first launch that holds a solution (every earlier
+               prefix is searched, so its solutions hold the DFS-first one):
+               worth it when the stage is predicted to take much longer than
+               the host round trip each launch adds */
+            uint64_t c0 = o.stage_launch > 0 ? (uint64_t)o.stage_launch : 0;
+            if (!c0) {
+                double evals = 0;
+                for (int i = 0; i < nt; i++)
+                    if (active[i]) evals += (double)runs[i].res.evaluations[K];
+                if (evals * e->t_eval_ms[s] > 32.0 * e->launch_rt_ms && LS.n >= 256)
+                    c0 = std::max<uint64_t>(LS.n / 16, 1);
+            }
+            if (c0) {
+                so.order = nullptr;
+                so.chunk = c0;
+                so.stop_at_first = true;
+                sop = &so;
+            }
         }
         /* a task searched at depth K: its counters, and done when it has
            solutions or K is its last depth */
@@ -1301,6 +1455,7 @@ int run_batch(pcagb_engine *e, std::vector<TaskRun> &runs, const pcagb_opts_t &o
         tr.res.insert_launches = e->insert_launches;
         tr.res.suffix_launches = e->suffix_launches;
         tr.res.insert_children = e->insert_children;
+        tr.res.evaluations_run = e->evals_run;
         tr.res.h2d_bytes = e->h2d;
         tr.res.d2h_bytes = e->d2h;
         tr.res.seconds = tr.t_done;
@@ -1359,6 +1514,7 @@ int ensure_device_tables(int device)
         const uint32_t *pp = pr;
         const uint16_t *pc = pr_cls;
         CK(cudaMemcpyToSymbol(c_pr_off, gt.pr_off.data(), gt.pr_off.size() * 4));
+        CK(cudaMemcpyToSymbol(c_pr_ev, gt.pr_ev.data(), gt.pr_ev.size() * 4));
         CK(cudaMemcpyToSymbol(c_pr, &pp, sizeof pp));
         CK(cudaMemcpyToSymbol(c_pr_cls, &pc, sizeof pc));
     }
@@ -1413,7 +1569,7 @@ int engine_init(pcagb_engine *e, int device, size_t budget)
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_expand_insert<32>, kThreads, 0) ==
                 cudaSuccess && nb > 0)
             e->occ_insert = nb;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_suffix<32, 1>, kThreads, 0) ==
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_suffix<32, 1, 2>, kThreads, 0) ==
                 cudaSuccess && nb > 0)
             e->occ_suffix = nb;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_materialize<32>, kThreads, 0) ==
@@ -1423,12 +1579,18 @@ int engine_init(pcagb_engine *e, int device, size_t budget)
     }
     size_t free_b = 0, total_b = 0;
     CK(cudaMemGetInfo(&free_b, &total_b));
-    if (budget == 0) budget = (size_t)(free_b * 0.6);
-    if (budget > free_b) budget = free_b - (256u << 20);
-    budget &= ~size_t(4095);
-    CK(cudaMalloc(&e->arena, budget));
-    e->cap = budget;
-    e->top = budget;
+    if (budget == kArenaExternal) {
+        /* the arena comes with each solve (pcagb_internal_solve_batch_arena) */
+        e->arena = nullptr;
+        e->cap = e->top = 0;
+    } else {
+        if (budget == 0) budget = (size_t)(free_b * 0.6);
+        if (budget > free_b) budget = free_b - (256u << 20);
+        budget &= ~size_t(4095);
+        CK(cudaMalloc(&e->arena, budget));
+        e->cap = budget;
+        e->top = budget;
+    }
     int trc = ensure_device_tables(device);
     if (trc) return trc;
     CK(cudaMalloc(&e->d_small, 256 * sizeof(unsigned long long)));
@@ -1452,6 +1614,12 @@ bool make_run(const task_spec_t *task, const pcagb_opts_t &o, TaskRun *tr)
     }
     if (o.max_depth < 0 || o.max_depth > 12 || task->num_inputs + o.max_depth + 2 > 16) {
         set_err("max_depth %d out of range (program length is limited to 16)", o.max_depth);
+        return false;
+    }
+    if (o.first_tests < 0 || o.first_tests > 3 || o.suffix_chunk < 0 || o.suffix_chunk > 64 ||
+        o.stage_launch < -1) {
+        set_err("launch choices out of range (first_tests 0..3, suffix_chunk 0..64, "
+                "stage_launch >= -1)");
         return false;
     }
     search_state_init_root(&ctx, &tr->root);
@@ -1740,6 +1908,23 @@ void pcagb_engine_destroy(pcagb_engine_t *e)
 
 void *pcagb_engine_stream(pcagb_engine_t *e) { return e ? (void *)e->stream : nullptr; }
 
+int pcagb_tuning(pcagb_engine_t *e, pcagb_tuning_t *out)
+{
+    if (!e || !out) { set_err("null argument"); return PCAGB_EINVAL; }
+    memset(out, 0, sizeof *out);
+    for (int i = 0; i < 4; i++) out->t_eval_ms[i] = e->t_eval_ms[i];
+    out->t_child_ms = e->t_child_ms;
+    out->t_build_fixed_ms = e->t_build_fixed_ms;
+    out->dedup_ratio = e->dedup_ratio;
+    memcpy(out->first_tests_ms, e->ft_ms, sizeof e->ft_ms);
+    memcpy(out->first_tests_n, e->ft_n, sizeof e->ft_n);
+    memcpy(out->chunk_ms, e->ck_ms, sizeof e->ck_ms);
+    memcpy(out->chunk_n, e->ck_n, sizeof e->ck_n);
+    memcpy(out->chunk_choices, kChunkChoices, sizeof kChunkChoices);
+    out->launch_rt_ms = e->launch_rt_ms;
+    return PCAGB_OK;
+}
+
 int pcagb_device_memory(int device, size_t *free_bytes, size_t *total_bytes)
 {
     int n = 0;
@@ -1813,6 +1998,55 @@ void deliver(int i, void *p)
     if (c.cb) c.cb(i, &c.results[i], c.user);
 }
 }  // namespace
+
+/* For the solve server (server.cu): an engine without an arena of its own,
+   and a batched solve on an arena slice the caller owns (each task with its
+   own depth limit), results delivered per task as they are decided. */
+int pcagb_internal_engine_create_bare(int device, pcagb_engine_t **out)
+{
+    if (!out) { set_err("null argument"); return PCAGB_EINVAL; }
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) {
+        cudaGetLastError();
+        set_err("no CUDA device %d: the PCA-16 engine runs only on the GPU", device);
+        return PCAGB_ENODEV;
+    }
+    pcagb_engine *e = new pcagb_engine();
+    int rc = engine_init(e, device, kArenaExternal);
+    if (rc) {
+        pcagb_engine_destroy(e);
+        return rc;
+    }
+    *out = e;
+    return PCAGB_OK;
+}
+
+int pcagb_internal_solve_batch_arena(pcagb_engine_t *e, void *arena, size_t bytes,
+                                     const task_spec_t *tasks, const int *max_depths, int ntasks,
+                                     const pcagb_opts_t *opts, pcagb_result_t *results,
+                                     uint16_t *sol_progs, int *sol_lens, int cap,
+                                     pcagb_done_cb on_done, void *user)
+{
+    if (!e || !arena || !tasks || !max_depths || !results || ntasks < 1 || !opts) {
+        set_err("null argument");
+        return PCAGB_EINVAL;
+    }
+    if (ntasks > kMaxBatch) { set_err("at most %d tasks per batch", kMaxBatch); return PCAGB_EINVAL; }
+    std::vector<TaskRun> runs(ntasks);
+    pcagb_opts_t o = *opts;
+    for (int i = 0; i < ntasks; i++) {
+        o.max_depth = max_depths[i];
+        if (!make_run(&tasks[i], o, &runs[i])) return PCAGB_EINVAL;
+    }
+    e->arena = (char *)arena;
+    e->cap = bytes & ~size_t(255);
+    DoneCtx c{tasks, &o, &runs, results, sol_progs, sol_lens, cap, on_done, user, 0};
+    int rc = run_batch(e, runs, o, deliver, &c);
+    e->arena = nullptr;
+    e->cap = e->top = e->bottom = 0;
+    return rc ? rc : c.rc;
+}
 
 int pcagb_solve_batch_cb(pcagb_engine_t *e, const task_spec_t *tasks, int ntasks,
                          const pcagb_opts_t *opts, pcagb_result_t *results, uint16_t *sol_progs,

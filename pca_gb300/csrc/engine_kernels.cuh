@@ -70,6 +70,7 @@ __constant__ const uint16_t *c_vcr;        /* their indices in the mask's class 
 __constant__ uint32_t c_pr_off[128 * 8 + 1];  /* [mask*8 + r]: the same, by operand pair */
 __constant__ const uint32_t *c_pr;         /* a | b << 3 | opmask << 6 | imm << 16 */
 __constant__ const uint16_t *c_pr_cls;     /* [entry][10] class index per opmask bit */
+__constant__ uint32_t c_pr_ev[128 * 8];    /* [mask*8 + r]: class evaluations of its pair list */
 
 /* Per-task parameters of a batch: device arrays indexed by task id. A
    state's task id travels with it through the levels; states of different
@@ -94,6 +95,8 @@ struct LevelDev {
     const uint32_t *parent; /* [n] rank of the parent in the level above */
     const uint8_t *own;     /* [n] registers whose last write is unread and dead-able (below);
                                bit 0: the last instruction is an LDI */
+    const uint8_t *twin;    /* [n] 1: an earlier state of the level has the same registers,
+                               live mask and task (k_twins) */
 };
 
 struct LevelOut {
@@ -407,6 +410,7 @@ k_expand_insert(LevelDev P, TaskDev task, unsigned long long *table, uint64_t tm
         const uint32_t ka = min(k1, k0 + g * per), kb = min(k1, ka + per);
         const uint32_t wdead = deadable_writes(P, fcr_up, q);
         const uint32_t wldi = fcr_up && (P.own[q] & 1u) ? P.rdl[q] : 0u;
+        const bool twin_later = P.twin[q] != 0;
         for (uint32_t k = ka; k < kb; k++) {
             const uint32_t ch = c_chunks[k], start = ch >> 8, cnt = ch & 255u;
             bool valid = (uint32_t)lane < cnt;
@@ -416,6 +420,7 @@ k_expand_insert(LevelDev P, TaskDev task, unsigned long long *table, uint64_t tm
             if ((wdead >> rd & 1u) && op != PCA_OP_LDI && !uop_reads(u, rd)) valid = false;
             if (ldi_swap(u, wldi)) valid = false;
             if (u >> 31) valid = false;   /* an earlier sibling's state (same value and flags) */
+            if (twin_later && op != PCA_OP_LDI) valid = false;   /* k_twins */
             if (!__any_sync(0xFFFFFFFFu, valid)) continue;
             uint64_t h, hf;
             __syncwarp();   /* the previous chunk's compares are done with colA */
@@ -490,6 +495,94 @@ k_expand_insert(LevelDev P, TaskDev task, unsigned long long *table, uint64_t tm
                         }
                     }
                 }
+            }
+        }
+    }
+}
+
+/* Flag twins. Two states of a level with the same registers, live mask and
+   task but different flags (e.g. two independent instructions in either
+   order, or two ops that write the same value with different flags) have,
+   for every flag-setting candidate c (every op but LDI), children that are
+   the same state under either pruning key: the same registers, c's flags
+   and the same live mask; and c has the same index in both parents' lists
+   (the lists depend on live only). The earlier state's child is the smaller
+   ref, so no flag-setting child of a later twin is ever the DFS-first
+   representative: k_twins marks the later twins (twin[q] = 1) and the insert
+   kernel skips those children. One warp per state (lane = test): a hash of
+   r1..r7, live and task, then an open-addressed table whose slot keeps the
+   class's lowest rank, every tag match settled by an exact warp-wide
+   compare. Probing is bounded (kStatusTableFull). twin[] is zeroed
+   beforehand. */
+template <int TPC>
+__global__ void k_twins(LevelDev P, TaskDev task, unsigned long long *table, uint64_t tmask,
+                        uint8_t *twin, uint32_t *status)
+{
+    const int lane = threadIdx.x & 31;
+    const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t q = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < P.n; q += nw) {
+        const uint32_t tid = P.task[q];
+        if (!task.active[tid]) continue;
+        const uint32_t live = P.live[q];
+        uint32_t col[7];
+        uint64_t h = 0;
+        if (lane < TPC) {
+            const uint16_t *src = P.regs + q * 8 * TPC + lane;
+            uint64_t w = 0x243F6A8885A308D3ull ^ (uint64_t)lane;
+#pragma unroll
+            for (int r = 1; r < 8; r++) {
+                col[r - 1] = src[r * TPC];
+                w = chain(w, col[r - 1]);
+            }
+            h = fmix64(w);
+        }
+#pragma unroll
+        for (int o = 16; o; o >>= 1) h += __shfl_xor_sync(0xFFFFFFFFu, h, o);
+        const uint64_t H = h + live_final(live) + task_final(tid);
+        const unsigned long long mine = ((H >> 40) << 40) | (q + 1);
+        uint64_t idx = H & tmask;
+        uint32_t probes = 0;
+        for (;;) {
+            unsigned long long s = 0;
+            if (lane == 0) {
+                s = *((volatile unsigned long long *)&table[idx]);
+                if (s == 0) s = atomicCAS(&table[idx], 0ull, mine);
+            }
+            s = __shfl_sync(0xFFFFFFFFu, s, 0);
+            if (s == 0) break;   /* the first of its class so far */
+            bool eq = false;
+            if ((s >> 40) == (mine >> 40)) {
+                const uint64_t qB = (s & kRefMask) - 1;
+                eq = P.task[qB] == tid && P.live[qB] == live;
+                if (eq) {
+                    bool ok = true;
+                    if (lane < TPC) {
+                        const uint16_t *srcB = P.regs + qB * 8 * TPC + lane;
+#pragma unroll
+                        for (int r = 1; r < 8; r++) ok &= srcB[r * TPC] == col[r - 1];
+                    }
+                    eq = __all_sync(0xFFFFFFFFu, ok);
+                }
+            }
+            if (eq) {
+                /* one class: the slot keeps the lowest rank, every other
+                   member is marked */
+                if (lane == 0) {
+                    unsigned long long cur = s;
+                    for (;;) {
+                        const uint64_t m = (cur & kRefMask) - 1;
+                        if (q > m) { twin[q] = 1; break; }
+                        const unsigned long long old = atomicCAS(&table[idx], cur, mine);
+                        if (old == cur) { twin[m] = 1; break; }
+                        cur = old;
+                    }
+                }
+                break;
+            }
+            idx = (idx + 1) & tmask;
+            if (++probes >= kMaxProbes) {
+                if (lane == 0) atomicOr(status, kStatusTableFull);
+                break;
             }
         }
     }
@@ -713,7 +806,17 @@ struct SolBuf {
     ulonglong2 *rec;              /* x = prefix rank, y = m1<<32 | m2<<16 | class */
     uint64_t cap;
     unsigned long long *first;    /* atomicMin of a packed DFS-order key */
+    unsigned long long *evals;    /* value-class evaluations the suffix kernels ran
+                                     (each class of an operand pair counts one) */
 };
+
+/* Adds a warp's per-lane evaluation counts to S.evals (all lanes call it). */
+__device__ __forceinline__ void flush_evals(const SolBuf &S, unsigned long long nev, int lane)
+{
+#pragma unroll
+    for (int o = 16; o; o >>= 1) nev += __shfl_down_sync(0xFFFFFFFFu, nev, o);
+    if (lane == 0 && nev) atomicAdd(S.evals, nev);
+}
 
 __device__ __forceinline__ void record_solution(const SolBuf &S, uint64_t q, uint32_t m1,
                                                 uint32_t m2, uint32_t vc, uint32_t first_c)
@@ -796,18 +899,19 @@ __device__ __forceinline__ uint32_t pair_op(uint32_t k)
  * reads the register the one before it wrote (need1), and need2 names an
  * earlier write nothing else read. Only classes that read need1 are
  * scanned, from the per-register class lists; the solutions are the same. */
-template <int TPC>
+template <int TPC, int FT>
 __device__ __forceinline__ void scan_last(const WarpState<TPC> &ws, int T,
                                           uint32_t m, uint32_t rd1, uint32_t rd2, uint32_t tgt,
-                                          uint32_t tgt0, uint32_t tgt1, int lane,
+                                          uint32_t tgt0, uint32_t tgt1, uint32_t tgt2, int lane,
                                           const SolBuf &S, uint64_t q, uint32_t m1, uint32_t m2,
-                                          uint32_t need1, uint32_t need2)
+                                          uint32_t need1, uint32_t need2, unsigned long long &nev)
 {
     const uint32_t vbase = c_vc_off[m];
     if (need1) {
         /* the classes reading need1, one operand pair (or ADDI) per lane,
            every op of the pair evaluated on the first two tests at once */
         const uint32_t p0 = c_pr_off[m * 8 + need1], np = c_pr_off[m * 8 + need1 + 1] - p0;
+        if (!need2 && lane == 0) nev += c_pr_ev[m * 8 + need1];
         for (uint32_t b0 = 0; b0 < np; b0 += 32) {
             const uint32_t i = b0 + lane;
             uint32_t hits = 0, ra = 0, rb = 0, e = 0;
@@ -815,11 +919,15 @@ __device__ __forceinline__ void scan_last(const WarpState<TPC> &ws, int T,
                 const uint32_t d = c_pr[p0 + i];
                 const uint32_t a = d & 7u, b = (d >> 3) & 7u;
                 if (!need2 || a == need2 || b == need2) {
+                    if (need2) nev += __popc((d >> 6) & 0x3FFu);
                     ra = a == rd2 ? 9u : a == rd1 ? 8u : a;
                     rb = b == rd2 ? 9u : b == rd1 ? 8u : b;
                     e = (uint32_t)(uint16_t)(int16_t)(int8_t)(uint8_t)(d >> 16);
                     hits = pair_hits(ws.R[ra][0], ws.R[rb][0], e, tgt0) & (d >> 6) & 0x3FFu;
-                    if (T >= 2 && hits) hits &= pair_hits(ws.R[ra][1], ws.R[rb][1], e, tgt1);
+                    if (FT >= 2 && T >= 2 && hits)
+                        hits &= pair_hits(ws.R[ra][1], ws.R[rb][1], e, tgt1);
+                    if (FT >= 3 && T >= 3 && hits)
+                        hits &= pair_hits(ws.R[ra][2], ws.R[rb][2], e, tgt2);
                 }
             }
             uint32_t bal = __ballot_sync(0xFFFFFFFFu, hits != 0);
@@ -855,15 +963,17 @@ __device__ __forceinline__ void scan_last(const WarpState<TPC> &ws, int T,
         uint32_t u = 0;
         bool pass = false;
         if (i < nvc) {
-            /* first two tests per lane; survivors are checked on all tests below */
+            /* the first FT tests per lane; survivors are checked on all tests below */
             u = uops[i];
             uint32_t ra = UOP_A(u), rb = UOP_B(u);
             const bool reads2 = !need2 || ra == need2 || rb == need2;
             ra = ra == rd2 ? 9u : ra == rd1 ? 8u : ra;
             rb = rb == rd2 ? 9u : rb == rd1 ? 8u : rb;
             const uint32_t op = UOP_OP(u), imm = UOP_IMM(u);
+            nev += reads2 ? 1u : 0u;
             pass = reads2 && pca_alu(op, ws.R[ra][0], ws.R[rb][0], imm) == tgt0 &&
-                   (T < 2 || pca_alu(op, ws.R[ra][1], ws.R[rb][1], imm) == tgt1);
+                   (FT < 2 || T < 2 || pca_alu(op, ws.R[ra][1], ws.R[rb][1], imm) == tgt1) &&
+                   (FT < 3 || T < 3 || pca_alu(op, ws.R[ra][2], ws.R[rb][2], imm) == tgt2);
         }
         uint32_t bal = __ballot_sync(0xFFFFFFFFu, pass);
         while (bal) {
@@ -930,7 +1040,7 @@ struct PrefixRange {
  * less latency and six spill the prefetched columns; at SD = 2 five CTAs
  * instead of the four that 56 registers allow cut a two-input depth-4
  * stage from 39 to 30 ms. */
-template <int TPC, int SD>
+template <int TPC, int SD, int FT>
 __global__ void __launch_bounds__(kThreads, 5)
 k_suffix(LevelDev P, TaskDev task, SolBuf S, uint32_t chunks_per_prefix, uint32_t chunk,
          PrefixRange R)
@@ -941,8 +1051,9 @@ k_suffix(LevelDev P, TaskDev task, SolBuf S, uint32_t chunks_per_prefix, uint32_
     const uint64_t nw = (uint64_t)gridDim.x * kWarpsPerBlock;
     const uint64_t items = R.count * chunks_per_prefix;
     uint64_t loaded = ~0ull;
-    uint32_t cur_task = ~0u, tgt = 0, tgt0 = 0, tgt1 = 0;
+    uint32_t cur_task = ~0u, tgt = 0, tgt0 = 0, tgt1 = 0, tgt2 = 0;
     int T = 0;
+    unsigned long long nev = 0;
     if (lane < TPC) ws.R[0][lane] = 0;
     bool cur_active = false;
     if constexpr (SD == 1) {
@@ -986,13 +1097,16 @@ k_suffix(LevelDev P, TaskDev task, SolBuf S, uint32_t chunks_per_prefix, uint32_
                 tgt = lane < T ? task.target[tid * 32 + lane] : 0u;
                 tgt0 = task.target[tid * 32];
                 tgt1 = task.target[tid * 32 + 1];
+                if (FT >= 3) tgt2 = task.target[tid * 32 + 2];
             }
             if (!cur_active) continue;
             /* w0: the prefix's last write (0 at a root); some later
                instruction must read it (the rule scan_last states) */
-            scan_last<TPC>(ws, T, (live >> 1) & 127u, 8, 8, tgt, tgt0, tgt1, lane, S, q, 0, 0, w0,
-                           0);
+            scan_last<TPC, FT>(ws, T, (live >> 1) & 127u, 8, 8, tgt, tgt0, tgt1, tgt2, lane, S, q, 0, 0, w0,
+                           0, nev);
         }
+        /* no flush: k_count_evals counts this depth's evaluations (nev is
+           dead here and costs no register) */
         return;
     }
     for (uint64_t it = (uint64_t)blockIdx.x * kWarpsPerBlock + wib; it < items; it += nw) {
@@ -1008,6 +1122,7 @@ k_suffix(LevelDev P, TaskDev task, SolBuf S, uint32_t chunks_per_prefix, uint32_
             tgt = lane < T ? task.target[tid * 32 + lane] : 0u;
             tgt0 = task.target[tid * 32];
             tgt1 = task.target[tid * 32 + 1];
+            if (FT >= 3) tgt2 = task.target[tid * 32 + 2];
         }
         if (!cur_active) continue;
         const uint32_t live = P.live[q];
@@ -1042,7 +1157,8 @@ k_suffix(LevelDev P, TaskDev task, SolBuf S, uint32_t chunks_per_prefix, uint32_
             __syncwarp();
             const uint32_t m1 = (m0 | (1u << (rd1 - 1))) & 127u;
             if (SD == 2) {
-                scan_last<TPC>(ws, T, m1, rd1, 8, tgt, tgt0, tgt1, lane, S, q, i1, 0, rd1, owe0);
+                scan_last<TPC, FT>(ws, T, m1, rd1, 8, tgt, tgt0, tgt1, tgt2, lane, S, q, i1, 0, rd1, owe0,
+                               nev);
                 continue;
             }
             const uint32_t cb1 = c_cand_off[m1], nc1 = c_cand_off[m1 + 1] - cb1;
@@ -1068,11 +1184,31 @@ k_suffix(LevelDev P, TaskDev task, SolBuf S, uint32_t chunks_per_prefix, uint32_
                                              : 0u;
                 __syncwarp();
                 const uint32_t m2 = (m1 | (1u << (rd2 - 1))) & 127u;
-                scan_last<TPC>(ws, T, m2, rd2 == rd1 ? 8u : rd1, rd2, tgt, tgt0, tgt1, lane, S,
-                               q, i1, i2, rd2, need2);
+                scan_last<TPC, FT>(ws, T, m2, rd2 == rd1 ? 8u : rd1, rd2, tgt, tgt0, tgt1, tgt2, lane, S,
+                               q, i1, i2, rd2, need2, nev);
             }
         }
     }
+    flush_evals(S, nev, lane);
+}
+
+/* Value-class evaluations k_suffix<TPC, 1> runs over range R: a prefix of
+   mask m whose last write is w0 scans the pair list of (m, w0) (c_pr_ev),
+   a root every class of its mask. Added to S.evals, one atomic per warp. */
+__global__ void k_count_evals(LevelDev P, TaskDev task, PrefixRange R, SolBuf S)
+{
+    const int lane = threadIdx.x & 31;
+    unsigned long long nev = 0;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    const uint64_t n_round = (R.count + 31) & ~31ull;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_round; i += stride) {
+        if (i >= R.count) continue;
+        const uint64_t q = R.order ? (uint64_t)R.order[R.begin + i] : R.begin + i;
+        if (q >= P.n || !task.active[P.task[q]]) continue;
+        const uint32_t m = (P.live[q] >> 1) & 127u, w0 = P.rdl[q];
+        nev += w0 ? c_pr_ev[m * 8 + w0] : c_vc_off[m + 1] - c_vc_off[m];
+    }
+    flush_evals(S, nev, lane);
 }
 
 /* ---- recording: the reference's keys and records of level states --------- */

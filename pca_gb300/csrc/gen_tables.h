@@ -65,6 +65,9 @@ struct GenTables {
     std::vector<uint32_t> pr_off;      /* size 128*8+1 */
     std::vector<uint32_t> pr;
     std::vector<uint16_t> pr_cls;
+    /* pr_ev[m*8+r]: class evaluations one pass over the pair list of (m, r)
+       runs (every admitted op of every entry) */
+    std::vector<uint32_t> pr_ev;
     int max_nc = 0;
     int max_nvc = 0;
 

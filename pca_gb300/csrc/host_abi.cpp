@@ -189,6 +189,10 @@ static GenTables build_tables()
             }
         }
     t.pr_off[128 * 8] = (uint32_t)t.pr.size();
+    t.pr_ev.assign(128 * 8, 0);
+    for (int i = 0; i < 128 * 8; i++)
+        for (uint32_t e = t.pr_off[i]; e < t.pr_off[i + 1]; e++)
+            t.pr_ev[i] += (uint32_t)__builtin_popcount((t.pr[e] >> 6) & 0x3FFu);
     for (int s = 0; s < 5; s++) t.ev[s].assign(128, 0);
     for (int m = 0; m < 128; m++) t.ev[1][m] = t.vc_off[m + 1] - t.vc_off[m];
     for (int s = 2; s < 5; s++)

@@ -62,7 +62,10 @@ class SolveOpts(ctypes.Structure):
                 ("oep_mode", ctypes.c_int),
                 ("count_levels", ctypes.c_int),
                 ("first_only", ctypes.c_int),
-                ("reserved", ctypes.c_int * 6)]
+                ("first_tests", ctypes.c_int),
+                ("suffix_chunk", ctypes.c_int),
+                ("stage_launch", ctypes.c_int),
+                ("reserved", ctypes.c_int * 3)]
 
 
 class SolveResult(ctypes.Structure):
@@ -90,7 +93,36 @@ class SolveResult(ctypes.Structure):
                 ("prefixes_at_optimal", ctypes.c_uint64),
                 ("prefixes_to_first", ctypes.c_uint64),
                 ("ms_to_first", ctypes.c_double),
-                ("reserved", ctypes.c_int * 2)]
+                ("evaluations_run", ctypes.c_uint64)]
+
+
+class Tuning(ctypes.Structure):
+    _fields_ = [("t_eval_ms", ctypes.c_double * 4),
+                ("t_child_ms", ctypes.c_double),
+                ("t_build_fixed_ms", ctypes.c_double),
+                ("dedup_ratio", ctypes.c_double),
+                ("first_tests_ms", (ctypes.c_double * 4) * 4),
+                ("first_tests_n", (ctypes.c_int * 4) * 4),
+                ("chunk_ms", (ctypes.c_double * 4) * 4),
+                ("chunk_n", (ctypes.c_int * 4) * 4),
+                ("chunk_choices", (ctypes.c_uint32 * 4) * 4),
+                ("launch_rt_ms", ctypes.c_double)]
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int),
+                ("pool_bytes", ctypes.c_size_t),
+                ("arena_bytes", ctypes.c_size_t),
+                ("workers", ctypes.c_int),
+                ("max_batch", ctypes.c_int),
+                ("sol_cap", ctypes.c_int),
+                ("opts", SolveOpts)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint64) for n in (
+        "queued", "running_solves", "max_running_solves", "admitted", "finished", "batches",
+        "pool_bytes", "pool_used", "pool_peak", "pool_largest_free")]
 
 
 class LevelView(ctypes.Structure):
@@ -128,7 +160,10 @@ EXPORTS = [
     "pcagb_complete", "pcagb_record", "pcagb_solve_branch", "pcagb_solve_branch_ex",
     "pcagb_branch_last_error",
     "pcagb_num_candidates",
-    "pcagb_engine_stream", "pcagb_device_memory",
+    "pcagb_engine_stream", "pcagb_tuning", "pcagb_device_memory",
+    "pcagb_server_default_config", "pcagb_server_create", "pcagb_server_submit",
+    "pcagb_server_next", "pcagb_server_collect", "pcagb_server_stats", "pcagb_server_destroy",
+    "pcagb_server_last_error",
     "pcagb_solve_small_noalloc", "pcagb_noalloc_last_error",
 ]
 
@@ -181,8 +216,21 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
         "pcagb_branch_last_error": ([], ctypes.c_char_p),
         "pcagb_num_candidates": ([ctypes.c_uint8], ctypes.c_int),
         "pcagb_engine_stream": ([ctypes.c_void_p], ctypes.c_void_p),
+        "pcagb_tuning": ([ctypes.c_void_p, P(Tuning)], ctypes.c_int),
         "pcagb_device_memory": ([ctypes.c_int, P(ctypes.c_size_t), P(ctypes.c_size_t)],
                                 ctypes.c_int),
+        "pcagb_server_default_config": ([P(ServerConfig)], None),
+        "pcagb_server_create": ([P(ServerConfig), P(ctypes.c_void_p)], ctypes.c_int),
+        "pcagb_server_submit": ([ctypes.c_void_p, P(TaskSpec), ctypes.c_int, P(ctypes.c_uint64)],
+                                ctypes.c_int),
+        "pcagb_server_next": ([ctypes.c_void_p, ctypes.c_double, P(ctypes.c_uint64)],
+                              ctypes.c_int),
+        "pcagb_server_collect": ([ctypes.c_void_p, ctypes.c_uint64, P(SolveResult),
+                                  P(ctypes.c_uint16), P(ctypes.c_int), ctypes.c_int,
+                                  P(ctypes.c_double)], ctypes.c_int),
+        "pcagb_server_stats": ([ctypes.c_void_p, P(ServerStats)], ctypes.c_int),
+        "pcagb_server_destroy": ([ctypes.c_void_p], None),
+        "pcagb_server_last_error": ([], ctypes.c_char_p),
         "pcagb_solve_small_noalloc": ([P(TaskSpec), ctypes.c_int, ctypes.c_void_p,
                                        P(ctypes.c_int), P(ctypes.c_uint64), P(ctypes.c_uint16),
                                        P(ctypes.c_int), ctypes.c_int], ctypes.c_int),
@@ -333,10 +381,34 @@ class Solution:
     prefixes_at_optimal: int = 0
     prefixes_to_first: int = 0
     ms_to_first: float = 0.0
+    evaluations_run: int = 0
 
 
 class EngineError(RuntimeError):
     pass
+
+
+RESULT_SCALARS = ("seconds", "gpu_ms_expand", "gpu_ms_suffix", "gpu_ms_insert", "kernel_launches",
+                  "insert_launches", "suffix_launches", "h2d_bytes", "d2h_bytes",
+                  "insert_children", "split_used", "prefixes_at_optimal", "prefixes_to_first",
+                  "ms_to_first", "evaluations_run")
+RESULT_ARRAYS = ("candidates", "evaluations", "tried", "pruned_cum", "level_children",
+                 "level_survivors")
+
+
+def solution_from_result(r: "SolveResult", progs, lens, base: int, max_depth: int) -> "Solution":
+    """A Solution from a pcagb_result_t and its programs (progs[(base + k) *
+    16 ...], lens[base + k] for k < r.stored)."""
+    sol = Solution(optimal_depth=r.optimal_depth, total_solutions=r.total_solutions)
+    for name in RESULT_SCALARS:
+        setattr(sol, name, getattr(r, name))
+    for k in range(r.stored):
+        sol.programs.append([progs[(base + k) * 16 + j] for j in range(lens[base + k])])
+    last = r.optimal_depth if r.optimal_depth >= 0 else max_depth
+    for name in RESULT_ARRAYS:
+        arr = getattr(r, name)
+        setattr(sol, name, [arr[k] for k in range(min(last + 1, MAXD))])
+    return sol
 
 
 def device_memory(device: int = 0, lib: ctypes.CDLL | None = None):
@@ -371,11 +443,13 @@ class Engine:
             pass
 
     def solve(self, task: TaskSpec, max_depth=4, oep_mode=OEP_EXACT_LIVE, split_depth=-1,
-              count_levels=False, first_only=False, min_depth=0, sol_cap=4096) -> Solution:
+              count_levels=False, first_only=False, min_depth=0, sol_cap=4096, first_tests=0,
+              suffix_chunk=0, stage_launch=0) -> Solution:
         o = SolveOpts()
         self.lib.pcagb_default_opts(ctypes.byref(o))
         o.max_depth, o.min_depth, o.split_depth = max_depth, min_depth, split_depth
         o.oep_mode, o.count_levels, o.first_only = oep_mode, int(count_levels), int(first_only)
+        o.first_tests, o.suffix_chunk, o.stage_launch = first_tests, suffix_chunk, stage_launch
         r = SolveResult()
         progs = (ctypes.c_uint16 * (16 * max(sol_cap, 1)))()
         lens = (ctypes.c_int * max(sol_cap, 1))()
@@ -387,7 +461,7 @@ class Engine:
         for name in ("seconds", "gpu_ms_expand", "gpu_ms_suffix", "gpu_ms_insert",
                      "kernel_launches", "insert_launches", "suffix_launches", "h2d_bytes",
                      "d2h_bytes", "insert_children", "split_used", "prefixes_at_optimal",
-                     "prefixes_to_first", "ms_to_first"):
+                     "prefixes_to_first", "ms_to_first", "evaluations_run"):
             setattr(sol, name, getattr(r, name))
         for i in range(r.stored):
             sol.programs.append([progs[i * 16 + j] for j in range(lens[i])])
@@ -398,8 +472,21 @@ class Engine:
             setattr(sol, name, [arr[k] for k in range(min(last + 1, MAXD))])
         return sol
 
+    def tuning(self) -> dict:
+        """The autotuner's measured costs and launch choices (pcagb_tuning)."""
+        t = Tuning()
+        if self.lib.pcagb_tuning(self.h, ctypes.byref(t)) != 0:
+            raise EngineError(self.lib.pcagb_last_error().decode())
+        grid = lambda a: [[a[i][j] for j in range(4)] for i in range(4)]  # noqa: E731
+        return {"t_eval_ms": list(t.t_eval_ms), "t_child_ms": t.t_child_ms,
+                "t_build_fixed_ms": t.t_build_fixed_ms, "dedup_ratio": t.dedup_ratio,
+                "first_tests_ms": grid(t.first_tests_ms), "first_tests_n": grid(t.first_tests_n),
+                "chunk_ms": grid(t.chunk_ms), "chunk_n": grid(t.chunk_n),
+                "chunk_choices": grid(t.chunk_choices), "launch_rt_ms": t.launch_rt_ms}
+
     def solve_batch(self, tasks, max_depth=4, oep_mode=OEP_EXACT_LIVE, split_depth=-1,
-                    count_levels=False, sol_cap=64, on_done=None, first_only=False):
+                    count_levels=False, sol_cap=64, on_done=None, first_only=False,
+                    first_tests=0, suffix_chunk=0):
         """Solve many tasks in shared launches; returns one Solution per task
         (its `seconds` is that task's time-to-proven-optimal in the batch).
         on_done(i, Solution), if given, runs as soon as task i is decided."""
@@ -409,6 +496,7 @@ class Engine:
         self.lib.pcagb_default_opts(ctypes.byref(o))
         o.max_depth, o.split_depth, o.oep_mode = max_depth, split_depth, oep_mode
         o.count_levels, o.first_only = int(count_levels), int(first_only)
+        o.first_tests, o.suffix_chunk = first_tests, suffix_chunk
         res = (SolveResult * n)()
         cap = max(sol_cap, 1)
         progs = (ctypes.c_uint16 * (16 * cap * n))()
@@ -418,7 +506,7 @@ class Engine:
             sol = Solution(optimal_depth=r.optimal_depth, total_solutions=r.total_solutions)
             for name in ("seconds", "gpu_ms_expand", "gpu_ms_suffix", "gpu_ms_insert",
                          "kernel_launches", "insert_launches", "suffix_launches", "h2d_bytes",
-                         "d2h_bytes", "insert_children", "split_used"):
+                         "d2h_bytes", "insert_children", "split_used", "evaluations_run"):
                 setattr(sol, name, getattr(r, name))
             base = i * cap
             for k in range(r.stored):

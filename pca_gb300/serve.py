@@ -16,6 +16,8 @@ that fails (an engine error) hands its exception to every request of the
 batch still open (Request.error); the worker goes on with the next batch.
 `close()` stops new submissions and answers every request queued before it.
 
+`NativeServer` is the native server (server.cu) behind the same interface.
+
 `replay(trace)` drives a server from an arrival trace ((seconds, task)
 pairs, e.g. taskgen.poisson_stream) in real time and returns per-request
 records: arrival, completion, latency (time-to-proven-optimal), optimal
@@ -23,13 +25,15 @@ depth and programs.
 """
 from __future__ import annotations
 
+import ctypes
 import queue
 import threading
 import time
 import warnings
 from dataclasses import dataclass, field
 
-from .pcalib import Engine, OEP_EXACT_LIVE, Solution, device_memory
+from .pcalib import (Engine, EngineError, OEP_EXACT_LIVE, ServerConfig, ServerStats, Solution,
+                     SolveResult, device_memory, load_library, solution_from_result)
 
 
 @dataclass
@@ -43,6 +47,8 @@ class Request:
     solution: Solution | None = None
     batch_size: int = 0
     error: Exception | None = None   # the engine's error, when the solve failed
+    admitted: float = -1.0           # NativeServer: when a worker took it (server clock)
+    finished: float = -1.0           # NativeServer: when its task was decided (server clock)
 
     @property
     def latency(self) -> float:
@@ -155,6 +161,103 @@ class SerialServer(Server):
         super().__init__(slots=1, max_batch=1, max_depth=max_depth, device=device,
                          hbm_fraction=hbm_fraction, sol_cap=sol_cap, oep_mode=oep_mode,
                          engine_factory=engine_factory)
+
+
+class NativeServer:
+    """The native server (pcagb_server, server.cu) behind Server's interface:
+    admission by free HBM from one device pool (each solve reserves an arena
+    slice), up to `workers` solves at once on their own CUDA streams,
+    requests found queued together sharing one batched solve, and each
+    answer delivered when its task is decided. A collector thread takes
+    finished requests from the server in the order they finish."""
+
+    def __init__(self, workers: int = 8, max_batch: int = 64, max_depth: int = 4,
+                 device: int = 0, pool_bytes: int = 0, arena_bytes: int = 1 << 30,
+                 sol_cap: int = 16, oep_mode: int = OEP_EXACT_LIVE, lib=None):
+        self.lib = lib or load_library()
+        cfg = ServerConfig()
+        self.lib.pcagb_server_default_config(ctypes.byref(cfg))
+        cfg.device, cfg.pool_bytes, cfg.arena_bytes = device, pool_bytes, arena_bytes
+        cfg.workers, cfg.max_batch, cfg.sol_cap = workers, max_batch, sol_cap
+        cfg.opts.oep_mode = oep_mode
+        cfg.opts.first_only = 1
+        self.h = ctypes.c_void_p()
+        rc = self.lib.pcagb_server_create(ctypes.byref(cfg), ctypes.byref(self.h))
+        if rc != 0:
+            raise EngineError(f"server create failed ({rc}): "
+                              f"{self.lib.pcagb_server_last_error().decode()}")
+        self.max_depth = max_depth
+        self.sol_cap = sol_cap
+        self.t0 = time.perf_counter()
+        self.batches: list[int] = []
+        self._pending: dict[int, Request] = {}
+        self._lock = threading.Lock()
+        self._stop = False
+        self._collector = threading.Thread(target=self._collect, daemon=True)
+        self._collector.start()
+
+    def now(self) -> float:
+        return time.perf_counter() - self.t0
+
+    def submit(self, rid: int, task, max_depth: int | None = None) -> Request:
+        r = Request(rid, task, self.now(), self.max_depth if max_depth is None else max_depth)
+        with self._lock:
+            if self._stop:
+                raise RuntimeError("the server is closed")
+            nid = ctypes.c_uint64(0)
+            rc = self.lib.pcagb_server_submit(self.h, ctypes.byref(task), r.max_depth,
+                                              ctypes.byref(nid))
+            if rc != 0:
+                raise EngineError(self.lib.pcagb_server_last_error().decode())
+            self._pending[nid.value] = r
+        return r
+
+    def _collect(self):
+        cap = max(self.sol_cap, 1)
+        progs = (ctypes.c_uint16 * (16 * cap))()
+        lens = (ctypes.c_int * cap)()
+        times = (ctypes.c_double * 4)()
+        res = SolveResult()
+        nid = ctypes.c_uint64(0)
+        while True:
+            got = self.lib.pcagb_server_next(self.h, 0.1, ctypes.byref(nid))
+            if got != 1:
+                with self._lock:
+                    if self._stop and not self._pending:
+                        return
+                continue
+            rc = self.lib.pcagb_server_collect(self.h, nid.value, ctypes.byref(res), progs, lens,
+                                               cap, times)
+            with self._lock:
+                r = self._pending.pop(nid.value, None)
+            if r is None:
+                continue
+            if rc == 0:
+                r.solution = solution_from_result(res, progs, lens, 0, r.max_depth)
+            else:
+                r.error = EngineError(f"solve failed ({rc}): "
+                                      f"{self.lib.pcagb_server_last_error().decode()}")
+            r.batch_size = int(times[3])
+            r.admitted, r.finished = times[1], times[2]
+            r.finish = self.now()
+            r.done.set()
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        self.lib.pcagb_server_stats(self.h, ctypes.byref(st))
+        return {n: getattr(st, n) for n, _ in ServerStats._fields_}
+
+    def close(self, timeout: float = 120.0):
+        """Take no new requests, answer those already submitted, free the
+        server."""
+        with self._lock:
+            self._stop = True
+        self._collector.join(timeout=timeout)
+        if self.h:
+            st = self.stats()
+            self.batches = [0] * int(st["batches"])
+            self.lib.pcagb_server_destroy(self.h)
+            self.h = ctypes.c_void_p()
 
 
 def replay(server: Server, trace, max_depth: int | None = None) -> list[Request]:

@@ -28,3 +28,66 @@ def test_batch_first_only_matches_single(engine):
     for t, b in zip(tasks, batch):
         single = engine.solve(t, max_depth=4, first_only=True, sol_cap=1)
         assert (b.optimal_depth, b.programs) == (single.optimal_depth, single.programs)
+
+
+def test_launch_choices_change_no_answer(engine):
+    """The autotuner's other choices -- tests checked per lane before the
+    warp-wide check, middle chunk of the deeper suffix kernels, chunked
+    first-only stages -- forced to every value: the same optimal depth and
+    the same DFS-first program, from splits that run suffix depths 1-3."""
+    tasks = taskgen.synthetic_batch(120, seed=29)
+    sols = engine.solve_batch(tasks, max_depth=4, sol_cap=1, first_only=True)
+    picked = [t for t, s in zip(tasks, sols) if s.optimal_depth >= 3][:8]
+    picked += [t for t, s in zip(tasks, sols) if s.optimal_depth < 0][:2]
+    assert picked
+    for t in picked:
+        auto = engine.solve(t, max_depth=4, first_only=True, sol_cap=1)
+        for split in (1, 2, 3):
+            for ft in (1, 2, 3):
+                for ck in (1, 5, 16, 64):
+                    if split == 3 and ck != 1:
+                        continue   # suffix depth 1 has no middle chunk
+                    f = engine.solve(t, max_depth=4, first_only=True, sol_cap=1, split_depth=split,
+                                     first_tests=ft, suffix_chunk=ck)
+                    assert (f.optimal_depth, f.programs) == (auto.optimal_depth, auto.programs)
+        for launch in (-1, 1, 7, 4096):
+            f = engine.solve(t, max_depth=4, first_only=True, sol_cap=1, stage_launch=launch)
+            assert (f.optimal_depth, f.programs) == (auto.optimal_depth, auto.programs)
+
+
+def test_launch_choices_keep_full_sets(engine):
+    """Every solving program, not only the first: the full set at the
+    optimal depth is the same under each tests-per-lane and chunk choice."""
+    tasks = taskgen.synthetic_batch(60, seed=31)
+    sols = engine.solve_batch(tasks, max_depth=3, sol_cap=1, first_only=True)
+    picked = [t for t, s in zip(tasks, sols) if s.optimal_depth >= 2][:5]
+    for t in picked:
+        base = engine.solve(t, max_depth=3, split_depth=0, sol_cap=1 << 14)
+        for ft in (1, 2, 3):
+            for ck in (1, 3, 16):
+                s = engine.solve(t, max_depth=3, split_depth=0, sol_cap=1 << 14, first_tests=ft,
+                                 suffix_chunk=ck)
+                assert s.optimal_depth == base.optimal_depth
+                assert s.total_solutions == base.total_solutions
+                assert s.programs == base.programs
+
+
+def test_tuner_measures_every_choice():
+    """On stages large enough to time, the tuner tries each tests-per-lane
+    choice once before settling on the cheapest: after four is_power2
+    depth-4 solves (their depth-4 stage, suffix depth 1, is large enough)
+    every choice has a measured cost, and the answers never change. A fresh
+    engine on the device starts from the costs earlier engines measured, so
+    the check is on the counts having grown to at least one."""
+    from pca_gb300.pcalib import Engine
+    t = taskgen.is_power2_task(1)
+    eng = Engine(0, 8 << 30)
+    try:
+        outs = [eng.solve(t, max_depth=4, split_depth=3, sol_cap=1) for _ in range(4)]
+        tun = eng.tuning()
+    finally:
+        eng.close()
+    assert all(o.optimal_depth == -1 for o in outs)
+    assert all(tun["first_tests_n"][1][ft] >= 1 for ft in (1, 2, 3))
+    assert all(tun["first_tests_ms"][1][ft] > 0 for ft in (1, 2, 3))
+    assert tun["t_eval_ms"][1] > 0 and tun["launch_rt_ms"] > 0

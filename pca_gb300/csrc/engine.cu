@@ -693,8 +693,10 @@ int take_records(pcagb_engine *e, int S, int K, std::vector<TaskRun> &runs, bool
 /* Middle-instruction chunks the depth-2 and depth-3 suffix kernels may take
    per work item, by suffix depth (index 0 is unused). */
 constexpr uint32_t kChunkChoices[4][4] = {{1, 1, 1, 1}, {1, 1, 1, 1}, {4, 8, 16, 32}, {1, 2, 4, 8}};
-/* A stage is large enough to measure a launch choice on. */
+/* A stage is large enough to measure a launch choice on; each choice is
+   measured this many times before the cheapest is kept. */
 constexpr uint64_t kTuneMinEvals = 20000000ull;
+constexpr int kTuneSamples = 2;
 
 /* The option to use among n with measured costs ms[i] (n_meas[i] stages):
    an unmeasured one first when exploring, else the cheapest measured; def
@@ -702,8 +704,9 @@ constexpr uint64_t kTuneMinEvals = 20000000ull;
 int pick_option(const double *ms, const int *n_meas, int n, int def, bool explore)
 {
     if (explore)
-        for (int i = 0; i < n; i++)
-            if (n_meas[i] == 0) return i;
+        for (int round = 1; round <= kTuneSamples; round++)
+            for (int i = 0; i < n; i++)
+                if (n_meas[i] < round) return i;
     int best = -1;
     for (int i = 0; i < n; i++)
         if (n_meas[i] > 0 && (best < 0 || ms[i] < ms[best])) best = i;
@@ -777,7 +780,8 @@ int run_stage(pcagb_engine *e, int S, int K, std::vector<TaskRun> &runs, bool fi
                 chunk = (uint32_t)std::min(e->force_chunk, 64);
             } else {
                 /* chunks are explored once the tests-per-lane choice is */
-                const bool ft_done = e->ft_n[s][1] && e->ft_n[s][2] && e->ft_n[s][3];
+                const bool ft_done = e->ft_n[s][1] >= kTuneSamples &&
+                                     e->ft_n[s][2] >= kTuneSamples && e->ft_n[s][3] >= kTuneSamples;
                 ck = pick_option(e->ck_ms[s], e->ck_n[s], 4, s == 2 ? 2 : 0, explore && ft_done);
                 chunk = kChunkChoices[s][ck];
             }
@@ -1559,6 +1563,30 @@ int engine_init(pcagb_engine *e, int device, size_t budget)
     CK(cudaEventCreate(&e->ev2));
     CK(cudaEventCreate(&e->ev3));
     {
+        /* CUDA loads a kernel at its first launch; load them all now, so no
+           solve pays a module load inside its timing (the autotuner's
+           measured costs) or a served request's latency */
+        cudaFuncAttributes fa;
+#define PCAGB_PRELOAD(...) cudaFuncGetAttributes(&fa, __VA_ARGS__)
+        PCAGB_PRELOAD(k_suffix<16, 1, 1>); PCAGB_PRELOAD(k_suffix<16, 1, 2>);
+        PCAGB_PRELOAD(k_suffix<16, 1, 3>); PCAGB_PRELOAD(k_suffix<16, 2, 1>);
+        PCAGB_PRELOAD(k_suffix<16, 2, 2>); PCAGB_PRELOAD(k_suffix<16, 2, 3>);
+        PCAGB_PRELOAD(k_suffix<16, 3, 1>); PCAGB_PRELOAD(k_suffix<16, 3, 2>);
+        PCAGB_PRELOAD(k_suffix<16, 3, 3>); PCAGB_PRELOAD(k_suffix<32, 1, 1>);
+        PCAGB_PRELOAD(k_suffix<32, 1, 2>); PCAGB_PRELOAD(k_suffix<32, 1, 3>);
+        PCAGB_PRELOAD(k_suffix<32, 2, 1>); PCAGB_PRELOAD(k_suffix<32, 2, 2>);
+        PCAGB_PRELOAD(k_suffix<32, 2, 3>); PCAGB_PRELOAD(k_suffix<32, 3, 1>);
+        PCAGB_PRELOAD(k_suffix<32, 3, 2>); PCAGB_PRELOAD(k_suffix<32, 3, 3>);
+        PCAGB_PRELOAD(k_expand_insert<16>); PCAGB_PRELOAD(k_expand_insert<32>);
+        PCAGB_PRELOAD(k_materialize<16>); PCAGB_PRELOAD(k_materialize<32>);
+        PCAGB_PRELOAD(k_twins<16>); PCAGB_PRELOAD(k_twins<32>);
+        PCAGB_PRELOAD(k_leaf<16>); PCAGB_PRELOAD(k_leaf<32>);
+        PCAGB_PRELOAD(k_count_evals); PCAGB_PRELOAD(k_mark); PCAGB_PRELOAD(k_mark_all);
+        PCAGB_PRELOAD(k_popc); PCAGB_PRELOAD(k_child_counts); PCAGB_PRELOAD(k_task_hist);
+        PCAGB_PRELOAD(k_task_hist_smem); PCAGB_PRELOAD(k_scan_local); PCAGB_PRELOAD(k_scan_add);
+        PCAGB_PRELOAD(k_gather_paths); PCAGB_PRELOAD(k_check_perm);
+#undef PCAGB_PRELOAD
+        cudaGetLastError();
         /* the insert kernel keeps each warp's children in shared memory:
            its occupancy needs the largest shared-memory carveout */
         cudaFuncSetAttribute(k_expand_insert<32>, cudaFuncAttributePreferredSharedMemoryCarveout,

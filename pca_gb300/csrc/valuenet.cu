@@ -14,12 +14,12 @@
  * flag bits (4). Every state has 32 feature rows; rows of tests >= T are
  * zero and are left out of the pooling.
  *
- * All matrix products are BF16 tensor-core MMAs with FP32 accumulation
- * (mma.sync m16n8k16): C[M,N] = A[M,K] . B[N,K]^T for the forward pass and
- * the input gradients, and a split-K dW[N,K] += dY[M,N]^T . X[M,K] for the
- * weight gradients. Parameters are FP32 masters with BF16 copies (row-major
- * [out][in] and transposed [in][out]) refreshed by the Adam kernel.
- * Launches go to the stream the caller passes.
+ * The matrix products run on the fifth-generation tensor cores
+ * (valuenet_tc.cu: the fused scoring encoder and the training GEMM); this
+ * file holds the features, pooling, loss, Adam and sampling kernels.
+ * Parameters are FP32 masters with BF16 copies (row-major [out][in] and
+ * transposed [in][out]) refreshed by the Adam kernel. Launches go to the
+ * stream the caller passes.
  */
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -32,172 +32,6 @@
 #include "../../include/pca_gb300.h"
 
 namespace {
-
-constexpr int BM = 64, BN = 64, BK = 32, PAD = 8;
-
-__device__ __forceinline__ void mma_bf16(float (&c)[4], uint32_t a0, uint32_t a1, uint32_t a2,
-                                         uint32_t a3, uint32_t b0, uint32_t b1)
-{
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
-        "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
-        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
-}
-
-/* Warp computes a 32x32 tile from As[64][BK+PAD] / Bs[64][BK+PAD] rows
- * (wm, wn) over one BK slab. */
-__device__ __forceinline__ void warp_tile_mma(const __nv_bfloat16 (*As)[BK + PAD],
-                                              const __nv_bfloat16 (*Bs)[BK + PAD], int wm, int wn,
-                                              int lane, float (&acc)[2][4][4])
-{
-    const int g = lane >> 2, t = lane & 3;
-#pragma unroll
-    for (int kk = 0; kk < BK; kk += 16) {
-        uint32_t a[2][4], b[4][2];
-#pragma unroll
-        for (int mi = 0; mi < 2; mi++) {
-            const int r = wm + mi * 16 + g;
-            a[mi][0] = *(const uint32_t *)&As[r][kk + 2 * t];
-            a[mi][1] = *(const uint32_t *)&As[r + 8][kk + 2 * t];
-            a[mi][2] = *(const uint32_t *)&As[r][kk + 2 * t + 8];
-            a[mi][3] = *(const uint32_t *)&As[r + 8][kk + 2 * t + 8];
-        }
-#pragma unroll
-        for (int ni = 0; ni < 4; ni++) {
-            const int r = wn + ni * 8 + g;
-            b[ni][0] = *(const uint32_t *)&Bs[r][kk + 2 * t];
-            b[ni][1] = *(const uint32_t *)&Bs[r][kk + 2 * t + 8];
-        }
-#pragma unroll
-        for (int mi = 0; mi < 2; mi++)
-#pragma unroll
-            for (int ni = 0; ni < 4; ni++)
-                mma_bf16(acc[mi][ni], a[mi][0], a[mi][1], a[mi][2], a[mi][3], b[ni][0], b[ni][1]);
-    }
-}
-
-/* Load a 64 x 32 bf16 tile of a row-major matrix (rows r0.., cols k0..),
- * zero outside [rows, cols). cols is a multiple of 8. */
-__device__ __forceinline__ void load_tile(__nv_bfloat16 (*S)[BK + PAD], const __nv_bfloat16 *G,
-                                          int ld, int r0, int k0, int rows, int cols, int tid)
-{
-#pragma unroll
-    for (int i = 0; i < 2; i++) {
-        const int c = tid + i * 128;      /* 256 chunks of 8 bf16 */
-        const int r = c >> 2, kc = (c & 3) * 8;
-        uint4 v = make_uint4(0, 0, 0, 0);
-        if (r0 + r < rows && k0 + kc < cols)
-            v = *(const uint4 *)(G + (size_t)(r0 + r) * ld + k0 + kc);
-        *(uint4 *)&S[r][kc] = v;
-    }
-}
-
-/* C[M,N] = A[M,K] . B[N,K]^T (+ bias[N]) (ReLU); bf16 or fp32 output. */
-__global__ void __launch_bounds__(128)
-k_gemm_nt(const __nv_bfloat16 *A, const __nv_bfloat16 *B, const float *bias, __nv_bfloat16 *Cb,
-          float *Cf, int M, int N, int K, int lda, int ldb, int ldc, int relu)
-{
-    __shared__ __align__(16) __nv_bfloat16 As[BM][BK + PAD];
-    __shared__ __align__(16) __nv_bfloat16 Bs[BN][BK + PAD];
-    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-    const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
-    const int wm = (w >> 1) * 32, wn = (w & 1) * 32;
-    float acc[2][4][4] = {};
-    for (int k0 = 0; k0 < K; k0 += BK) {
-        load_tile(As, A, lda, m0, k0, M, K, tid);
-        load_tile(Bs, B, ldb, n0, k0, N, K, tid);
-        __syncthreads();
-        warp_tile_mma(As, Bs, wm, wn, lane, acc);
-        __syncthreads();
-    }
-    const int g = lane >> 2, t = lane & 3;
-#pragma unroll
-    for (int mi = 0; mi < 2; mi++)
-#pragma unroll
-        for (int ni = 0; ni < 4; ni++)
-#pragma unroll
-            for (int h = 0; h < 2; h++) {
-                const int r = m0 + wm + mi * 16 + g + h * 8;
-                const int c = n0 + wn + ni * 8 + 2 * t;
-                if (r >= M || c >= N) continue;
-                float v0 = acc[mi][ni][2 * h], v1 = acc[mi][ni][2 * h + 1];
-                if (bias) {
-                    v0 += bias[c];
-                    v1 += bias[c + 1];
-                }
-                if (relu) {
-                    v0 = fmaxf(v0, 0.f);
-                    v1 = fmaxf(v1, 0.f);
-                }
-                if (Cb) *(__nv_bfloat162 *)(Cb + (size_t)r * ldc + c) = __floats2bfloat162_rn(v0, v1);
-                if (Cf) {
-                    Cf[(size_t)r * ldc + c] = v0;
-                    Cf[(size_t)r * ldc + c + 1] = v1;
-                }
-            }
-}
-
-/* dW[N,K] += dY[M,N]^T . X[M,K]; blocks split M (grid.z) and add with
- * atomics. Tiles are loaded along m and transposed into shared memory. */
-__global__ void __launch_bounds__(128)
-k_gemm_tn_acc(const __nv_bfloat16 *Y, const __nv_bfloat16 *X, float *dW, int M, int N, int K,
-              int ldy, int ldx, int m_per_split)
-{
-    __shared__ __align__(16) __nv_bfloat16 As[BM][BK + PAD];   /* [n][m] */
-    __shared__ __align__(16) __nv_bfloat16 Bs[BN][BK + PAD];   /* [k][m] */
-    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-    const int n0 = blockIdx.y * BM, k0 = blockIdx.x * BN;
-    const int wm = (w >> 1) * 32, wn = (w & 1) * 32;
-    const int mbeg = blockIdx.z * m_per_split;
-    const int mend = min(M, mbeg + m_per_split);
-    float acc[2][4][4] = {};
-    for (int ms = mbeg; ms < mend; ms += BK) {
-        /* 32 m-rows x 64 columns of each operand: 256 chunks of 8 bf16 */
-#pragma unroll
-        for (int i = 0; i < 2; i++) {
-            const int c = tid + i * 128;
-            const int mr = c >> 3, cc = (c & 7) * 8;
-            uint4 vy = make_uint4(0, 0, 0, 0), vx = make_uint4(0, 0, 0, 0);
-            if (ms + mr < mend) {
-                if (n0 + cc < N) vy = *(const uint4 *)(Y + (size_t)(ms + mr) * ldy + n0 + cc);
-                if (k0 + cc < K) vx = *(const uint4 *)(X + (size_t)(ms + mr) * ldx + k0 + cc);
-            }
-            const __nv_bfloat16 *py = (const __nv_bfloat16 *)&vy, *px = (const __nv_bfloat16 *)&vx;
-#pragma unroll
-            for (int j = 0; j < 8; j++) {
-                As[cc + j][mr] = py[j];
-                Bs[cc + j][mr] = px[j];
-            }
-        }
-        __syncthreads();
-        warp_tile_mma(As, Bs, wm, wn, lane, acc);
-        __syncthreads();
-    }
-    const int g = lane >> 2, t = lane & 3;
-#pragma unroll
-    for (int mi = 0; mi < 2; mi++)
-#pragma unroll
-        for (int ni = 0; ni < 4; ni++)
-#pragma unroll
-            for (int h = 0; h < 2; h++) {
-                const int r = n0 + wm + mi * 16 + g + h * 8;
-                const int c = k0 + wn + ni * 8 + 2 * t;
-                if (r >= N || c >= K) continue;
-                atomicAdd(&dW[(size_t)r * K + c], acc[mi][ni][2 * h]);
-                atomicAdd(&dW[(size_t)r * K + c + 1], acc[mi][ni][2 * h + 1]);
-            }
-}
-
-/* db[n] += sum over rows of dY[M][N] (bf16). */
-__global__ void k_colsum(const __nv_bfloat16 *Y, float *db, int M, int N, int ld)
-{
-    const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= N) return;
-    float s = 0.f;
-    for (int m = blockIdx.y; m < M; m += gridDim.y) s += __bfloat162float(Y[(size_t)m * ld + n]);
-    atomicAdd(&db[n], s);
-}
 
 /* Features of states in the engine's level layout. Row (state i, test t)
  * of X[n*32][176]; rows of tests >= T are zero. */
@@ -288,10 +122,11 @@ __global__ void k_relu_bwd(__nv_bfloat16 *dY, const __nv_bfloat16 *Y, size_t cou
  * the remaining steps over the positives. Writes dLogits[n][16] (bf16) of the
  * mean loss, and accumulates [bce_sum, ce_sum, n_pos] into stats. */
 __global__ void k_loss(const float *logits, const float *label, const int32_t *remaining, int n,
-                       float pos_weight, float n_pos_total, __nv_bfloat16 *dlogits, float *stats)
+                       float pos_weight, const float *n_pos, __nv_bfloat16 *dlogits, float *stats)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const float n_pos_total = *n_pos;   /* positives in the batch (on the device) */
     const float *z = logits + (size_t)i * 16;
     const float y = label[i];
     const float zr = z[0];
@@ -321,13 +156,16 @@ __global__ void k_loss(const float *logits, const float *label, const int32_t *r
     atomicAdd(&stats[1], ce);
 }
 
-/* Adam on fp32 masters, then the bf16 copies [out][in] and [in][out]. */
+/* Adam on fp32 masters, then the bf16 copies [out][in] and [in][out]. The
+   step count lives on the device (so a captured training step replays with
+   the right bias corrections). */
 __global__ void k_adam(float *W, const float *G, float *m, float *v, int out, int in, float lr,
-                       float b1, float b2, float eps, float bc1, float bc2, __nv_bfloat16 *Wb,
+                       float b1, float b2, float eps, const int *step, __nv_bfloat16 *Wb,
                        __nv_bfloat16 *Wt)
 {
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= out * in) return;
+    const float bc1 = 1.f - powf(b1, (float)*step), bc2 = 1.f - powf(b2, (float)*step);
     const float g = G[idx];
     const float mi = b1 * m[idx] + (1.f - b1) * g;
     const float vi = b2 * v[idx] + (1.f - b2) * g * g;
@@ -427,41 +265,6 @@ int pcagb_vnet_compose_order(const void *src, const long long *ranked, int m, ui
     return launch_ok();
 }
 
-int pcagb_vnet_gemm_nt(const void *A, const void *B, const float *bias, void *C_bf16,
-                       float *C_f32, int M, int N, int K, int lda, int ldb, int ldc, int relu,
-                       void *stream)
-{
-    if (M <= 0 || N <= 0 || K <= 0 || (K & 7) || (N & 1)) return PCAGB_EINVAL;
-    dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM);
-    k_gemm_nt<<<grid, 128, 0, (cudaStream_t)stream>>>(
-        (const __nv_bfloat16 *)A, (const __nv_bfloat16 *)B, bias, (__nv_bfloat16 *)C_bf16, C_f32,
-        M, N, K, lda, ldb, ldc, relu);
-    return launch_ok();
-}
-
-int pcagb_vnet_gemm_tn_acc(const void *Y, const void *X, float *dW, int M, int N, int K, int ldy,
-                           int ldx, void *stream)
-{
-    if (M <= 0 || N <= 0 || K <= 0 || (K & 7) || (N & 7)) return PCAGB_EINVAL;
-    int splits = (M + 4095) / 4096;
-    if (splits > 1024) splits = 1024;
-    int per = (M + splits - 1) / splits;
-    per = (per + BK - 1) / BK * BK;
-    splits = (M + per - 1) / per;
-    dim3 grid((K + BN - 1) / BN, (N + BM - 1) / BM, splits);
-    k_gemm_tn_acc<<<grid, 128, 0, (cudaStream_t)stream>>>((const __nv_bfloat16 *)Y,
-                                                          (const __nv_bfloat16 *)X, dW, M, N, K,
-                                                          ldy, ldx, per);
-    return launch_ok();
-}
-
-int pcagb_vnet_colsum(const void *Y, float *db, int M, int N, int ld, void *stream)
-{
-    dim3 grid((N + 127) / 128, M < 256 ? M : 256);
-    k_colsum<<<grid, 128, 0, (cudaStream_t)stream>>>((const __nv_bfloat16 *)Y, db, M, N, ld);
-    return launch_ok();
-}
-
 int pcagb_vnet_features(const uint16_t *regs, const uint8_t *flags, const uint16_t *task, int TP,
                         int n, const uint16_t *task_io, const int32_t *task_T, void *X,
                         void *stream)
@@ -501,21 +304,22 @@ int pcagb_vnet_relu_bwd(void *dY, const void *Y, size_t count, void *stream)
 }
 
 int pcagb_vnet_loss(const float *logits, const float *label, const int32_t *remaining, int n,
-                    float pos_weight, float n_pos_total, void *dlogits, float *stats, void *stream)
+                    float pos_weight, const float *n_pos, void *dlogits, float *stats,
+                    void *stream)
 {
     if (n <= 0) return PCAGB_OK;
     k_loss<<<(n + 255) / 256, 256, 0, (cudaStream_t)stream>>>(
-        logits, label, remaining, n, pos_weight, n_pos_total, (__nv_bfloat16 *)dlogits, stats);
+        logits, label, remaining, n, pos_weight, n_pos, (__nv_bfloat16 *)dlogits, stats);
     return launch_ok();
 }
 
 int pcagb_vnet_adam(float *W, const float *G, float *m, float *v, int out, int in, float lr,
-                    float b1, float b2, float eps, int step, void *Wb, void *Wt, void *stream)
+                    float b1, float b2, float eps, const int *step, void *Wb, void *Wt,
+                    void *stream)
 {
-    const float bc1 = 1.f - powf(b1, (float)step), bc2 = 1.f - powf(b2, (float)step);
     const int count = out * in;
     k_adam<<<(count + 255) / 256, 256, 0, (cudaStream_t)stream>>>(
-        W, G, m, v, out, in, lr, b1, b2, eps, bc1, bc2, (__nv_bfloat16 *)Wb, (__nv_bfloat16 *)Wt);
+        W, G, m, v, out, in, lr, b1, b2, eps, step, (__nv_bfloat16 *)Wb, (__nv_bfloat16 *)Wt);
     return launch_ok();
 }
 

@@ -509,6 +509,203 @@ k_encode_pool_tc(const __grid_constant__ CUtensorMap map_w1, const __grid_consta
                      : "memory");
 }
 
+/* ---- the training GEMM ------------------------------------------------------
+ *
+ * C[M,N] = A[M,K] . B[N,K]^T on tcgen05, both operands K-major bf16 in HBM,
+ * FP32 accumulation in TMEM. One CTA per 128 x bn tile of C (bn <= 256, a
+ * multiple of 16), grid.z splits K. Warp 0 (one thread) streams 64-column K
+ * blocks of A (128 rows) and B (bn rows) by TMA with 128-byte swizzle
+ * through a two-stage mbarrier ring; warp 1 owns TMEM and one thread issues
+ * four tcgen05.mma (M=128, N=bn, K=16) per block; then all four warps drain
+ * the accumulators (warp w: TMEM lanes 32w..32w+31 = tile rows) with
+ * tcgen05.ld. Epilogue: with one K split, + bias, x (mask > 0) (the ReLU
+ * derivative through a stored activation), ReLU, stored as bf16 or fp32;
+ * with several, fp32 atomic adds into C (zeroed by the caller). Out-of-range
+ * rows and columns of A and B are TMA zero fill; stores are bounds checked.
+ * Every wait is bounded by the global timer; a wait that runs out sets the
+ * abort flag and *status, each role leaves, and TMEM is freed. Two CTAs fit
+ * an SM (96 KB of shared memory at bn = 256), so one CTA's epilogue overlaps
+ * the other's loads and MMAs. */
+constexpr int kGRows = 128, kGBK = 64, kGStages = 2;
+constexpr int kGABytes = kGRows * 128;              /* 16 KB per A stage */
+
+__global__ void __launch_bounds__(128, 2)
+k_gemm_tc(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
+          const float *__restrict__ bias, const __nv_bfloat16 *__restrict__ mask, int ldm,
+          __nv_bfloat16 *__restrict__ Cb, float *__restrict__ Cf, int ldc, int M, int N,
+          int kblocks, int kb_per_split, int bn, uint32_t idesc, uint32_t tmem_cols, int relu,
+          int atomic_out, int *status)
+{
+    extern __shared__ uint8_t gsmem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)gsmem_raw + 1023) & ~(uintptr_t)1023);
+    const uint32_t b_bytes = (uint32_t)bn * 128u;
+    const uint32_t sA = smem_u32(smem);
+    const uint32_t sB = sA + kGStages * kGABytes;
+    uint8_t *ctl = smem + kGStages * (kGABytes + b_bytes);
+    const uint32_t sBar = smem_u32(ctl);
+    uint32_t *tmem_slot = (uint32_t *)(ctl + 64);
+    volatile int *abort_flag = (volatile int *)(ctl + 68);
+    auto full = [&](int s) { return sBar + 8u * (uint32_t)s; };
+    auto empty = [&](int s) { return sBar + 8u * (uint32_t)(kGStages + s); };
+    const uint32_t done_bar = sBar + 8u * (uint32_t)(2 * kGStages);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int m0 = blockIdx.y * kGRows, n0 = blockIdx.x * bn;
+    const int kb0 = blockIdx.z * kb_per_split;
+    const int nk = min(kblocks, kb0 + kb_per_split) - kb0;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kGStages; s++) {
+            mbar_init(full(s), 1);
+            mbar_init(empty(s), 1);
+        }
+        mbar_init(done_bar, 1);
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        fence_async_smem();
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32(tmem_slot)), "r"(tmem_cols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_before();
+    __syncthreads();
+    tc_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0 && lane == 0 && nk > 0) {
+        /* producer */
+        int i = 0;
+        for (; i < nk; i++) {
+            const int st = i % kGStages;
+            const uint32_t ph = (uint32_t)(i / kGStages) & 1u;
+            if (!mbar_wait(empty(st), ph ^ 1u, abort_flag, status, 11)) break;
+            mbar_expect_tx(full(st), kGABytes + b_bytes);
+            const int x = (kb0 + i) * kGBK;
+            tma_load_2d(sA + st * kGABytes, &map_a, full(st), x, m0);
+            tma_load_2d(sB + st * b_bytes, &map_b, full(st), x, n0);
+        }
+        /* the copies this thread issued land before the CTA leaves */
+        for (int j = i - 1; j >= 0 && j >= i - kGStages; j--) {
+            const unsigned long long t0 = global_ns();
+            while (!mbar_test(full(j % kGStages), (uint32_t)(j / kGStages) & 1u) &&
+                   global_ns() - t0 < kWaitNs) {
+            }
+        }
+    } else if (warp == 1 && lane == 0) {
+        /* MMA issuer */
+        for (int i = 0; i < nk; i++) {
+            const int st = i % kGStages;
+            const uint32_t ph = (uint32_t)(i / kGStages) & 1u;
+            if (!mbar_wait(full(st), ph, abort_flag, status, 12)) break;
+            tc_after();
+            const uint32_t a0 = sA + st * kGABytes, b0 = sB + st * b_bytes;
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const uint64_t da = sw128_desc(a0 + 32 * k), db = sw128_desc(b0 + 32 * k);
+                const uint32_t acc = (i | k) != 0;
+                asm volatile(
+                    "{\n\t.reg .pred p;\n\t"
+                    "setp.ne.b32 p, %4, 0;\n\t"
+                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+                    "l"(da), "l"(db), "r"(idesc), "r"(acc)
+                    : "memory");
+            }
+            mma_commit(empty(st));
+        }
+        /* arrives once every MMA above has completed (also after an abort);
+           this thread waits for it, so TMEM is never freed under an MMA */
+        mma_commit(done_bar);
+        const unsigned long long t0 = global_ns();
+        while (!mbar_test(done_bar, 0) && global_ns() - t0 < kWaitNs) {
+        }
+    }
+    __syncwarp();
+    /* epilogue: all four warps */
+    bool ok = nk > 0 && mbar_wait(done_bar, 0, abort_flag, status, 13);
+    ok = __all_sync(0xFFFFFFFFu, ok) && !*abort_flag;
+    tc_after();
+    if (ok) {
+        const int row = m0 + warp * 32 + lane;
+        const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+        for (int c0 = 0; c0 < bn; c0 += 32) {
+            uint32_t acc[32];
+            tmem_ld32(tmem + lane_base + (uint32_t)c0, acc);
+            if (row >= M) continue;
+            const int colb = n0 + c0;
+            if (atomic_out) {
+#pragma unroll
+                for (int j = 0; j < 32; j++)
+                    if (colb + j < N) atomicAdd(Cf + (size_t)row * ldc + colb + j, __uint_as_float(acc[j]));
+                continue;
+            }
+#pragma unroll
+            for (int j = 0; j < 32; j += 2) {
+                const int c = colb + j;
+                if (c >= N) continue;
+                float v0 = __uint_as_float(acc[j]), v1 = __uint_as_float(acc[j + 1]);
+                if (bias) {
+                    v0 += bias[c];
+                    if (c + 1 < N) v1 += bias[c + 1];
+                }
+                if (mask) {
+                    const __nv_bfloat16 *mr = mask + (size_t)row * ldm + c;
+                    if (!(__bfloat162float(mr[0]) > 0.f)) v0 = 0.f;
+                    if (c + 1 < N && !(__bfloat162float(mr[1]) > 0.f)) v1 = 0.f;
+                }
+                if (relu) {
+                    v0 = fmaxf(v0, 0.f);
+                    v1 = fmaxf(v1, 0.f);
+                }
+                if (Cb) {
+                    if (c + 1 < N)
+                        *(__nv_bfloat162 *)(Cb + (size_t)row * ldc + c) = __floats2bfloat162_rn(v0, v1);
+                    else
+                        Cb[(size_t)row * ldc + c] = __float2bfloat16(v0);
+                }
+                if (Cf) {
+                    Cf[(size_t)row * ldc + c] = v0;
+                    if (c + 1 < N) Cf[(size_t)row * ldc + c + 1] = v1;
+                }
+            }
+        }
+    }
+    tc_before();
+    __syncthreads();
+    tc_after();
+    if (warp == 1)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                     "r"(tmem_cols)
+                     : "memory");
+}
+
+/* T[c][r] = S[r][c] for c < C; row C of T is ones when `ones` (the bias
+   column of an augmented operand), rows up to Cp zeros. 32 x 32 tiles
+   through shared memory: both sides coalesced. */
+__global__ void k_transpose_aug(const __nv_bfloat16 *__restrict__ S, int R, int C, int lds,
+                                __nv_bfloat16 *__restrict__ T, int Cp, int ldt, int ones)
+{
+    __shared__ __nv_bfloat16 tile[32][33];
+    const int r0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
+    const int tx = threadIdx.x, ty = threadIdx.y;   /* 32 x 8 */
+    for (int k = ty; k < 32; k += 8) {
+        const int r = r0 + k, c = c0 + tx;
+        float v = 0.f;
+        if (r < R) {
+            if (c < C) v = __bfloat162float(S[(size_t)r * lds + c]);
+            else if (c == C && ones) v = 1.f;
+        }
+        tile[k][tx] = __float2bfloat16(v);
+    }
+    __syncthreads();
+    for (int k = ty; k < 32; k += 8) {
+        const int c = c0 + k, r = r0 + tx;
+        if (c < Cp && r < R) T[(size_t)c * ldt + r] = tile[tx][k];
+    }
+}
+
 typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
                                   const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
                                   const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
@@ -544,7 +741,80 @@ bool weight_map(CUtensorMap *m, const void *W, int K)
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+/* Tensor map of a row-major [rows][cols] bf16 matrix (row stride ld
+   elements), boxes of 64 columns x box_rows rows, 128-byte swizzle. */
+bool tile_map(CUtensorMap *m, const void *ptr, int rows, int cols, int ld, int box_rows)
+{
+    EncodeTiledFn fn = encode_fn();
+    if (!fn) return false;
+    cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
+    cuuint32_t box[2] = {64, (cuuint32_t)box_rows};
+    cuuint32_t estr[2] = {1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(ptr), dims, strides, box,
+              estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+              CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 }  // namespace
+
+/* C[M,N] = A[M,K] . B[N,K]^T on tcgen05 (k_gemm_tc): bias[N] added, then
+ * columns where mask[M][N] (bf16, leading dimension ldm) is not positive
+ * zeroed, then ReLU, into Cb (bf16) and/or Cf (fp32), leading dimension ldc.
+ * splits > 1 divides K among CTAs that add fp32 partial sums into Cf (zeroed
+ * by the caller; no bias, mask, ReLU or Cb then). A and B: leading
+ * dimensions multiples of 8 elements, 16-byte aligned. *status gets a
+ * nonzero code if a barrier wait ran out (the result is then void). */
+extern "C" int pcagb_vnet_gemm_tc(const void *A, int lda, const void *B, int ldb,
+                                  const float *bias, const void *mask, int ldm, void *Cb,
+                                  float *Cf, int ldc, int M, int N, int K, int relu, int splits,
+                                  int *status, void *stream)
+{
+    if (M <= 0 || N <= 0 || K <= 0) return PCAGB_OK;
+    if (!A || !B || !status || (!Cb && !Cf) || (lda & 7) || (ldb & 7) || lda < K || ldb < K ||
+        ((uintptr_t)A & 15) || ((uintptr_t)B & 15) || splits < 1 ||
+        (splits > 1 && (!Cf || Cb || bias || mask || relu)))
+        return PCAGB_EINVAL;
+    const int bn = N > 256 ? 256 : (N + 15) / 16 * 16;
+    uint32_t tcols = 32;
+    while (tcols < (uint32_t)bn) tcols <<= 1;
+    CUtensorMap ma, mb;
+    if (!tile_map(&ma, A, M, K, lda, kGRows) || !tile_map(&mb, B, N, K, ldb, bn))
+        return PCAGB_ECUDA;
+    const int kblocks = (K + kGBK - 1) / kGBK;
+    if (splits > kblocks) splits = kblocks;
+    const int per = (kblocks + splits - 1) / splits;
+    splits = (kblocks + per - 1) / per;
+    const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(bn >> 3) << 17) |
+                           ((uint32_t)(kGRows >> 4) << 24);
+    const int smem = kGStages * (kGABytes + bn * 128) + 256 + 1024;
+    static std::once_flag attr_once;
+    static cudaError_t attr_err = cudaSuccess;
+    std::call_once(attr_once, [] {
+        attr_err = cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        kGStages * (kGABytes + 256 * 128) + 256 + 1024);
+    });
+    if (attr_err != cudaSuccess) return PCAGB_ECUDA;
+    dim3 grid((N + bn - 1) / bn, (M + kGRows - 1) / kGRows, splits);
+    k_gemm_tc<<<grid, 128, smem, (cudaStream_t)stream>>>(
+        ma, mb, bias, (const __nv_bfloat16 *)mask, ldm, (__nv_bfloat16 *)Cb, Cf, ldc, M, N,
+        kblocks, per, bn, idesc, tcols, relu, splits > 1, status);
+    return cudaGetLastError() == cudaSuccess ? PCAGB_OK : PCAGB_ECUDA;
+}
+
+/* T[Cp][ldt] from S[R][lds]: T[c][r] = S[r][c] for c < C, row C ones when
+ * `ones` (else zeros), rows C+1..Cp-1 zeros. */
+extern "C" int pcagb_vnet_transpose_aug(const void *S, int R, int C, int lds, void *T, int Cp,
+                                        int ldt, int ones, void *stream)
+{
+    if (R <= 0 || Cp <= 0) return PCAGB_OK;
+    if (!S || !T || Cp < C || ldt < R) return PCAGB_EINVAL;
+    dim3 grid((R + 31) / 32, (Cp + 31) / 32);
+    k_transpose_aug<<<grid, dim3(32, 8), 0, (cudaStream_t)stream>>>(
+        (const __nv_bfloat16 *)S, R, C, lds, (__nv_bfloat16 *)T, Cp, ldt, ones);
+    return cudaGetLastError() == cudaSuccess ? PCAGB_OK : PCAGB_ECUDA;
+}
 
 extern "C" int pcagb_vnet_encode_pool_tc(const void *W1, const float *b1, const void *W2,
                                          const float *b2, const uint16_t *regs,

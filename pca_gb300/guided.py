@@ -157,11 +157,13 @@ def train(net: ValueNet, ds: Dataset, epochs=8, batch=2048, seed=0, log=None):
     gen = torch.Generator().manual_seed(seed)
     losses = []
     for ep in range(epochs):
-        tot, nb = 0.0, 0
+        tot, nb = None, 0
         for b in ds.batches(batch, gen):
-            tot += net.train_step(b)
+            loss = net.train_step_graph(b)
+            tot = loss if tot is None else tot + loss
             nb += 1
-        losses.append(tot / max(nb, 1))
+        losses.append(float(tot) / max(nb, 1) if nb else 0.0)   # one read per epoch
+        net.check_status()
         if log:
             log(f"epoch {ep + 1}: loss {losses[-1]:.4f}")
     return losses
@@ -235,7 +237,8 @@ class ValueOrder:
                 ev1.record(stream)
                 ev1.synchronize()
                 if int(status.item()):
-                    raise RuntimeError("fused encoder aborted (barrier wait timed out)")
+                    status.zero_()
+                    raise RuntimeError("tensor-core kernel aborted (barrier wait timed out)")
                 self.score_ms += ev0.elapsed_time(ev1)
                 self._cache = {key: order}
                 return order
@@ -282,11 +285,11 @@ class ValueOrder:
                 m, tp, st)
             if rc != 0:
                 raise RuntimeError(f"sample gather failed ({rc})")
-            n_before = len(self.net._status)
             logits = self.net.forward_fused(G["regs"], G["flags"], G["live"], G["task"], G["depth"],
                                             tp, task_io, task_T)
-            G["status"] = self.net._status.pop()
-            assert len(self.net._status) == n_before
+            # the network's status word (a fixed address the captured
+            # launches keep reporting to)
+            G["status"] = self.net._status_word()
             G["ranked"] = torch.argsort(logits[:, 0], descending=True, stable=True)
 
         # the warm-up and capture runs read the sample buffers themselves, a

@@ -4,6 +4,12 @@ own BF16 tensor-core kernels (pca_gb300/csrc/valuenet.cu).
 torch provides device memory and the stream; every layer, gradient and
 optimizer update is one of the C kernels, called through the C ABI.
 
+Every matrix product runs on the fifth-generation tensor cores
+(pcagb_vnet_gemm_tc: TMA, tcgen05.mma into TMEM, FP32 accumulation): the
+forward layers, the input gradients (with the ReLU derivative applied in the
+epilogue) and the weight gradients, whose bias gradients come out of the
+same split-K GEMM as a column of ones appended to the layer input.
+
 Network (the reference's ValueNetwork, python/model.py:16-84, with bit
 features): per-test encoder 176 -> 256 -> 256 (ReLU), mean + max pooling
 over the task's tests with the live mask and depth, trunk 528 -> 256 -> 128
@@ -31,15 +37,14 @@ def _lib():
     vp, i, f = ctypes.c_void_p, ctypes.c_int, ctypes.c_float
     sz = ctypes.c_size_t
     sigs = {
-        "pcagb_vnet_gemm_nt": [vp, vp, vp, vp, vp, i, i, i, i, i, i, i, vp],
-        "pcagb_vnet_gemm_tn_acc": [vp, vp, vp, i, i, i, i, i, vp],
-        "pcagb_vnet_colsum": [vp, vp, i, i, i, vp],
+        "pcagb_vnet_gemm_tc": [vp, i, vp, i, vp, vp, i, vp, vp, i, i, i, i, i, i, vp, vp],
+        "pcagb_vnet_transpose_aug": [vp, i, i, i, vp, i, i, i, vp],
         "pcagb_vnet_features": [vp, vp, vp, i, i, vp, vp, vp, vp],
         "pcagb_vnet_pool": [vp, vp, vp, vp, vp, i, vp, vp, vp],
         "pcagb_vnet_pool_bwd": [vp, vp, vp, vp, i, vp, vp],
         "pcagb_vnet_relu_bwd": [vp, vp, sz, vp],
-        "pcagb_vnet_loss": [vp, vp, vp, i, f, f, vp, vp, vp],
-        "pcagb_vnet_adam": [vp, vp, vp, vp, i, i, f, f, f, f, i, vp, vp, vp],
+        "pcagb_vnet_loss": [vp, vp, vp, i, f, vp, vp, vp, vp],
+        "pcagb_vnet_adam": [vp, vp, vp, vp, i, i, f, f, f, f, vp, vp, vp, vp],
         "pcagb_vnet_to_bf16": [vp, vp, sz, vp],
         "pcagb_vnet_encode_pool_tc": [vp, vp, vp, vp, vp, vp, vp, vp, vp, i, i, vp, vp, vp, vp,
                                       vp],
@@ -77,7 +82,10 @@ class ValueNet:
             for d in (self.mb, self.vb):
                 d[name] = torch.zeros_like(self.b[name])
         self.step_n = 0
+        self.step_dev = torch.zeros(1, device=self.dev, dtype=torch.int32)
+        self._train_graphs = {}
         self._status = []
+        self.sms = torch.cuda.get_device_properties(self.dev).multi_processor_count
         self._refresh_bf16()
 
     @property
@@ -97,22 +105,60 @@ class ValueNet:
         return sum(w.numel() + self.b[k].numel() for k, w in self.W.items())
 
     # ---- kernels -----------------------------------------------------------
-    def _gemm(self, A, name, relu, out_f32=False, transposed=False):
-        """A[M,K] . W^T (+b) or, for the input gradient, A[M,N] . W."""
+    def _status_word(self):
+        """The status word every tcgen05 launch of this network reports a
+        barrier time-out to (nonzero: the launch's result is void)."""
+        if not self._status:
+            self._status.append(torch.zeros(1, device=self.dev, dtype=torch.int32))
+        return self._status[0]
+
+    def _gemm(self, A, name, relu, out_f32=False, transposed=False, mask=None):
+        """A[M,K] . W^T (+b), ReLU; or, for the input gradient, A[M,N] . W,
+        zeroed where `mask` (the layer input's stored activation) is not
+        positive. One tcgen05 GEMM (pcagb_vnet_gemm_tc)."""
         M, K = A.shape
         if transposed:
             B = self.Wt[name]          # [in][out]: rows are the output
-            N = B.shape[0]
             bias = None
         else:
             B = self.Wb[name]          # [out][in]
-            N = B.shape[0]
             bias = self.b[name]
+        N = B.shape[0]
         C = torch.empty(M, N, device=self.dev, dtype=torch.float32 if out_f32 else torch.bfloat16)
-        self._ck(self.lib.pcagb_vnet_gemm_nt(
-            _p(A), _p(B), _p(bias), None if out_f32 else _p(C), _p(C) if out_f32 else None,
-            M, N, K, K, B.shape[1], N, int(relu), self.stream))
+        self._ck(self.lib.pcagb_vnet_gemm_tc(
+            _p(A), A.stride(0), _p(B), B.stride(0), _p(bias), _p(mask),
+            mask.stride(0) if mask is not None else 0, None if out_f32 else _p(C),
+            _p(C) if out_f32 else None, N, M, N, K, int(relu), 1, _p(self._status_word()),
+            self.stream))
         return C
+
+    def _transpose_aug(self, S, ones):
+        """S[R][C] -> T[Cp][R]: S transposed, with a row of ones at C when
+        `ones` (the bias column of the weight gradient), padded to 16 rows."""
+        R, C = S.shape
+        Cp = (C + (1 if ones else 0) + 15) // 16 * 16
+        ld = (R + 7) // 8 * 8          # a TMA row stride is a multiple of 16 bytes
+        T = torch.empty(Cp, ld, device=self.dev, dtype=torch.bfloat16)
+        self._ck(self.lib.pcagb_vnet_transpose_aug(_p(S), R, C, S.stride(0), _p(T), Cp, ld,
+                                                   int(ones), self.stream))
+        return T
+
+    def _wgrad(self, dY, X, name):
+        """dW = dY^T . X and db = column sums of dY in one split-K tcgen05
+        GEMM: dY^T [out][M] times [X | 1]^T [in + 1 (padded)][M]."""
+        out, inp = self.W[name].shape
+        M = dY.shape[0]
+        dYT = self._transpose_aug(dY, False)[:out]
+        XT = self._transpose_aug(X, True)
+        Kp = XT.shape[0]
+        G = torch.zeros(out, Kp, device=self.dev, dtype=torch.float32)
+        tiles = ((out + 127) // 128) * ((Kp + 255) // 256)
+        kblocks = (M + 63) // 64
+        splits = max(1, min(kblocks, (2 * self.sms) // max(tiles, 1)))
+        self._ck(self.lib.pcagb_vnet_gemm_tc(
+            _p(dYT), dYT.stride(0), _p(XT), XT.stride(0), None, None, 0, None, _p(G), Kp, out,
+            Kp, M, 0, splits, _p(self._status_word()), self.stream))
+        return G[:, :inp], G[:, inp].contiguous()
 
     def features(self, regs, flags, task, TP, task_io, task_T):
         n = task.shape[0]
@@ -140,22 +186,23 @@ class ValueNet:
         the pooled rows P[n][528] without X, H1 or H2 in HBM."""
         n = task.shape[0]
         P = torch.empty(n, 528, device=self.dev, dtype=torch.bfloat16)
-        status = torch.zeros(1, device=self.dev, dtype=torch.int32)
+        status = self._status_word()
         self._ck(self.lib.pcagb_vnet_encode_pool_tc(
             _p(self.Wb["E1"]), _p(self.b["E1"]), _p(self.Wb["E2"]), _p(self.b["E2"]), _p(regs),
             _p(flags), _p(live), _p(task), _p(depth), TP, n, _p(task_io), _p(task_T), _p(P),
             _p(status), self.stream))
-        self._status.append(status)
         return P
 
     def check_status(self):
-        """Raise if a fused encoder launch gave up on a barrier wait (reads
-        the status words: synchronises with their stream)."""
-        st, self._status = self._status, []
-        for s in st:
-            v = int(s.item())
-            if v:
-                raise RuntimeError(f"fused encoder aborted (barrier wait {v} timed out)")
+        """Raise if a tcgen05 launch (fused encoder or GEMM) gave up on a
+        barrier wait (reads the status words: synchronises with their
+        stream)."""
+        if not self._status:
+            return
+        v = int(self._status[0].item())
+        self._status[0].zero_()
+        if v:
+            raise RuntimeError(f"tensor-core kernel aborted (barrier wait {v} timed out)")
 
     def trunk(self, P):
         Z1 = self._gemm(P, "T1", True)
@@ -166,16 +213,6 @@ class ValueNet:
         """Logits [n][16] through the fused encoder and the trunk."""
         return self.trunk(self.encode_pool(regs, flags, live, task, depth, TP, task_io, task_T))
 
-    def _wgrad(self, dY, X, name):
-        out, inp = self.W[name].shape
-        G = torch.zeros(out, inp, device=self.dev, dtype=torch.float32)
-        self._ck(self.lib.pcagb_vnet_gemm_tn_acc(_p(dY), _p(X), _p(G), dY.shape[0], out, inp,
-                                                 dY.shape[1], X.shape[1], self.stream))
-        gb = torch.zeros(out, device=self.dev, dtype=torch.float32)
-        self._ck(self.lib.pcagb_vnet_colsum(_p(dY), _p(gb), dY.shape[0], out, dY.shape[1],
-                                            self.stream))
-        return G, gb
-
     def _relu_bwd(self, dY, Y):
         self._ck(self.lib.pcagb_vnet_relu_bwd(_p(dY), _p(Y), dY.numel(), self.stream))
 
@@ -185,11 +222,9 @@ class ValueNet:
         a = self._acts
         grads = {}
         grads["H"] = self._wgrad(dL, a["Z2"], "H")
-        dZ2 = self._gemm(dL, "H", False, transposed=True)
-        self._relu_bwd(dZ2, a["Z2"])
+        dZ2 = self._gemm(dL, "H", False, transposed=True, mask=a["Z2"])
         grads["T2"] = self._wgrad(dZ2, a["Z1"], "T2")
-        dZ1 = self._gemm(dZ2, "T2", False, transposed=True)
-        self._relu_bwd(dZ1, a["Z1"])
+        dZ1 = self._gemm(dZ2, "T2", False, transposed=True, mask=a["Z1"])
         grads["T1"] = self._wgrad(dZ1, a["P"], "T1")
         dP = self._gemm(dZ1, "T1", False, transposed=True)
         n = a["task"].shape[0]
@@ -198,32 +233,34 @@ class ValueNet:
                                               _p(a["task_T"]), n, _p(dH2), self.stream))
         self._relu_bwd(dH2, a["H2"])
         grads["E2"] = self._wgrad(dH2, a["H1"], "E2")
-        dH1 = self._gemm(dH2, "E2", False, transposed=True)
-        self._relu_bwd(dH1, a["H1"])
+        dH1 = self._gemm(dH2, "E2", False, transposed=True, mask=a["H1"])
         grads["E1"] = self._wgrad(dH1, a["X"], "E1")
         return grads
 
     def loss(self, L, label, remaining):
+        """The loss (a device scalar: nothing is read back) and its
+        gradient w.r.t. the logits."""
         n = L.shape[0]
         dL = torch.empty(n, 16, device=self.dev, dtype=torch.bfloat16)
         stats = torch.zeros(3, device=self.dev, dtype=torch.float32)
-        npos = float((label > 0.5).sum().item())
+        npos = (label > 0.5).sum(dtype=torch.float32).reshape(1)
         self._ck(self.lib.pcagb_vnet_loss(_p(L), _p(label), _p(remaining), n, self.pos_weight,
-                                          npos, _p(dL), _p(stats), self.stream))
-        bce, ce, _ = stats.tolist()
-        return bce / n + (0.5 * ce / npos if npos else 0.0), dL
+                                          _p(npos), _p(dL), _p(stats), self.stream))
+        loss = stats[0] / n + 0.5 * stats[1] / npos[0].clamp(min=1.0)
+        return loss, dL
 
     def adam(self, grads, b1=0.9, b2=0.999, eps=1e-8):
         self.step_n += 1
+        self.step_dev += 1
         for name, out, inp in LAYERS:
             G, gb = grads[name]
             self._ck(self.lib.pcagb_vnet_adam(_p(self.W[name]), _p(G), _p(self.mW[name]),
                                               _p(self.vW[name]), out, inp, self.lr, b1, b2, eps,
-                                              self.step_n, _p(self.Wb[name]), _p(self.Wt[name]),
-                                              self.stream))
+                                              _p(self.step_dev), _p(self.Wb[name]),
+                                              _p(self.Wt[name]), self.stream))
             self._ck(self.lib.pcagb_vnet_adam(_p(self.b[name]), _p(gb), _p(self.mb[name]),
                                               _p(self.vb[name]), 1, out, self.lr, b1, b2, eps,
-                                              self.step_n, None, None, self.stream))
+                                              _p(self.step_dev), None, None, self.stream))
         with torch.no_grad():
             self.W["T1"][:, 521:] = 0.0
             self.Wb["T1"][:, 521:] = 0.0
@@ -232,13 +269,45 @@ class ValueNet:
     def train_step(self, batch):
         """One step on a batch dict (device tensors): regs, flags, live, task,
         task_io, task_T, TP, depth (uint8 per state), label, remaining.
-        Returns the loss."""
+        Returns the loss as a device scalar."""
         X = self.features(batch["regs"], batch["flags"], batch["task"], batch["TP"],
                           batch["task_io"], batch["task_T"])
         L = self.forward(X, batch["live"], batch["task"], batch["task_T"], batch["depth"])
         loss, dL = self.loss(L, batch["label"], batch["remaining"])
         self.adam(self.backward(dL))
         return loss
+
+    BATCH_KEYS = ("regs", "flags", "live", "task", "task_io", "task_T", "depth", "label",
+                  "remaining")
+
+    def train_step_graph(self, batch):
+        """train_step as one CUDA graph replay: the step (features, forward,
+        loss, backward, Adam: about sixty launches) is captured once per
+        batch shape into static buffers, and each call copies the batch in
+        and replays it. Returns the loss as a device scalar."""
+        key = (batch["task"].shape[0], batch["task_io"].shape[0], batch["TP"])
+        G = self._train_graphs.get(key)
+        if G is None:
+            static = {k: batch[k].clone() for k in self.BATCH_KEYS}
+            static["TP"] = batch["TP"]
+            side = torch.cuda.Stream(device=self.dev)
+            side.wait_stream(torch.cuda.current_stream(self.dev))
+            with torch.cuda.stream(side):
+                first = self.train_step(static)   # this call's step, outside the capture
+            torch.cuda.current_stream(self.dev).wait_stream(side)
+            graph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(graph, stream=side):
+                loss = self.train_step(static)
+            torch.cuda.current_stream(self.dev).wait_stream(side)
+            # the capture recorded a step without running it
+            self.step_n -= 1
+            self._train_graphs[key] = {"graph": graph, "static": static, "loss": loss}
+            return first
+        for k in self.BATCH_KEYS:
+            G["static"][k].copy_(batch[k])
+        G["graph"].replay()
+        self.step_n += 1
+        return G["loss"].clone()
 
     def score(self, regs, flags, live, task, task_io, task_T, TP, depth):
         X = self.features(regs, flags, task, TP, task_io, task_T)

@@ -7,6 +7,7 @@
     python profile_cases.py orders          # k_check_perm
     python profile_cases.py branch          # branch-mode kernels
     python profile_cases.py branch_saturating_add   # the same, two inputs, depth 4
+    python profile_cases.py misc            # leaf, mark-all, paths, recording, twins, sampling
 
 Each case runs its work `--reps` times (default 2) and prints one timing line
 per repetition (CUDA events); the device memory it holds stays below a few
@@ -31,8 +32,8 @@ def case_engine_depths(reps: int):
     """is_power2 (32 tests) to kernel depth 4 with the suffix stage started
     from level 1 and level 2 (suffix depths 3 and 2), and depth 3 from level
     3 (the leaf check)."""
-    from .pcalib import Engine
-    from .taskgen import is_power2_task
+    from pca_gb300.pcalib import Engine
+    from pca_gb300.taskgen import is_power2_task
     eng = Engine(0, 4 << 30)
     task = is_power2_task()
     for _ in range(reps):
@@ -46,8 +47,8 @@ def case_engine_depths(reps: int):
 def case_suffix_depth2(reps: int):
     """is_power2 (32 tests) to kernel depth 4 from level 2: the depth-4 stage
     is one k_suffix<32, 2> launch (the fourth k_suffix launch of a solve)."""
-    from .pcalib import Engine
-    from .taskgen import is_power2_task
+    from pca_gb300.pcalib import Engine
+    from pca_gb300.taskgen import is_power2_task
     eng = Engine(0, 4 << 30)
     task = is_power2_task()
     for _ in range(reps):
@@ -61,8 +62,8 @@ def case_noalloc(reps: int):
     """The no-allocation entry point to kernel depth 3 on is_power2 (32
     tests, no program that short: every depth searched completely) and on a
     2-input synthetic task (27 tests)."""
-    from .pcalib import load_library
-    from .taskgen import is_power2_task, synthetic_task
+    from pca_gb300.pcalib import load_library
+    from pca_gb300.taskgen import is_power2_task, synthetic_task
     lib = load_library()
     cap = 1 << 12
     progs = (ctypes.c_uint16 * (16 * cap))()
@@ -103,7 +104,7 @@ def case_valuenet(reps: int):
     backward, pooling, loss, Adam) and scoring of 131,072 states through the
     fused tcgen05 encoder and the trunk."""
     import torch
-    from .valuenet import ValueNet
+    from pca_gb300.valuenet import ValueNet
     net = ValueNet(seed=0, lr=1e-3, pos_weight=8.0)
     train = _random_states(8192, 32, seed=1)
     score = _random_states(131072, 32, seed=2)
@@ -113,8 +114,15 @@ def case_valuenet(reps: int):
         loss = net.train_step(train)
         e1.record()
         torch.cuda.synchronize()
-        print(f"valuenet train step (8192 states): {e0.elapsed_time(e1):.3f} ms loss {loss:.4f}",
-              flush=True)
+        print(f"valuenet train step (8192 states): {e0.elapsed_time(e1):.3f} ms "
+              f"loss {float(loss):.4f}", flush=True)
+        e0, e1 = _events()
+        e0.record()
+        loss = net.train_step_graph(train)
+        e1.record()
+        torch.cuda.synchronize()
+        print(f"valuenet train step, graph replay (8192 states): {e0.elapsed_time(e1):.3f} ms "
+              f"loss {float(loss):.4f}", flush=True)
         e0, e1 = _events()
         e0.record()
         L = net.forward_fused(score["regs"], score["flags"], score["live"], score["task"],
@@ -130,8 +138,8 @@ def case_orders(reps: int):
     """An ordered solve (random order) of is_power2 to depth 4 from level 2:
     every stage's order is checked on the device before use."""
     import torch
-    from .pcalib import Engine
-    from .taskgen import is_power2_task
+    from pca_gb300.pcalib import Engine
+    from pca_gb300.taskgen import is_power2_task
     eng = Engine(0, 4 << 30)
     gen = torch.Generator().manual_seed(0)
 
@@ -147,7 +155,7 @@ def case_orders(reps: int):
 def _branch_case(name: str, reps: int):
     import json
     import os
-    from .pcalib import Engine, task_from_dict
+    from pca_gb300.pcalib import Engine, task_from_dict
     fx = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "tests",
                       "golden", "ref_published.json")
     spec = next(t for t in json.load(open(fx)) if t["name"] == name)
@@ -174,7 +182,42 @@ def case_branch_saturating_add(reps: int):
     _branch_case("saturating_add", reps)
 
 
-CASES = {"engine_depths": case_engine_depths, "suffix_depth2": case_suffix_depth2,
+def case_misc(reps: int):
+    """The engine's smaller kernels on small cases: the leaf check of a
+    built level (k_leaf, count mode), the unpruned level marking (k_mark_all,
+    no OEP), solution paths (k_gather_paths), the recording pass
+    (k_record_keys, k_record_states), the flag-twin pass (k_twins), the
+    depth-1 evaluation count (k_count_evals), and a sampled value ranking
+    (k_gather_sample, k_compose_order)."""
+    import os
+    import tempfile
+
+    import torch
+    from pca_gb300.guided import ValueOrder
+    from pca_gb300.pcalib import Engine, OEP_EXACT, OEP_NONE
+    from pca_gb300.taskgen import negate_task, synthetic_task
+    from pca_gb300.valuenet import ValueNet
+    eng = Engine(0, 4 << 30)
+    t3, _ = synthetic_task(659, 3)
+    net = ValueNet(seed=0)
+    vo = ValueOrder(net, sample=4096, min_states=1, gain=0.0)
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        a = eng.solve(t3, max_depth=3, oep_mode=OEP_EXACT, count_levels=True, sol_cap=4096)
+        b = eng.solve(negate_task(1), max_depth=2, oep_mode=OEP_NONE, count_levels=True)
+        with tempfile.TemporaryDirectory() as d:
+            st = eng.record(t3, d, max_depth=3, task_id=1, neg_stride=8)
+            n_files = len(os.listdir(d))
+        c = eng.solve_ordered(t3, vo, chunk=256, max_depth=3, split_depth=2)
+        torch.cuda.synchronize()
+        print(f"misc: K*={a.optimal_depth} ({len(a.programs)} programs), no-OEP "
+              f"K*={b.optimal_depth}, recorded {n_files} files ({st}), ordered "
+              f"K*={c.optimal_depth}: {time.perf_counter() - t0:.3f} s", flush=True)
+    vo.close()
+    eng.close()
+
+
+CASES = {"engine_depths": case_engine_depths, "suffix_depth2": case_suffix_depth2, "misc": case_misc,
          "noalloc": case_noalloc,
          "valuenet": case_valuenet, "orders": case_orders, "branch": case_branch,
          "branch_saturating_add": case_branch_saturating_add}
@@ -185,7 +228,7 @@ def main(argv=None):
     ap.add_argument("case", choices=sorted(CASES))
     ap.add_argument("--reps", type=int, default=2)
     args = ap.parse_args(argv)
-    from .build import build_engine
+    from pca_gb300.build import build_engine
     build_engine()
     CASES[args.case](args.reps)
 

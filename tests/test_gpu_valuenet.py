@@ -1,8 +1,10 @@
-"""The value network's own kernels (BF16 tensor-core GEMMs with FP32
-accumulation, pooling, loss, Adam) against an fp32 CPU restatement of the
-same network: features exactly, logits and every gradient within BF16
+"""The value network's own kernels (the tcgen05 GEMM with FP32
+accumulation in TMEM, pooling, loss, Adam) against an fp32 CPU restatement
+of the same network: features exactly, logits and every gradient within BF16
 tolerance (relative error <= 5e-2 and cosine >= 0.999 on each tensor), and a
-training run that lowers the loss."""
+training run that lowers the loss. The GEMM itself against an fp32 product
+of the same bf16 operands over the shapes the network uses and ragged ones
+(relative error <= 1e-2: fp32 accumulation, bf16 output rounding)."""
 import numpy as np
 import pytest
 
@@ -103,6 +105,28 @@ def test_training_lowers_loss():
     assert last < 0.5 * first
 
 
+def test_graph_step_matches_eager_steps():
+    """The captured training step (one CUDA graph replay) updates the
+    network as the eager step does: after six steps the weights agree
+    within the split-K gradient sums' rounding (their fp32 adds run in no
+    fixed order), and the losses too."""
+    from pca_gb300.valuenet import ValueNet
+    b, (regs, *_rest) = random_batch(200, seed=5)
+    label = ((regs[:, 1, 0] >> 5) & 1).astype(np.float32)
+    b["label"] = torch.from_numpy(label).cuda()
+    b["remaining"] = torch.from_numpy(np.where(label > 0, 1, -1).astype(np.int32)).cuda()
+    eager, graph = ValueNet(seed=11, lr=1e-3), ValueNet(seed=11, lr=1e-3)
+    le = [float(eager.train_step(b)) for _ in range(6)]
+    lg = [float(graph.train_step_graph(b)) for _ in range(6)]
+    torch.cuda.synchronize()
+    assert graph.step_n == eager.step_n == 6
+    assert int(graph.step_dev.item()) == 6
+    for name in eager.W:
+        assert rel(graph.W[name], eager.W[name]) < 1e-3, name
+        assert rel(graph.b[name], eager.b[name]) < 1e-3, name
+    assert max(abs(a - c) for a, c in zip(le, lg)) < 1e-2 * max(abs(x) for x in le)
+
+
 def _batch_tp(n, TP, seed):
     """States in a level layout of TP test columns (16 or 32)."""
     rng = np.random.default_rng(seed)
@@ -160,3 +184,68 @@ def test_fused_tcgen05_encoder_matches(TP, n):
                                torch.from_numpy(depth))
         assert rel(Lf.cpu(), Lr) < 5e-2
         assert cos(Lf[:, 0].cpu(), Lr[:, 0]) > 0.999
+
+
+@pytest.mark.parametrize("M,N,K", [(128, 256, 64), (300, 176, 176), (262144 // 64, 256, 256),
+                                   (8192, 528, 256), (8192, 16, 128), (777, 48, 16),
+                                   (96, 256, 528)])
+def test_tc_gemm_matches_fp32(M, N, K):
+    """C = A . B^T (+ bias, ReLU) into bf16 and fp32, and the ReLU mask of an
+    input gradient, against torch in fp32 on the same bf16 values."""
+    import ctypes
+    from pca_gb300.valuenet import _lib, _p
+    lib = _lib()
+    g = torch.Generator(device="cuda").manual_seed(M * 7 + N)
+    A = torch.randn(M, K, device="cuda", generator=g).to(torch.bfloat16)
+    B = torch.randn(N, K, device="cuda", generator=g).to(torch.bfloat16)
+    bias = torch.randn(N, device="cuda", generator=g)
+    mask = torch.randn(M, N, device="cuda", generator=g).to(torch.bfloat16)
+    st = torch.zeros(1, device="cuda", dtype=torch.int32)
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    ref = A.float() @ B.float().t()
+    Cb = torch.empty(M, N, device="cuda", dtype=torch.bfloat16)
+    Cf = torch.empty(M, N, device="cuda", dtype=torch.float32)
+    assert lib.pcagb_vnet_gemm_tc(_p(A), K, _p(B), K, _p(bias), None, 0, _p(Cb), _p(Cf), N, M, N,
+                                  K, 1, 1, _p(st), s) == 0
+    want = torch.relu(ref + bias)
+    torch.cuda.synchronize()
+    assert int(st.item()) == 0
+    assert rel(Cf, want) < 1e-4 and rel(Cb.float(), want) < 1e-2
+    Cm = torch.empty(M, N, device="cuda", dtype=torch.bfloat16)
+    assert lib.pcagb_vnet_gemm_tc(_p(A), K, _p(B), K, None, _p(mask), N, _p(Cm), None, N, M, N, K,
+                                  0, 1, _p(st), s) == 0
+    want = torch.where(mask.float() > 0, ref, torch.zeros_like(ref))
+    torch.cuda.synchronize()
+    assert rel(Cm.float(), want) < 1e-2
+
+
+@pytest.mark.parametrize("splits", [1, 3, 64])
+def test_tc_gemm_split_k_and_augmented_weight_gradient(splits):
+    """The weight gradient's form: dW | db = dY^T . [X | 1] through the
+    augmented transposes and split-K fp32 adds, against torch."""
+    import ctypes
+    from pca_gb300.valuenet import _lib, _p
+    lib = _lib()
+    M, out, inp = 4096 + 40, 256, 176
+    g = torch.Generator(device="cuda").manual_seed(splits)
+    dY = torch.randn(M, out, device="cuda", generator=g).to(torch.bfloat16)
+    X = torch.randn(M, inp, device="cuda", generator=g).to(torch.bfloat16)
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    Kp = (inp + 1 + 15) // 16 * 16
+    dYT = torch.empty(out, M, device="cuda", dtype=torch.bfloat16)
+    XT = torch.empty(Kp, M, device="cuda", dtype=torch.bfloat16)
+    assert lib.pcagb_vnet_transpose_aug(_p(dY), M, out, out, _p(dYT), out, M, 0, s) == 0
+    assert lib.pcagb_vnet_transpose_aug(_p(X), M, inp, inp, _p(XT), Kp, M, 1, s) == 0
+    torch.cuda.synchronize()
+    assert torch.equal(dYT, dY.t())
+    assert torch.equal(XT[:inp], X.t()) and bool((XT[inp] == 1).all()) and bool((XT[inp + 1:] == 0).all())
+    G = torch.zeros(out, Kp, device="cuda", dtype=torch.float32)
+    st = torch.zeros(1, device="cuda", dtype=torch.int32)
+    assert lib.pcagb_vnet_gemm_tc(_p(dYT), M, _p(XT), M, None, None, 0, None, _p(G), Kp, out, Kp,
+                                  M, 0, splits, _p(st), s) == 0
+    torch.cuda.synchronize()
+    assert int(st.item()) == 0
+    dW = dY.float().t() @ X.float()
+    db = dY.float().sum(0)
+    assert rel(G[:, :inp], dW) < 1e-4 and rel(G[:, inp], db) < 1e-4
+    assert float(G[:, inp + 1:].abs().max()) == 0.0

@@ -47,11 +47,11 @@ CANDIDATES = ("candidates as the reference's enumerator counts them (tools/enume
 # The suffix kernel's capture (profiles/k_suffix_is_power2_t32_k4.md): warp
 # instructions of the depth-4 launch, valid for the kernel source it was
 # taken from (SHA-256 of pca_gb300/csrc/engine_kernels.cuh, first 16 hex).
-SUFFIX_CAPTURE = {"inst": 1255101666, "ms": 1.501504, "source_sha16": "6ff4384c1f782676",
+SUFFIX_CAPTURE = {"inst": 1255101666, "ms": 1.527168, "source_sha16": "205d10f9618ae177",
                   "file": "profiles/k_suffix_is_power2_t32_k4.md"}
 # The insert kernel's capture (profiles/k_expand_insert_is_power2_t32_level3.md):
 # DRAM bytes read + written by the level-3 launch (99.6% of a solve's children).
-INSERT_CAPTURE = {"dram_bytes": 558502144 + 170077440, "source_sha16": "6ff4384c1f782676",
+INSERT_CAPTURE = {"dram_bytes": 529504000 + 169235200, "source_sha16": "205d10f9618ae177",
                   "file": "profiles/k_expand_insert_is_power2_t32_level3.md"}
 
 

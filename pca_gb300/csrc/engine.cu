@@ -795,7 +795,10 @@ int run_stage(pcagb_engine *e, int S, int K, std::vector<TaskRun> &runs, bool fi
                 else launch_suffix<32, 1>(ft, g, e->stream, V, e->td, sb, 1, 1, R);
                 const int rc0 = check_launch(e);
                 if (rc0) return rc0;
-                k_count_evals<<<e->grid(2), 256, 0, e->stream>>>(V, e->td, R, sb);
+                /* a thread per prefix (the pass is latency bound) */
+                const unsigned cb = (unsigned)std::min<uint64_t>((R.count + 255) / 256,
+                                                                 (uint64_t)e->sms * 32);
+                k_count_evals<<<std::max(cb, 1u), 256, 0, e->stream>>>(V, e->td, R, sb);
             } else if (s == 2) {
                 if (t16) launch_suffix<16, 2>(ft, g, e->stream, V, e->td, sb, cpp, chunk, R);
                 else launch_suffix<32, 2>(ft, g, e->stream, V, e->td, sb, cpp, chunk, R);
@@ -1519,6 +1522,18 @@ int ensure_device_tables(int device)
         const uint16_t *pc = pr_cls;
         CK(cudaMemcpyToSymbol(c_pr_off, gt.pr_off.data(), gt.pr_off.size() * 4));
         CK(cudaMemcpyToSymbol(c_pr_ev, gt.pr_ev.data(), gt.pr_ev.size() * 4));
+        /* the same counts in global memory for k_count_evals, whose lanes
+           read different entries (constant memory serialises those); entry
+           (m, 0) is a root's scan: every class of mask m */
+        std::vector<uint32_t> ev1(128 * 8);
+        for (int m = 0; m < 128; m++)
+            for (int r = 0; r < 8; r++)
+                ev1[m * 8 + r] = r ? gt.pr_ev[m * 8 + r] : (uint32_t)gt.nvc(m);
+        uint32_t *ev1_d = nullptr;
+        CK(cudaMalloc(&ev1_d, ev1.size() * 4));
+        CK(cudaMemcpy(ev1_d, ev1.data(), ev1.size() * 4, cudaMemcpyHostToDevice));
+        const uint32_t *ev1p = ev1_d;
+        CK(cudaMemcpyToSymbol(c_ev_sd1, &ev1p, sizeof ev1p));
         CK(cudaMemcpyToSymbol(c_pr, &pp, sizeof pp));
         CK(cudaMemcpyToSymbol(c_pr_cls, &pc, sizeof pc));
     }

@@ -71,6 +71,7 @@ __constant__ uint32_t c_pr_off[128 * 8 + 1];  /* [mask*8 + r]: the same, by oper
 __constant__ const uint32_t *c_pr;         /* a | b << 3 | opmask << 6 | imm << 16 */
 __constant__ const uint16_t *c_pr_cls;     /* [entry][10] class index per opmask bit */
 __constant__ uint32_t c_pr_ev[128 * 8];    /* [mask*8 + r]: class evaluations of its pair list */
+__constant__ const uint32_t *c_ev_sd1;     /* the same in global memory, [mask*8 + 0] = all classes */
 
 /* Per-task parameters of a batch: device arrays indexed by task id. A
    state's task id travels with it through the levels; states of different
@@ -1193,8 +1194,9 @@ k_suffix(LevelDev P, TaskDev task, SolBuf S, uint32_t chunks_per_prefix, uint32_
 }
 
 /* Value-class evaluations k_suffix<TPC, 1> runs over range R: a prefix of
-   mask m whose last write is w0 scans the pair list of (m, w0) (c_pr_ev),
-   a root every class of its mask. Added to S.evals, one atomic per warp. */
+   mask m whose last write is w0 scans the pair list of (m, w0), a root
+   every class of its mask (c_ev_sd1, in global memory: the lanes read
+   different entries). Added to S.evals, one atomic per warp. */
 __global__ void k_count_evals(LevelDev P, TaskDev task, PrefixRange R, SolBuf S)
 {
     const int lane = threadIdx.x & 31;
@@ -1206,7 +1208,7 @@ __global__ void k_count_evals(LevelDev P, TaskDev task, PrefixRange R, SolBuf S)
         const uint64_t q = R.order ? (uint64_t)R.order[R.begin + i] : R.begin + i;
         if (q >= P.n || !task.active[P.task[q]]) continue;
         const uint32_t m = (P.live[q] >> 1) & 127u, w0 = P.rdl[q];
-        nev += w0 ? c_pr_ev[m * 8 + w0] : c_vc_off[m + 1] - c_vc_off[m];
+        nev += __ldg(c_ev_sd1 + m * 8 + w0);
     }
     flush_evals(S, nev, lane);
 }

@@ -34,34 +34,42 @@
 namespace {
 
 /* Features of states in the engine's level layout. Row (state i, test t)
- * of X[n*32][176]; rows of tests >= T are zero. */
+ * of X[n*32][176] is eleven 16-bit words expanded to 0.0 / 1.0 bf16 values,
+ * bit 0 first: input 0, input 1, target, r1..r7, the flags (4 bits, then
+ * zeros); rows of tests >= T are zero. One thread per (row, word), writing
+ * its 16 values as two 16-byte pieces. */
+__device__ __forceinline__ uint4 bits8_to_bf16(uint32_t b)
+{
+    uint32_t w[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        const uint32_t t = b >> (2 * j);
+        w[j] = (t & 1u) * 0x3F80u + (t & 2u) * 0x1FC00000u;
+    }
+    return make_uint4(w[0], w[1], w[2], w[3]);
+}
+
 __global__ void k_features(const uint16_t *regs, const uint8_t *flags, const uint16_t *task, int TP,
                            int n, const uint16_t *task_io, const int32_t *task_T,
                            __nv_bfloat16 *X)
 {
-    const size_t row = (size_t)blockIdx.x * blockDim.y + threadIdx.y;
-    if (row >= (size_t)n * 32) return;
-    const int i = (int)(row >> 5), t = (int)(row & 31);
-    const int tid = task[i];
-    const int T = task_T[tid];
-    const int c = threadIdx.x;  /* 0..175, one column per thread of the row */
-    float v = 0.f;
-    if (t < T && c < 164) {
-        uint32_t word, bit;
-        if (c < 48) {           /* in0, in1, target */
-            word = task_io[((size_t)tid * 3 + c / 16) * 32 + t];
-            bit = c & 15;
-        } else if (c < 160) {   /* r1..r7 */
-            const int r = 1 + (c - 48) / 16;
-            word = regs[((size_t)i * 8 + r) * TP + t];
-            bit = (c - 48) & 15;
-        } else {
-            word = flags[(size_t)i * TP + t];
-            bit = c - 160;
+    const size_t items = (size_t)n * 32 * 11;
+    for (size_t it = (size_t)blockIdx.x * blockDim.x + threadIdx.x; it < items;
+         it += (size_t)gridDim.x * blockDim.x) {
+        const size_t row = it / 11;
+        const int w = (int)(it - row * 11);
+        const int i = (int)(row >> 5), t = (int)(row & 31);
+        const int tid = task[i];
+        uint32_t word = 0;
+        if (t < task_T[tid]) {
+            if (w < 3) word = task_io[((size_t)tid * 3 + w) * 32 + t];
+            else if (w < 10) word = regs[((size_t)i * 8 + (w - 2)) * TP + t];
+            else word = flags[(size_t)i * TP + t] & 0xFu;
         }
-        v = (float)((word >> bit) & 1u);
+        uint4 *dst = reinterpret_cast<uint4 *>(X + row * 176 + w * 16);
+        dst[0] = bits8_to_bf16(word & 0xFFu);
+        dst[1] = bits8_to_bf16(word >> 8);
     }
-    X[row * 176 + c] = __float2bfloat16(v);
 }
 
 /* Mean and max over each state's valid test rows of H[n*32][256], plus
@@ -92,9 +100,11 @@ __global__ void k_pool(const __nv_bfloat16 *H, const uint8_t *live, const uint16
     }
 }
 
-/* Backward of k_pool into dH[n*32][256] (rows >= T get zero). */
+/* Backward of k_pool, then of the ReLU that produced H, into dH[n*32][256]:
+   rows >= T and units whose H is not positive get zero. */
 __global__ void k_pool_bwd(const __nv_bfloat16 *dP, const uint8_t *argmax, const uint16_t *task,
-                           const int32_t *task_T, int n, __nv_bfloat16 *dH)
+                           const int32_t *task_T, const __nv_bfloat16 *H, int n,
+                           __nv_bfloat16 *dH)
 {
     const int i = blockIdx.x, u = threadIdx.x;
     if (i >= n) return;
@@ -103,18 +113,11 @@ __global__ void k_pool_bwd(const __nv_bfloat16 *dP, const uint8_t *argmax, const
     const float dx = __bfloat162float(dP[(size_t)i * 528 + 256 + u]);
     const int am = argmax[(size_t)i * 256 + u];
     for (int t = 0; t < 32; t++) {
+        const size_t at = ((size_t)i * 32 + t) * 256 + u;
         float g = 0.f;
-        if (t < T) g = dm + (t == am ? dx : 0.f);
-        dH[((size_t)i * 32 + t) * 256 + u] = __float2bfloat16(g);
+        if (t < T && __bfloat162float(H[at]) > 0.f) g = dm + (t == am ? dx : 0.f);
+        dH[at] = __float2bfloat16(g);
     }
-}
-
-/* dX = dY * (Y > 0) in place (ReLU backward through the stored output). */
-__global__ void k_relu_bwd(__nv_bfloat16 *dY, const __nv_bfloat16 *Y, size_t count)
-{
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;
-         i += (size_t)gridDim.x * blockDim.x)
-        if (!(__bfloat162float(Y[i]) > 0.f)) dY[i] = __float2bfloat16(0.f);
 }
 
 /* Loss of the reference's recipe (python/train.py:48-60): BCE with
@@ -270,10 +273,11 @@ int pcagb_vnet_features(const uint16_t *regs, const uint8_t *flags, const uint16
                         void *stream)
 {
     if (n <= 0) return PCAGB_OK;
-    dim3 block(176, 4);
-    const size_t rows = (size_t)n * 32;
-    k_features<<<(unsigned)((rows + 3) / 4), block, 0, (cudaStream_t)stream>>>(
-        regs, flags, task, TP, n, task_io, task_T, (__nv_bfloat16 *)X);
+    if ((uintptr_t)X & 15) return PCAGB_EINVAL;
+    const size_t items = (size_t)n * 32 * 11;
+    const unsigned blocks = (unsigned)std::min<size_t>((items + 255) / 256, 65536);
+    k_features<<<blocks, 256, 0, (cudaStream_t)stream>>>(regs, flags, task, TP, n, task_io, task_T,
+                                                         (__nv_bfloat16 *)X);
     return launch_ok();
 }
 
@@ -288,18 +292,12 @@ int pcagb_vnet_pool(const void *H, const uint8_t *live, const uint16_t *task,
 }
 
 int pcagb_vnet_pool_bwd(const void *dP, const uint8_t *argmax, const uint16_t *task,
-                        const int32_t *task_T, int n, void *dH, void *stream)
+                        const int32_t *task_T, const void *H, int n, void *dH, void *stream)
 {
     if (n <= 0) return PCAGB_OK;
     k_pool_bwd<<<n, 256, 0, (cudaStream_t)stream>>>((const __nv_bfloat16 *)dP, argmax, task, task_T,
-                                                    n, (__nv_bfloat16 *)dH);
-    return launch_ok();
-}
-
-int pcagb_vnet_relu_bwd(void *dY, const void *Y, size_t count, void *stream)
-{
-    k_relu_bwd<<<1024, 256, 0, (cudaStream_t)stream>>>((__nv_bfloat16 *)dY,
-                                                       (const __nv_bfloat16 *)Y, count);
+                                                    (const __nv_bfloat16 *)H, n,
+                                                    (__nv_bfloat16 *)dH);
     return launch_ok();
 }
 

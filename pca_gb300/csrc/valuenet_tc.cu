@@ -534,7 +534,7 @@ k_gemm_tc(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUt
           const float *__restrict__ bias, const __nv_bfloat16 *__restrict__ mask, int ldm,
           __nv_bfloat16 *__restrict__ Cb, float *__restrict__ Cf, int ldc, int M, int N,
           int kblocks, int kb_per_split, int bn, uint32_t idesc, uint32_t tmem_cols, int relu,
-          int atomic_out, int *status)
+          int atomic_out, int stage_mode, int vec_atomic, int *status)
 {
     extern __shared__ uint8_t gsmem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)gsmem_raw + 1023) & ~(uintptr_t)1023);
@@ -623,11 +623,111 @@ k_gemm_tc(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUt
         }
     }
     __syncwarp();
-    /* epilogue: all four warps */
+    /* epilogue: all four warps. The tile's bias goes to shared memory
+       first (every thread takes part, so the barrier below is reached by
+       all of them whatever the waits return). */
+    float *sbias = (float *)(ctl + 256);
+    for (int c = threadIdx.x; c < bn; c += 128) sbias[c] = (bias && n0 + c < N) ? bias[n0 + c] : 0.f;
     bool ok = nk > 0 && mbar_wait(done_bar, 0, abort_flag, status, 13);
     ok = __all_sync(0xFFFFFFFFu, ok) && !*abort_flag;
     tc_after();
-    if (ok) {
+    __syncthreads();
+    if (ok && stage_mode) {
+        /* Staged: each warp drains its 32 rows of accumulators (+ bias,
+           ReLU, rounding) into the drained stage buffers, a row of bn values
+           at a stride of one row + 16 bytes (16-byte stores of eight lanes
+           fall on distinct bank groups), then writes its rows to C in
+           16-byte pieces, lanes along a row (coalesced), applying the mask
+           on the way. stage_mode 1: bf16 C; 2: fp32 C (bn <= 112). */
+        const int esz = stage_mode == 1 ? 2 : 4;
+        const uint32_t S = (uint32_t)(bn * esz + 16);
+        const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+        uint8_t *myrow = smem + (uint32_t)(warp * 32 + lane) * S;
+        for (int c0 = 0; c0 < bn; c0 += 32) {
+            uint32_t acc[32];
+            tmem_ld32(tmem + lane_base + (uint32_t)c0, acc);
+            if (stage_mode == 1) {
+                uint32_t w[16];
+#pragma unroll
+                for (int j = 0; j < 16; j++) {
+                    const float v0 = __uint_as_float(acc[2 * j]) + sbias[c0 + 2 * j];
+                    const float v1 = __uint_as_float(acc[2 * j + 1]) + sbias[c0 + 2 * j + 1];
+                    if (relu) {
+                        w[j] = relu_bf16x2(v0, v1);
+                    } else {
+                        __nv_bfloat162 h = __floats2bfloat162_rn(v0, v1);
+                        w[j] = *reinterpret_cast<uint32_t *>(&h);
+                    }
+                }
+                /* the tile may end inside this group of 32 (bn = 16) */
+#pragma unroll
+                for (int k = 0; k < 4; k++)
+                    if (c0 + 8 * k < bn)
+                        *(uint4 *)(myrow + c0 * 2 + 16 * k) =
+                            make_uint4(w[4 * k], w[4 * k + 1], w[4 * k + 2], w[4 * k + 3]);
+            } else {
+#pragma unroll
+                for (int k = 0; k < 8; k++) {
+                    float v[4];
+#pragma unroll
+                    for (int q = 0; q < 4; q++) {
+                        v[q] = __uint_as_float(acc[4 * k + q]) + sbias[c0 + 4 * k + q];
+                        if (relu) v[q] = fmaxf(v[q], 0.f);
+                    }
+                    if (c0 + 4 * k < bn)
+                        *(float4 *)(myrow + c0 * 4 + 16 * k) = make_float4(v[0], v[1], v[2], v[3]);
+                }
+            }
+        }
+        __syncwarp();
+        const int per = 16 / esz;                 /* values per 16-byte piece */
+        const int cpr = bn / per;                 /* pieces per row */
+        for (int it = lane; it < 32 * cpr; it += 32) {
+            const int r = it / cpr, ch = it - r * cpr;
+            const int grow = m0 + warp * 32 + r, gcol = n0 + ch * per;
+            if (grow >= M || gcol >= N) continue;
+            const uint8_t *src = smem + (uint32_t)(warp * 32 + r) * S + ch * 16;
+            if (stage_mode == 1) {
+                uint4 v = *(const uint4 *)src;
+                if (mask) {
+                    const uint4 mk = *(const uint4 *)(mask + (size_t)grow * ldm + gcol);
+                    /* keep a value where its mask half is a positive bf16 */
+                    auto keep = [](uint32_t m) {
+                        return (__uint_as_float(m << 16) > 0.f ? 0x0000FFFFu : 0u) |
+                               (__uint_as_float(m & 0xFFFF0000u) > 0.f ? 0xFFFF0000u : 0u);
+                    };
+                    v.x &= keep(mk.x);
+                    v.y &= keep(mk.y);
+                    v.z &= keep(mk.z);
+                    v.w &= keep(mk.w);
+                }
+                if (gcol + per <= N) {
+                    *(uint4 *)(Cb + (size_t)grow * ldc + gcol) = v;
+                } else {
+                    const uint32_t w4[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                    for (int q = 0; q < 8; q++)
+                        if (gcol + q < N) {
+                            const uint32_t b = (w4[q >> 1] >> (16 * (q & 1))) & 0xFFFFu;
+                            reinterpret_cast<uint16_t *>(Cb)[(size_t)grow * ldc + gcol + q] =
+                                (uint16_t)b;
+                        }
+                }
+            } else {
+                const float4 v = *(const float4 *)src;
+                if (gcol + per <= N) {
+                    *(float4 *)(Cf + (size_t)grow * ldc + gcol) = v;
+                } else {
+                    const float f4[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                    for (int q = 0; q < 4; q++)
+                        if (gcol + q < N) Cf[(size_t)grow * ldc + gcol + q] = f4[q];
+                }
+            }
+        }
+    } else if (ok) {
+        /* direct: split-K partial sums (fp32 adds, four at a time where
+           aligned) or outputs the staged forms do not cover */
         const int row = m0 + warp * 32 + lane;
         const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
         for (int c0 = 0; c0 < bn; c0 += 32) {
@@ -636,20 +736,27 @@ k_gemm_tc(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUt
             if (row >= M) continue;
             const int colb = n0 + c0;
             if (atomic_out) {
+                float *dst = Cf + (size_t)row * ldc + colb;
 #pragma unroll
-                for (int j = 0; j < 32; j++)
-                    if (colb + j < N) atomicAdd(Cf + (size_t)row * ldc + colb + j, __uint_as_float(acc[j]));
+                for (int j = 0; j < 32; j += 4) {
+                    if (vec_atomic && colb + j + 3 < N) {
+                        atomicAdd((float4 *)(dst + j),
+                                  make_float4(__uint_as_float(acc[j]), __uint_as_float(acc[j + 1]),
+                                              __uint_as_float(acc[j + 2]), __uint_as_float(acc[j + 3])));
+                    } else {
+#pragma unroll
+                        for (int q = 0; q < 4; q++)
+                            if (colb + j + q < N) atomicAdd(dst + j + q, __uint_as_float(acc[j + q]));
+                    }
+                }
                 continue;
             }
 #pragma unroll
             for (int j = 0; j < 32; j += 2) {
                 const int c = colb + j;
                 if (c >= N) continue;
-                float v0 = __uint_as_float(acc[j]), v1 = __uint_as_float(acc[j + 1]);
-                if (bias) {
-                    v0 += bias[c];
-                    if (c + 1 < N) v1 += bias[c + 1];
-                }
+                float v0 = __uint_as_float(acc[j]) + sbias[c0 + j];
+                float v1 = __uint_as_float(acc[j + 1]) + sbias[c0 + j + 1];
                 if (mask) {
                     const __nv_bfloat16 *mr = mask + (size_t)row * ldm + c;
                     if (!(__bfloat162float(mr[0]) > 0.f)) v0 = 0.f;
@@ -682,27 +789,47 @@ k_gemm_tc(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUt
 }
 
 /* T[c][r] = S[r][c] for c < C; row C of T is ones when `ones` (the bias
-   column of an augmented operand), rows up to Cp zeros. 32 x 32 tiles
-   through shared memory: both sides coalesced. */
-__global__ void k_transpose_aug(const __nv_bfloat16 *__restrict__ S, int R, int C, int lds,
-                                __nv_bfloat16 *__restrict__ T, int Cp, int ldt, int ones)
+   column of an augmented operand), rows up to Cp zeros. 64 x 64 tiles
+   through shared memory, 256 threads: each reads and writes pairs of bf16
+   (4 bytes), so a warp moves 128 contiguous bytes per row on both sides. */
+__global__ void __launch_bounds__(256)
+k_transpose_aug(const __nv_bfloat16 *__restrict__ S, int R, int C, int lds,
+                __nv_bfloat16 *__restrict__ T, int Cp, int ldt, int ones)
 {
-    __shared__ __nv_bfloat16 tile[32][33];
-    const int r0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
-    const int tx = threadIdx.x, ty = threadIdx.y;   /* 32 x 8 */
-    for (int k = ty; k < 32; k += 8) {
-        const int r = r0 + k, c = c0 + tx;
-        float v = 0.f;
-        if (r < R) {
-            if (c < C) v = __bfloat162float(S[(size_t)r * lds + c]);
-            else if (c == C && ones) v = 1.f;
+    __shared__ uint16_t tile[64][66];
+    const int r0 = blockIdx.x * 64, c0 = blockIdx.y * 64;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;   /* 32 x 8 */
+    const uint16_t *src = reinterpret_cast<const uint16_t *>(S);
+    const uint16_t one = 0x3F80u;                               /* bf16 1.0 */
+    for (int k = ty; k < 64; k += 8) {
+        const int r = r0 + k;
+        uint16_t a = 0, b = 0;
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int c = c0 + 2 * tx + h;
+            uint16_t v = 0;
+            if (r < R) {
+                if (c < C) v = src[(size_t)r * lds + c];
+                else if (c == C && ones) v = one;
+            }
+            if (h) b = v; else a = v;
         }
-        tile[k][tx] = __float2bfloat16(v);
+        tile[k][2 * tx] = a;
+        tile[k][2 * tx + 1] = b;
     }
     __syncthreads();
-    for (int k = ty; k < 32; k += 8) {
-        const int c = c0 + k, r = r0 + tx;
-        if (c < Cp && r < R) T[(size_t)c * ldt + r] = tile[tx][k];
+    uint16_t *dst = reinterpret_cast<uint16_t *>(T);
+    for (int k = ty; k < 64; k += 8) {
+        const int c = c0 + k;
+        if (c >= Cp) continue;
+        const int r = r0 + 2 * tx;
+        if (r + 1 < R && !(((size_t)c * ldt + r) & 1)) {
+            const uint32_t pr = (uint32_t)tile[2 * tx][k] | ((uint32_t)tile[2 * tx + 1][k] << 16);
+            *reinterpret_cast<uint32_t *>(dst + (size_t)c * ldt + r) = pr;
+        } else {
+            if (r < R) dst[(size_t)c * ldt + r] = tile[2 * tx][k];
+            if (r + 1 < R) dst[(size_t)c * ldt + r + 1] = tile[2 * tx + 1][k];
+        }
     }
 }
 
@@ -788,18 +915,30 @@ extern "C" int pcagb_vnet_gemm_tc(const void *A, int lda, const void *B, int ldb
     splits = (kblocks + per - 1) / per;
     const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(bn >> 3) << 17) |
                            ((uint32_t)(kGRows >> 4) << 24);
-    const int smem = kGStages * (kGABytes + bn * 128) + 256 + 1024;
+    /* stage buffers, then 256 bytes of barriers and flags, the tile's bias
+       (bn floats), 1 KB of alignment slack */
+    const int smem = kGStages * (kGABytes + bn * 128) + 256 + 1024 + 1024;
     static std::once_flag attr_once;
     static cudaError_t attr_err = cudaSuccess;
     std::call_once(attr_once, [] {
         attr_err = cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        kGStages * (kGABytes + 256 * 128) + 256 + 1024);
+                                        kGStages * (kGABytes + 256 * 128) + 256 + 2048);
     });
+    /* the epilogue: staged through shared memory and stored in 16-byte
+       pieces where the output's alignment allows */
+    int stage_mode = 0;
+    if (splits == 1 && Cb && !Cf && ldc % 8 == 0 && !((uintptr_t)Cb & 15) &&
+        (!mask || (ldm % 8 == 0 && !((uintptr_t)mask & 15))))
+        stage_mode = 1;
+    else if (splits == 1 && Cf && !Cb && !mask && bn <= 112 && ldc % 4 == 0 &&
+             !((uintptr_t)Cf & 15))
+        stage_mode = 2;
+    const int vec_atomic = splits > 1 && ldc % 4 == 0 && !((uintptr_t)Cf & 15);
     if (attr_err != cudaSuccess) return PCAGB_ECUDA;
     dim3 grid((N + bn - 1) / bn, (M + kGRows - 1) / kGRows, splits);
     k_gemm_tc<<<grid, 128, smem, (cudaStream_t)stream>>>(
         ma, mb, bias, (const __nv_bfloat16 *)mask, ldm, (__nv_bfloat16 *)Cb, Cf, ldc, M, N,
-        kblocks, per, bn, idesc, tcols, relu, splits > 1, status);
+        kblocks, per, bn, idesc, tcols, relu, splits > 1, stage_mode, vec_atomic, status);
     return cudaGetLastError() == cudaSuccess ? PCAGB_OK : PCAGB_ECUDA;
 }
 
@@ -810,8 +949,8 @@ extern "C" int pcagb_vnet_transpose_aug(const void *S, int R, int C, int lds, vo
 {
     if (R <= 0 || Cp <= 0) return PCAGB_OK;
     if (!S || !T || Cp < C || ldt < R) return PCAGB_EINVAL;
-    dim3 grid((R + 31) / 32, (Cp + 31) / 32);
-    k_transpose_aug<<<grid, dim3(32, 8), 0, (cudaStream_t)stream>>>(
+    dim3 grid((R + 63) / 64, (Cp + 63) / 64);
+    k_transpose_aug<<<grid, 256, 0, (cudaStream_t)stream>>>(
         (const __nv_bfloat16 *)S, R, C, lds, (__nv_bfloat16 *)T, Cp, ldt, ones);
     return cudaGetLastError() == cudaSuccess ? PCAGB_OK : PCAGB_ECUDA;
 }

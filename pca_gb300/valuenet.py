@@ -41,8 +41,7 @@ def _lib():
         "pcagb_vnet_transpose_aug": [vp, i, i, i, vp, i, i, i, vp],
         "pcagb_vnet_features": [vp, vp, vp, i, i, vp, vp, vp, vp],
         "pcagb_vnet_pool": [vp, vp, vp, vp, vp, i, vp, vp, vp],
-        "pcagb_vnet_pool_bwd": [vp, vp, vp, vp, i, vp, vp],
-        "pcagb_vnet_relu_bwd": [vp, vp, sz, vp],
+        "pcagb_vnet_pool_bwd": [vp, vp, vp, vp, vp, i, vp, vp],
         "pcagb_vnet_loss": [vp, vp, vp, i, f, vp, vp, vp, vp],
         "pcagb_vnet_adam": [vp, vp, vp, vp, i, i, f, f, f, f, vp, vp, vp, vp],
         "pcagb_vnet_to_bf16": [vp, vp, sz, vp],
@@ -213,9 +212,6 @@ class ValueNet:
         """Logits [n][16] through the fused encoder and the trunk."""
         return self.trunk(self.encode_pool(regs, flags, live, task, depth, TP, task_io, task_T))
 
-    def _relu_bwd(self, dY, Y):
-        self._ck(self.lib.pcagb_vnet_relu_bwd(_p(dY), _p(Y), dY.numel(), self.stream))
-
     def backward(self, dL):
         """dL: bf16 [n,16] gradient of the loss w.r.t. the logits. Returns
         {name: (dW, db)} in fp32."""
@@ -230,8 +226,8 @@ class ValueNet:
         n = a["task"].shape[0]
         dH2 = torch.empty(n * ROWS, 256, device=self.dev, dtype=torch.bfloat16)
         self._ck(self.lib.pcagb_vnet_pool_bwd(_p(dP), _p(a["am"]), _p(a["task"]),
-                                              _p(a["task_T"]), n, _p(dH2), self.stream))
-        self._relu_bwd(dH2, a["H2"])
+                                              _p(a["task_T"]), _p(a["H2"]), n, _p(dH2),
+                                              self.stream))
         grads["E2"] = self._wgrad(dH2, a["H1"], "E2")
         dH1 = self._gemm(dH2, "E2", False, transposed=True, mask=a["H1"])
         grads["E1"] = self._wgrad(dH1, a["X"], "E1")

@@ -89,15 +89,21 @@ def parse():
     ap.add_argument("--hbm-gb", type=float, default=0.0,
                     help="engine arena size in GB (0: 60%% of free HBM)")
     ap.add_argument("--workload", default="power2",
-                    choices=["power2", "batched", "served", "guided", "branch"],
+                    choices=["power2", "batched", "served", "guided", "deep", "branch"],
                     help="power2: the headline solve (default); batched: 1,000 synthetic "
                          "tasks plain vs batched; served: Poisson arrivals, served vs plain; "
-                         "guided: value-ordered vs DFS-ordered search")
+                         "guided: value-ordered vs DFS-ordered search; deep: value-ordered "
+                         "search on 200 tasks of source length 8-10")
     ap.add_argument("--rate", type=float, default=50.0, help="served: arrivals per second")
     ap.add_argument("--sat-rate", type=float, default=1000.0,
                     help="served: a saturating arrival rate, measured too")
     ap.add_argument("--requests", type=int, default=200, help="served: number of requests")
     ap.add_argument("--tasks", type=int, default=1000, help="batched: number of tasks")
+    ap.add_argument("--deep-tasks", type=int, default=200, help="deep: number of tasks")
+    ap.add_argument("--deep-depth", type=int, default=5,
+                    help="deep: kernel depth up to which each task is searched exhaustively")
+    ap.add_argument("--deep-budget-s", type=float, default=1200.0,
+                    help="deep: solving time after which no further task is started")
     ap.add_argument("--source", default="synthetic", choices=["synthetic", "reference"],
                     help="batched: this project's generator of the configured distribution, or "
                          "the reference's own corpus generator (10 tests, length 3-8)")
@@ -193,6 +199,34 @@ def reference_binary():
         return None
     with open(stamp) as f:
         return exe if f.read().strip() == platform.machine() else None
+
+
+def reference_gpu_hybrid():
+    """The reference's hybrid CPU/GPU solver (gpu/hybrid.cu), compiled on
+    this machine for sm_103a by oracle/build_ref.sh (None when not built)."""
+    exe = os.path.join(REPO, "oracle", "_ref", "gpu_hybrid")
+    return exe if reference_binary() and os.path.exists(exe) else None
+
+
+def run_gpu_hybrid(exe: str, path: str, depth: int, timeout: float) -> dict:
+    """One run of `gpu_hybrid <task> <depth> 1`: its own solve time (the
+    "Total elapsed" it prints, which excludes CUDA set-up), the kernel depth
+    of the first solution and whether the reference's CPU re-check of that
+    program passed."""
+    import re
+    t0 = time.perf_counter()
+    try:
+        p = subprocess.run([exe, path, str(depth), "1"], capture_output=True, text=True,
+                           timeout=timeout)
+    except subprocess.TimeoutExpired:
+        return {"timeout_s": timeout}
+    wall = time.perf_counter() - t0
+    out = p.stdout
+    m = re.search(r"Total elapsed: ([0-9.]+) sec", out)
+    k = re.search(r"kernel depth (\d+)\)", out)
+    return {"seconds": float(m.group(1)) if m else None, "process_seconds": wall,
+            "kernel_depth": int(k.group(1)) if k else -1, "exit": p.returncode,
+            "cpu_verify_ok": "cpu_verify" in out and " FAIL" not in out}
 
 
 def task_file(task, directory: str, name: str) -> str:
@@ -385,6 +419,8 @@ def run_reference(args):
     from pca_gb300 import taskgen
     from oracle.build import build_oracle
     build_oracle()
+    if args.workload == "branch":
+        return run_reference_branch(args)
     task = taskgen.is_power2_task(args.seed)
     cores = os.cpu_count() or 1
     exe = reference_binary()
@@ -430,6 +466,53 @@ def run_reference(args):
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": kind,
                              "sample": sample},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_reference_branch(args):
+    """Reference arm of the branch workload: the reference's own hybrid
+    CPU/GPU solver (gpu/hybrid.cu, compiled here for sm_103a) on each of the
+    reference's task files at its documented optimal length, on this
+    machine's GPU: its IDDFS from depth 0 (CPU DFS with its 32-bit hash
+    pruning to depth K-1, GPU suffixes of one instruction), stopping at the
+    first depth with a solution. Per task, one untimed run first."""
+    import tempfile
+    from pca_gb300.pcalib import task_from_dict
+    exe = reference_gpu_hybrid()
+    if not exe:
+        print(json.dumps({"impl": "reference", "workload": "branch",
+                          "unavailable": "the reference's gpu_hybrid was not built on this "
+                                         "machine (no staged sources or no nvcc)"}), flush=True)
+        return
+    fixture = os.path.join(REPO, "tests", "golden", "ref_published.json")
+    rows = []
+    with tempfile.TemporaryDirectory() as tmp:
+        for t in json.load(open(fixture)):
+            task = task_from_dict(t["task"])
+            K = t["published_length"] - task.num_inputs - 2
+            path = task_file(task, tmp, t["name"])
+            run_gpu_hybrid(exe, path, K, 600.0)
+            r = run_gpu_hybrid(exe, path, K, 600.0)
+            r.update({"task": t["name"], "published_length": t["published_length"],
+                      "found_length": r["kernel_depth"] + task.num_inputs + 2
+                      if r.get("kernel_depth", -1) >= 0 else None})
+            rows.append(r)
+    done = [r for r in rows if r.get("seconds") is not None]
+    total = sum(r["seconds"] for r in done)
+    line = {"impl": "reference", "metric": "branch-mode time to proven optimal (sum over the "
+            "reference's tasks)", "value": total, "unit": "s", "higher_is_better": False,
+            "n_gpus": 1, "data": "the reference's task files",
+            "config": {"workload": "branch mode, reference tasks at their documented optimal "
+                                   "lengths; the reference's gpu_hybrid (gpu/hybrid.cu) built "
+                                   "for sm_103a, default split (K-1) and batch (4,096)"},
+            "all_tasks_finished": len(done) == len(rows),
+            "all_lengths_match": all(r["found_length"] == r["published_length"] for r in rows),
+            "cpu_baseline": {"value": total, "unit": "s", "cores": 1, "kind": "reference",
+                             "sample": "the reference's gpu_hybrid: one host thread driving "
+                                       "the GPU, every task once after an untimed run"},
+            "e2e": {"value": total, "unit": "s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "tasks": rows}
     print(json.dumps(line), flush=True)
 
 
@@ -543,6 +626,23 @@ def run_served(args):
     print(json.dumps(line), flush=True)
 
 
+def train_value_net(eng):
+    """The value network trained on labels the exhaustive solver gives on
+    3,000 tasks of the batched config's generator (10 epochs on the GPU)."""
+    import torch
+    from pca_gb300 import taskgen
+    from pca_gb300.guided import build_dataset, train
+    from pca_gb300.valuenet import ValueNet
+    t0 = time.perf_counter()
+    ds, used = build_dataset(eng, taskgen.synthetic_batch(3000, seed=101), max_depth=4, seed=1)
+    t_label = time.perf_counter() - t0
+    net = ValueNet(seed=0, lr=1e-3, pos_weight=8.0)
+    t0 = time.perf_counter()
+    losses = train(net, ds, epochs=10)
+    torch.cuda.synchronize()
+    return net, ds, used, losses, t_label, time.perf_counter() - t0
+
+
 def run_guided(args):
     """The value network trained on the solver's own labels, then held-out
     tasks solved by the plain engine (the whole optimal-depth stage) and by
@@ -552,18 +652,10 @@ def run_guided(args):
     the first correct program."""
     import torch
     from pca_gb300 import taskgen
-    from pca_gb300.guided import RandomOrder, ValueOrder, build_dataset, train
+    from pca_gb300.guided import RandomOrder, ValueOrder
     from pca_gb300.pcalib import Engine
-    from pca_gb300.valuenet import ValueNet
     eng = Engine(0, int(args.hbm_gb * (1 << 30)))
-    t0 = time.perf_counter()
-    ds, used = build_dataset(eng, taskgen.synthetic_batch(3000, seed=101), max_depth=4, seed=1)
-    t_label = time.perf_counter() - t0
-    net = ValueNet(seed=0, lr=1e-3, pos_weight=8.0)
-    t0 = time.perf_counter()
-    losses = train(net, ds, epochs=10)
-    torch.cuda.synchronize()
-    t_train = time.perf_counter() - t0
+    net, ds, used, losses, t_label, t_train = train_value_net(eng)
     ev = taskgen.synthetic_batch(2000, seed=202)
     sols = eng.solve_batch(ev, max_depth=4, sol_cap=1, first_only=True)
     sel = [t for t, s in zip(ev, sols) if s.optimal_depth in (3, 4)]
@@ -625,6 +717,127 @@ def run_guided(args):
     print(json.dumps(line), flush=True)
 
 
+def run_deep(args):
+    """Value-ordered search on the deep workload: tasks whose source programs
+    have 8..10 instructions, each searched exhaustively up to kernel depth
+    --deep-depth by three methods, one task at a time: the plain engine (its
+    default first-only solve: a long stage runs as launches of prefixes in
+    DFS order, doubling, stopping at the first launch with a solution), and
+    ordered solves in random order and in the value network's order (256
+    prefixes in a stage's first launch, doubling, stopping at the first
+    launch of the optimal depth with a correct program). Every method must
+    report the same optimal depth for every task (or that none exists within
+    the bound) and only correct programs; an optimum is claimed only where
+    every shorter depth was searched to completion. Tasks are taken in order
+    until --deep-budget-s of solving time is spent. Reported: time to proven
+    optimal (mean, p50, p99, total) over the tasks run and over those
+    searched at the bound, and for the tasks whose optimum is at the bound
+    the fraction of that depth's prefixes visited before the first correct
+    program."""
+    import torch
+    from pca_gb300 import taskgen
+    from pca_gb300.guided import RandomOrder, ValueOrder
+    from pca_gb300.pcalib import Engine, PCALib
+    lib = PCALib()
+    eng = Engine(0, int(args.hbm_gb * (1 << 30)))
+    D = args.deep_depth
+    tasks = taskgen.deep_tasks(args.deep_tasks)
+    net, ds, used, losses, t_label, t_train = train_value_net(eng)
+    vo = ValueOrder(net, sample=4096)
+    methods = (
+        ("plain", lambda t: eng.solve(t, max_depth=D, sol_cap=1, first_only=True)),
+        ("random", lambda t: eng.solve_ordered(t, RandomOrder(1), chunk=256, max_depth=D,
+                                               split_depth=-1, sol_cap=1)),
+        ("value", lambda t: eng.solve_ordered(t, vo, chunk=256, max_depth=D, split_depth=-1,
+                                              sol_cap=1)))
+    # untimed: lazy kernel loading, the ranking graph's capture, and the
+    # autotuner's calibration of large stages (a depth-5 search of is_power2)
+    pool = taskgen.synthetic_batch(300, seed=202)
+    warm = [taskgen.is_power2_task(1)] + [t for t, s in zip(
+        pool, eng.solve_batch(pool, max_depth=4, sol_cap=1, first_only=True))
+        if s.optimal_depth in (3, 4)][:4]
+    for t in warm:
+        for _, fn in methods:
+            fn(t)
+    vo.score_ms = 0.0
+    t0 = time.perf_counter()
+    first4 = eng.solve_batch(tasks, max_depth=4, sol_cap=1, first_only=True)
+    t_batch4 = time.perf_counter() - t0
+    rows = []
+    t_start = time.perf_counter()
+    for i, t in enumerate(tasks):
+        if time.perf_counter() - t_start > args.deep_budget_s:
+            break
+        row = {"task": t.name.decode() if isinstance(t.name, bytes) else str(t.name),
+               "tests": t.num_tests, "inputs": t.num_inputs}
+        depth = None
+        for name, fn in methods:
+            s = fn(t)
+            if depth is None:
+                depth = s.optimal_depth
+                row["optimal_depth"] = depth
+            assert s.optimal_depth == depth, (row["task"], name, s.optimal_depth, depth)
+            assert (depth >= 0) == bool(s.programs)
+            for prog in s.programs:
+                assert lib.evaluate(t, prog) == t.num_tests, (row["task"], name)
+            row[name] = {"s": s.seconds,
+                         "frac": s.prefixes_to_first / max(s.prefixes_at_optimal, 1)
+                         if depth >= 0 else None}
+        assert first4[i].optimal_depth == (depth if 0 <= depth <= 4 else -1)
+        rows.append(row)
+        print(json.dumps({"deep_progress": i, **row}), file=sys.stderr, flush=True)
+
+    def summary(sel, name):
+        v = sorted(r[name]["s"] for r in sel)
+        if not v:
+            return None
+        out = {"mean_s": statistics.mean(v), "p50_s": v[len(v) // 2],
+               "p99_s": v[min(len(v) - 1, int(0.99 * len(v)))], "total_s": sum(v)}
+        fr = [r[name]["frac"] for r in sel if r["optimal_depth"] == D]
+        if fr:
+            out["mean_fraction_to_first_at_bound"] = statistics.mean(fr)
+            out["median_fraction_to_first_at_bound"] = statistics.median(fr)
+        return out
+
+    hist = {}
+    for r in rows:
+        hist[str(r["optimal_depth"])] = hist.get(str(r["optimal_depth"]), 0) + 1
+    at_bound = [r for r in rows if not 0 <= r["optimal_depth"] <= 4]
+    names = [m[0] for m in methods]
+    summ = {"all_tasks": {n: summary(rows, n) for n in names},
+            "searched_at_bound": {n: summary(at_bound, n) for n in names}}
+    for grp in summ.values():
+        for n in names:
+            if grp[n] and grp["plain"]:
+                grp[n]["speedup_vs_plain"] = grp["plain"]["mean_s"] / grp[n]["mean_s"]
+    allv = summ["all_tasks"]
+    line = {"metric": "time-to-proven-optimal, plain engine / value-ordered (mean over tasks)",
+            "value": allv["value"]["speedup_vs_plain"], "unit": "x",
+            "higher_is_better": True, "n_gpus": 1, "data": "synthetic",
+            "tasks_run": len(rows), "tasks_drawn": len(tasks),
+            "config": {"workload": f"{len(rows)} synthetic tasks of source length 8-10 "
+                                   f"(16-32 tests, 1-2 inputs), each searched exhaustively up "
+                                   f"to kernel depth {D}; value order ranks a 4,096-prefix "
+                                   "sample of the split level by a CUDA-graph replay; first "
+                                   "launch 256 prefixes, doubling",
+                       "train_tasks_used": used, "train_states": ds.n,
+                       "params": net.n_params(), "epochs": 10},
+            "optimal_depth_histogram": hist,
+            "depth4_histogram_all_drawn": {str(k): sum(1 for x in first4 if x.optimal_depth == k)
+                                           for k in sorted({x.optimal_depth for x in first4})},
+            "proven_optimal": sum(1 for r in rows if r["optimal_depth"] >= 0),
+            "none_within_bound": sum(1 for r in rows if r["optimal_depth"] < 0),
+            "batch_to_depth4_seconds": t_batch4,
+            "label_seconds": t_label, "train_seconds": t_train, "train_loss": losses,
+            "orders": summ, "value_scoring_ms_per_task": vo.score_ms / max(len(rows), 1),
+            "tasks_at_bound": [{"task": r["task"], "optimal_depth": r["optimal_depth"],
+                                "tests": r["tests"], "inputs": r["inputs"],
+                                **{n: r[n] for n in names}} for r in at_bound]}
+    vo.close()
+    torch.cuda.synchronize()
+    print(json.dumps(line), flush=True)
+
+
 def run_branch(args):
     """Branch mode (CMP, forward BR, DIV, MOD) on the reference's own task
     files at their documented optimal lengths: time to the proven optimum
@@ -665,6 +878,7 @@ def main():
         from pca_gb300.build import build_engine
         build_engine()
         return {"batched": run_batched, "served": run_served, "guided": run_guided,
+                "deep": run_deep,
                 "branch": run_branch}[args.workload](args)
     rank, world, local = dist_env()
     import torch

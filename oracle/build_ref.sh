@@ -1,7 +1,10 @@
 #!/bin/sh
 # Compile the reference's own CPU solver and its libpca.so from the reference
 # sources, in place, into oracle/_ref/ (git-ignored). Used only as a checker:
-# tests and golden-fixture generation compare against these outputs.
+# tests and golden-fixture generation compare against these outputs. Where
+# nvcc is present, also its hybrid CPU/GPU solver gpu/hybrid.cu for sm_103a
+# (gpu_hybrid), which the benchmark's reference arm times as the reference's
+# GPU baseline; a failure there leaves the CPU builds in place.
 #
 #   oracle/build_ref.sh REFERENCE_ROOT
 #
@@ -25,5 +28,11 @@ gcc $CFLAGS -shared -fPIC -o "$OUT/libpca.so" \
 gcc $CFLAGS -o "$OUT/gen_tasks" \
     "$REF/src/vm.c" "$REF/src/asm.c" "$REF/src/search_state.c" \
     "$REF/tasks/spec.c" "$REF/tools/gen_tasks.c"
+NVCC=$(command -v nvcc || echo "${CUDA_HOME:-/usr/local/cuda}/bin/nvcc")
+if [ -f "$REF/gpu/hybrid.cu" ] && [ -x "$NVCC" ]; then
+    "$NVCC" -O3 -w -gencode arch=compute_103a,code=sm_103a -o "$OUT/gpu_hybrid" \
+        "$REF/gpu/hybrid.cu" "$REF/tasks/spec.c" "$REF/src/vm.c" "$REF/src/asm.c" \
+        || { rm -f "$OUT/gpu_hybrid"; echo "build_ref: gpu_hybrid not built" >&2; }
+fi
 uname -m > "$OUT/.machine"
 echo "build_ref: built $OUT/enumerate $OUT/libpca.so $OUT/gen_tasks"

@@ -1,7 +1,8 @@
 #!/bin/sh
 # Stage the reference's sources for its CPU solver path (tools/enumerate.c
 # and what it links: src/vm.c, src/asm.c, src/search_state.c, tasks/spec.c
-# and their headers) into baseline/_ref/src, which git ignores, so that the
+# and their headers) and for its hybrid CPU/GPU solver (gpu/hybrid.cu) into
+# baseline/_ref/src, which git ignores, so that the
 # reference can be compiled from them on a machine without the reference
 # tree (oracle/build_ref.sh; oracle/build.py does it when the staged copy
 # exists). Nothing staged is committed.
@@ -15,9 +16,9 @@ if [ -z "$REF" ] || [ ! -f "$REF/tools/enumerate.c" ]; then
     echo "stage_ref: no reference tree given; nothing staged" >&2
     exit 0
 fi
-mkdir -p "$DEST/src" "$DEST/tasks" "$DEST/tools"
+mkdir -p "$DEST/src" "$DEST/tasks" "$DEST/tools" "$DEST/gpu"
 for f in src/vm.c src/asm.c src/search_state.c src/pca.h src/search_state.h \
-         tasks/spec.c tasks/spec.h tools/enumerate.c tools/gen_tasks.c; do
+         tasks/spec.c tasks/spec.h tools/enumerate.c tools/gen_tasks.c gpu/hybrid.cu; do
     cp "$REF/$f" "$DEST/$f"
 done
-echo "stage_ref: staged the reference's CPU solver sources in $DEST"
+echo "stage_ref: staged the reference's solver sources in $DEST"

@@ -195,10 +195,16 @@ def case_misc(reps: int):
     import torch
     from pca_gb300.guided import ValueOrder
     from pca_gb300.pcalib import Engine, OEP_EXACT, OEP_NONE
-    from pca_gb300.taskgen import negate_task, synthetic_task
+    from pca_gb300.taskgen import negate_task, synthetic_batch
     from pca_gb300.valuenet import ValueNet
     eng = Engine(0, 4 << 30)
-    t3, _ = synthetic_task(659, 3)
+    # tasks of the batched workload's generator whose optimum is at kernel
+    # depth 3 (one input: the recording pass) and 4 (the ordered solve ranks
+    # a sample of its level 2 or 3)
+    pool = synthetic_batch(400, seed=41)
+    sols = eng.solve_batch(pool, max_depth=4, sol_cap=1, first_only=True)
+    t3 = next(t for t, s in zip(pool, sols) if s.optimal_depth == 3 and t.num_inputs == 1)
+    t4 = next(t for t, s in zip(pool, sols) if s.optimal_depth == 4)
     net = ValueNet(seed=0)
     vo = ValueOrder(net, sample=4096, min_states=1, gain=0.0)
     for _ in range(reps):
@@ -208,7 +214,7 @@ def case_misc(reps: int):
         with tempfile.TemporaryDirectory() as d:
             st = eng.record(t3, d, max_depth=3, task_id=1, neg_stride=8)
             n_files = len(os.listdir(d))
-        c = eng.solve_ordered(t3, vo, chunk=256, max_depth=3, split_depth=2)
+        c = eng.solve_ordered(t4, vo, chunk=256, max_depth=4, split_depth=2)
         torch.cuda.synchronize()
         print(f"misc: K*={a.optimal_depth} ({len(a.programs)} programs), no-OEP "
               f"K*={b.optimal_depth}, recorded {n_files} files ({st}), ordered "

@@ -82,7 +82,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-proof", action="store_true",
                     help="skip the time-to-proven-optimal runs after the timed region")
-    ap.add_argument("--proof-depth", type=int, default=5,
+    ap.add_argument("--proof-depth", type=int, default=6,
                     help="kernel depth the headline task's IDDFS continues to after the timing")
     ap.add_argument("--c3-tasks", type=int, default=100,
                     help="synthetic tasks scanned for the CPU/GPU time-to-proven comparison")
@@ -305,8 +305,15 @@ def suffix_roofline(suffix_ms: float, peak_issue: float, evals_run_per_s: float)
 def proof_and_time_to_optimal(eng, task, args) -> dict:
     """Time to a proven optimum, outside the timed region.
 
-    is_power2_full: the headline task's IDDFS continued past kernel depth 4
-    (up to --proof-depth), split 3: the proven optimal depth and program.
+    is_power2_k5: the headline task's plain IDDFS continued past kernel
+    depth 4 to depth 5, split 3 (no program there).
+    is_power2_full: the same task solved to --proof-depth by the
+    value-ordered solve (every depth below the optimum searched completely,
+    the optimal depth's stage visited in the value network's order of the
+    whole level, stopping at the first launch with a correct program): the
+    proven optimal depth and programs, each verified on every test by the
+    host VM. The network is trained first on the solver's labels of 3,000
+    tasks of the batched workload (not timed with the solve).
     is_power2_k3 / synthetic_k3: configurations the CPU finishes, timed on
     both sides: the headline task to kernel depth 3, and the synthetic tasks
     of the batched workload whose optimum is within kernel depth 3, on the
@@ -320,16 +327,37 @@ def proof_and_time_to_optimal(eng, task, args) -> dict:
     out = {}
     cores = os.cpu_count() or 1
     if args.proof_depth > args.max_depth:
+        from pca_gb300.guided import ValueOrder
+        from pca_gb300.pcalib import PCALib
+        lib = PCALib()
+        d5 = min(5, args.proof_depth)
         t0 = time.perf_counter()
-        s = eng.solve(task, max_depth=args.proof_depth, split_depth=args.split, sol_cap=64)
+        s = eng.solve(task, max_depth=d5, split_depth=args.split, sol_cap=64)
         dt = time.perf_counter() - t0
-        out["is_power2_full"] = {
-            "max_kernel_depth": args.proof_depth, "optimal_depth": s.optimal_depth,
-            "program_length": s.optimal_depth + task.num_inputs + 2 if s.optimal_depth >= 0 else None,
-            "first_program": s.programs[0] if s.programs else None,
-            "programs_at_optimal": s.total_solutions, "seconds": dt,
+        out["is_power2_k5"] = {
+            "max_kernel_depth": d5, "optimal_depth": s.optimal_depth, "seconds": dt,
             "gpu_ms_suffix": s.gpu_ms_suffix, "evaluations_run": s.evaluations_run,
             "candidates_decided": int(sum(s.candidates))}
+        if args.proof_depth > 5 or s.optimal_depth < 0:
+            net, ds, used, losses, t_label, t_train = train_value_net(eng)
+            vo = ValueOrder(net, min_states=1, gain=0.0)
+            t0 = time.perf_counter()
+            s = eng.solve_ordered(task, vo, chunk=256, max_depth=args.proof_depth,
+                                  split_depth=args.split, sol_cap=4)
+            dt = time.perf_counter() - t0
+            out["is_power2_full"] = {
+                "max_kernel_depth": args.proof_depth, "order": "value network, whole level",
+                "optimal_depth": s.optimal_depth,
+                "program_length": s.optimal_depth + task.num_inputs + 2
+                if s.optimal_depth >= 0 else None,
+                "programs": [" ; ".join(lib.disasm(w) for w in p) for p in s.programs],
+                "tests_passed": [lib.evaluate(task, p) for p in s.programs],
+                "num_tests": task.num_tests, "seconds": dt,
+                "prefixes_to_first": s.prefixes_to_first,
+                "prefixes_at_optimal": s.prefixes_at_optimal, "ms_to_first": s.ms_to_first,
+                "scoring_ms": vo.score_ms, "train_states": ds.n, "label_seconds": t_label,
+                "train_seconds": t_train}
+            vo.close()
     # the headline task to kernel depth 3
     gpu = []
     for _ in range(3):
@@ -780,7 +808,7 @@ def run_deep(args):
             assert (depth >= 0) == bool(s.programs)
             for prog in s.programs:
                 assert lib.evaluate(t, prog) == t.num_tests, (row["task"], name)
-            row[name] = {"s": s.seconds,
+            row[name] = {"s": s.seconds, "split": s.split_used,
                          "frac": s.prefixes_to_first / max(s.prefixes_at_optimal, 1)
                          if depth >= 0 else None}
         assert first4[i].optimal_depth == (depth if 0 <= depth <= 4 else -1)
@@ -805,15 +833,21 @@ def run_deep(args):
     at_bound = [r for r in rows if not 0 <= r["optimal_depth"] <= 4]
     names = [m[0] for m in methods]
     summ = {"all_tasks": {n: summary(rows, n) for n in names},
-            "searched_at_bound": {n: summary(at_bound, n) for n in names}}
+            "searched_at_bound": {n: summary(at_bound, n) for n in names},
+            "optimum_at_bound": {n: summary([r for r in rows if r["optimal_depth"] == D], n)
+                                 for n in names},
+            "none_within_bound": {n: summary([r for r in rows if r["optimal_depth"] < 0], n)
+                                  for n in names}}
     for grp in summ.values():
         for n in names:
             if grp[n] and grp["plain"]:
                 grp[n]["speedup_vs_plain"] = grp["plain"]["mean_s"] / grp[n]["mean_s"]
     allv = summ["all_tasks"]
+    opt = summ["optimum_at_bound"]["value"]
     line = {"metric": "time-to-proven-optimal, plain engine / value-ordered (mean over tasks)",
             "value": allv["value"]["speedup_vs_plain"], "unit": "x",
             "higher_is_better": True, "n_gpus": 1, "data": "synthetic",
+            "value_on_optimum_at_bound": opt["speedup_vs_plain"] if opt else None,
             "tasks_run": len(rows), "tasks_drawn": len(tasks),
             "config": {"workload": f"{len(rows)} synthetic tasks of source length 8-10 "
                                    f"(16-32 tests, 1-2 inputs), each searched exhaustively up "

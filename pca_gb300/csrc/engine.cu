@@ -75,6 +75,7 @@ constexpr uint64_t kOneSyncBytes = 64ull << 20;
 /* ordered solves with an automatic split (see run_batch) */
 constexpr double kOrderMinStageMs = 2.0;
 constexpr double kOrderStageShare = 0.1;
+constexpr double kOrderMaxOverhead = 1.02;
 
 struct Level {
     uint64_t n = 0;
@@ -1023,9 +1024,13 @@ typedef void (*done_fn)(int task, void *user);
  * level D: evals(S, K-S) ~ evals(D, K-D) x dedup_ratio^(S-D). The cheapest
  * S within the HBM budget (max_feasible) wins. stage_scale weights the
  * stage term (an ordered stage that stops at its first solution is expected
- * to run a fraction of it); *pred_ms receives the winner's predicted time. */
+ * to run a fraction of it); *pred_ms receives the winner's predicted time.
+ * With full_cap set, a level whose whole stage (builds + every prefix) is
+ * predicted to cost more than full_cap is not chosen (-1 when none is
+ * left). */
 int autotune_split(pcagb_engine *e, int K, const std::vector<uint8_t> &active,
-                   double stage_scale = 1.0, double *pred_ms = nullptr)
+                   double stage_scale = 1.0, double *pred_ms = nullptr,
+                   double full_cap = 1e300)
 {
     const GenTables &gt = gen_tables();
     const int D = (int)e->levels.size() - 1;
@@ -1057,9 +1062,10 @@ int autotune_split(pcagb_engine *e, int K, const std::vector<uint8_t> &active,
     double best_ms = 1e300;
     for (int S = std::max(lo, 0); S <= hi; S++) {
         if (K - S > 3) continue;
-        double ms;
+        double ms, full;
         if (S <= D) {
-            ms = evals_from(S, K - S) * e->t_eval_ms[K - S] * stage_scale;
+            full = evals_from(S, K - S) * e->t_eval_ms[K - S];
+            ms = full * stage_scale;
         } else {
             /* build D+1..S from D, then the suffix from S. A build that would
                not fit the arena (its table, bitmap and ranks, plus the new
@@ -1082,12 +1088,16 @@ int autotune_split(pcagb_engine *e, int K, const std::vector<uint8_t> &active,
                 kids *= e->dedup_ratio * 800.0;  /* ~children per state deeper down */
             }
             if (!fits) continue;
-            ms = build + evals_from(D, K - D) * states_scale * e->t_eval_ms[K - S] * stage_scale;
+            const double stage = evals_from(D, K - D) * states_scale * e->t_eval_ms[K - S];
+            full = build + stage;
+            ms = build + stage * stage_scale;
         }
+        if (full > full_cap) continue;
         if (ms < best_ms) { best_ms = ms; best = S; }
     }
     if (pred_ms) *pred_ms = best_ms;
-    return best < 0 ? std::max(hi, lo) : best;
+    if (best < 0) return full_cap < 1e300 ? -1 : std::max(hi, lo);
+    return best;
 }
 
 typedef CUresult (*AddressRangeFn)(CUdeviceptr *, size_t *, CUdeviceptr);
@@ -1317,7 +1327,10 @@ int run_batch(pcagb_engine *e, std::vector<TaskRun> &runs, const pcagb_opts_t &o
            worth it: a stage the autotuner expects to finish in under
            kOrderMinStageMs runs plain from its cheapest level; the others
            start from the level that minimises builds + a tenth of the stage
-           (the share an ordered stage is expected to run) */
+           (the share an ordered stage is expected to run) among the levels
+           whose whole stage is predicted within kOrderMaxOverhead of the
+           plain choice's: a depth without a solution is searched completely
+           in any order, and then costs about what the plain solve pays */
         bool ordered_stage = ord != nullptr;
         if (o.split_depth >= 0) {
             S_target = std::min(S_target, o.split_depth);
@@ -1328,7 +1341,9 @@ int run_batch(pcagb_engine *e, std::vector<TaskRun> &runs, const pcagb_opts_t &o
                 S_target = Sp;
                 ordered_stage = false;
             } else {
-                S_target = autotune_split(e, K, active, kOrderStageShare);
+                const int So = autotune_split(e, K, active, kOrderStageShare, nullptr,
+                                              plain_ms * kOrderMaxOverhead);
+                S_target = So >= 0 ? So : Sp;
             }
         } else if (o.first_only && !o.count_levels) {
             S_target = autotune_split(e, K, active);

@@ -181,7 +181,9 @@ class ValueOrder:
     many prefixes spread over it (prefix (a * i + b) mod n for sample i, a
     coprime to n, a and b drawn per level): the order is the sample by
     decreasing score, then every other prefix in the same map's order (a
-    permutation of the whole level). The first correct program usually sits
+    permutation of the whole level). A stage expected to take at least
+    `full_gain` times the cost of scoring the whole level (a deep stage:
+    seconds against milliseconds) has its whole level ranked instead. The first correct program usually sits
     in the first few percent of a good order, so the ranked sample decides
     the first launches at a fraction of the scoring cost. The ranking (the
     gather of the sample, the fused encoder, the trunk and the sort) is a
@@ -190,12 +192,16 @@ class ValueOrder:
     device buffer, so one replay and one order kernel serve any level."""
 
     def __init__(self, net: ValueNet, chunk_states=1 << 20, min_states=4096, gain=2.0,
-                 fixed_ms=0.25, states_per_ms=1.0e5, sample=None, seed=0):
+                 fixed_ms=0.25, states_per_ms=1.0e5, sample=None, seed=0, full_gain=50.0):
         self.net = net
         self.chunk_states = chunk_states
         self.min_states = min_states
         self.gain, self.fixed_ms, self.states_per_ms = gain, fixed_ms, states_per_ms
         self.sample = sample
+        # with `sample` set, a stage the engine expects to take at least
+        # full_gain x the cost of scoring its whole level is ranked whole
+        # (None: always sampled)
+        self.full_gain = full_gain
         self.rng = random.Random(seed)
         self.score_ms = 0.0
         self._cache = {}
@@ -217,6 +223,9 @@ class ValueOrder:
             return None
         key = (view.regs, n, view.depth)
         scored = n if not self.sample else min(n, self.sample)
+        if scored < n and self.full_gain is not None and \
+                view.est_stage_ms >= self.full_gain * (self.fixed_ms + n / self.states_per_ms):
+            scored = n
         if key not in self._cache and \
                 view.est_stage_ms < self.gain * (self.fixed_ms + scored / self.states_per_ms):
             return None
@@ -358,13 +367,21 @@ def map_multiplier(n: int, start: int = 0) -> int:
 
 
 class RandomOrder:
-    def __init__(self, seed=0):
-        self.gen = torch.Generator().manual_seed(seed)
+    """Order callback: a uniformly random permutation of each level, drawn
+    on the device (a level of tens of millions of prefixes would take the
+    host seconds)."""
+
+    def __init__(self, seed=0, device="cuda"):
+        self.gen = torch.Generator(device=device).manual_seed(seed)
+        self.device = device
 
     def __call__(self, view):
         if view.n == 0:
             return None
-        return torch.randperm(view.n, generator=self.gen).to(torch.int32).cuda()
+        stream = torch.cuda.ExternalStream(view.stream, device=self.device)
+        with torch.cuda.stream(stream):
+            return torch.randperm(view.n, generator=self.gen, device=self.device,
+                                  dtype=torch.int32)
 
 
 def _device_view(addr, count, dtype, dev):

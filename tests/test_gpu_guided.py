@@ -47,14 +47,20 @@ def test_positive_labels_are_exact(engine):
     assert checked > 0
 
 
-@pytest.mark.parametrize("order", ["dfs", "random", "value", "value_sampled"])
+@pytest.mark.parametrize("order", ["dfs", "random", "value", "value_sampled",
+                                   "value_sampled_long_stage"])
 def test_ordered_solve_is_exact(engine, order):
     from pca_gb300.guided import RandomOrder, ValueOrder
     from pca_gb300.valuenet import ValueNet
     lib = PCALib()
     fn = {"dfs": lambda v: None, "random": RandomOrder(5),
           "value": ValueOrder(ValueNet(seed=1), min_states=1, gain=0.0),
-          "value_sampled": ValueOrder(ValueNet(seed=1), min_states=1, gain=0.0, sample=512)}[order]
+          "value_sampled": ValueOrder(ValueNet(seed=1), min_states=1, gain=0.0, sample=512,
+                                      full_gain=None),
+          # every stage counts as long: the whole level is ranked though a
+          # sample size is set
+          "value_sampled_long_stage": ValueOrder(ValueNet(seed=1), min_states=1, gain=0.0,
+                                                 sample=512, full_gain=0.0)}[order]
     for task in pick(engine, 41, 300, (3, 4))[:6]:
         plain = engine.solve(task, max_depth=4, split_depth=2, sol_cap=1 << 14)
         got = engine.solve_ordered(task, fn, chunk=64, max_depth=4, split_depth=2, sol_cap=1 << 14)

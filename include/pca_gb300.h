@@ -370,6 +370,19 @@ int  pcagb_solve_branch(pcagb_engine_t *e, const task_spec_t *task, int max_dept
 int  pcagb_solve_branch_ex(pcagb_engine_t *e, const task_spec_t *task, int max_depth,
                            uint64_t last_level_max_children, pcagb_result_t *res,
                            uint16_t *sol_progs, int *sol_lens, int sol_cap);
+/* Branch mode with the reference hybrid solver's stopping rule
+ * (gpu/hybrid.cu:524-555: the search ends at the first batch of prefixes
+ * with a solution): every depth below the optimum is searched completely;
+ * at each depth the last position is searched without building its level,
+ * over the parents in depth-first order in launches of 1/64 of them,
+ * doubling, and the depth ends at the first launch that holds a solution.
+ * The optimal depth is the same as pcagb_solve_branch's, and so are the
+ * programs returned: the first in depth-first order, up to sol_cap, all
+ * from that launch. tried[K] / candidates[K] count the children built
+ * plus the last-position children of the parents visited. */
+int  pcagb_solve_branch_first(pcagb_engine_t *e, const task_spec_t *task, int max_depth,
+                              pcagb_result_t *res, uint16_t *sol_progs, int *sol_lens,
+                              int sol_cap);
 const char *pcagb_branch_last_error(void);
 
 /* The CUDA stream (cudaStream_t) every kernel of this engine runs on, so a

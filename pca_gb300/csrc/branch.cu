@@ -42,6 +42,7 @@
 
 #include "../../include/pca_gb300.h"
 #include "pca_isa.h"
+#include "scan.cuh"
 
 namespace {
 
@@ -536,7 +537,7 @@ struct BSol {
 template <int TP>
 __global__ void __launch_bounds__(kBThreads)
 k_bsuffix(BDev P, BTab tab, int T, uint32_t p, const uint32_t *target, BSol *out,
-          unsigned long long *count, uint64_t cap)
+          unsigned long long *count, uint64_t cap, uint64_t q_begin, uint64_t q_end)
 {
     __shared__ uint32_t sRall[kWarps][8][TP + 1];
     __shared__ uint32_t sFall[kWarps][TP], sSall[kWarps][TP];
@@ -544,7 +545,9 @@ k_bsuffix(BDev P, BTab tab, int T, uint32_t p, const uint32_t *target, BSol *out
     uint32_t (&sR)[8][TP + 1] = sRall[wib];
     uint32_t *sF = sFall[wib], *sS = sSall[wib];
     const uint64_t nw = (uint64_t)gridDim.x * kWarps;
-    for (uint64_t q = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < P.n; q += nw) {
+    const uint64_t qe = q_end < P.n ? q_end : P.n;
+    for (uint64_t q = q_begin + (((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5); q < qe;
+         q += nw) {
         uint32_t pm = 0;
         bool faulted = false;
         for (int r = 1; r < 8; r++) {
@@ -627,6 +630,30 @@ __global__ void k_bpairs_equal(BDev P, BTab tab, int T, uint32_t p, const uint4 
     }
 }
 
+/* The tree links of solving children, gathered on the device so that no
+   level's links cross the bus: for solution i (state qs[i] of level K-1 and
+   candidate c), out[i][d] = (live mask of its level-d ancestor) << 16 |
+   (candidate index that ancestor's child on the path took), d = 0..K-1. */
+struct BPath {
+    const uint32_t *parent[16];
+    const uint16_t *cidx[16];
+    const uint8_t *live[16];
+};
+
+__global__ void k_bpath(BPath L, int K, const uint32_t *qs, const uint16_t *cs, int ns,
+                        uint32_t *out)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ns; i += gridDim.x * blockDim.x) {
+        uint64_t st = qs[i];
+        out[(size_t)i * K + K - 1] = (uint32_t)L.live[K - 1][st] << 16 | cs[i];
+        for (int d = K - 1; d >= 1; d--) {
+            const uint32_t par = L.parent[d][st];
+            out[(size_t)i * K + d - 1] = (uint32_t)L.live[d - 1][par] << 16 | L.cidx[d][st];
+            st = par;
+        }
+    }
+}
+
 /* ---- host driver ----------------------------------------------------------- */
 
 struct BranchRun {
@@ -700,6 +727,25 @@ int blaunch(BranchRun &b)
     return PCAGB_OK;
 }
 
+/* Exclusive scan of a[0..n) in place on the stream (nothing read back). */
+int bscan(BranchRun &b, uint64_t *a, uint64_t n)
+{
+    if (n == 0) return PCAGB_OK;
+    const uint64_t nb = (n + kScanBlock - 1) / kScanBlock;
+    uint64_t *sums = b.alloc<uint64_t>(nb + 1);
+    if (!sums) { set_berr("device memory exhausted in a scan"); return PCAGB_ENOMEM; }
+    k_scan_local<<<(unsigned)nb, 256, 0, b.st>>>(a, n, sums);
+    int rc = blaunch(b);
+    if (rc) return rc;
+    if (nb > 1) {
+        rc = bscan(b, sums, nb);
+        if (rc) return rc;
+        k_scan_add<<<(unsigned)nb, 256, 0, b.st>>>(a, n, sums);
+        rc = blaunch(b);
+    }
+    return rc;
+}
+
 /* Expand level P (position p of a depth-K pass) into C. Fills the number of
    generated children. */
 /* Children of every state of P at a position with mf forward offsets:
@@ -709,24 +755,17 @@ int count_bchildren(BranchRun &b, BLevel &P, int mf)
     const BTab tab = b.tab(mf);
     P.child_off = b.alloc<uint64_t>(P.n + 1);
     if (!P.child_off) { set_berr("device memory exhausted"); return PCAGB_ENOMEM; }
+    BCK(cudaMemsetAsync(P.child_off + P.n, 0, 8, b.st));
     k_bchild_counts<<<b.grid(2), 256, 0, b.st>>>(bdev(P), tab, P.child_off);
     int rc = blaunch(b);
     if (rc) return rc;
-    /* exclusive scan on the host side of the copy (levels here are small
-       enough that one round trip is cheaper than a device scan) */
-    std::vector<uint64_t> cnt(P.n + 1, 0);
-    BCK(cudaMemcpyAsync(cnt.data(), P.child_off, P.n * 8, cudaMemcpyDeviceToHost, b.st));
-    BCK(cudaStreamSynchronize(b.st));
-    b.d2h += P.n * 8;
+    /* exclusive scan on the device; the total lands in child_off[n] */
+    rc = bscan(b, P.child_off, P.n + 1);
+    if (rc) return rc;
     uint64_t total = 0;
-    for (uint64_t i = 0; i < P.n; i++) {
-        const uint64_t c = cnt[i];
-        cnt[i] = total;
-        total += c;
-    }
-    cnt[P.n] = total;
-    BCK(cudaMemcpyAsync(P.child_off, cnt.data(), (P.n + 1) * 8, cudaMemcpyHostToDevice, b.st));
-    b.h2d += (P.n + 1) * 8;
+    BCK(cudaMemcpyAsync(&total, P.child_off + P.n, 8, cudaMemcpyDeviceToHost, b.st));
+    BCK(cudaStreamSynchronize(b.st));
+    b.d2h += 8;
     P.children = total;
     if (P.n >= (1ull << 28) || total >= (1ull << 38)) {
         set_berr("level too large (%llu states, %llu children)", (unsigned long long)P.n,
@@ -761,24 +800,21 @@ int build_blevel(BranchRun &b, BLevel &P, uint32_t p, int mf, BLevel &C)
     k_bmark<<<b.grid(4), 256, 0, b.st>>>(table, slots, P.child_off, bitmap);
     rc = blaunch(b);
     if (rc) return rc;
+    BCK(cudaMemsetAsync(rank + words, 0, 8, b.st));
     k_bpopc<<<b.grid(2), 256, 0, b.st>>>(bitmap, words, rank);
     rc = blaunch(b);
     if (rc) return rc;
-    std::vector<uint64_t> r(words + 1, 0);
+    /* each word's rank of kept children, scanned on the device; the kept
+       total lands in rank[words] */
+    rc = bscan(b, rank, words + 1);
+    if (rc) return rc;
+    uint64_t kept = 0;
     uint32_t status = 0;
-    BCK(cudaMemcpyAsync(r.data(), rank, words * 8, cudaMemcpyDeviceToHost, b.st));
+    BCK(cudaMemcpyAsync(&kept, rank + words, 8, cudaMemcpyDeviceToHost, b.st));
     BCK(cudaMemcpyAsync(&status, b.d_status, 4, cudaMemcpyDeviceToHost, b.st));
     BCK(cudaStreamSynchronize(b.st));
-    b.d2h += words * 8 + 4;
+    b.d2h += 12;
     if (status) { set_berr("pruning table probe limit reached"); return PCAGB_ELIMIT; }
-    uint64_t kept = 0;
-    for (uint64_t i = 0; i < words; i++) {
-        const uint64_t c = r[i];
-        r[i] = kept;
-        kept += c;
-    }
-    BCK(cudaMemcpyAsync(rank, r.data(), words * 8, cudaMemcpyHostToDevice, b.st));
-    b.h2d += words * 8;
     rc = alloc_blevel(b, C, kept);
     if (rc) return rc;
     if (kept) {
@@ -816,15 +852,68 @@ int fetch_links(BranchRun &b, const BLevel &L, HostLevel &H, bool links)
     return PCAGB_OK;
 }
 
+/* Kernel words of solutions (state q of level K-1, candidate c) from their
+ * tree links, gathered on the device (k_bpath). */
+int solution_kernels(BranchRun &b, const BranchTables &bt, std::vector<BLevel> &lv, int K,
+                     const std::vector<std::pair<uint32_t, uint16_t>> &sols,
+                     std::vector<std::vector<uint16_t>> *kernels)
+{
+    kernels->clear();
+    if (sols.empty()) return PCAGB_OK;
+    BPath L{};
+    for (int d = 0; d < K; d++) {
+        L.parent[d] = lv[d].parent;
+        L.cidx[d] = lv[d].cidx;
+        L.live[d] = lv[d].live;
+    }
+    const int ns = (int)sols.size();
+    uint32_t *d_q = b.alloc<uint32_t>(ns);
+    uint16_t *d_c = b.alloc<uint16_t>(ns);
+    uint32_t *d_out = b.alloc<uint32_t>((size_t)ns * K);
+    if (!d_q || !d_c || !d_out) { set_berr("device memory exhausted"); return PCAGB_ENOMEM; }
+    std::vector<uint32_t> q(ns);
+    std::vector<uint16_t> c(ns);
+    for (int i = 0; i < ns; i++) {
+        q[i] = sols[i].first;
+        c[i] = sols[i].second;
+    }
+    BCK(cudaMemcpyAsync(d_q, q.data(), ns * 4, cudaMemcpyHostToDevice, b.st));
+    BCK(cudaMemcpyAsync(d_c, c.data(), ns * 2, cudaMemcpyHostToDevice, b.st));
+    k_bpath<<<(ns + 127) / 128, 128, 0, b.st>>>(L, K, d_q, d_c, ns, d_out);
+    int rc = blaunch(b);
+    if (rc) return rc;
+    std::vector<uint32_t> out((size_t)ns * K);
+    BCK(cudaMemcpyAsync(out.data(), d_out, out.size() * 4, cudaMemcpyDeviceToHost, b.st));
+    BCK(cudaStreamSynchronize(b.st));
+    b.h2d += ns * 6;
+    b.d2h += out.size() * 4;
+    for (int i = 0; i < ns; i++) {
+        std::vector<uint16_t> kern(K);
+        for (int d = 0; d < K; d++) {
+            const uint32_t w = out[(size_t)i * K + d];
+            /* position d of a depth-K kernel: forward offsets up to K-d-1 */
+            BTab ht{bt.pre_off.data(), bt.post_off.data(), bt.pre.data(), bt.post.data(), K - d - 1};
+            kern[d] = bcand(ht, ((w >> 16) >> 1) & 127u, w & 0xFFFFu);
+        }
+        kernels->push_back(std::move(kern));
+    }
+    return PCAGB_OK;
+}
+
 /* The last position of a depth-K pass without building level K: solving
  * children from k_bsuffix; a child counts only if it is the depth-first
  * first of its key (the pruner would have dropped it otherwise), the
  * smallest child index among k_bsuffix's records with that key, checked by
- * full compares. Returns the number of solutions found (0 = none at this
- * depth). */
+ * full compares. With first_only the parents are visited in depth-first
+ * order in launches of 1/64 of them, doubling, and the search stops at the
+ * first launch whose records hold a solution: every child of an earlier
+ * launch is earlier in depth-first order, so the records gathered so far
+ * settle the first of every key met. Returns the number of solutions found
+ * (0 = none at this depth); *searched gets the children of the parents
+ * visited. */
 int64_t branch_suffix(BranchRun &b, const BranchTables &bt, std::vector<BLevel> &lv, int K,
                       const task_spec_t *task, pcagb_result_t *res, uint16_t *sol_progs,
-                      int *sol_lens, int cap)
+                      int *sol_lens, int cap, bool first_only, uint64_t *searched)
 {
     BLevel &P = lv[K - 1];
     const BTab tab = b.tab(0);
@@ -833,121 +922,138 @@ int64_t branch_suffix(BranchRun &b, const BranchTables &bt, std::vector<BLevel> 
     BSol *d_sol = b.alloc<BSol>(kCap);
     unsigned long long *d_cnt = b.alloc<unsigned long long>(1);
     if (!d_sol || !d_cnt) { set_berr("device memory exhausted"); return PCAGB_ENOMEM; }
-    BCK(cudaMemsetAsync(d_cnt, 0, 8, b.st));
-    if (b.TP == 16)
-        k_bsuffix<16><<<b.grid(4), kBThreads, 0, b.st>>>(bdev(P), tab, b.T, p, b.d_target, d_sol, d_cnt, kCap);
-    else
-        k_bsuffix<32><<<b.grid(4), kBThreads, 0, b.st>>>(bdev(P), tab, b.T, p, b.d_target, d_sol, d_cnt, kCap);
-    int rc = blaunch(b);
-    if (rc) return rc;
-    unsigned long long cnt = 0;
-    BCK(cudaMemcpyAsync(&cnt, d_cnt, 8, cudaMemcpyDeviceToHost, b.st));
-    BCK(cudaStreamSynchronize(b.st));
-    if (cnt > kCap) {
-        set_berr("%llu solving children at depth %d: more than the last-position buffer holds",
-                 (unsigned long long)cnt, K);
-        return PCAGB_ELIMIT;
-    }
-    if (cnt == 0) return 0;
-    std::vector<BSol> sol(cnt);
-    BCK(cudaMemcpyAsync(sol.data(), d_sol, cnt * sizeof(BSol), cudaMemcpyDeviceToHost, b.st));
-    BCK(cudaStreamSynchronize(b.st));
-    b.d2h += cnt * sizeof(BSol) + 8;
-    /* the depth-first first child of every solving key: the smallest L
-       among the records with that key (every child equal to a solving one
-       is a record) */
-    std::unordered_map<uint64_t, size_t> first;
-    first.reserve(cnt * 2);
-    for (size_t i = 0; i < cnt; i++) {
-        auto it = first.find(sol[i].key);
-        if (it == first.end()) first.emplace(sol[i].key, i);
-        else if (sol[i].L < sol[it->second].L) it->second = i;
-    }
-    /* a solving child that is not the first of its key is dropped when the
-       first is equal to it in full (a 64-bit key collision would stop here) */
-    std::vector<uint4> pairs;
-    std::vector<size_t> pair_of;
-    std::vector<uint8_t> keep(cnt, 0);
-    for (size_t i = 0; i < cnt; i++) {
-        if (!sol[i].mask) continue;
-        keep[i] = 1;
-        const size_t f = first[sol[i].key];
-        if (f == i) continue;
-        pairs.push_back(make_uint4(sol[i].q, sol[i].c, sol[f].q, sol[f].c));
-        pair_of.push_back(i);
-    }
-    if (!pairs.empty()) {
-        uint4 *d_pairs = b.alloc<uint4>(pairs.size());
-        uint8_t *d_eq = b.alloc<uint8_t>(pairs.size());
-        if (!d_pairs || !d_eq) { set_berr("device memory exhausted"); return PCAGB_ENOMEM; }
-        BCK(cudaMemcpyAsync(d_pairs, pairs.data(), pairs.size() * sizeof(uint4), cudaMemcpyHostToDevice, b.st));
-        b.h2d += pairs.size() * sizeof(uint4);
+    std::vector<BSol> sol;
+    std::vector<size_t> idx;   /* kept solving records, depth-first order */
+    uint64_t q0 = 0, step = first_only ? std::max<uint64_t>(P.n / 64, 1) : P.n;
+    *searched = 0;
+    while (q0 < P.n) {
+        const uint64_t q1 = std::min(P.n, q0 + step);
+        BCK(cudaMemsetAsync(d_cnt, 0, 8, b.st));
         if (b.TP == 16)
-            k_bpairs_equal<16><<<b.grid(2), 256, 0, b.st>>>(bdev(P), tab, b.T, p, d_pairs, pairs.size(), d_eq);
+            k_bsuffix<16><<<b.grid(4), kBThreads, 0, b.st>>>(bdev(P), tab, b.T, p, b.d_target,
+                                                             d_sol, d_cnt, kCap, q0, q1);
         else
-            k_bpairs_equal<32><<<b.grid(2), 256, 0, b.st>>>(bdev(P), tab, b.T, p, d_pairs, pairs.size(), d_eq);
-        rc = blaunch(b);
+            k_bsuffix<32><<<b.grid(4), kBThreads, 0, b.st>>>(bdev(P), tab, b.T, p, b.d_target,
+                                                             d_sol, d_cnt, kCap, q0, q1);
+        int rc = blaunch(b);
         if (rc) return rc;
-        std::vector<uint8_t> eq(pairs.size());
-        BCK(cudaMemcpyAsync(eq.data(), d_eq, pairs.size(), cudaMemcpyDeviceToHost, b.st));
+        unsigned long long cnt = 0;
+        uint64_t off_end = 0;
+        BCK(cudaMemcpyAsync(&cnt, d_cnt, 8, cudaMemcpyDeviceToHost, b.st));
+        BCK(cudaMemcpyAsync(&off_end, P.child_off + q1, 8, cudaMemcpyDeviceToHost, b.st));
         BCK(cudaStreamSynchronize(b.st));
-        b.d2h += pairs.size();
-        for (size_t j = 0; j < pairs.size(); j++) {
-            if (!eq[j]) {
-                set_berr("64-bit key collision between distinct children at depth %d", K);
-                return PCAGB_ELIMIT;
-            }
-            keep[pair_of[j]] = 0;
+        b.d2h += 16;
+        *searched = off_end;
+        if (cnt > kCap) {
+            set_berr("%llu solving children at depth %d: more than the last-position buffer holds",
+                     (unsigned long long)cnt, K);
+            return PCAGB_ELIMIT;
         }
+        q0 = q1;
+        step *= 2;
+        if (cnt == 0) continue;
+        const size_t base = sol.size();
+        sol.resize(base + cnt);
+        BCK(cudaMemcpyAsync(sol.data() + base, d_sol, cnt * sizeof(BSol), cudaMemcpyDeviceToHost,
+                            b.st));
+        BCK(cudaStreamSynchronize(b.st));
+        b.d2h += cnt * sizeof(BSol);
+        bool any = false;
+        for (size_t i = base; i < sol.size(); i++) any |= sol[i].mask != 0;
+        if (!any) continue;
+        /* the depth-first first child of every solving key: the smallest L
+           among the records with that key (every child equal to a solving
+           one is a record, and no later launch holds a smaller L) */
+        std::unordered_map<uint64_t, size_t> first;
+        first.reserve(sol.size() * 2);
+        for (size_t i = 0; i < sol.size(); i++) {
+            auto it = first.find(sol[i].key);
+            if (it == first.end()) first.emplace(sol[i].key, i);
+            else if (sol[i].L < sol[it->second].L) it->second = i;
+        }
+        /* a solving child that is not the first of its key is dropped when
+           the first is equal to it in full (a 64-bit key collision stops
+           here) */
+        std::vector<uint4> pairs;
+        std::vector<size_t> pair_of;
+        std::vector<uint8_t> keep(sol.size(), 0);
+        for (size_t i = 0; i < sol.size(); i++) {
+            if (!sol[i].mask) continue;
+            keep[i] = 1;
+            const size_t f = first[sol[i].key];
+            if (f == i) continue;
+            pairs.push_back(make_uint4(sol[i].q, sol[i].c, sol[f].q, sol[f].c));
+            pair_of.push_back(i);
+        }
+        if (!pairs.empty()) {
+            uint4 *d_pairs = b.alloc<uint4>(pairs.size());
+            uint8_t *d_eq = b.alloc<uint8_t>(pairs.size());
+            if (!d_pairs || !d_eq) { set_berr("device memory exhausted"); return PCAGB_ENOMEM; }
+            BCK(cudaMemcpyAsync(d_pairs, pairs.data(), pairs.size() * sizeof(uint4),
+                                cudaMemcpyHostToDevice, b.st));
+            b.h2d += pairs.size() * sizeof(uint4);
+            if (b.TP == 16)
+                k_bpairs_equal<16><<<b.grid(2), 256, 0, b.st>>>(bdev(P), tab, b.T, p, d_pairs,
+                                                                pairs.size(), d_eq);
+            else
+                k_bpairs_equal<32><<<b.grid(2), 256, 0, b.st>>>(bdev(P), tab, b.T, p, d_pairs,
+                                                                pairs.size(), d_eq);
+            rc = blaunch(b);
+            if (rc) return rc;
+            std::vector<uint8_t> eq(pairs.size());
+            BCK(cudaMemcpyAsync(eq.data(), d_eq, pairs.size(), cudaMemcpyDeviceToHost, b.st));
+            BCK(cudaStreamSynchronize(b.st));
+            b.d2h += pairs.size();
+            for (size_t j = 0; j < pairs.size(); j++) {
+                if (!eq[j]) {
+                    set_berr("64-bit key collision between distinct children at depth %d", K);
+                    return PCAGB_ELIMIT;
+                }
+                keep[pair_of[j]] = 0;
+            }
+        }
+        idx.clear();
+        for (size_t i = 0; i < sol.size(); i++)
+            if (keep[i]) idx.push_back(i);
+        if (!idx.empty() && first_only) break;
     }
-    std::vector<std::pair<uint64_t, int>> order;  /* (L, register) in depth-first order */
-    std::vector<size_t> idx;
-    for (size_t i = 0; i < cnt; i++)
-        if (keep[i]) idx.push_back(i);
+    if (idx.empty()) return 0;
     std::sort(idx.begin(), idx.end(), [&](size_t a, size_t c) { return sol[a].L < sol[c].L; });
-    uint64_t found = 0;
-    for (size_t i : idx) found += __builtin_popcount(sol[i].mask);
-    if (found == 0) return 0;
-    /* programs: prefix links of levels 1..K-1, then the last candidate */
-    std::vector<HostLevel> H(K);
-    for (int d = 0; d < K; d++) {
-        rc = fetch_links(b, lv[d], H[d], d > 0);
-        if (rc) return rc;
-    }
-    /* the reference's walk stops at the leaf that brings its count to 100 */
-    int stored = 0;
+    /* the reference's walk stops at the leaf that brings its count to 100:
+       the (state, register) pairs listed, and the programs of the first cap */
+    std::vector<std::pair<uint32_t, uint16_t>> want;
+    std::vector<int> want_reg;
     uint64_t listed = 0;
     for (size_t i : idx) {
         for (int r = 1; r < 8; r++) {
             if (!(sol[i].mask >> r & 1u)) continue;
             listed++;
-            if (stored >= cap || !sol_progs) continue;
-            std::vector<uint16_t> kern(K);
-            BTab last{bt.pre_off.data(), bt.post_off.data(), bt.pre.data(), bt.post.data(), 0};
-            kern[K - 1] = bcand(last, (H[K - 1].live[sol[i].q] >> 1) & 127u, sol[i].c);
-            uint64_t s = sol[i].q;
-            for (int d = K - 1; d >= 1; d--) {
-                const uint32_t par = H[d].parent[s];
-                BTab ht{bt.pre_off.data(), bt.post_off.data(), bt.pre.data(), bt.post.data(), K - d};
-                kern[d - 1] = bcand(ht, (H[d - 1].live[par] >> 1) & 127u, H[d].cidx[s]);
-                s = par;
+            if ((int)want.size() < cap && sol_progs) {
+                want.emplace_back(sol[i].q, sol[i].c);
+                want_reg.push_back(r);
             }
-            uint16_t prog[16] = {0};
-            int n = 0;
-            for (int q = 0; q < task->num_inputs; q++)
-                prog[n++] = (uint16_t)PCA_ENC_I(PCA_OP_IN, q + 1, task->input_ports[q]);
-            for (uint16_t w : kern) prog[n++] = w;
-            prog[n++] = (uint16_t)PCA_ENC_I(PCA_OP_OUT, r, task->output_ports[0]);
-            prog[n++] = (uint16_t)PCA_ENC_R(PCA_OP_HLT, 0, 0, 0);
-            if (task_evaluate(task, prog, n) != task->num_tests) {
-                set_berr("internal: a branch-mode solution failed the VM re-check");
-                return PCAGB_ELIMIT;
-            }
-            memcpy(sol_progs + (size_t)stored * 16, prog, sizeof prog);
-            if (sol_lens) sol_lens[stored] = n;
-            stored++;
         }
         if (listed >= 100) break;
+    }
+    std::vector<std::vector<uint16_t>> kerns;
+    int rc = solution_kernels(b, bt, lv, K, want, &kerns);
+    if (rc) return rc;
+    int stored = 0;
+    for (size_t j = 0; j < kerns.size(); j++) {
+        uint16_t prog[16] = {0};
+        int n = 0;
+        for (int q = 0; q < task->num_inputs; q++)
+            prog[n++] = (uint16_t)PCA_ENC_I(PCA_OP_IN, q + 1, task->input_ports[q]);
+        for (uint16_t w : kerns[j]) prog[n++] = w;
+        prog[n++] = (uint16_t)PCA_ENC_I(PCA_OP_OUT, want_reg[j], task->output_ports[0]);
+        prog[n++] = (uint16_t)PCA_ENC_R(PCA_OP_HLT, 0, 0, 0);
+        if (task_evaluate(task, prog, n) != task->num_tests) {
+            set_berr("internal: a branch-mode solution failed the VM re-check");
+            return PCAGB_ELIMIT;
+        }
+        memcpy(sol_progs + (size_t)stored * 16, prog, sizeof prog);
+        if (sol_lens) sol_lens[stored] = n;
+        stored++;
     }
     res->stored = stored;
     res->total_solutions = listed;
@@ -971,9 +1077,16 @@ int pcagb_solve_branch(pcagb_engine_t *e, const task_spec_t *task, int max_depth
                                  sol_cap);
 }
 
-int pcagb_solve_branch_ex(pcagb_engine_t *e, const task_spec_t *task, int max_depth,
-                          uint64_t last_level_max_children, pcagb_result_t *res,
-                          uint16_t *sol_progs, int *sol_lens, int sol_cap)
+}  // extern "C"
+
+namespace {
+
+/* Branch-mode IDDFS. first_only: the last position of every depth is
+   searched without its level, in depth-first launches that stop at the
+   first holding a solution (branch_suffix). */
+int solve_branch(pcagb_engine_t *e, const task_spec_t *task, int max_depth,
+                 uint64_t last_level_max_children, bool first_only, pcagb_result_t *res,
+                 uint16_t *sol_progs, int *sol_lens, int sol_cap)
 {
     if (!e || !task || !res) { set_berr("null argument"); return PCAGB_EINVAL; }
     memset(res, 0, sizeof *res);
@@ -1049,7 +1162,7 @@ int pcagb_solve_branch_ex(pcagb_engine_t *e, const task_spec_t *task, int max_de
             if (d == K - 1) {
                 int rc = count_bchildren(b, lv[d], mf);
                 if (rc) return rc;
-                if (lv[d].children > last_level_max_children) {
+                if (first_only || lv[d].children > last_level_max_children) {
                     unbuilt_last = true;
                     break;
                 }
@@ -1068,8 +1181,14 @@ int pcagb_solve_branch_ex(pcagb_engine_t *e, const task_spec_t *task, int max_de
             res->pruned_cum[K] = pruned_cum + pruned;
             res->candidates[K] = res->tried[K];
             res->level_children[K] = lv[K - 1].children;
-            const int64_t got = branch_suffix(b, bt, lv, K, task, res, sol_progs, sol_lens, cap);
+            uint64_t searched = 0;
+            const int64_t got = branch_suffix(b, bt, lv, K, task, res, sol_progs, sol_lens, cap,
+                                              first_only, &searched);
             if (got < 0) return (int)got;
+            if (first_only) {
+                res->tried[K] = tried + searched;
+                res->candidates[K] = res->tried[K];
+            }
             pruned_cum += pruned;
             if (got > 0) {
                 res->optimal_depth = K;
@@ -1193,6 +1312,24 @@ int pcagb_solve_branch_ex(pcagb_engine_t *e, const task_spec_t *task, int max_de
     res->h2d_bytes = b.h2d;
     res->d2h_bytes = b.d2h;
     return PCAGB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pcagb_solve_branch_ex(pcagb_engine_t *e, const task_spec_t *task, int max_depth,
+                          uint64_t last_level_max_children, pcagb_result_t *res,
+                          uint16_t *sol_progs, int *sol_lens, int sol_cap)
+{
+    return solve_branch(e, task, max_depth, last_level_max_children, false, res, sol_progs,
+                        sol_lens, sol_cap);
+}
+
+int pcagb_solve_branch_first(pcagb_engine_t *e, const task_spec_t *task, int max_depth,
+                             pcagb_result_t *res, uint16_t *sol_progs, int *sol_lens, int sol_cap)
+{
+    return solve_branch(e, task, max_depth, 0, true, res, sol_progs, sol_lens, sol_cap);
 }
 
 }  // extern "C"

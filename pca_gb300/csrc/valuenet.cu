@@ -190,6 +190,45 @@ __global__ void k_to_bf16(const float *src, __nv_bfloat16 *dst, size_t count)
         dst[i] = __float2bfloat16(src[i]);
 }
 
+/* Column sums of a bf16 [rows][cols] matrix (leading dimension ld, both
+   multiples of 8) added into out[cols] (fp32): a thread per 8 columns and
+   row slot (16-byte loads, fp32 sums in registers), the 8 row slots of a
+   block reduced in shared memory, one atomic add per column and block. */
+__global__ void __launch_bounds__(256) k_colsum(const __nv_bfloat16 *Y, long long rows, int cols,
+                                               int ld, float *out)
+{
+    __shared__ float part[8][32][8];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    for (int g0 = 0; g0 < cols / 8; g0 += 32) {
+        const int g = g0 + tx;
+        float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        if (g < cols / 8) {
+            for (long long r = (long long)blockIdx.x * 8 + ty; r < rows; r += (long long)gridDim.x * 8) {
+                const uint4 w = *(const uint4 *)(Y + r * ld + g * 8);
+                const __nv_bfloat162 *h = (const __nv_bfloat162 *)&w;
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const float2 f = __bfloat1622float2(h[j]);
+                    acc[2 * j] += f.x;
+                    acc[2 * j + 1] += f.y;
+                }
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < 8; j++) part[ty][tx][j] = acc[j];
+        __syncthreads();
+        if (ty == 0 && g < cols / 8) {
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                float v = 0;
+                for (int y = 0; y < 8; y++) v += part[y][tx][j];
+                atomicAdd(&out[g * 8 + j], v);
+            }
+        }
+        __syncthreads();
+    }
+}
+
 int launch_ok()
 {
     return cudaGetLastError() == cudaSuccess ? PCAGB_OK : PCAGB_ECUDA;
@@ -248,6 +287,20 @@ __global__ void k_compose_order(const SampleSrc *src, const long long *ranked, i
 }
 
 extern "C" {
+
+/* out[c] += sum over rows of Y[r][c] (the bias gradient of a layer from
+   its output gradient). cols and ld multiples of 8, Y 16-byte aligned. */
+int pcagb_vnet_colsum(const void *Y, long long rows, int cols, int ld, float *out, int sms,
+                      void *stream)
+{
+    if (rows <= 0 || cols <= 0) return PCAGB_OK;
+    if (!Y || !out || (cols & 7) || (ld & 7) || ld < cols || ((uintptr_t)Y & 15))
+        return PCAGB_EINVAL;
+    const long long blocks = std::min<long long>((rows + 7) / 8, (long long)std::max(sms, 1) * 8);
+    k_colsum<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>((const __nv_bfloat16 *)Y, rows,
+                                                                 cols, ld, out);
+    return launch_ok();
+}
 
 int pcagb_vnet_gather_sample(const void *src, uint16_t *regs, uint8_t *flags, uint8_t *live,
                              uint16_t *task, uint8_t *depth, int m, int TP, void *stream)

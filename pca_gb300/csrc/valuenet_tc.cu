@@ -171,6 +171,20 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr)
     return d;
 }
 
+/* Shared-memory matrix descriptor: MN-major operand in 128-byte swizzle
+   atoms (8 K-rows x 128 B = 64 elements along M or N), 8-row groups 1024 B
+   apart along K, 64-element groups along M or N 8 KB apart (one 64 x 64
+   TMA box each). */
+__device__ __forceinline__ uint64_t sw128_mn_desc(uint32_t saddr)
+{
+    uint64_t d = (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)(8192 >> 4) << 16;  /* leading byte offset: next 64 along M/N */
+    d |= (uint64_t)(1024 >> 4) << 32;  /* stride byte offset: next 8 along K */
+    d |= (uint64_t)1 << 46;            /* descriptor version */
+    d |= (uint64_t)2 << 61;            /* 128-byte swizzle */
+    return d;
+}
+
 __device__ __forceinline__ void mma_f16(uint32_t dtmem, uint64_t a, uint64_t b, uint32_t acc)
 {
     asm volatile(
@@ -525,7 +539,13 @@ k_encode_pool_tc(const __grid_constant__ CUtensorMap map_w1, const __grid_consta
  * Every wait is bounded by the global timer; a wait that runs out sets the
  * abort flag and *status, each role leaves, and TMEM is freed. Two CTAs fit
  * an SM (96 KB of shared memory at bn = 256), so one CTA's epilogue overlaps
- * the other's loads and MMAs. */
+ * the other's loads and MMAs.
+ *
+ * mn_major: A and B are given K-row by K-row instead ([K][M] and [K][N],
+ * M and N contiguous: the weight gradient dY^T . X reads dY [batch][out]
+ * and X [batch][in] as stored), loaded as 64 x 64 boxes (64 K-rows of 64
+ * elements along M or N) and described to the MMA as MN-major operands;
+ * bn is then a multiple of 64. */
 constexpr int kGRows = 128, kGBK = 64, kGStages = 2;
 constexpr int kGABytes = kGRows * 128;              /* 16 KB per A stage */
 
@@ -534,7 +554,7 @@ k_gemm_tc(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUt
           const float *__restrict__ bias, const __nv_bfloat16 *__restrict__ mask, int ldm,
           __nv_bfloat16 *__restrict__ Cb, float *__restrict__ Cf, int ldc, int M, int N,
           int kblocks, int kb_per_split, int bn, uint32_t idesc, uint32_t tmem_cols, int relu,
-          int atomic_out, int stage_mode, int vec_atomic, int *status)
+          int atomic_out, int stage_mode, int vec_atomic, int mn_major, int *status)
 {
     extern __shared__ uint8_t gsmem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)gsmem_raw + 1023) & ~(uintptr_t)1023);
@@ -584,8 +604,16 @@ k_gemm_tc(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUt
             if (!mbar_wait(empty(st), ph ^ 1u, abort_flag, status, 11)) break;
             mbar_expect_tx(full(st), kGABytes + b_bytes);
             const int x = (kb0 + i) * kGBK;
-            tma_load_2d(sA + st * kGABytes, &map_a, full(st), x, m0);
-            tma_load_2d(sB + st * b_bytes, &map_b, full(st), x, n0);
+            if (mn_major) {
+                /* boxes of 64 K-rows x 64 columns, 8 KB each */
+                for (int h = 0; h < kGRows / 64; h++)
+                    tma_load_2d(sA + st * kGABytes + h * 8192, &map_a, full(st), m0 + 64 * h, x);
+                for (int h = 0; h < bn / 64; h++)
+                    tma_load_2d(sB + st * b_bytes + h * 8192, &map_b, full(st), n0 + 64 * h, x);
+            } else {
+                tma_load_2d(sA + st * kGABytes, &map_a, full(st), x, m0);
+                tma_load_2d(sB + st * b_bytes, &map_b, full(st), x, n0);
+            }
         }
         /* the copies this thread issued land before the CTA leaves */
         for (int j = i - 1; j >= 0 && j >= i - kGStages; j--) {
@@ -604,7 +632,10 @@ k_gemm_tc(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUt
             const uint32_t a0 = sA + st * kGABytes, b0 = sB + st * b_bytes;
 #pragma unroll
             for (int k = 0; k < 4; k++) {
-                const uint64_t da = sw128_desc(a0 + 32 * k), db = sw128_desc(b0 + 32 * k);
+                /* 16 K per MMA: 32 bytes along a K-major row, or two 8-row
+                   groups (2 KB) of an MN-major box */
+                const uint64_t da = mn_major ? sw128_mn_desc(a0 + 2048 * k) : sw128_desc(a0 + 32 * k);
+                const uint64_t db = mn_major ? sw128_mn_desc(b0 + 2048 * k) : sw128_desc(b0 + 32 * k);
                 const uint32_t acc = (i | k) != 0;
                 asm volatile(
                     "{\n\t.reg .pred p;\n\t"
@@ -788,50 +819,6 @@ k_gemm_tc(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUt
                      : "memory");
 }
 
-/* T[c][r] = S[r][c] for c < C; row C of T is ones when `ones` (the bias
-   column of an augmented operand), rows up to Cp zeros. 64 x 64 tiles
-   through shared memory, 256 threads: each reads and writes pairs of bf16
-   (4 bytes), so a warp moves 128 contiguous bytes per row on both sides. */
-__global__ void __launch_bounds__(256)
-k_transpose_aug(const __nv_bfloat16 *__restrict__ S, int R, int C, int lds,
-                __nv_bfloat16 *__restrict__ T, int Cp, int ldt, int ones)
-{
-    __shared__ uint16_t tile[64][66];
-    const int r0 = blockIdx.x * 64, c0 = blockIdx.y * 64;
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;   /* 32 x 8 */
-    const uint16_t *src = reinterpret_cast<const uint16_t *>(S);
-    const uint16_t one = 0x3F80u;                               /* bf16 1.0 */
-    for (int k = ty; k < 64; k += 8) {
-        const int r = r0 + k;
-        uint16_t a = 0, b = 0;
-#pragma unroll
-        for (int h = 0; h < 2; h++) {
-            const int c = c0 + 2 * tx + h;
-            uint16_t v = 0;
-            if (r < R) {
-                if (c < C) v = src[(size_t)r * lds + c];
-                else if (c == C && ones) v = one;
-            }
-            if (h) b = v; else a = v;
-        }
-        tile[k][2 * tx] = a;
-        tile[k][2 * tx + 1] = b;
-    }
-    __syncthreads();
-    uint16_t *dst = reinterpret_cast<uint16_t *>(T);
-    for (int k = ty; k < 64; k += 8) {
-        const int c = c0 + k;
-        if (c >= Cp) continue;
-        const int r = r0 + 2 * tx;
-        if (r + 1 < R && !(((size_t)c * ldt + r) & 1)) {
-            const uint32_t pr = (uint32_t)tile[2 * tx][k] | ((uint32_t)tile[2 * tx + 1][k] << 16);
-            *reinterpret_cast<uint32_t *>(dst + (size_t)c * ldt + r) = pr;
-        } else {
-            if (r < R) dst[(size_t)c * ldt + r] = tile[2 * tx][k];
-            if (r + 1 < R) dst[(size_t)c * ldt + r + 1] = tile[2 * tx + 1][k];
-        }
-    }
-}
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
                                   const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
@@ -938,22 +925,67 @@ extern "C" int pcagb_vnet_gemm_tc(const void *A, int lda, const void *B, int ldb
     dim3 grid((N + bn - 1) / bn, (M + kGRows - 1) / kGRows, splits);
     k_gemm_tc<<<grid, 128, smem, (cudaStream_t)stream>>>(
         ma, mb, bias, (const __nv_bfloat16 *)mask, ldm, (__nv_bfloat16 *)Cb, Cf, ldc, M, N,
-        kblocks, per, bn, idesc, tcols, relu, splits > 1, stage_mode, vec_atomic, status);
+        kblocks, per, bn, idesc, tcols, relu, splits > 1, stage_mode, vec_atomic, 0, status);
     return cudaGetLastError() == cudaSuccess ? PCAGB_OK : PCAGB_ECUDA;
 }
 
-/* T[Cp][ldt] from S[R][lds]: T[c][r] = S[r][c] for c < C, row C ones when
- * `ones` (else zeros), rows C+1..Cp-1 zeros. */
-extern "C" int pcagb_vnet_transpose_aug(const void *S, int R, int C, int lds, void *T, int Cp,
-                                        int ldt, int ones, void *stream)
+/* Tensor map of a [krows][cols] bf16 matrix (row stride ld elements) read
+   as an MN-major operand: boxes of 64 columns x 64 rows, 128-byte swizzle. */
+bool tile_map_mn(CUtensorMap *m, const void *ptr, int krows, int cols, int ld)
 {
-    if (R <= 0 || Cp <= 0) return PCAGB_OK;
-    if (!S || !T || Cp < C || ldt < R) return PCAGB_EINVAL;
-    dim3 grid((R + 63) / 64, (Cp + 63) / 64);
-    k_transpose_aug<<<grid, 256, 0, (cudaStream_t)stream>>>(
-        (const __nv_bfloat16 *)S, R, C, lds, (__nv_bfloat16 *)T, Cp, ldt, ones);
+    EncodeTiledFn fn = encode_fn();
+    if (!fn) return false;
+    cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)krows};
+    cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
+    cuuint32_t box[2] = {64, 64};
+    cuuint32_t estr[2] = {1, 1};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(ptr), dims, strides, box,
+              estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+              CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+/* Weight gradient on tcgen05 without transposes: C[M][N] += dY^T . X over
+ * K rows, dY [K][M] (leading dimension ldy) and X [K][N] (ldx) read as
+ * stored (MN-major operands), fp32 partial sums of `splits` K ranges added
+ * into C (zeroed by the caller, leading dimension ldc). ldy and ldx are
+ * multiples of 8 elements, dY and X 16-byte aligned. */
+extern "C" int pcagb_vnet_wgrad_tc(const void *dY, int ldy, const void *X, int ldx, float *C,
+                                   int ldc, int M, int N, int K, int splits, int *status,
+                                   void *stream)
+{
+    if (M <= 0 || N <= 0 || K <= 0) return PCAGB_OK;
+    if (!dY || !X || !C || !status || (ldy & 7) || (ldx & 7) || ldy < M || ldx < N ||
+        ldc < N || ((uintptr_t)dY & 15) || ((uintptr_t)X & 15) || splits < 1)
+        return PCAGB_EINVAL;
+    const int bn = N > 192 ? 256 : (N + 63) / 64 * 64;
+    uint32_t tcols = 32;
+    while (tcols < (uint32_t)bn) tcols <<= 1;
+    CUtensorMap ma, mb;
+    if (!tile_map_mn(&ma, dY, K, M, ldy) || !tile_map_mn(&mb, X, K, N, ldx)) return PCAGB_ECUDA;
+    const int kblocks = (K + kGBK - 1) / kGBK;
+    if (splits > kblocks) splits = kblocks;
+    const int per = (kblocks + splits - 1) / splits;
+    splits = (kblocks + per - 1) / per;
+    /* bits 15 and 16: A and B MN-major */
+    const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | (1u << 15) | (1u << 16) |
+                           ((uint32_t)(bn >> 3) << 17) | ((uint32_t)(kGRows >> 4) << 24);
+    const int smem = kGStages * (kGABytes + bn * 128) + 256 + 1024 + 1024;
+    static std::once_flag attr_once;
+    static cudaError_t attr_err = cudaSuccess;
+    std::call_once(attr_once, [] {
+        attr_err = cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        kGStages * (kGABytes + 256 * 128) + 256 + 2048);
+    });
+    if (attr_err != cudaSuccess) return PCAGB_ECUDA;
+    const int vec_atomic = ldc % 4 == 0 && !((uintptr_t)C & 15);
+    dim3 grid((N + bn - 1) / bn, (M + kGRows - 1) / kGRows, splits);
+    k_gemm_tc<<<grid, 128, smem, (cudaStream_t)stream>>>(
+        ma, mb, nullptr, nullptr, 0, nullptr, C, ldc, M, N, kblocks, per, bn, idesc, tcols, 0, 1,
+        0, vec_atomic, 1, status);
     return cudaGetLastError() == cudaSuccess ? PCAGB_OK : PCAGB_ECUDA;
 }
+
 
 extern "C" int pcagb_vnet_encode_pool_tc(const void *W1, const float *b1, const void *W2,
                                          const float *b2, const uint16_t *regs,

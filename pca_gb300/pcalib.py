@@ -158,7 +158,7 @@ EXPORTS = [
     "pcagb_last_error", "pcagb_default_opts", "pcagb_engine_create", "pcagb_engine_destroy",
     "pcagb_solve", "pcagb_solve_batch", "pcagb_solve_batch_cb", "pcagb_solve_ordered",
     "pcagb_complete", "pcagb_record", "pcagb_solve_branch", "pcagb_solve_branch_ex",
-    "pcagb_branch_last_error",
+    "pcagb_solve_branch_first", "pcagb_branch_last_error",
     "pcagb_num_candidates",
     "pcagb_engine_stream", "pcagb_tuning", "pcagb_device_memory",
     "pcagb_server_default_config", "pcagb_server_create", "pcagb_server_submit",
@@ -213,6 +213,9 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
         "pcagb_solve_branch_ex": ([ctypes.c_void_p, P(TaskSpec), ctypes.c_int, ctypes.c_uint64,
                                    P(SolveResult), P(ctypes.c_uint16), P(ctypes.c_int), ctypes.c_int],
                                   ctypes.c_int),
+        "pcagb_solve_branch_first": ([ctypes.c_void_p, P(TaskSpec), ctypes.c_int, P(SolveResult),
+                                      P(ctypes.c_uint16), P(ctypes.c_int), ctypes.c_int],
+                                     ctypes.c_int),
         "pcagb_branch_last_error": ([], ctypes.c_char_p),
         "pcagb_num_candidates": ([ctypes.c_uint8], ctypes.c_int),
         "pcagb_engine_stream": ([ctypes.c_void_p], ctypes.c_void_p),
@@ -598,16 +601,22 @@ class Engine:
         return self.lib.pcagb_engine_stream(self.h) or 0
 
     def solve_branch(self, task: TaskSpec, max_depth: int = 4, sol_cap: int = 100,
-                     last_level_max_children: int | None = None) -> Solution:
+                     last_level_max_children: int | None = None,
+                     first_only: bool = False) -> Solution:
         """Branch mode (CMP / forward BR / DIV / MOD): the reference solver's
         default search, with its per-depth counters and its first programs.
         last_level_max_children: above it a depth's last level is not built
-        (None = the library's default)."""
+        (None = the library's default). first_only: the reference hybrid
+        solver's stopping rule (the optimal depth's search ends at the first
+        launch with a solution; the same optimal depth and first programs)."""
         r = SolveResult()
         cap = max(sol_cap, 1)
         progs = (ctypes.c_uint16 * (16 * cap))()
         lens = (ctypes.c_int * cap)()
-        if last_level_max_children is None:
+        if first_only:
+            rc = self.lib.pcagb_solve_branch_first(self.h, ctypes.byref(task), max_depth,
+                                                   ctypes.byref(r), progs, lens, cap)
+        elif last_level_max_children is None:
             rc = self.lib.pcagb_solve_branch(self.h, ctypes.byref(task), max_depth,
                                              ctypes.byref(r), progs, lens, cap)
         else:

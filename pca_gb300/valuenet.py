@@ -38,7 +38,8 @@ def _lib():
     sz = ctypes.c_size_t
     sigs = {
         "pcagb_vnet_gemm_tc": [vp, i, vp, i, vp, vp, i, vp, vp, i, i, i, i, i, i, vp, vp],
-        "pcagb_vnet_transpose_aug": [vp, i, i, i, vp, i, i, i, vp],
+        "pcagb_vnet_wgrad_tc": [vp, i, vp, i, vp, i, i, i, i, i, vp, vp],
+        "pcagb_vnet_colsum": [vp, ctypes.c_longlong, i, i, vp, i, vp],
         "pcagb_vnet_features": [vp, vp, vp, i, i, vp, vp, vp, vp],
         "pcagb_vnet_pool": [vp, vp, vp, vp, vp, i, vp, vp, vp],
         "pcagb_vnet_pool_bwd": [vp, vp, vp, vp, vp, i, vp, vp],
@@ -131,33 +132,24 @@ class ValueNet:
             self.stream))
         return C
 
-    def _transpose_aug(self, S, ones):
-        """S[R][C] -> T[Cp][R]: S transposed, with a row of ones at C when
-        `ones` (the bias column of the weight gradient), padded to 16 rows."""
-        R, C = S.shape
-        Cp = (C + (1 if ones else 0) + 15) // 16 * 16
-        ld = (R + 7) // 8 * 8          # a TMA row stride is a multiple of 16 bytes
-        T = torch.empty(Cp, ld, device=self.dev, dtype=torch.bfloat16)
-        self._ck(self.lib.pcagb_vnet_transpose_aug(_p(S), R, C, S.stride(0), _p(T), Cp, ld,
-                                                   int(ones), self.stream))
-        return T
-
     def _wgrad(self, dY, X, name):
-        """dW = dY^T . X and db = column sums of dY in one split-K tcgen05
-        GEMM: dY^T [out][M] times [X | 1]^T [in + 1 (padded)][M]."""
+        """dW = dY^T . X as one split-K tcgen05 GEMM reading dY [M][out] and
+        X [M][in] as stored (MN-major operands, no transposes), and db =
+        the column sums of dY."""
         out, inp = self.W[name].shape
         M = dY.shape[0]
-        dYT = self._transpose_aug(dY, False)[:out]
-        XT = self._transpose_aug(X, True)
-        Kp = XT.shape[0]
-        G = torch.zeros(out, Kp, device=self.dev, dtype=torch.float32)
-        tiles = ((out + 127) // 128) * ((Kp + 255) // 256)
+        G = torch.zeros(out, inp, device=self.dev, dtype=torch.float32)
+        db = torch.zeros(out, device=self.dev, dtype=torch.float32)
+        bn = 256 if inp > 192 else (inp + 63) // 64 * 64
+        tiles = ((out + 127) // 128) * ((inp + bn - 1) // bn)
         kblocks = (M + 63) // 64
         splits = max(1, min(kblocks, (2 * self.sms) // max(tiles, 1)))
-        self._ck(self.lib.pcagb_vnet_gemm_tc(
-            _p(dYT), dYT.stride(0), _p(XT), XT.stride(0), None, None, 0, None, _p(G), Kp, out,
-            Kp, M, 0, splits, _p(self._status_word()), self.stream))
-        return G[:, :inp], G[:, inp].contiguous()
+        self._ck(self.lib.pcagb_vnet_wgrad_tc(
+            _p(dY), dY.stride(0), _p(X), X.stride(0), _p(G), inp, out, inp, M, splits,
+            _p(self._status_word()), self.stream))
+        self._ck(self.lib.pcagb_vnet_colsum(_p(dY), M, out, dY.stride(0), _p(db), self.sms,
+                                            self.stream))
+        return G, db
 
     def features(self, regs, flags, task, TP, task_io, task_T):
         n = task.shape[0]

@@ -115,3 +115,30 @@ def test_published_branch_mode_lengths(engine, t):
     for prog in sol.programs:
         assert len(prog) == t["published_length"]
         assert lib.evaluate(task, prog) == task.num_tests
+
+
+@pytest.mark.parametrize("t", PUBLISHED, ids=lambda t: t["name"])
+def test_first_only_branch_mode_same_first_programs(engine, t):
+    """The hybrid solver's stopping rule (the optimal depth ends at the
+    first launch of parents with a solution, every shorter depth searched
+    completely) finds the same optimal length, and its programs are the
+    full search's first programs in depth-first order."""
+    task = spec_from_json(t["task"])
+    K = t["published_length"] - task.num_inputs - 2
+    full = engine.solve_branch(task, max_depth=K)
+    first = engine.solve_branch(task, max_depth=K, first_only=True)
+    assert first.optimal_depth == full.optimal_depth == K
+    assert first.programs and first.programs == full.programs[:len(first.programs)]
+    assert first.split_used == K - 1
+
+
+@pytest.mark.parametrize("fx", [f for f in BRANCH if f["optimal_depth"] in (1, 2)][::3],
+                         ids=lambda f: f"task{f['index']}")
+def test_first_only_branch_mode_on_recorded_runs(engine, fx):
+    """On the recorded reference runs: the same optimal length (or none
+    within the depth), and the first programs of the full search."""
+    task = spec_from_json(fx["task"])
+    full = engine.solve_branch(task, max_depth=fx["max_depth"])
+    first = engine.solve_branch(task, max_depth=fx["max_depth"], first_only=True)
+    assert first.optimal_depth == full.optimal_depth
+    assert first.programs == full.programs[:len(first.programs)]

@@ -219,33 +219,52 @@ def test_tc_gemm_matches_fp32(M, N, K):
     assert rel(Cm.float(), want) < 1e-2
 
 
-@pytest.mark.parametrize("splits", [1, 3, 64])
-def test_tc_gemm_split_k_and_augmented_weight_gradient(splits):
-    """The weight gradient's form: dW | db = dY^T . [X | 1] through the
-    augmented transposes and split-K fp32 adds, against torch."""
+@pytest.mark.parametrize("splits", [1, 7, 64])
+@pytest.mark.parametrize("out,inp", [(256, 176), (16, 128), (128, 256), (256, 528)])
+def test_tc_weight_gradient_mn_major(splits, out, inp):
+    """The weight gradient's form: dW = dY^T . X with dY [M][out] and X
+    [M][in] read as stored (MN-major operands of the tcgen05 MMA, no
+    transposes) and split-K fp32 adds, and db = the column sums of dY,
+    against torch, on the network's layer shapes and a ragged batch."""
     import ctypes
     from pca_gb300.valuenet import _lib, _p
     lib = _lib()
-    M, out, inp = 4096 + 40, 256, 176
-    g = torch.Generator(device="cuda").manual_seed(splits)
+    M = 4096 + 40
+    g = torch.Generator(device="cuda").manual_seed(splits * 1000 + out + inp)
     dY = torch.randn(M, out, device="cuda", generator=g).to(torch.bfloat16)
     X = torch.randn(M, inp, device="cuda", generator=g).to(torch.bfloat16)
     s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
-    Kp = (inp + 1 + 15) // 16 * 16
-    dYT = torch.empty(out, M, device="cuda", dtype=torch.bfloat16)
-    XT = torch.empty(Kp, M, device="cuda", dtype=torch.bfloat16)
-    assert lib.pcagb_vnet_transpose_aug(_p(dY), M, out, out, _p(dYT), out, M, 0, s) == 0
-    assert lib.pcagb_vnet_transpose_aug(_p(X), M, inp, inp, _p(XT), Kp, M, 1, s) == 0
-    torch.cuda.synchronize()
-    assert torch.equal(dYT, dY.t())
-    assert torch.equal(XT[:inp], X.t()) and bool((XT[inp] == 1).all()) and bool((XT[inp + 1:] == 0).all())
-    G = torch.zeros(out, Kp, device="cuda", dtype=torch.float32)
+    G = torch.zeros(out, inp, device="cuda", dtype=torch.float32)
+    db = torch.zeros(out, device="cuda", dtype=torch.float32)
     st = torch.zeros(1, device="cuda", dtype=torch.int32)
-    assert lib.pcagb_vnet_gemm_tc(_p(dYT), M, _p(XT), M, None, None, 0, None, _p(G), Kp, out, Kp,
-                                  M, 0, splits, _p(st), s) == 0
+    assert lib.pcagb_vnet_wgrad_tc(_p(dY), out, _p(X), inp, _p(G), inp, out, inp, M, splits,
+                                   _p(st), s) == 0
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    assert lib.pcagb_vnet_colsum(_p(dY), M, out, out, _p(db), sms, s) == 0
     torch.cuda.synchronize()
     assert int(st.item()) == 0
-    dW = dY.float().t() @ X.float()
-    db = dY.float().sum(0)
-    assert rel(G[:, :inp], dW) < 1e-4 and rel(G[:, inp], db) < 1e-4
-    assert float(G[:, inp + 1:].abs().max()) == 0.0
+    assert rel(G, dY.float().t() @ X.float()) < 1e-4
+    assert rel(db, dY.float().sum(0)) < 1e-4
+
+
+def test_adam_applies_each_layers_gradient():
+    """Adam reads each layer's weight and bias gradients as the backward
+    pass lays them out: the first step moves every weight by lr * g / (|g|
+    + eps) against its gradient g."""
+    from pca_gb300.valuenet import ValueNet
+    net = ValueNet(seed=3, lr=1e-3)
+    b, _ = random_batch(96, seed=1)
+    X = net.features(b["regs"], b["flags"], b["task"], 32, b["task_io"], b["task_T"])
+    net.forward(X, b["live"], b["task"], b["task_T"], b["depth"])
+    gl = torch.randn(96, 16, generator=torch.Generator().manual_seed(5)).to(torch.bfloat16)
+    grads = net.backward(gl.cuda())
+    W0 = {k: net.W[k].clone() for k in net.W}
+    b0 = {k: net.b[k].clone() for k in net.b}
+    net.adam(grads)
+    torch.cuda.synchronize()
+    for k in net.W:
+        dW, dbk = grads[k]
+        want = W0[k] - 1e-3 * dW / (dW.abs() + 1e-8)
+        cols = 521 if k == "T1" else want.shape[1]   # T1's padding columns stay zero
+        assert rel(net.W[k][:, :cols], want[:, :cols]) < 1e-5, k
+        assert rel(net.b[k], b0[k] - 1e-3 * dbk / (dbk.abs() + 1e-8)) < 1e-5, k

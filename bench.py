@@ -945,8 +945,9 @@ def main():
                          oep_mode=OEP_EXACT_LIVE, sol_cap=1 << 12)
 
     # the autotuner measures each of its launch choices twice on stages this
-    # size before keeping the cheapest: those solves are untimed calibration
-    for _ in range(8):
+    # size before keeping the cheapest (three tests-per-lane choices, then
+    # two last-position shapes): those solves are untimed calibration
+    for _ in range(12):
         step()
     for _ in range(max(3, args.warmup)):
         step()

@@ -193,7 +193,10 @@ typedef struct {
     int first_tests;    /* 1..3: tests a lane checks a value class on before
                            the warp checks its survivors on every test       */
     int suffix_chunk;   /* 1..64: first suffix instructions per work item of
-                           the depth-2 and depth-3 suffix kernels            */
+                           the depth-2 and depth-3 suffix kernels, 1024: a
+                           lane per innermost middle instruction there; at
+                           depth 1 (past the root) 1 = a warp per prefix,
+                           >= 32 = a lane per prefix                         */
     int stage_launch;   /* first-only solves of one task: -1 = one launch per
                            stage; n > 0 = a first launch of n prefixes in DFS
                            order, doubling, stopping at the first launch that
@@ -392,9 +395,11 @@ void *pcagb_engine_stream(pcagb_engine_t *e);
 /* The autotuner's measured costs on this engine's device: device ms per
  * value-class evaluation of each suffix depth (t_eval_ms) and per child of a
  * level build, and for each suffix depth s the cost of each launch choice
- * (first_tests 1..3 at [s][1..3], middle chunk choice c at [s][c] with
- * chunk_choices[s][c] first instructions per work item) with the number of
- * stages it was measured on; the host round trip of a chunked launch. */
+ * (first_tests 1..3 at [s][1..3], work-item shape c at [s][c]: for s >= 2
+ * chunk_choices[s][c] first instructions per work item, 1024 meaning a lane
+ * per innermost middle, for s = 1 the prefixes a warp scans at once, 1 or
+ * 32) with the number of stages it was measured on; the host round trip of
+ * a chunked launch. */
 typedef struct {
     double   t_eval_ms[4];
     double   t_child_ms;

@@ -88,6 +88,8 @@ struct Level {
     uint8_t *rdl = nullptr;         /* register each state's last instruction wrote */
     uint8_t *own = nullptr;         /* dead-able older writes (engine_kernels.cuh) */
     uint8_t *twin = nullptr;        /* later member of a flag-twin class (k_twins) */
+    uint16_t *probe = nullptr;      /* [n][8][4] r0..r7 on the first four tests (64 bytes:
+                                       what a lane-per-prefix scan reads) */
     uint32_t *fcr = nullptr;        /* [n][8] rank of the first kept child writing r (set
                                        when the level below is materialised) */
     uint64_t *child_off = nullptr;  /* set when this level is expanded */
@@ -142,7 +144,8 @@ struct pcagb_engine {
     unsigned long long *h_pin = nullptr;
     std::vector<uint8_t> h_active;           /* host copy of d_task_active */
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
-    int occ_insert = 4, occ_suffix = 8, occ_mat = 4;   /* resident blocks per SM */
+    int occ_insert = 4, occ_suffix = 8, occ_mat = 4, occ_lanes = 4,
+        occ_mid_lanes = 4;   /* resident blocks per SM */
     uint64_t launches = 0;
     uint64_t h2d = 0, d2h = 0;
     uint64_t insert_launches = 0, suffix_launches = 0, insert_children = 0;
@@ -296,7 +299,7 @@ int exclusive_scan(pcagb_engine *e, uint64_t *a, uint64_t n, uint64_t *total)
 LevelDev view(const Level &L)
 {
     return LevelDev{L.regs, L.flags, L.live, L.task, L.child_off, L.n, L.rdl, L.parent, L.own,
-                    L.twin};
+                    L.twin, L.probe};
 }
 
 int alloc_level(pcagb_engine *e, Level &L, uint64_t n)
@@ -311,8 +314,9 @@ int alloc_level(pcagb_engine *e, Level &L, uint64_t n)
     L.rdl = (uint8_t *)e->alloc_bottom(n);
     L.own = (uint8_t *)e->alloc_bottom(n);
     L.twin = (uint8_t *)e->alloc_bottom(n);
+    L.probe = (uint16_t *)e->alloc_bottom(n * 64);
     if (!L.regs || !L.flags || !L.live || !L.task || !L.parent || !L.cidx || !L.rdl || !L.own ||
-        !L.twin)
+        !L.twin || !L.probe)
         return PCAGB_ENOMEM;
     return PCAGB_OK;
 }
@@ -367,7 +371,7 @@ template <int TPC>
 int launch_materialize(pcagb_engine *e, const Level &P, const uint32_t *fcr_up,
                        const uint32_t *bitmap, const uint64_t *word_off, Level &C)
 {
-    LevelOut out{C.regs, C.flags, C.live, C.task, C.parent, C.cidx, C.rdl, C.own};
+    LevelOut out{C.regs, C.flags, C.live, C.task, C.parent, C.cidx, C.rdl, C.own, C.probe};
     const int g = e->grid(e->occ_mat);
     k_materialize<TPC><<<g, kThreads, 0, e->stream>>>(view(P), e->td, bitmap, word_off, out,
                                                       split_log2(P.n, g), P.fcr, fcr_up);
@@ -423,7 +427,7 @@ int build_level(pcagb_engine *e, int d)
     const uint64_t children = P.children;
     if (children >= (1ull << 38)) return fail(PCAGB_ENOMEM);
     const uint64_t words = (children + 31) / 32;
-    const uint64_t state_bytes = 8ull * 2 * e->TPC + e->TPC + 1 + 2 + 4 + 2 + 1 + 1 + 1;
+    const uint64_t state_bytes = 8ull * 2 * e->TPC + e->TPC + 1 + 2 + 4 + 2 + 1 + 1 + 1 + 64;
     const bool one_sync = children * state_bytes <= kOneSyncBytes;
 
     cudaEventRecord(e->ev0, e->stream);
@@ -691,9 +695,15 @@ int take_records(pcagb_engine *e, int S, int K, std::vector<TaskRun> &runs, bool
     return PCAGB_OK;
 }
 
-/* Middle-instruction chunks the depth-2 and depth-3 suffix kernels may take
-   per work item, by suffix depth (index 0 is unused). */
-constexpr uint32_t kChunkChoices[4][4] = {{1, 1, 1, 1}, {1, 1, 1, 1}, {4, 8, 16, 32}, {1, 2, 4, 8}};
+/* Work-item shapes of the suffix kernels, by suffix depth (index 0 is
+   unused): at depth 1 the prefixes a warp scans at once (1: a warp per
+   prefix, k_suffix; 32: a lane per prefix, k_suffix_lanes); at depths 2
+   and 3 the middle-instruction chunk a warp-per-item work item takes, or
+   kLaneShape: a lane per innermost middle (k_suffix_mid_lanes). */
+constexpr uint32_t kLaneShape = 1024;
+constexpr uint32_t kChunkChoices[4][4] = {
+    {1, 1, 1, 1}, {1, 32, 1, 32}, {8, 16, 32, kLaneShape}, {1, 2, 4, kLaneShape}};
+constexpr int kChunkOptions[4] = {1, 2, 4, 4};
 /* A stage is large enough to measure a launch choice on; each choice is
    measured this many times before the cheapest is kept. */
 constexpr uint64_t kTuneMinEvals = 20000000ull;
@@ -718,6 +728,24 @@ void record_cost(double &ms, int &n, double v)
 {
     ms = n == 0 ? v : 0.7 * ms + 0.3 * v;
     n++;
+}
+
+template <int TPC>
+void launch_suffix_lanes(int ft, int g, cudaStream_t st, const LevelDev &L, const TaskDev &td,
+                         const SolBuf &sb, const PrefixRange &R)
+{
+    if (ft == 1) k_suffix_lanes<TPC, 1><<<g, kThreads, 0, st>>>(L, td, sb, R);
+    else if (ft == 3) k_suffix_lanes<TPC, 3><<<g, kThreads, 0, st>>>(L, td, sb, R);
+    else k_suffix_lanes<TPC, 2><<<g, kThreads, 0, st>>>(L, td, sb, R);
+}
+
+template <int TPC, int SD>
+void launch_mid_lanes(int ft, int g, cudaStream_t st, const LevelDev &L, const TaskDev &td,
+                      const SolBuf &sb, uint32_t cpp, const PrefixRange &R)
+{
+    if (ft == 1) k_suffix_mid_lanes<TPC, SD, 1><<<g, kThreads, 0, st>>>(L, td, sb, cpp, R);
+    else if (ft == 3) k_suffix_mid_lanes<TPC, SD, 3><<<g, kThreads, 0, st>>>(L, td, sb, cpp, R);
+    else k_suffix_mid_lanes<TPC, SD, 2><<<g, kThreads, 0, st>>>(L, td, sb, cpp, R);
 }
 
 template <int TPC, int SD>
@@ -776,30 +804,55 @@ int run_stage(pcagb_engine *e, int S, int K, std::vector<TaskRun> &runs, bool fi
         if (ft < 1 || ft > 3) ft = 1 + pick_option(&e->ft_ms[s][1], &e->ft_n[s][1], 3, 1, explore);
         int ck = -1;
         uint32_t chunk = 1;
-        if (s >= 2) {
+        /* a lane per prefix needs every prefix's last write: not at the root */
+        const bool lanes_ok = s == 1 && S >= 1;
+        if (s >= 2 || lanes_ok) {
             if (e->force_chunk >= 1) {
-                chunk = (uint32_t)std::min(e->force_chunk, 64);
+                chunk = s == 1 ? (e->force_chunk >= 32 ? 32u : 1u)
+                        : e->force_chunk == (int)kLaneShape ? kLaneShape
+                                                             : (uint32_t)std::min(e->force_chunk, 64);
             } else {
-                /* chunks are explored once the tests-per-lane choice is */
+                /* shapes are explored once the tests-per-lane choice is */
                 const bool ft_done = e->ft_n[s][1] >= kTuneSamples &&
                                      e->ft_n[s][2] >= kTuneSamples && e->ft_n[s][3] >= kTuneSamples;
-                ck = pick_option(e->ck_ms[s], e->ck_n[s], 4, s == 2 ? 2 : 0, explore && ft_done);
+                ck = pick_option(e->ck_ms[s], e->ck_n[s], kChunkOptions[s], s == 2 ? 1 : 0,
+                                 explore && ft_done);
                 chunk = kChunkChoices[s][ck];
             }
         }
+        /* work items per prefix: one (depth 1); the middle chunks; with a
+           lane per middle, 32 first middles (depth 2) or one (depth 3) */
         const uint32_t cpp =
-            s == 1 ? 1 : std::max(1u, (uint32_t)((ncmax + chunk - 1) / chunk));
+            s == 1                ? 1u
+            : chunk == kLaneShape ? std::max(1u, s == 2 ? (uint32_t)(ncmax + 31) / 32
+                                                        : (uint32_t)ncmax)
+                                  : std::max(1u, (uint32_t)((ncmax + chunk - 1) / chunk));
         auto launch = [&](const PrefixRange &R) {
             const LevelDev V = view(L);
             if (s == 1) {
-                if (t16) launch_suffix<16, 1>(ft, g, e->stream, V, e->td, sb, 1, 1, R);
-                else launch_suffix<32, 1>(ft, g, e->stream, V, e->td, sb, 1, 1, R);
+                if (chunk == 32) {
+                    const int gl = e->grid(e->occ_lanes);
+                    if (t16) launch_suffix_lanes<16>(ft, gl, e->stream, V, e->td, sb, R);
+                    else launch_suffix_lanes<32>(ft, gl, e->stream, V, e->td, sb, R);
+                } else {
+                    if (t16) launch_suffix<16, 1>(ft, g, e->stream, V, e->td, sb, 1, 1, R);
+                    else launch_suffix<32, 1>(ft, g, e->stream, V, e->td, sb, 1, 1, R);
+                }
                 const int rc0 = check_launch(e);
                 if (rc0) return rc0;
                 /* a thread per prefix (the pass is latency bound) */
                 const unsigned cb = (unsigned)std::min<uint64_t>((R.count + 255) / 256,
                                                                  (uint64_t)e->sms * 32);
                 k_count_evals<<<std::max(cb, 1u), 256, 0, e->stream>>>(V, e->td, R, sb);
+            } else if (chunk == kLaneShape) {
+                const int gl = e->grid(e->occ_mid_lanes);
+                if (s == 2) {
+                    if (t16) launch_mid_lanes<16, 2>(ft, gl, e->stream, V, e->td, sb, cpp, R);
+                    else launch_mid_lanes<32, 2>(ft, gl, e->stream, V, e->td, sb, cpp, R);
+                } else {
+                    if (t16) launch_mid_lanes<16, 3>(ft, gl, e->stream, V, e->td, sb, cpp, R);
+                    else launch_mid_lanes<32, 3>(ft, gl, e->stream, V, e->td, sb, cpp, R);
+                }
             } else if (s == 2) {
                 if (t16) launch_suffix<16, 2>(ft, g, e->stream, V, e->td, sb, cpp, chunk, R);
                 else launch_suffix<32, 2>(ft, g, e->stream, V, e->td, sb, cpp, chunk, R);
@@ -1073,7 +1126,7 @@ int autotune_split(pcagb_engine *e, int K, const std::vector<uint8_t> &active,
                it would only find that out after its insert. */
             double kids = children_of(D), build = 0, states_scale = 1.0;
             double parents = (double)e->levels[D].n, held = 0;
-            const double state_bytes = 16.0 * e->TPC + e->TPC + 12;
+            const double state_bytes = 16.0 * e->TPC + e->TPC + 12 + 64;
             const double free_b = (double)(e->top - e->bottom);
             bool fits = true;
             for (int d = D + 1; d <= S; d++) {
@@ -1242,7 +1295,7 @@ int run_batch(pcagb_engine *e, std::vector<TaskRun> &runs, const pcagb_opts_t &o
     if (alloc_level(e, L0, nt) != PCAGB_OK) { set_err("arena too small"); return PCAGB_ENOMEM; }
     {
         const int TPC = e->TPC;
-        std::vector<uint16_t> regs((size_t)nt * 8 * TPC, 0);
+        std::vector<uint16_t> regs((size_t)nt * 8 * TPC, 0), probe((size_t)nt * 32, 0);
         std::vector<uint8_t> flags((size_t)nt * TPC, 0), live(nt);
         std::vector<uint16_t> task(nt), cidx(nt, 0);
         std::vector<uint32_t> parent(nt, 0);
@@ -1250,8 +1303,10 @@ int run_batch(pcagb_engine *e, std::vector<TaskRun> &runs, const pcagb_opts_t &o
         for (int i = 0; i < nt; i++) {
             const TaskRun &tr = runs[i];
             for (int t = 0; t < tr.T; t++) {
-                for (int r = 1; r < 8; r++)
+                for (int r = 1; r < 8; r++) {
                     regs[((size_t)i * 8 + r) * TPC + t] = tr.root.regs[tr.order[t]][r];
+                    if (t < 4) probe[(size_t)i * 32 + r * 4 + t] = tr.root.regs[tr.order[t]][r];
+                }
                 flags[(size_t)i * TPC + t] = tr.root.flags[tr.order[t]];
             }
             live[i] = tr.root.live;
@@ -1267,6 +1322,7 @@ int run_batch(pcagb_engine *e, std::vector<TaskRun> &runs, const pcagb_opts_t &o
         CK(cudaMemsetAsync(L0.rdl, 0, nt, e->stream));
         CK(cudaMemsetAsync(L0.own, 0, nt, e->stream));
         CK(cudaMemsetAsync(L0.twin, 0, nt, e->stream));
+        CK(e_copy(e, L0.probe, probe.data(), probe.size() * 2, cudaMemcpyHostToDevice, e->stream));
     }
     e->levels.push_back(std::move(L0));
 
@@ -1549,6 +1605,11 @@ int ensure_device_tables(int device)
         CK(cudaMemcpy(ev1_d, ev1.data(), ev1.size() * 4, cudaMemcpyHostToDevice));
         const uint32_t *ev1p = ev1_d;
         CK(cudaMemcpyToSymbol(c_ev_sd1, &ev1p, sizeof ev1p));
+        uint32_t *pro_d = nullptr;
+        CK(cudaMalloc(&pro_d, gt.pr_off.size() * 4));
+        CK(cudaMemcpy(pro_d, gt.pr_off.data(), gt.pr_off.size() * 4, cudaMemcpyHostToDevice));
+        const uint32_t *prop = pro_d;
+        CK(cudaMemcpyToSymbol(c_pr_off_g, &prop, sizeof prop));
         CK(cudaMemcpyToSymbol(c_pr, &pp, sizeof pp));
         CK(cudaMemcpyToSymbol(c_pr_cls, &pc, sizeof pc));
     }
@@ -1607,6 +1668,15 @@ int engine_init(pcagb_engine *e, int device, size_t budget)
         PCAGB_PRELOAD(k_suffix<32, 2, 1>); PCAGB_PRELOAD(k_suffix<32, 2, 2>);
         PCAGB_PRELOAD(k_suffix<32, 2, 3>); PCAGB_PRELOAD(k_suffix<32, 3, 1>);
         PCAGB_PRELOAD(k_suffix<32, 3, 2>); PCAGB_PRELOAD(k_suffix<32, 3, 3>);
+        PCAGB_PRELOAD(k_suffix_lanes<16, 1>); PCAGB_PRELOAD(k_suffix_lanes<16, 2>);
+        PCAGB_PRELOAD(k_suffix_lanes<16, 3>); PCAGB_PRELOAD(k_suffix_lanes<32, 1>);
+        PCAGB_PRELOAD(k_suffix_lanes<32, 2>); PCAGB_PRELOAD(k_suffix_lanes<32, 3>);
+        PCAGB_PRELOAD(k_suffix_mid_lanes<16, 2, 1>); PCAGB_PRELOAD(k_suffix_mid_lanes<16, 2, 2>);
+        PCAGB_PRELOAD(k_suffix_mid_lanes<16, 2, 3>); PCAGB_PRELOAD(k_suffix_mid_lanes<16, 3, 1>);
+        PCAGB_PRELOAD(k_suffix_mid_lanes<16, 3, 2>); PCAGB_PRELOAD(k_suffix_mid_lanes<16, 3, 3>);
+        PCAGB_PRELOAD(k_suffix_mid_lanes<32, 2, 1>); PCAGB_PRELOAD(k_suffix_mid_lanes<32, 2, 2>);
+        PCAGB_PRELOAD(k_suffix_mid_lanes<32, 2, 3>); PCAGB_PRELOAD(k_suffix_mid_lanes<32, 3, 1>);
+        PCAGB_PRELOAD(k_suffix_mid_lanes<32, 3, 2>); PCAGB_PRELOAD(k_suffix_mid_lanes<32, 3, 3>);
         PCAGB_PRELOAD(k_expand_insert<16>); PCAGB_PRELOAD(k_expand_insert<32>);
         PCAGB_PRELOAD(k_materialize<16>); PCAGB_PRELOAD(k_materialize<32>);
         PCAGB_PRELOAD(k_twins<16>); PCAGB_PRELOAD(k_twins<32>);
@@ -1633,6 +1703,12 @@ int engine_init(pcagb_engine *e, int device, size_t budget)
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_materialize<32>, kThreads, 0) ==
                 cudaSuccess && nb > 0)
             e->occ_mat = nb;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_suffix_lanes<32, 2>, kThreads, 0) ==
+                cudaSuccess && nb > 0)
+            e->occ_lanes = nb;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_suffix_mid_lanes<32, 2, 2>,
+                                                          kThreads, 0) == cudaSuccess && nb > 0)
+            e->occ_mid_lanes = nb;
         cudaGetLastError();
     }
     size_t free_b = 0, total_b = 0;
@@ -1674,9 +1750,10 @@ bool make_run(const task_spec_t *task, const pcagb_opts_t &o, TaskRun *tr)
         set_err("max_depth %d out of range (program length is limited to 16)", o.max_depth);
         return false;
     }
-    if (o.first_tests < 0 || o.first_tests > 3 || o.suffix_chunk < 0 || o.suffix_chunk > 64 ||
+    if (o.first_tests < 0 || o.first_tests > 3 || o.suffix_chunk < 0 ||
+        (o.suffix_chunk > 64 && o.suffix_chunk != (int)kLaneShape) ||
         o.stage_launch < -1) {
-        set_err("launch choices out of range (first_tests 0..3, suffix_chunk 0..64, "
+        set_err("launch choices out of range (first_tests 0..3, suffix_chunk 0..64 or 1024, "
                 "stage_launch >= -1)");
         return false;
     }

@@ -73,6 +73,7 @@ __constant__ const uint32_t *c_pr;         /* a | b << 3 | opmask << 6 | imm << 
 __constant__ const uint16_t *c_pr_cls;     /* [entry][10] class index per opmask bit */
 __constant__ uint32_t c_pr_ev[128 * 8];    /* [mask*8 + r]: class evaluations of its pair list */
 __constant__ const uint32_t *c_ev_sd1;     /* the same in global memory, [mask*8 + 0] = all classes */
+__constant__ const uint32_t *c_pr_off_g;   /* c_pr_off in global memory (lanes of different masks) */
 
 /* Per-task parameters of a batch: device arrays indexed by task id. A
    state's task id travels with it through the levels; states of different
@@ -99,6 +100,7 @@ struct LevelDev {
                                bit 0: the last instruction is an LDI */
     const uint8_t *twin;    /* [n] 1: an earlier state of the level has the same registers,
                                live mask and task (k_twins) */
+    const uint16_t *probe;  /* [n][8][4] r0..r7 on the first four tests, 64 bytes a state */
 };
 
 struct LevelOut {
@@ -110,6 +112,7 @@ struct LevelOut {
     uint16_t *cidx;
     uint8_t *rdl;
     uint8_t *own;
+    uint16_t *probe;
 };
 
 /* ---- hashing (a multiply-rotate chain; the table compares full states, so
@@ -744,9 +747,14 @@ k_materialize(LevelDev P, TaskDev task, const uint32_t *bitmap, const uint64_t *
                     ms.FB[lane] = (uint8_t)f;
                 }
                 __syncwarp();
-                if (lane < kPieces)
-                    reinterpret_cast<uint4 *>(C.regs + rk * 8 * TPC)[lane] =
-                        *(my_col == rd ? my_new : my_old);
+                if (lane < kPieces) {
+                    const uint4 pv = *(my_col == rd ? my_new : my_old);
+                    reinterpret_cast<uint4 *>(C.regs + rk * 8 * TPC)[lane] = pv;
+                    /* the lane holding tests 0..7 of a column also writes
+                       tests 0..3 of it into the probe (8 lanes, 64 bytes) */
+                    if (lane % kPiecesPerCol == 0)
+                        reinterpret_cast<uint2 *>(C.probe + rk * 32)[my_col] = make_uint2(pv.x, pv.y);
+                }
                 if (lane < kFlagPieces)
                     reinterpret_cast<uint4 *>(C.flags + rk * TPC)[lane] =
                         reinterpret_cast<const uint4 *>(ms.FB)[lane];
@@ -1188,6 +1196,321 @@ k_suffix(LevelDev P, TaskDev task, SolBuf S, uint32_t chunks_per_prefix, uint32_
                 const uint32_t m2 = (m1 | (1u << (rd2 - 1))) & 127u;
                 scan_last<TPC, FT>(ws, T, m2, rd2 == rd1 ? 8u : rd1, rd2, tgt, tgt0, tgt1, tgt2, lane, S,
                                q, i1, i2, rd2, need2, nev);
+            }
+        }
+    }
+    flush_evals(S, nev, lane);
+}
+
+/* The last position (suffix depth 1) with a lane per prefix: a warp takes
+ * 32 prefixes of range R at once, each lane the operand pairs of its own
+ * prefix that read the prefix's last write (the read rule, as scan_last),
+ * every op of a pair evaluated on the first FT tests at once. A lane holds
+ * nothing but its prefix's first FT test values of r0..r7 (in shared
+ * memory, [test][register][lane], so lanes reading different registers hit
+ * different banks) instead of the whole state: per prefix 7 sectors of the
+ * level instead of seven 64-byte columns, and the warp's instructions are
+ * not repeated for every prefix. A pair that passes the first FT tests is
+ * checked on every test by the whole warp (lane = test) straight from the
+ * level and recorded as the warp-per-prefix kernel records it, so the
+ * records are the same. Every prefix of a level past the root has a last
+ * write (no candidate of the branchless set writes r0); root prefixes
+ * (w0 = 0) are left to k_suffix. */
+template <int TPC, int FT>
+__global__ void __launch_bounds__(kThreads, 5)
+k_suffix_lanes(LevelDev P, TaskDev task, SolBuf S, PrefixRange R)
+{
+    __shared__ uint32_t sV[kWarpsPerBlock][FT][8][32];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    uint32_t (&V)[FT][8][32] = sV[wib];
+#pragma unroll
+    for (int t = 0; t < FT; t++) V[t][0][lane] = 0;
+    const uint64_t nw = (uint64_t)gridDim.x * kWarpsPerBlock;
+    for (uint64_t base = ((uint64_t)blockIdx.x * kWarpsPerBlock + wib) * 32; base < R.count;
+         base += nw * 32) {
+        const uint64_t i = base + lane;
+        uint64_t q = ~0ull;
+        if (i < R.count) {
+            q = R.order ? (uint64_t)R.order[R.begin + i] : R.begin + i;
+            if (q >= P.n) q = ~0ull;   /* orders are checked on the host; never index outside */
+        }
+        uint32_t tid = 0, live = 0, w0 = 0, p0 = 0, np = 0, T = 0;
+        uint32_t t0 = 0, t1 = 0, t2 = 0;
+        if (q != ~0ull) {
+            tid = P.task[q];
+            live = P.live[q];
+            w0 = P.rdl[q];
+            if (task.active[tid] && w0) {
+                const uint32_t m = (live >> 1) & 127u;
+                p0 = c_pr_off_g[m * 8 + w0];
+                np = c_pr_off_g[m * 8 + w0 + 1] - p0;
+                T = (uint32_t)task.T[tid];
+                t0 = task.target[tid * 32];
+                if (FT >= 2) t1 = task.target[tid * 32 + 1];
+                if (FT >= 3) t2 = task.target[tid * 32 + 2];
+            }
+        }
+        __syncwarp();
+        if (np) {
+            /* the prefix's probe: registers 2h and 2h+1 on tests 0..3 in
+               16-byte piece h */
+            const uint4 *pp = reinterpret_cast<const uint4 *>(P.probe + q * 32);
+#pragma unroll
+            for (int h = 0; h < 4; h++) {
+                const uint4 w = pp[h];
+                const uint32_t lo[2] = {w.x, w.z}, hi[2] = {w.y, w.w};
+#pragma unroll
+                for (int k = 0; k < 2; k++) {
+                    const int r = 2 * h + k;
+                    if (r == 0) continue;
+                    V[0][r][lane] = lo[k] & 0xFFFFu;
+                    if (FT >= 2) V[FT >= 2 ? 1 : 0][r][lane] = lo[k] >> 16;
+                    if (FT >= 3) V[FT >= 3 ? 2 : 0][r][lane] = hi[k] & 0xFFFFu;
+                }
+            }
+        }
+        __syncwarp();
+        uint32_t jn = np;
+#pragma unroll
+        for (int o = 16; o; o >>= 1) jn = max(jn, __shfl_xor_sync(0xFFFFFFFFu, jn, o));
+        for (uint32_t j = 0; j < jn; j++) {
+            uint32_t hits = 0;
+            if (j < np) {
+                const uint32_t d = c_pr[p0 + j];
+                const uint32_t a = d & 7u, b = (d >> 3) & 7u;
+                const uint32_t e = (uint32_t)(uint16_t)(int16_t)(int8_t)(uint8_t)(d >> 16);
+                hits = pair_hits(V[0][a][lane], V[0][b][lane], e, t0) & (d >> 6) & 0x3FFu;
+                if (FT >= 2 && T >= 2 && hits)
+                    hits &= pair_hits(V[FT >= 2 ? 1 : 0][a][lane], V[FT >= 2 ? 1 : 0][b][lane], e, t1);
+                if (FT >= 3 && T >= 3 && hits)
+                    hits &= pair_hits(V[FT >= 3 ? 2 : 0][a][lane], V[FT >= 3 ? 2 : 0][b][lane], e, t2);
+            }
+            uint32_t bal = __ballot_sync(0xFFFFFFFFu, hits != 0);
+            while (bal) {
+                const int L = __ffs(bal) - 1;
+                bal &= bal - 1;
+                uint32_t hj = __shfl_sync(0xFFFFFFFFu, hits, L);
+                const unsigned long long qL = __shfl_sync(0xFFFFFFFFu, (unsigned long long)q, L);
+                const uint32_t tidL = __shfl_sync(0xFFFFFFFFu, tid, L);
+                const uint32_t liveL = __shfl_sync(0xFFFFFFFFu, live, L);
+                const uint32_t pj = __shfl_sync(0xFFFFFFFFu, p0, L) + j;
+                const uint32_t d = c_pr[pj];
+                const uint32_t a = d & 7u, b = (d >> 3) & 7u;
+                const uint32_t e = (uint32_t)(uint16_t)(int16_t)(int8_t)(uint8_t)(d >> 16);
+                const int TL = task.T[tidL];
+                const uint32_t tgt = lane < TL ? task.target[tidL * 32 + lane] : 0u;
+                uint32_t x = 0, y = 0;
+                if (lane < TL) {
+                    x = P.regs[(qL * 8 + a) * TPC + lane];
+                    y = P.regs[(qL * 8 + b) * TPC + lane];
+                }
+                const uint32_t vbase = c_vc_off[(liveL >> 1) & 127u];
+                while (hj) {
+                    const uint32_t k = (uint32_t)(__ffs(hj) - 1);
+                    hj &= hj - 1;
+                    bool ok = true;
+                    if (lane < TL)
+                        ok = (k == 9 ? ((x + e) & 0xFFFFu) : pca_alu(pair_op(k), x, y, 0)) == tgt;
+                    if (__all_sync(0xFFFFFFFFu, ok) && lane == 0) {
+                        const uint32_t cj = c_pr_cls[(uint64_t)pj * 10 + k];
+                        record_solution(S, qL, 0, 0, cj, c_vc_first[vbase + cj]);
+                    }
+                }
+            }
+        }
+    }
+}
+
+/* The value of register x on test t after the middles (first FT tests):
+   the innermost middle's own value, else the first middle's (suffix depth
+   3), else the prefix's. */
+template <int FT>
+__device__ __forceinline__ uint32_t mid_val(const uint32_t (&V)[FT][8], int t, uint32_t x,
+                                            uint32_t rdA, uint32_t vA, uint32_t rdB, uint32_t vB)
+{
+    return x == rdB ? vB : x == rdA ? vA : V[t][x];
+}
+
+/* Suffix depths 2 and 3 with a lane per instruction of the innermost
+ * middle. SD = 2: a work item is a prefix and 32 of its middle candidates,
+ * one per lane; SD = 3: a work item is a prefix and one first middle, whose
+ * second middles the lanes take 32 at a time. A lane computes its middle's
+ * value on the first FT tests from the prefix's probe (and the first
+ * middle's, computed by every lane), applies k_suffix's rules (same-state
+ * middles skipped under OEP; a write overwritten unread skips the branch;
+ * the last instruction reads the innermost write and the one write still
+ * owed a read, at most one), and walks the operand pairs of its mask that
+ * read its middle's write, every op of a pair evaluated at once. A pair that
+ * passes the first FT tests is checked on every test by the warp (lane =
+ * test, the whole chain recomputed from the level's columns) and recorded
+ * as k_suffix records it, so the records are the same. */
+template <int TPC, int SD, int FT>
+__global__ void __launch_bounds__(kThreads, 4)
+k_suffix_mid_lanes(LevelDev P, TaskDev task, SolBuf S, uint32_t chunks_per_prefix, PrefixRange R)
+{
+    static_assert(SD == 2 || SD == 3, "middle lanes serve suffix depths 2 and 3");
+    __shared__ uint32_t sV[kWarpsPerBlock][FT][8];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    uint32_t (&V)[FT][8] = sV[wib];
+    const uint64_t nw = (uint64_t)gridDim.x * kWarpsPerBlock;
+    const uint64_t items = R.count * chunks_per_prefix;
+    uint64_t loaded = ~0ull;
+    uint32_t cur_task = ~0u, T = 0, t0 = 0, t1 = 0, t2 = 0;
+    bool cur_active = false;
+    unsigned long long nev = 0;
+    for (uint64_t it = (uint64_t)blockIdx.x * kWarpsPerBlock + wib; it < items; it += nw) {
+        const uint64_t qi = it / chunks_per_prefix;
+        const uint32_t ck = (uint32_t)(it - qi * chunks_per_prefix);
+        const uint64_t q = R.order ? (uint64_t)R.order[R.begin + qi] : R.begin + qi;
+        if (q >= P.n) continue;  /* orders are checked on the host; never index outside */
+        const uint32_t tid = P.task[q];
+        if (tid != cur_task) {
+            cur_task = tid;
+            cur_active = task.active[tid] != 0;
+            T = (uint32_t)task.T[tid];
+            t0 = task.target[tid * 32];
+            if (FT >= 2) t1 = task.target[tid * 32 + 1];
+            if (FT >= 3) t2 = task.target[tid * 32 + 2];
+        }
+        if (!cur_active) continue;
+        const uint32_t live = P.live[q], w0 = P.rdl[q];
+        const uint32_t m0 = (live >> 1) & 127u;
+        const uint32_t cb0 = c_cand_off[m0], nc0 = c_cand_off[m0 + 1] - cb0;
+        if (q != loaded) {
+            __syncwarp();
+            if (lane < FT * 8) V[lane >> 3][lane & 7] = P.probe[q * 32 + (lane & 7) * 4 + (lane >> 3)];
+            __syncwarp();
+            loaded = q;
+        }
+        /* the first middle: each lane's own (SD 2) or the work item's (SD 3) */
+        const uint32_t i1 = SD == 2 ? ck * 32 + (uint32_t)lane : ck;
+        if (SD == 3 && i1 >= nc0) continue;
+        bool act1 = i1 < nc0;
+        const uint32_t u1 = act1 ? c_cand_uop[cb0 + i1] : 0u;
+        if (task.dedup_mid && (u1 >> 31)) act1 = false;
+        const uint32_t rd1 = UOP_RD(u1);
+        const uint32_t owe0 = w0 && !uop_reads(u1, w0) ? w0 : 0u;
+        if (owe0 && rd1 == owe0) act1 = false;
+        if (SD == 3 && !act1) continue;    /* uniform for the warp at SD 3 */
+        uint32_t v1[FT];
+#pragma unroll
+        for (int t = 0; t < FT; t++)
+            v1[t] = pca_alu(UOP_OP(u1), V[t][UOP_A(u1)], V[t][UOP_B(u1)], UOP_IMM(u1));
+        /* (an inactive lane's micro-op is 0: rd 0, no bit to set) */
+        const uint32_t m1 = rd1 ? (m0 | (1u << (rd1 - 1))) & 127u : m0;
+        const uint32_t nc1 = SD == 3 ? c_cand_off[m1 + 1] - c_cand_off[m1] : 32u;
+        for (uint32_t b2 = 0; b2 < nc1; b2 += 32) {
+            /* the innermost middle of this lane and the last position's
+               requirements */
+            bool act = act1;
+            uint32_t i2 = 0, u2 = 0, rdA = 8, rdB = rd1, need1 = rd1, need2 = owe0, m = m1;
+            uint32_t vA[FT], vB[FT];
+#pragma unroll
+            for (int t = 0; t < FT; t++) {
+                vA[t] = 0;
+                vB[t] = v1[t];
+            }
+            if (SD == 3) {
+                i2 = b2 + (uint32_t)lane;
+                act = i2 < nc1;
+                u2 = act ? c_cand_uop[c_cand_off[m1] + i2] : 0u;
+                if (task.dedup_mid && (u2 >> 31)) act = false;
+                const uint32_t rd2 = UOP_RD(u2);
+                const uint32_t owe1 = uop_reads(u2, rd1) ? 0u : rd1;
+                const uint32_t owe0b = owe0 && !uop_reads(u2, owe0) ? owe0 : 0u;
+                if ((owe1 && rd2 == owe1) || (owe0b && rd2 == owe0b)) act = false;
+                if (owe1 && owe0b) act = false;   /* three registers to read */
+                need2 = owe1 ? owe1 : owe0b;
+                need1 = rd2;
+                m = rd2 ? (m1 | (1u << (rd2 - 1))) & 127u : m1;
+                rdA = rd1;
+                rdB = rd2;
+#pragma unroll
+                for (int t = 0; t < FT; t++) {
+                    vA[t] = v1[t];
+                    vB[t] = pca_alu(UOP_OP(u2), mid_val<FT>(V, t, UOP_A(u2), 8, 0, rd1, v1[t]),
+                                    mid_val<FT>(V, t, UOP_B(u2), 8, 0, rd1, v1[t]), UOP_IMM(u2));
+                }
+            }
+            uint32_t p0 = 0, np = 0;
+            if (act) {
+                p0 = c_pr_off_g[m * 8 + need1];
+                np = c_pr_off_g[m * 8 + need1 + 1] - p0;
+                if (!need2) nev += c_ev_sd1[m * 8 + need1];
+            }
+            uint32_t jn = np;
+#pragma unroll
+            for (int o = 16; o; o >>= 1) jn = max(jn, __shfl_xor_sync(0xFFFFFFFFu, jn, o));
+            for (uint32_t j = 0; j < jn; j++) {
+                uint32_t hits = 0;
+                if (j < np) {
+                    const uint32_t d = c_pr[p0 + j];
+                    const uint32_t a = d & 7u, b = (d >> 3) & 7u;
+                    if (!need2 || a == need2 || b == need2) {
+                        if (need2) nev += __popc((d >> 6) & 0x3FFu);
+                        const uint32_t e = (uint32_t)(uint16_t)(int16_t)(int8_t)(uint8_t)(d >> 16);
+                        hits = pair_hits(mid_val<FT>(V, 0, a, rdA, vA[0], rdB, vB[0]),
+                                         mid_val<FT>(V, 0, b, rdA, vA[0], rdB, vB[0]), e, t0) &
+                               (d >> 6) & 0x3FFu;
+                        if (FT >= 2 && T >= 2 && hits)
+                            hits &= pair_hits(
+                                mid_val<FT>(V, FT >= 2 ? 1 : 0, a, rdA, vA[FT >= 2 ? 1 : 0], rdB,
+                                            vB[FT >= 2 ? 1 : 0]),
+                                mid_val<FT>(V, FT >= 2 ? 1 : 0, b, rdA, vA[FT >= 2 ? 1 : 0], rdB,
+                                            vB[FT >= 2 ? 1 : 0]), e, t1);
+                        if (FT >= 3 && T >= 3 && hits)
+                            hits &= pair_hits(
+                                mid_val<FT>(V, FT >= 3 ? 2 : 0, a, rdA, vA[FT >= 3 ? 2 : 0], rdB,
+                                            vB[FT >= 3 ? 2 : 0]),
+                                mid_val<FT>(V, FT >= 3 ? 2 : 0, b, rdA, vA[FT >= 3 ? 2 : 0], rdB,
+                                            vB[FT >= 3 ? 2 : 0]), e, t2);
+                    }
+                }
+                uint32_t bal = __ballot_sync(0xFFFFFFFFu, hits != 0);
+                while (bal) {
+                    const int L = __ffs(bal) - 1;
+                    bal &= bal - 1;
+                    uint32_t hj = __shfl_sync(0xFFFFFFFFu, hits, L);
+                    const uint32_t uL1 = __shfl_sync(0xFFFFFFFFu, u1, L);
+                    const uint32_t uL2 = __shfl_sync(0xFFFFFFFFu, u2, L);
+                    const uint32_t iL1 = __shfl_sync(0xFFFFFFFFu, i1, L);
+                    const uint32_t iL2 = __shfl_sync(0xFFFFFFFFu, i2, L);
+                    const uint32_t mL = __shfl_sync(0xFFFFFFFFu, m, L);
+                    const uint32_t pj = __shfl_sync(0xFFFFFFFFu, p0, L) + j;
+                    const uint32_t d = c_pr[pj];
+                    const uint32_t a = d & 7u, b = (d >> 3) & 7u;
+                    const uint32_t e = (uint32_t)(uint16_t)(int16_t)(int8_t)(uint8_t)(d >> 16);
+                    /* the chain on test `lane`, from the level's columns */
+                    uint32_t x = 0, y = 0, tg = 0;
+                    if (lane < (int)T) {
+                        const uint16_t *col = P.regs + q * 8 * TPC + lane;
+                        const uint32_t r1 = UOP_RD(uL1);
+                        const uint32_t m1v = pca_alu(UOP_OP(uL1), col[UOP_A(uL1) * TPC],
+                                                     col[UOP_B(uL1) * TPC], UOP_IMM(uL1));
+                        uint32_t r2 = 8, m2v = 0;
+                        if (SD == 3) {
+                            r2 = UOP_RD(uL2);
+                            const uint32_t xa = UOP_A(uL2) == r1 ? m1v : col[UOP_A(uL2) * TPC];
+                            const uint32_t xb = UOP_B(uL2) == r1 ? m1v : col[UOP_B(uL2) * TPC];
+                            m2v = pca_alu(UOP_OP(uL2), xa, xb, UOP_IMM(uL2));
+                        }
+                        x = a == r2 ? m2v : a == r1 ? m1v : col[a * TPC];
+                        y = b == r2 ? m2v : b == r1 ? m1v : col[b * TPC];
+                        tg = task.target[tid * 32 + lane];
+                    }
+                    const uint32_t vbase = c_vc_off[mL];
+                    while (hj) {
+                        const uint32_t k = (uint32_t)(__ffs(hj) - 1);
+                        hj &= hj - 1;
+                        bool ok = true;
+                        if (lane < (int)T)
+                            ok = (k == 9 ? ((x + e) & 0xFFFFu) : pca_alu(pair_op(k), x, y, 0)) == tg;
+                        if (__all_sync(0xFFFFFFFFu, ok) && lane == 0) {
+                            const uint32_t cj = c_pr_cls[(uint64_t)pj * 10 + k];
+                            record_solution(S, q, iL1, SD == 3 ? iL2 : 0u, cj, c_vc_first[vbase + cj]);
+                        }
+                    }
+                }
             }
         }
     }

@@ -191,19 +191,43 @@ __global__ void k_to_bf16(const float *src, __nv_bfloat16 *dst, size_t count)
 }
 
 /* Column sums of a bf16 [rows][cols] matrix (leading dimension ld, both
-   multiples of 8) added into out[cols] (fp32): a thread per 8 columns and
-   row slot (16-byte loads, fp32 sums in registers), the 8 row slots of a
-   block reduced in shared memory, one atomic add per column and block. */
-__global__ void __launch_bounds__(256) k_colsum(const __nv_bfloat16 *Y, long long rows, int cols,
-                                               int ld, float *out)
+   multiples of 8), in two deterministic stages: k_colsum_part gives each
+   block's partial sums (a thread per 8 columns and row slot, eight rows in
+   flight per thread, 16-byte loads, the 8 row slots of a block reduced in
+   shared memory) in part[block][cols]; k_colsum_final adds the blocks'
+   partials of each column into out (32 columns per block, 32 slices of the
+   partials, reduced in shared memory). No atomics: a column's sum does not
+   depend on the order blocks finish in. */
+constexpr int kColsumRows = 8;   /* rows a thread loads before adding */
+
+__global__ void __launch_bounds__(256) k_colsum_part(const __nv_bfloat16 *Y, long long rows,
+                                                    int cols, int ld, float *part)
 {
-    __shared__ float part[8][32][8];
+    __shared__ float sp[8][32][8];
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const long long stride = (long long)gridDim.x * 8;
     for (int g0 = 0; g0 < cols / 8; g0 += 32) {
         const int g = g0 + tx;
         float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
         if (g < cols / 8) {
-            for (long long r = (long long)blockIdx.x * 8 + ty; r < rows; r += (long long)gridDim.x * 8) {
+            long long r = (long long)blockIdx.x * 8 + ty;
+            for (; r + (kColsumRows - 1) * stride < rows; r += kColsumRows * stride) {
+                uint4 w[kColsumRows];
+#pragma unroll
+                for (int u = 0; u < kColsumRows; u++)
+                    w[u] = *(const uint4 *)(Y + (r + u * stride) * ld + g * 8);
+#pragma unroll
+                for (int u = 0; u < kColsumRows; u++) {
+                    const __nv_bfloat162 *h = (const __nv_bfloat162 *)&w[u];
+#pragma unroll
+                    for (int j = 0; j < 4; j++) {
+                        const float2 f = __bfloat1622float2(h[j]);
+                        acc[2 * j] += f.x;
+                        acc[2 * j + 1] += f.y;
+                    }
+                }
+            }
+            for (; r < rows; r += stride) {
                 const uint4 w = *(const uint4 *)(Y + r * ld + g * 8);
                 const __nv_bfloat162 *h = (const __nv_bfloat162 *)&w;
 #pragma unroll
@@ -215,17 +239,35 @@ __global__ void __launch_bounds__(256) k_colsum(const __nv_bfloat16 *Y, long lon
             }
         }
 #pragma unroll
-        for (int j = 0; j < 8; j++) part[ty][tx][j] = acc[j];
+        for (int j = 0; j < 8; j++) sp[ty][tx][j] = acc[j];
         __syncthreads();
         if (ty == 0 && g < cols / 8) {
 #pragma unroll
             for (int j = 0; j < 8; j++) {
                 float v = 0;
-                for (int y = 0; y < 8; y++) v += part[y][tx][j];
-                atomicAdd(&out[g * 8 + j], v);
+                for (int y = 0; y < 8; y++) v += sp[y][tx][j];
+                part[(size_t)blockIdx.x * cols + g * 8 + j] = v;
             }
         }
         __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(1024) k_colsum_final(const float *part, int blocks, int cols,
+                                                      float *out)
+{
+    __shared__ float sp[32][33];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int c = blockIdx.x * 32 + tx;
+    float v = 0;
+    if (c < cols)
+        for (int b = ty; b < blocks; b += 32) v += part[(size_t)b * cols + c];
+    sp[ty][tx] = v;
+    __syncthreads();
+    if (ty == 0 && c < cols) {
+        float t = 0;
+        for (int y = 0; y < 32; y++) t += sp[y][tx];
+        out[c] += t;
     }
 }
 
@@ -289,16 +331,26 @@ __global__ void k_compose_order(const SampleSrc *src, const long long *ranked, i
 extern "C" {
 
 /* out[c] += sum over rows of Y[r][c] (the bias gradient of a layer from
-   its output gradient). cols and ld multiples of 8, Y 16-byte aligned. */
-int pcagb_vnet_colsum(const void *Y, long long rows, int cols, int ld, float *out, int sms,
-                      void *stream)
+   its output gradient). cols and ld multiples of 8, Y 16-byte aligned;
+   part: scratch for pcagb_vnet_colsum_blocks(rows, sms) x cols floats. */
+int pcagb_vnet_colsum_blocks(long long rows, int sms)
+{
+    return (int)std::max<long long>(1, std::min<long long>((rows + 7) / 8,
+                                                           (long long)std::max(sms, 1) * 2));
+}
+
+int pcagb_vnet_colsum(const void *Y, long long rows, int cols, int ld, float *out, float *part,
+                      int sms, void *stream)
 {
     if (rows <= 0 || cols <= 0) return PCAGB_OK;
-    if (!Y || !out || (cols & 7) || (ld & 7) || ld < cols || ((uintptr_t)Y & 15))
+    if (!Y || !out || !part || (cols & 7) || (ld & 7) || ld < cols || ((uintptr_t)Y & 15))
         return PCAGB_EINVAL;
-    const long long blocks = std::min<long long>((rows + 7) / 8, (long long)std::max(sms, 1) * 8);
-    k_colsum<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>((const __nv_bfloat16 *)Y, rows,
-                                                                 cols, ld, out);
+    const int blocks = pcagb_vnet_colsum_blocks(rows, sms);
+    k_colsum_part<<<blocks, 256, 0, (cudaStream_t)stream>>>((const __nv_bfloat16 *)Y, rows, cols,
+                                                            ld, part);
+    int rc = launch_ok();
+    if (rc) return rc;
+    k_colsum_final<<<(cols + 31) / 32, 1024, 0, (cudaStream_t)stream>>>(part, blocks, cols, out);
     return launch_ok();
 }
 

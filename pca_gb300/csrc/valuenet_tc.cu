@@ -713,7 +713,22 @@ k_gemm_tc(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUt
         __syncwarp();
         const int per = 16 / esz;                 /* values per 16-byte piece */
         const int cpr = bn / per;                 /* pieces per row */
+        /* the mask's pieces of four iterations are loaded before any of
+           them is used, so each lane has four global loads in flight */
+        uint4 mkq[4];
         for (int it = lane; it < 32 * cpr; it += 32) {
+            const int u = ((it - lane) >> 5) & 3;
+            if (stage_mode == 1 && mask && u == 0) {
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    const int itk = it + 32 * k;
+                    const int rk = itk / cpr, gr = m0 + warp * 32 + rk;
+                    const int gc = n0 + (itk - rk * cpr) * per;
+                    mkq[k] = itk < 32 * cpr && gr < M && gc < N
+                                 ? *(const uint4 *)(mask + (size_t)gr * ldm + gc)
+                                 : make_uint4(0u, 0u, 0u, 0u);
+                }
+            }
             const int r = it / cpr, ch = it - r * cpr;
             const int grow = m0 + warp * 32 + r, gcol = n0 + ch * per;
             if (grow >= M || gcol >= N) continue;
@@ -721,7 +736,10 @@ k_gemm_tc(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUt
             if (stage_mode == 1) {
                 uint4 v = *(const uint4 *)src;
                 if (mask) {
-                    const uint4 mk = *(const uint4 *)(mask + (size_t)grow * ldm + gcol);
+                    uint4 mk = mkq[0];
+#pragma unroll
+                    for (int k = 1; k < 4; k++)
+                        if (u == k) mk = mkq[k];
                     /* keep a value where its mask half is a positive bf16 */
                     auto keep = [](uint32_t m) {
                         return (__uint_as_float(m << 16) > 0.f ? 0x0000FFFFu : 0u) |

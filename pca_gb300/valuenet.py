@@ -4,11 +4,12 @@ own BF16 tensor-core kernels (pca_gb300/csrc/valuenet.cu).
 torch provides device memory and the stream; every layer, gradient and
 optimizer update is one of the C kernels, called through the C ABI.
 
-Every matrix product runs on the fifth-generation tensor cores
-(pcagb_vnet_gemm_tc: TMA, tcgen05.mma into TMEM, FP32 accumulation): the
-forward layers, the input gradients (with the ReLU derivative applied in the
-epilogue) and the weight gradients, whose bias gradients come out of the
-same split-K GEMM as a column of ones appended to the layer input.
+Every matrix product runs on the fifth-generation tensor cores (TMA,
+tcgen05.mma into TMEM, FP32 accumulation): the forward layers and the input
+gradients (pcagb_vnet_gemm_tc, the ReLU derivative applied in the epilogue),
+and the weight gradients (pcagb_vnet_wgrad_tc: split-K, both operands read
+as stored, MN-major), whose bias gradients are the output gradients' column
+sums (pcagb_vnet_colsum).
 
 Network (the reference's ValueNetwork, python/model.py:16-84, with bit
 features): per-test encoder 176 -> 256 -> 256 (ReLU), mean + max pooling
@@ -39,7 +40,8 @@ def _lib():
     sigs = {
         "pcagb_vnet_gemm_tc": [vp, i, vp, i, vp, vp, i, vp, vp, i, i, i, i, i, i, vp, vp],
         "pcagb_vnet_wgrad_tc": [vp, i, vp, i, vp, i, i, i, i, i, vp, vp],
-        "pcagb_vnet_colsum": [vp, ctypes.c_longlong, i, i, vp, i, vp],
+        "pcagb_vnet_colsum": [vp, ctypes.c_longlong, i, i, vp, vp, i, vp],
+        "pcagb_vnet_colsum_blocks": [ctypes.c_longlong, i],
         "pcagb_vnet_features": [vp, vp, vp, i, i, vp, vp, vp, vp],
         "pcagb_vnet_pool": [vp, vp, vp, vp, vp, i, vp, vp, vp],
         "pcagb_vnet_pool_bwd": [vp, vp, vp, vp, vp, i, vp, vp],
@@ -147,8 +149,10 @@ class ValueNet:
         self._ck(self.lib.pcagb_vnet_wgrad_tc(
             _p(dY), dY.stride(0), _p(X), X.stride(0), _p(G), inp, out, inp, M, splits,
             _p(self._status_word()), self.stream))
-        self._ck(self.lib.pcagb_vnet_colsum(_p(dY), M, out, dY.stride(0), _p(db), self.sms,
-                                            self.stream))
+        part = torch.empty(self.lib.pcagb_vnet_colsum_blocks(M, self.sms) * out,
+                           device=self.dev, dtype=torch.float32)
+        self._ck(self.lib.pcagb_vnet_colsum(_p(dY), M, out, dY.stride(0), _p(db), _p(part),
+                                            self.sms, self.stream))
         return G, db
 
     def features(self, regs, flags, task, TP, task_io, task_T):

@@ -30,18 +30,22 @@ def _events():
 
 def case_engine_depths(reps: int):
     """is_power2 (32 tests) to kernel depth 4 with the suffix stage started
-    from level 1 and level 2 (suffix depths 3 and 2), and depth 3 from level
-    3 (the leaf check)."""
+    from level 1 and level 2 (suffix depths 3 and 2), each with a warp per
+    (prefix, chunk of 16 middles) and with a lane per innermost middle, and
+    depth 3 from level 3 (the leaf check)."""
     from pca_gb300.pcalib import Engine
     from pca_gb300.taskgen import is_power2_task
     eng = Engine(0, 4 << 30)
     task = is_power2_task()
     for _ in range(reps):
-        for split, depth in ((1, 4), (2, 4), (3, 3)):
+        for split, depth, chunk in ((1, 4, 16), (1, 4, 1024), (2, 4, 16), (2, 4, 1024),
+                                    (3, 3, 0)):
             t0 = time.perf_counter()
-            s = eng.solve(task, max_depth=depth, split_depth=split, sol_cap=1, count_levels=split == 3)
-            print(f"engine_depths split={split} depth={depth}: K*={s.optimal_depth} "
-                  f"{time.perf_counter() - t0:.4f} s, suffix {s.gpu_ms_suffix:.3f} ms", flush=True)
+            s = eng.solve(task, max_depth=depth, split_depth=split, sol_cap=1,
+                          count_levels=split == 3, suffix_chunk=chunk)
+            print(f"engine_depths split={split} depth={depth} shape={chunk or 'auto'}: "
+                  f"K*={s.optimal_depth} {time.perf_counter() - t0:.4f} s, "
+                  f"suffix {s.gpu_ms_suffix:.3f} ms", flush=True)
 
 
 def case_suffix_depth2(reps: int):

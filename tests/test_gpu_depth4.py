@@ -44,24 +44,31 @@ def check_levels(sol, want):
     assert sol.pruned_cum[:K + 1] == want["pruned_cum"]
 
 
+@pytest.mark.parametrize("shape", [1, 32], ids=["warp_per_prefix", "lane_per_prefix"])
 @pytest.mark.parametrize("mode,key", [(OEP_EXACT_LIVE, "exact_live"), (OEP_EXACT, "exact")])
-def test_is_power2_headline_step(engine, mode, key):
+def test_is_power2_headline_step(engine, mode, key, shape):
     fx = D4["is_power2"]
     want = fx[key]
     spec = spec_from_json(fx["task"])
-    sol = engine.solve(spec, max_depth=4, split_depth=3, oep_mode=mode, sol_cap=1 << 12)
+    sol = engine.solve(spec, max_depth=4, split_depth=3, oep_mode=mode, sol_cap=1 << 12,
+                       suffix_chunk=shape)
     assert sol.optimal_depth == want["optimal_depth"] == -1
     assert sol.total_solutions == 0 and sol.programs == []
     check_levels(sol, want)
 
 
+@pytest.mark.parametrize("shape", [1, 32], ids=["warp_per_prefix", "lane_per_prefix"])
 @pytest.mark.parametrize("i", range(len(TASKS)), ids=IDS)
-def test_synthetic_depth4_full_set(engine, i):
+def test_synthetic_depth4_full_set(engine, i, shape):
+    """Every solving program of the benchmarked configuration's last
+    position, scanned a warp per prefix or a lane per prefix (suffix_chunk
+    1 / 32), against the oracle's full set."""
     fx = TASKS[i]
     want = fx["exact_live"]
     spec = spec_from_json(fx["task"])
     cap = max(want["total_solutions"], 1)
-    sol = engine.solve(spec, max_depth=4, split_depth=3, oep_mode=OEP_EXACT_LIVE, sol_cap=cap)
+    sol = engine.solve(spec, max_depth=4, split_depth=3, oep_mode=OEP_EXACT_LIVE, sol_cap=cap,
+                       suffix_chunk=shape)
     assert sol.optimal_depth == want["optimal_depth"]
     assert sol.total_solutions == want["total_solutions"]
     assert sol.programs[:64] == want["programs"]
@@ -112,3 +119,22 @@ def test_batch_full_sets_one_input(engine):
         assert digest(sol.programs) == want["digest"]
         S = len(want["survivors"]) - 1
         assert sol.level_survivors[:S + 1] == want["survivors"]
+
+
+@pytest.mark.parametrize("split", [1, 2])
+def test_depth4_middle_shapes_agree(engine, split):
+    """The depth-4 stage from level 2 (two suffix instructions) and from
+    level 1 (three): a warp per (prefix, chunk of middles) and a lane per
+    innermost middle find the same full set, and the first-only answer is
+    the oracle's first program."""
+    for fx in [f for f in TASKS if f["exact_live"]["optimal_depth"] == 4][:6]:
+        want = fx["exact_live"]
+        spec = spec_from_json(fx["task"])
+        runs = [engine.solve(spec, max_depth=4, split_depth=split, oep_mode=OEP_EXACT_LIVE,
+                             sol_cap=1 << 16, suffix_chunk=ck) for ck in (16, 1024)]
+        assert runs[0].optimal_depth == runs[1].optimal_depth == 4
+        assert runs[0].total_solutions == runs[1].total_solutions
+        assert runs[0].programs == runs[1].programs
+        first = engine.solve(spec, max_depth=4, split_depth=split, first_only=True, sol_cap=1,
+                             suffix_chunk=1024)
+        assert first.programs == want["programs"][:1]

@@ -240,7 +240,9 @@ def test_tc_weight_gradient_mn_major(splits, out, inp):
     assert lib.pcagb_vnet_wgrad_tc(_p(dY), out, _p(X), inp, _p(G), inp, out, inp, M, splits,
                                    _p(st), s) == 0
     sms = torch.cuda.get_device_properties(0).multi_processor_count
-    assert lib.pcagb_vnet_colsum(_p(dY), M, out, out, _p(db), sms, s) == 0
+    part = torch.empty(lib.pcagb_vnet_colsum_blocks(M, sms) * out, device="cuda",
+                       dtype=torch.float32)
+    assert lib.pcagb_vnet_colsum(_p(dY), M, out, out, _p(db), _p(part), sms, s) == 0
     torch.cuda.synchronize()
     assert int(st.item()) == 0
     assert rel(G, dY.float().t() @ X.float()) < 1e-4

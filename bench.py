@@ -44,14 +44,17 @@ CANDIDATES = ("candidates as the reference's enumerator counts them (tools/enume
               "decides the last position's candidates by value classes (evaluations_run_per_s "
               "counts the class evaluations its kernels execute)")
 
-# The suffix kernel's capture (profiles/k_suffix_is_power2_t32_k4.md): warp
-# instructions of the depth-4 launch, valid for the kernel source it was
-# taken from (SHA-256 of pca_gb300/csrc/engine_kernels.cuh, first 16 hex).
-SUFFIX_CAPTURE = {"inst": 1255101666, "ms": 1.527168, "source_sha16": "205d10f9618ae177",
-                  "file": "profiles/k_suffix_is_power2_t32_k4.md"}
+# The suffix kernel's capture (profiles/k_suffix_lanes_is_power2_t32_k4.md):
+# warp instructions and DRAM bytes of the depth-4 launch (the autotuner's
+# choice there, a lane per prefix with two tests per lane), valid for the
+# kernel source it was taken from (SHA-256 of
+# pca_gb300/csrc/engine_kernels.cuh, first 16 hex).
+SUFFIX_CAPTURE = {"kernel": "k_suffix_lanes<32,2>", "inst": 313365006, "ms": 0.47264,
+                  "dram_bytes": 436963840 + 3024384, "source_sha16": "45d6c322c421d9ac",
+                  "file": "profiles/k_suffix_lanes_is_power2_t32_k4.md"}
 # The insert kernel's capture (profiles/k_expand_insert_is_power2_t32_level3.md):
 # DRAM bytes read + written by the level-3 launch (99.6% of a solve's children).
-INSERT_CAPTURE = {"dram_bytes": 529504000 + 169235200, "source_sha16": "205d10f9618ae177",
+INSERT_CAPTURE = {"dram_bytes": 530220032 + 169304576, "source_sha16": "45d6c322c421d9ac",
                   "file": "profiles/k_expand_insert_is_power2_t32_level3.md"}
 
 
@@ -282,20 +285,23 @@ def insert_roofline(sol, T: int, insert_ms: float, hbm_gbs: float, pk_kind: str)
             "bytes_model": "per child 8 B slot + per duplicate 17*T B compare + per parent 17*T B"}
 
 
-def suffix_roofline(suffix_ms: float, peak_issue: float, evals_run_per_s: float) -> dict:
-    """k_suffix<32,1> against the integer-issue roofline (one warp
+def suffix_roofline(suffix_ms: float, peak_issue: float, evals_run_per_s: float,
+                    hbm_gbs: float) -> dict:
+    """The last-position kernel against the integer-issue roofline (one warp
     instruction per SM sub-partition per clock): the warp instructions of its
-    ncu capture over the live launch time, valid while the kernel source is
-    the captured one."""
+    ncu capture over the live stage time (the kernel and the evaluation
+    count) and over the captured launch time, valid while the kernel source
+    is the captured one; beside it the launch's DRAM bytes against HBM."""
     fresh = kernel_source_sha16() == SUFFIX_CAPTURE["source_sha16"]
-    out = {"kernel": "k_suffix<32,1> (last instruction over value classes)",
+    out = {"kernel": SUFFIX_CAPTURE["kernel"] + " (last instruction over operand pairs)",
            "bound": "int_issue", "unit": "Gwarp-inst/s", "peak": peak_issue / 1e9,
            "evaluations_run_per_s": evals_run_per_s, "ncu": SUFFIX_CAPTURE["file"]}
     if fresh and suffix_ms > 0:
         ach = SUFFIX_CAPTURE["inst"] / (suffix_ms / 1000.0)
+        cap_s = SUFFIX_CAPTURE["ms"] / 1000.0
         out.update({"achieved": ach / 1e9, "frac": ach / peak_issue,
-                    "frac_in_capture": SUFFIX_CAPTURE["inst"] / (SUFFIX_CAPTURE["ms"] / 1000.0)
-                    / peak_issue})
+                    "frac_in_capture": SUFFIX_CAPTURE["inst"] / cap_s / peak_issue,
+                    "hbm_frac_in_capture": SUFFIX_CAPTURE["dram_bytes"] / cap_s / 1e9 / hbm_gbs})
     else:
         out.update({"achieved": None, "frac": None,
                     "note": "kernel source changed since the capture: no instruction count"})
@@ -1032,7 +1038,8 @@ def main():
     # and the suffix kernel against integer issue
     line["roofline"] = insert_roofline(sol, task.num_tests, insert_ms / args.steps,
                                        pk["hbm_gbs"], pk_kind)
-    line["roofline_suffix"] = suffix_roofline(suffix_ms / args.steps, peak_issue, evals_run_per_s)
+    line["roofline_suffix"] = suffix_roofline(suffix_ms / args.steps, peak_issue, evals_run_per_s,
+                                              pk["hbm_gbs"])
     line["roofline_suffix"]["peak_source"] = (f"{sms} SMs x 4 issue slots x sm_max_mhz of "
                                               f"MEASURED_PEAKS.json ({pk_kind})")
     if not args.no_cpu_baseline:

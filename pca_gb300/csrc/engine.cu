@@ -704,6 +704,9 @@ constexpr uint32_t kLaneShape = 1024;
 constexpr uint32_t kChunkChoices[4][4] = {
     {1, 1, 1, 1}, {1, 32, 1, 32}, {8, 16, 32, kLaneShape}, {1, 2, 4, kLaneShape}};
 constexpr int kChunkOptions[4] = {1, 2, 4, 4};
+/* below this many prefixes a level gives a lane-per-prefix launch fewer
+   warps than the SMs hold: the depth-1 default is then a warp per prefix */
+constexpr uint64_t kLanesMinPrefixes = 32ull * 152 * 4;
 /* A stage is large enough to measure a launch choice on; each choice is
    measured this many times before the cheapest is kept. */
 constexpr uint64_t kTuneMinEvals = 20000000ull;
@@ -815,7 +818,14 @@ int run_stage(pcagb_engine *e, int S, int K, std::vector<TaskRun> &runs, bool fi
                 /* shapes are explored once the tests-per-lane choice is */
                 const bool ft_done = e->ft_n[s][1] >= kTuneSamples &&
                                      e->ft_n[s][2] >= kTuneSamples && e->ft_n[s][3] >= kTuneSamples;
-                ck = pick_option(e->ck_ms[s], e->ck_n[s], kChunkOptions[s], s == 2 ? 1 : 0,
+                /* unmeasured, the lane shapes: a stage that is not timed
+                   (an ordered or chunked first-only stage, or one too small
+                   to explore on) keeps its default, and the lanes measured
+                   2.3-3x faster on every stage that was timed; at depth 1 a
+                   level too small to fill the GPU with 32 prefixes a warp
+                   stays a warp per prefix */
+                const int def = s == 1 ? (L.n >= kLanesMinPrefixes ? 1 : 0) : 3;
+                ck = pick_option(e->ck_ms[s], e->ck_n[s], kChunkOptions[s], def,
                                  explore && ft_done);
                 chunk = kChunkChoices[s][ck];
             }

@@ -784,6 +784,24 @@ k_gemm_tc(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUt
             tmem_ld32(tmem + lane_base + (uint32_t)c0, acc);
             if (row >= M) continue;
             const int colb = n0 + c0;
+            if (atomic_out == 2) {
+                /* this K split's own slab: plain stores, summed later in
+                   split order (deterministic) */
+                float *dst = Cf + ((size_t)blockIdx.z * M + row) * ldc + colb;
+#pragma unroll
+                for (int j = 0; j < 32; j += 4) {
+                    if (vec_atomic && colb + j + 3 < N) {
+                        *(float4 *)(dst + j) =
+                            make_float4(__uint_as_float(acc[j]), __uint_as_float(acc[j + 1]),
+                                        __uint_as_float(acc[j + 2]), __uint_as_float(acc[j + 3]));
+                    } else {
+#pragma unroll
+                        for (int q = 0; q < 4; q++)
+                            if (colb + j + q < N) dst[j + q] = __uint_as_float(acc[j + q]);
+                    }
+                }
+                continue;
+            }
             if (atomic_out) {
                 float *dst = Cf + (size_t)row * ldc + colb;
 #pragma unroll
@@ -963,14 +981,39 @@ bool tile_map_mn(CUtensorMap *m, const void *ptr, int krows, int cols, int ld)
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+/* C[i] += the `splits` slabs' values at i, in slab order. */
+__global__ void k_split_sum(const float *part, int splits, size_t count, float *C)
+{
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+         i += (size_t)gridDim.x * blockDim.x) {
+        float v = 0.f;
+        for (int z = 0; z < splits; z++) v += part[(size_t)z * count + i];
+        C[i] += v;
+    }
+}
+
+/* The number of K splits pcagb_vnet_wgrad_tc uses for this shape when asked
+ * for `splits` (its partial buffer holds that many [M][ldc] slabs). */
+extern "C" int pcagb_vnet_wgrad_splits(int K, int splits)
+{
+    const int kblocks = (K + kGBK - 1) / kGBK;
+    if (splits < 1) splits = 1;
+    if (splits > kblocks) splits = kblocks;
+    const int per = (kblocks + splits - 1) / splits;
+    return (kblocks + per - 1) / per;
+}
+
 /* Weight gradient on tcgen05 without transposes: C[M][N] += dY^T . X over
  * K rows, dY [K][M] (leading dimension ldy) and X [K][N] (ldx) read as
- * stored (MN-major operands), fp32 partial sums of `splits` K ranges added
- * into C (zeroed by the caller, leading dimension ldc). ldy and ldx are
- * multiples of 8 elements, dY and X 16-byte aligned. */
+ * stored (MN-major operands), with the K rows in `splits` ranges. With
+ * `part` (pcagb_vnet_wgrad_splits(K, splits) slabs of M x ldc floats) each
+ * range writes its own slab and the slabs are added into C in range order,
+ * so the result is the same on every run; without it the ranges' fp32 sums
+ * are added into C atomically. C is zeroed by the caller (leading dimension
+ * ldc). ldy and ldx are multiples of 8 elements, dY and X 16-byte aligned. */
 extern "C" int pcagb_vnet_wgrad_tc(const void *dY, int ldy, const void *X, int ldx, float *C,
-                                   int ldc, int M, int N, int K, int splits, int *status,
-                                   void *stream)
+                                   int ldc, int M, int N, int K, int splits, float *part,
+                                   int *status, void *stream)
 {
     if (M <= 0 || N <= 0 || K <= 0) return PCAGB_OK;
     if (!dY || !X || !C || !status || (ldy & 7) || (ldx & 7) || ldy < M || ldx < N ||
@@ -996,12 +1039,20 @@ extern "C" int pcagb_vnet_wgrad_tc(const void *dY, int ldy, const void *X, int l
                                         kGStages * (kGABytes + 256 * 128) + 256 + 2048);
     });
     if (attr_err != cudaSuccess) return PCAGB_ECUDA;
-    const int vec_atomic = ldc % 4 == 0 && !((uintptr_t)C & 15);
+    float *out = part ? part : C;
+    const int vec_atomic = ldc % 4 == 0 && !((uintptr_t)out & 15);
     dim3 grid((N + bn - 1) / bn, (M + kGRows - 1) / kGRows, splits);
     k_gemm_tc<<<grid, 128, smem, (cudaStream_t)stream>>>(
-        ma, mb, nullptr, nullptr, 0, nullptr, C, ldc, M, N, kblocks, per, bn, idesc, tcols, 0, 1,
-        0, vec_atomic, 1, status);
-    return cudaGetLastError() == cudaSuccess ? PCAGB_OK : PCAGB_ECUDA;
+        ma, mb, nullptr, nullptr, 0, nullptr, out, ldc, M, N, kblocks, per, bn, idesc, tcols, 0,
+        part ? 2 : 1, 0, vec_atomic, 1, status);
+    if (cudaGetLastError() != cudaSuccess) return PCAGB_ECUDA;
+    if (part) {
+        const size_t count = (size_t)M * ldc;
+        const unsigned blocks = (unsigned)std::min<size_t>((count + 255) / 256, 4096);
+        k_split_sum<<<blocks, 256, 0, (cudaStream_t)stream>>>(part, splits, count, C);
+        if (cudaGetLastError() != cudaSuccess) return PCAGB_ECUDA;
+    }
+    return PCAGB_OK;
 }
 
 

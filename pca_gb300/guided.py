@@ -181,19 +181,30 @@ class ValueOrder:
     many prefixes spread over it (prefix (a * i + b) mod n for sample i, a
     coprime to n, a and b drawn per level): the order is the sample by
     decreasing score, then every other prefix in the same map's order (a
-    permutation of the whole level). A stage expected to take at least
-    `full_gain` times the cost of scoring the whole level (a deep stage:
-    seconds against milliseconds) has its whole level ranked instead. The first correct program usually sits
+    permutation of the whole level). The first correct program usually sits
     in the first few percent of a good order, so the ranked sample decides
     the first launches at a fraction of the scoring cost. The ranking (the
     gather of the sample, the fused encoder, the trunk and the sort) is a
     CUDA graph captured once per test width and task table and replayed on
     the engine's stream; the level's addresses reach it through a small
-    device buffer, so one replay and one order kernel serve any level."""
+    device buffer, so one replay and one order kernel serve any level. A
+    stage expected to take at least `full_gain` times the cost of scoring
+    the whole level (a deep stage: seconds against milliseconds) has its
+    whole level ranked instead.
+
+    The score of a state is the logit of "finishes optimally"; for a long
+    stage, ranked whole, with `steps_head` also the log-probability the
+    steps head gives a positive state for finishing in exactly the stage's
+    remaining instructions (target depth - level depth): a state that can
+    finish, but only in more steps, ranks lower. `net` may be a list of networks: the whole-level ranking
+    then orders by the sum of their scores; a sampled ranking uses the
+    first."""
 
     def __init__(self, net: ValueNet, chunk_states=1 << 20, min_states=4096, gain=2.0,
-                 fixed_ms=0.25, states_per_ms=1.0e5, sample=None, seed=0, full_gain=50.0):
-        self.net = net
+                 fixed_ms=0.25, states_per_ms=1.0e5, sample=None, seed=0, full_gain=50.0,
+                 steps_head=True):
+        self.nets = list(net) if isinstance(net, (list, tuple)) else [net]
+        self.net = self.nets[0]
         self.chunk_states = chunk_states
         self.min_states = min_states
         self.gain, self.fixed_ms, self.states_per_ms = gain, fixed_ms, states_per_ms
@@ -202,6 +213,10 @@ class ValueOrder:
         # full_gain x the cost of scoring its whole level is ranked whole
         # (None: always sampled)
         self.full_gain = full_gain
+        # whole-level ranking: add the log-probability the steps head gives
+        # a positive state for finishing in exactly the stage's remaining
+        # instructions (target depth - level depth)
+        self.steps_head = steps_head
         self.rng = random.Random(seed)
         self.score_ms = 0.0
         self._cache = {}
@@ -221,10 +236,15 @@ class ValueOrder:
         n = view.n
         if n < self.min_states:
             return None
-        key = (view.regs, n, view.depth)
+        # a long stage (full_gain x the cost of scoring its whole level) is
+        # ranked whole and for its own remaining depth; a short one reuses
+        # its level's order across depths
+        long_stage = self.full_gain is not None and \
+            view.est_stage_ms >= self.full_gain * (self.fixed_ms + n / self.states_per_ms)
+        rem = view.target_depth - view.depth if self.steps_head and long_stage else -1
+        key = (view.regs, n, view.depth, rem)
         scored = n if not self.sample else min(n, self.sample)
-        if scored < n and self.full_gain is not None and \
-                view.est_stage_ms >= self.full_gain * (self.fixed_ms + n / self.states_per_ms):
+        if scored < n and long_stage:
             scored = n
         if key not in self._cache and \
                 view.est_stage_ms < self.gain * (self.fixed_ms + scored / self.states_per_ms):
@@ -259,12 +279,20 @@ class ValueOrder:
                 live = _device_view(view.live + b0, m, torch.uint8, dev)
                 task = _device_view(view.task + b0 * 2, m, torch.int16, dev)
                 depth = torch.full((m,), view.depth, device=dev, dtype=torch.uint8)
-                scores[b0:b0 + m] = self.net.forward_fused(regs, flags, live, task, depth, tp,
-                                                           task_io, task_T)[:, 0]
+                sc = None
+                for nt in self.nets:
+                    L = nt.forward_fused(regs, flags, live, task, depth, tp, task_io,
+                                         task_T).float()
+                    lg = L[:, 0]
+                    if 0 <= rem <= 8:
+                        lg = lg + torch.log_softmax(L[:, 1:10], dim=1)[:, rem]
+                    sc = lg if sc is None else sc + lg
+                scores[b0:b0 + m] = sc
             order = torch.argsort(scores, descending=True, stable=True).to(torch.int32)
             ev1.record(stream)
         ev1.synchronize()
-        self.net.check_status()
+        for nt in self.nets:
+            nt.check_status()
         self.score_ms += ev0.elapsed_time(ev1)
         self._cache = {key: order}
         return order

@@ -39,7 +39,8 @@ def _lib():
     sz = ctypes.c_size_t
     sigs = {
         "pcagb_vnet_gemm_tc": [vp, i, vp, i, vp, vp, i, vp, vp, i, i, i, i, i, i, vp, vp],
-        "pcagb_vnet_wgrad_tc": [vp, i, vp, i, vp, i, i, i, i, i, vp, vp],
+        "pcagb_vnet_wgrad_tc": [vp, i, vp, i, vp, i, i, i, i, i, vp, vp, vp],
+        "pcagb_vnet_wgrad_splits": [i, i],
         "pcagb_vnet_colsum": [vp, ctypes.c_longlong, i, i, vp, vp, i, vp],
         "pcagb_vnet_colsum_blocks": [ctypes.c_longlong, i],
         "pcagb_vnet_features": [vp, vp, vp, i, i, vp, vp, vp, vp],
@@ -145,9 +146,13 @@ class ValueNet:
         bn = 256 if inp > 192 else (inp + 63) // 64 * 64
         tiles = ((out + 127) // 128) * ((inp + bn - 1) // bn)
         kblocks = (M + 63) // 64
-        splits = max(1, min(kblocks, (2 * self.sms) // max(tiles, 1)))
+        splits = self.lib.pcagb_vnet_wgrad_splits(
+            M, max(1, min(kblocks, (2 * self.sms) // max(tiles, 1))))
+        # each K split writes its own slab, added in split order: the same
+        # gradients (and so the same network) on every run
+        part = torch.empty(splits * out * inp, device=self.dev, dtype=torch.float32)
         self._ck(self.lib.pcagb_vnet_wgrad_tc(
-            _p(dY), dY.stride(0), _p(X), X.stride(0), _p(G), inp, out, inp, M, splits,
+            _p(dY), dY.stride(0), _p(X), X.stride(0), _p(G), inp, out, inp, M, splits, _p(part),
             _p(self._status_word()), self.stream))
         part = torch.empty(self.lib.pcagb_vnet_colsum_blocks(M, self.sms) * out,
                            device=self.dev, dtype=torch.float32)

@@ -781,6 +781,11 @@ int run_stage(pcagb_engine *e, int S, int K, std::vector<TaskRun> &runs, bool fi
     CK(cudaMemsetAsync(e->d_small + 1, 0xFF, 8, e->stream));
     SolBuf sb{e->d_small, e->d_sol, e->sol_cap, e->d_small + 1, e->d_small + 3};
     int tuned_ft = 0, tuned_ck = -1;   /* the launch choices this stage used */
+    /* launch choices are explored and timed on single-task stages only: a
+       batch's stage mixes tasks (and, in a server, shares the GPU with
+       other solves), so its times would not compare choices */
+    int nact_stage = 0;
+    for (size_t i = 0; i < e->h_active.size(); i++) nact_stage += e->h_active[i] ? 1 : 0;
     bool stopped_early = false;
     cudaEventRecord(e->ev0, e->stream);
     const bool t16 = e->TPC == 16;
@@ -802,7 +807,7 @@ int run_stage(pcagb_engine *e, int S, int K, std::vector<TaskRun> &runs, bool fi
             }
         /* launch choices: forced by the caller, else the cheapest measured
            (an unmeasured one is tried first on a stage large enough) */
-        const bool explore = evals_pred >= kTuneMinEvals && !so;
+        const bool explore = evals_pred >= kTuneMinEvals && !so && nact_stage == 1;
         int ft = e->force_ft;
         if (ft < 1 || ft > 3) ft = 1 + pick_option(&e->ft_ms[s][1], &e->ft_n[s][1], 3, 1, explore);
         int ck = -1;
@@ -974,7 +979,7 @@ int run_stage(pcagb_engine *e, int S, int K, std::vector<TaskRun> &runs, bool fi
         if (evals > 10000000ull) {
             const double per = ms / (double)evals;
             e->t_eval_ms[s] = 0.7 * e->t_eval_ms[s] + 0.3 * per;
-            if (evals >= kTuneMinEvals && s <= 3) {
+            if (evals >= kTuneMinEvals && s <= 3 && nact_stage == 1) {
                 if (tuned_ft >= 1) record_cost(e->ft_ms[s][tuned_ft], e->ft_n[s][tuned_ft], per);
                 if (tuned_ck >= 0) record_cost(e->ck_ms[s][tuned_ck], e->ck_n[s][tuned_ck], per);
             }

@@ -13,8 +13,9 @@
  *     one, it waits until a running solve releases memory.
  *   - Concurrent solves. Each worker thread drives one engine on its own
  *     CUDA stream, so the kernels of different solves overlap on the device;
- *     a worker that finds several requests queued takes up to max_batch of
- *     them into one batched solve (shared launches, one arena).
+ *     a worker that finds several requests queued takes the head request and
+ *     up to max_batch - 1 more of the same test width (16 or 32) in arrival
+ *     order into one batched solve (shared launches, one arena).
  *   - Per-request delivery. A request's answer is stored as soon as its own
  *     task is decided, before its batch ends, and pcagb_server_next hands
  *     out completions in the order they happen.
@@ -218,10 +219,21 @@ void pcagb_server::worker(int w)
                     cv_work.wait_for(lk, std::chrono::milliseconds(200));
                     continue;
                 }
+                /* the head request, then (with room for a batch) the queued
+                   requests of its test width in arrival order: a batch's
+                   states hold the width of its widest task, so a 16-test task
+                   in a 32-wide batch would do twice its work */
                 const size_t take = bytes == per ? 1 : k;
-                for (size_t i = 0; i < take; i++) {
-                    batch.push_back(queue.front());
-                    queue.pop_front();
+                const bool wide = queue.front()->task.num_tests > 16;
+                batch.push_back(queue.front());
+                queue.pop_front();
+                for (auto it = queue.begin(); it != queue.end() && batch.size() < take;) {
+                    if (((*it)->task.num_tests > 16) == wide) {
+                        batch.push_back(*it);
+                        it = queue.erase(it);
+                    } else {
+                        ++it;
+                    }
                 }
                 break;
             }

@@ -49,7 +49,7 @@ CANDIDATES = ("candidates as the reference's enumerator counts them (tools/enume
 # choice there, a lane per prefix with two tests per lane), valid for the
 # kernel source it was taken from (SHA-256 of
 # pca_gb300/csrc/engine_kernels.cuh, first 16 hex).
-SUFFIX_CAPTURE = {"kernel": "k_suffix_lanes<32,2>", "inst": 313365006, "ms": 0.47264,
+SUFFIX_CAPTURE = {"kernel": "k_suffix_lanes<32,2>", "choice": (2, 32), "inst": 313365006, "ms": 0.47264,
                   "dram_bytes": 436963840 + 3024384, "source_sha16": "45d6c322c421d9ac",
                   "file": "profiles/k_suffix_lanes_is_power2_t32_k4.md"}
 # The insert kernel's capture (profiles/k_expand_insert_is_power2_t32_level3.md):
@@ -285,26 +285,46 @@ def insert_roofline(sol, T: int, insert_ms: float, hbm_gbs: float, pk_kind: str)
             "bytes_model": "per child 8 B slot + per duplicate 17*T B compare + per parent 17*T B"}
 
 
-def suffix_roofline(suffix_ms: float, peak_issue: float, evals_run_per_s: float,
-                    hbm_gbs: float) -> dict:
+def tuned_depth1_choice(tuning: dict) -> tuple[int, int]:
+    """The tests per lane and the depth-1 shape (1: warp per prefix, 32:
+    lane per prefix) the autotuner keeps once explored: the cheapest
+    measured option."""
+    def best(ms, n):
+        got = [(m, i) for i, (m, k) in enumerate(zip(ms, n)) if k > 0]
+        return min(got)[1] if got else -1
+    ft = best(tuning["first_tests_ms"][1][1:], tuning["first_tests_n"][1][1:]) + 1
+    ck = best(tuning["chunk_ms"][1][:2], tuning["chunk_n"][1][:2])
+    return ft, (tuning["chunk_choices"][1][ck] if ck >= 0 else 0)
+
+
+def suffix_roofline(kernel_ms: float, stage_ms: float, peak_issue: float, evals_run_per_s: float,
+                    hbm_gbs: float, tuning: dict) -> dict:
     """The last-position kernel against the integer-issue roofline (one warp
     instruction per SM sub-partition per clock): the warp instructions of its
-    ncu capture over the live stage time (the kernel and the evaluation
-    count) and over the captured launch time, valid while the kernel source
-    is the captured one; beside it the launch's DRAM bytes against HBM."""
+    ncu capture (the kernel-depth-4 launch) over that launch's live device
+    time (CUDA events around the kernel alone, mean over the timed steps) and
+    over the captured launch time, valid while the kernel source is the
+    captured one; beside it the launch's DRAM bytes against HBM and the whole
+    last-position stage time (the kernel, its evaluation count and the
+    shallower depths' stages)."""
     fresh = kernel_source_sha16() == SUFFIX_CAPTURE["source_sha16"]
+    ft, shape = tuned_depth1_choice(tuning)
+    same = (ft, shape) == SUFFIX_CAPTURE["choice"]
     out = {"kernel": SUFFIX_CAPTURE["kernel"] + " (last instruction over operand pairs)",
            "bound": "int_issue", "unit": "Gwarp-inst/s", "peak": peak_issue / 1e9,
-           "evaluations_run_per_s": evals_run_per_s, "ncu": SUFFIX_CAPTURE["file"]}
-    if fresh and suffix_ms > 0:
-        ach = SUFFIX_CAPTURE["inst"] / (suffix_ms / 1000.0)
+           "evaluations_run_per_s": evals_run_per_s, "ncu": SUFFIX_CAPTURE["file"],
+           "kernel_ms_live": kernel_ms, "suffix_stages_ms_per_step": stage_ms}
+    if fresh and same and kernel_ms > 0:
+        ach = SUFFIX_CAPTURE["inst"] / (kernel_ms / 1000.0)
         cap_s = SUFFIX_CAPTURE["ms"] / 1000.0
         out.update({"achieved": ach / 1e9, "frac": ach / peak_issue,
                     "frac_in_capture": SUFFIX_CAPTURE["inst"] / cap_s / peak_issue,
                     "hbm_frac_in_capture": SUFFIX_CAPTURE["dram_bytes"] / cap_s / 1e9 / hbm_gbs})
     else:
         out.update({"achieved": None, "frac": None,
-                    "note": "kernel source changed since the capture: no instruction count"})
+                    "note": ("kernel source changed since the capture" if not fresh else
+                             f"the autotuner ran tests per lane {ft}, shape {shape}, not the "
+                             "captured instantiation") + ": no instruction count"})
     return out
 
 
@@ -965,6 +985,7 @@ def main():
     dev_ms, wall_s, cands, evals, evals_run = [], [], 0, 0, 0
     launches, h2d, d2h = 0, 0, 0
     insert_ms, insert_n, insert_children, suffix_ms, suffix_n = 0.0, 0, 0, 0.0, 0
+    lanes_ms = 0.0
     expand_ms = 0.0
     sol = None
     for _ in range(args.steps):
@@ -992,6 +1013,8 @@ def main():
         insert_children += sol.insert_children
         suffix_ms += sol.gpu_ms_suffix
         suffix_n += sol.suffix_launches
+        if len(sol.gpu_ms_lanes) > args.max_depth:
+            lanes_ms += sol.gpu_ms_lanes[args.max_depth]
     torch.cuda.synchronize()
     if world > 1:
         dist.barrier()
@@ -1038,8 +1061,9 @@ def main():
     # and the suffix kernel against integer issue
     line["roofline"] = insert_roofline(sol, task.num_tests, insert_ms / args.steps,
                                        pk["hbm_gbs"], pk_kind)
-    line["roofline_suffix"] = suffix_roofline(suffix_ms / args.steps, peak_issue, evals_run_per_s,
-                                              pk["hbm_gbs"])
+    line["roofline_suffix"] = suffix_roofline(lanes_ms / args.steps, suffix_ms / args.steps,
+                                              peak_issue, evals_run_per_s, pk["hbm_gbs"],
+                                              line["autotuner"])
     line["roofline_suffix"]["peak_source"] = (f"{sms} SMs x 4 issue slots x sm_max_mhz of "
                                               f"MEASURED_PEAKS.json ({pk_kind})")
     if not args.no_cpu_baseline:

@@ -201,7 +201,11 @@ typedef struct {
                            stage; n > 0 = a first launch of n prefixes in DFS
                            order, doubling, stopping at the first launch that
                            holds a solution                                  */
-    int reserved[3];
+    int shared_gpu;     /* 1: the solve shares the GPU with other solves (a
+                           server's): its stage times measure the mix, so
+                           they update none of the autotuner's costs and no
+                           launch choice is explored on it                   */
+    int reserved[2];
 } pcagb_opts_t;
 
 #define PCAGB_MAXD 17
@@ -240,6 +244,11 @@ typedef struct {
                                           operand pair counts one); below
                                           `evaluations`, which counts every
                                           class of the candidate space       */
+    double   gpu_ms_lanes[PCAGB_MAXD]; /* per target depth: device time of the
+                                          lane-per-prefix last-position kernel
+                                          alone (without the stage's other
+                                          passes) where the stage ran it in
+                                          one launch, else 0                 */
 } pcagb_result_t;
 
 const char *pcagb_last_error(void);

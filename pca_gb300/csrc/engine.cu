@@ -144,6 +144,7 @@ struct pcagb_engine {
     unsigned long long *h_pin = nullptr;
     std::vector<uint8_t> h_active;           /* host copy of d_task_active */
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
+    cudaEvent_t evk0 = nullptr, evk1 = nullptr;   /* around a lane-per-prefix launch */
     int occ_insert = 4, occ_suffix = 8, occ_mat = 4, occ_lanes = 4,
         occ_mid_lanes = 4;   /* resident blocks per SM */
     uint64_t launches = 0;
@@ -151,6 +152,7 @@ struct pcagb_engine {
     uint64_t insert_launches = 0, suffix_launches = 0, insert_children = 0;
     uint64_t evals_run = 0;                  /* value-class evaluations the suffix kernels ran */
     float ms_insert = 0;
+    double ms_lanes[PCAGB_MAXD] = {};        /* lane-per-prefix kernel device time per depth */
     /* autotuner: unit costs measured on this engine (running averages) */
     /* starting values: this engine's costs measured on a GB300 (one- and
        two-input depth-4 searches); every solve refines them */
@@ -167,6 +169,8 @@ struct pcagb_engine {
     int ck_n[4][4] = {};
     double launch_rt_ms = 0.03;     /* host round trip of one launch of a chunked stage */
     int force_ft = 0, force_chunk = 0;   /* per solve: pcagb_opts_t overrides */
+    bool measure = true;                 /* per solve: the GPU is its own (not
+                                            shared_gpu), so its times are costs */
 
     /* per batch */
     std::vector<Level> levels;
@@ -547,7 +551,9 @@ int build_level(pcagb_engine *e, int d)
     cudaEventElapsedTime(&ms, e->ev0, e->ev1);
     e->ms_expand += ms;
     e->top = top0;
-    if (children > 100000) {
+    if (!e->measure) {
+        /* a shared GPU: the build's time is the mix's, not a cost */
+    } else if (children > 100000) {
         const double per = std::max(0.0, (ms - e->t_build_fixed_ms) / (double)children);
         e->t_child_ms = 0.7 * e->t_child_ms + 0.3 * per;
         if (!e->no_oep) e->dedup_ratio = 0.7 * e->dedup_ratio + 0.3 * ((double)survivors / children);
@@ -781,6 +787,7 @@ int run_stage(pcagb_engine *e, int S, int K, std::vector<TaskRun> &runs, bool fi
     CK(cudaMemsetAsync(e->d_small + 1, 0xFF, 8, e->stream));
     SolBuf sb{e->d_small, e->d_sol, e->sol_cap, e->d_small + 1, e->d_small + 3};
     int tuned_ft = 0, tuned_ck = -1;   /* the launch choices this stage used */
+    int lane_launches = 0;             /* lane-per-prefix launches of this stage */
     /* launch choices are explored and timed on single-task stages only: a
        batch's stage mixes tasks (and, in a server, shares the GPU with
        other solves), so its times would not compare choices */
@@ -807,7 +814,7 @@ int run_stage(pcagb_engine *e, int S, int K, std::vector<TaskRun> &runs, bool fi
             }
         /* launch choices: forced by the caller, else the cheapest measured
            (an unmeasured one is tried first on a stage large enough) */
-        const bool explore = evals_pred >= kTuneMinEvals && !so && nact_stage == 1;
+        const bool explore = evals_pred >= kTuneMinEvals && !so && nact_stage == 1 && e->measure;
         int ft = e->force_ft;
         if (ft < 1 || ft > 3) ft = 1 + pick_option(&e->ft_ms[s][1], &e->ft_n[s][1], 3, 1, explore);
         int ck = -1;
@@ -847,8 +854,12 @@ int run_stage(pcagb_engine *e, int S, int K, std::vector<TaskRun> &runs, bool fi
             if (s == 1) {
                 if (chunk == 32) {
                     const int gl = e->grid(e->occ_lanes);
+                    /* the kernel's own device time (without the count pass) */
+                    cudaEventRecord(e->evk0, e->stream);
                     if (t16) launch_suffix_lanes<16>(ft, gl, e->stream, V, e->td, sb, R);
                     else launch_suffix_lanes<32>(ft, gl, e->stream, V, e->td, sb, R);
+                    cudaEventRecord(e->evk1, e->stream);
+                    lane_launches++;
                 } else {
                     if (t16) launch_suffix<16, 1>(ft, g, e->stream, V, e->td, sb, 1, 1, R);
                     else launch_suffix<32, 1>(ft, g, e->stream, V, e->td, sb, 1, 1, R);
@@ -946,7 +957,7 @@ int run_stage(pcagb_engine *e, int S, int K, std::vector<TaskRun> &runs, bool fi
                        device work is what the next launch pays in idle time */
                     const double rt = std::chrono::duration<double, std::milli>(
                                           std::chrono::steady_clock::now() - h0).count();
-                    e->launch_rt_ms = 0.9 * e->launch_rt_ms + 0.1 * std::min(rt, 1.0);
+                    if (e->measure) e->launch_rt_ms = 0.9 * e->launch_rt_ms + 0.1 * std::min(rt, 1.0);
                     if (e->h_pin[kPinCount]) {
                         so->prefixes_to_first = R.begin + R.count;
                         cudaEventElapsedTime(&so->ms_to_first, e->ev0, e->ev1);
@@ -970,7 +981,13 @@ int run_stage(pcagb_engine *e, int S, int K, std::vector<TaskRun> &runs, bool fi
     cudaEventElapsedTime(&ms, e->ev0, e->ev1);
     e->ms_suffix += ms;
     e->suffix_launches++;
-    if (s >= 1 && !stopped_early && !(so && so->order)) {
+    if (lane_launches == 1 && K < PCAGB_MAXD) {
+        /* one launch: its events bracket it alone */
+        float mk = 0;
+        cudaEventElapsedTime(&mk, e->evk0, e->evk1);
+        e->ms_lanes[K] += mk;
+    }
+    if (s >= 1 && !stopped_early && !(so && so->order) && e->measure) {
         /* value-class evaluations of this stage, for the autotuner */
         const std::vector<uint64_t> &g = gt.ev[s];
         uint64_t evals = 0;
@@ -1261,12 +1278,16 @@ int run_batch(pcagb_engine *e, std::vector<TaskRun> &runs, const pcagb_opts_t &o
     e->bottom = 0;
     e->top = e->cap;
     e->ms_expand = e->ms_suffix = e->ms_insert = 0;
+    std::fill(e->ms_lanes, e->ms_lanes + PCAGB_MAXD, 0.0);
     e->launches = 0;
     e->h2d = e->d2h = 0;
     e->insert_launches = e->suffix_launches = e->insert_children = 0;
     e->evals_run = 0;
     e->force_ft = o.first_tests;
     e->force_chunk = o.suffix_chunk;
+    e->measure = o.shared_gpu == 0;
+    /* a shared solve takes the costs its device's unshared solves measured */
+    if (!e->measure) load_costs(e);
     e->max_feasible = SEARCH_MAX_DEPTH;
     int maxT = 0, maxK = 0;
     for (TaskRun &tr : runs) {
@@ -1549,12 +1570,13 @@ int run_batch(pcagb_engine *e, std::vector<TaskRun> &runs, const pcagb_opts_t &o
         tr.res.suffix_launches = e->suffix_launches;
         tr.res.insert_children = e->insert_children;
         tr.res.evaluations_run = e->evals_run;
+        std::copy(e->ms_lanes, e->ms_lanes + PCAGB_MAXD, tr.res.gpu_ms_lanes);
         tr.res.h2d_bytes = e->h2d;
         tr.res.d2h_bytes = e->d2h;
         tr.res.seconds = tr.t_done;
     }
     for (int i = 0; i < nt; i++) notify(i);
-    store_costs(e);
+    if (e->measure) store_costs(e);
     return PCAGB_OK;
 }
 
@@ -1668,6 +1690,8 @@ int engine_init(pcagb_engine *e, int device, size_t budget)
     CK(cudaEventCreate(&e->ev1));
     CK(cudaEventCreate(&e->ev2));
     CK(cudaEventCreate(&e->ev3));
+    CK(cudaEventCreate(&e->evk0));
+    CK(cudaEventCreate(&e->evk1));
     {
         /* CUDA loads a kernel at its first launch; load them all now, so no
            solve pays a module load inside its timing (the autotuner's
@@ -2050,7 +2074,7 @@ void pcagb_engine_destroy(pcagb_engine_t *e)
     cudaFree(e->d_task_io);
     cudaFree(e->d_hist);
     if (e->h_pin) cudaFreeHost(e->h_pin);
-    for (cudaEvent_t ev : {e->ev0, e->ev1, e->ev2, e->ev3})
+    for (cudaEvent_t ev : {e->ev0, e->ev1, e->ev2, e->ev3, e->evk0, e->evk1})
         if (ev) cudaEventDestroy(ev);
     if (e->stream) cudaStreamDestroy(e->stream);
     delete e;

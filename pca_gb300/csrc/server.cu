@@ -316,6 +316,9 @@ int pcagb_server_create(const pcagb_server_config_t *cfg, pcagb_server_t **out)
     }
     pcagb_server *s = new pcagb_server();
     s->cfg = *cfg;
+    /* several workers run their solves at once: none of them times its
+       stages alone */
+    if (cfg->workers > 1) s->cfg.opts.shared_gpu = 1;
     if (cudaSetDevice(cfg->device) != cudaSuccess) {
         srv_err("cudaSetDevice(%d) failed", cfg->device);
         delete s;

@@ -65,7 +65,8 @@ class SolveOpts(ctypes.Structure):
                 ("first_tests", ctypes.c_int),
                 ("suffix_chunk", ctypes.c_int),
                 ("stage_launch", ctypes.c_int),
-                ("reserved", ctypes.c_int * 3)]
+                ("shared_gpu", ctypes.c_int),
+                ("reserved", ctypes.c_int * 2)]
 
 
 class SolveResult(ctypes.Structure):
@@ -93,7 +94,8 @@ class SolveResult(ctypes.Structure):
                 ("prefixes_at_optimal", ctypes.c_uint64),
                 ("prefixes_to_first", ctypes.c_uint64),
                 ("ms_to_first", ctypes.c_double),
-                ("evaluations_run", ctypes.c_uint64)]
+                ("evaluations_run", ctypes.c_uint64),
+                ("gpu_ms_lanes", ctypes.c_double * MAXD)]
 
 
 class Tuning(ctypes.Structure):
@@ -385,6 +387,7 @@ class Solution:
     prefixes_to_first: int = 0
     ms_to_first: float = 0.0
     evaluations_run: int = 0
+    gpu_ms_lanes: list = field(default_factory=list)
 
 
 class EngineError(RuntimeError):
@@ -396,7 +399,7 @@ RESULT_SCALARS = ("seconds", "gpu_ms_expand", "gpu_ms_suffix", "gpu_ms_insert", 
                   "insert_children", "split_used", "prefixes_at_optimal", "prefixes_to_first",
                   "ms_to_first", "evaluations_run")
 RESULT_ARRAYS = ("candidates", "evaluations", "tried", "pruned_cum", "level_children",
-                 "level_survivors")
+                 "level_survivors", "gpu_ms_lanes")
 
 
 def solution_from_result(r: "SolveResult", progs, lens, base: int, max_depth: int) -> "Solution":
@@ -461,16 +464,12 @@ class Engine:
         if rc != 0:
             raise EngineError(f"solve failed ({rc}): {self.lib.pcagb_last_error().decode()}")
         sol = Solution(optimal_depth=r.optimal_depth, total_solutions=r.total_solutions)
-        for name in ("seconds", "gpu_ms_expand", "gpu_ms_suffix", "gpu_ms_insert",
-                     "kernel_launches", "insert_launches", "suffix_launches", "h2d_bytes",
-                     "d2h_bytes", "insert_children", "split_used", "prefixes_at_optimal",
-                     "prefixes_to_first", "ms_to_first", "evaluations_run"):
+        for name in RESULT_SCALARS:
             setattr(sol, name, getattr(r, name))
         for i in range(r.stored):
             sol.programs.append([progs[i * 16 + j] for j in range(lens[i])])
         last = max(r.optimal_depth, max_depth if r.optimal_depth < 0 else r.optimal_depth)
-        for name in ("candidates", "evaluations", "tried", "pruned_cum", "level_children",
-                     "level_survivors"):
+        for name in RESULT_ARRAYS:
             arr = getattr(r, name)
             setattr(sol, name, [arr[k] for k in range(min(last + 1, MAXD))])
         return sol
@@ -489,10 +488,12 @@ class Engine:
 
     def solve_batch(self, tasks, max_depth=4, oep_mode=OEP_EXACT_LIVE, split_depth=-1,
                     count_levels=False, sol_cap=64, on_done=None, first_only=False,
-                    first_tests=0, suffix_chunk=0):
+                    first_tests=0, suffix_chunk=0, shared_gpu=False):
         """Solve many tasks in shared launches; returns one Solution per task
         (its `seconds` is that task's time-to-proven-optimal in the batch).
-        on_done(i, Solution), if given, runs as soon as task i is decided."""
+        on_done(i, Solution), if given, runs as soon as task i is decided.
+        shared_gpu: other solves run on the GPU meanwhile (a server's slots),
+        so this solve's times update none of the autotuner's costs."""
         n = len(tasks)
         arr = (TaskSpec * n)(*tasks)
         o = SolveOpts()
@@ -500,6 +501,7 @@ class Engine:
         o.max_depth, o.split_depth, o.oep_mode = max_depth, split_depth, oep_mode
         o.count_levels, o.first_only = int(count_levels), int(first_only)
         o.first_tests, o.suffix_chunk = first_tests, suffix_chunk
+        o.shared_gpu = int(shared_gpu)
         res = (SolveResult * n)()
         cap = max(sol_cap, 1)
         progs = (ctypes.c_uint16 * (16 * cap * n))()
@@ -507,16 +509,13 @@ class Engine:
 
         def convert(i, r):
             sol = Solution(optimal_depth=r.optimal_depth, total_solutions=r.total_solutions)
-            for name in ("seconds", "gpu_ms_expand", "gpu_ms_suffix", "gpu_ms_insert",
-                         "kernel_launches", "insert_launches", "suffix_launches", "h2d_bytes",
-                         "d2h_bytes", "insert_children", "split_used", "evaluations_run"):
+            for name in RESULT_SCALARS:
                 setattr(sol, name, getattr(r, name))
             base = i * cap
             for k in range(r.stored):
                 sol.programs.append([progs[(base + k) * 16 + j] for j in range(lens[base + k])])
             last = r.optimal_depth if r.optimal_depth >= 0 else max_depth
-            for name in ("candidates", "evaluations", "tried", "pruned_cum", "level_children",
-                         "level_survivors"):
+            for name in RESULT_ARRAYS:
                 arr2 = getattr(r, name)
                 setattr(sol, name, [arr2[k] for k in range(min(last + 1, MAXD))])
             return sol
@@ -586,9 +585,7 @@ class Engine:
         if rc != 0:
             raise EngineError(f"ordered solve failed ({rc}): {self.lib.pcagb_last_error().decode()}")
         sol = Solution(optimal_depth=r.optimal_depth, total_solutions=r.total_solutions)
-        for name in ("seconds", "gpu_ms_expand", "gpu_ms_suffix", "gpu_ms_insert",
-                     "kernel_launches", "split_used", "prefixes_at_optimal", "prefixes_to_first",
-                     "ms_to_first"):
+        for name in RESULT_SCALARS:
             setattr(sol, name, getattr(r, name))
         for i in range(r.stored):
             sol.programs.append([progs[i * 16 + j] for j in range(lens[i])])

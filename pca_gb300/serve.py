@@ -127,7 +127,8 @@ class Server:
 
             try:
                 eng.solve_batch([r.task for r in batch], max_depth=depth, oep_mode=self.oep_mode,
-                                sol_cap=self.sol_cap, on_done=deliver, first_only=True)
+                                sol_cap=self.sol_cap, on_done=deliver, first_only=True,
+                                shared_gpu=len(self.engines) > 1)
             except Exception as exc:  # noqa: BLE001 -- handed to the requests it leaves open
                 for r in batch:
                     if not r.done.is_set():

@@ -149,3 +149,37 @@ def test_task_load_keeps_at_most_32_tests(tmp_path):
                              "tests": [{"in": [i], "out": [i]} for i in range(40)]}))
     spec = L.load_task(str(p))
     assert spec.num_tests == 32 and spec.max_cycles == 1000
+
+
+def test_ctypes_mirrors_match_the_header(tmp_path):
+    """Every ctypes mirror of a struct in include/pca_gb300.h has the C
+    compiler's size and field offsets (a field appended to the header and
+    not to the mirror, or the other way round, fails here)."""
+    import shutil
+    import subprocess
+    from pca_gb300 import pcalib as P
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    mirrors = {"task_spec_t": P.TaskSpec, "search_state_t": P.SearchState,
+               "search_ctx_t": P.SearchCtx, "pcagb_opts_t": P.SolveOpts,
+               "pcagb_result_t": P.SolveResult, "pcagb_tuning_t": P.Tuning,
+               "pcagb_server_config_t": P.ServerConfig, "pcagb_server_stats_t": P.ServerStats,
+               "pcagb_level_view_t": P.LevelView, "pcagb_record_stats_t": P.RecordStats}
+    lines = ['#include <stdio.h>', '#include "pca_gb300.h"', "int main(void) {"]
+    for cname, cls in mirrors.items():
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, *_ in cls._fields_:
+            lines.append(f'printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", os.path.join(REPO, "include"), str(src), "-o", str(exe)], check=True)
+    got = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    want = []
+    for cname, cls in mirrors.items():
+        want.append(f"{cname} size {ctypes.sizeof(cls)}")
+        for fname, *_ in cls._fields_:
+            want.append(f"{cname} {fname} {getattr(cls, fname).offset}")
+    assert [g for g in got if g] == want

@@ -31,7 +31,8 @@ class FakeEngine:
         self.calls = []
         self.closed = False
 
-    def solve_batch(self, tasks, max_depth, oep_mode, sol_cap, on_done, first_only):
+    def solve_batch(self, tasks, max_depth, oep_mode, sol_cap, on_done, first_only,
+                    shared_gpu=False):
         assert first_only
         self.calls.append(list(tasks))
         time.sleep(self.delay)

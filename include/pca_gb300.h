@@ -205,7 +205,11 @@ typedef struct {
                            server's): its stage times measure the mix, so
                            they update none of the autotuner's costs and no
                            launch choice is explored on it                   */
-    int reserved[2];
+    int full_levels;    /* 1: every level with its register block; 0: the
+                           last depth's split level, which only its
+                           last-position stage reads, holds links and the
+                           first four tests (probes) only                    */
+    int reserved[1];
 } pcagb_opts_t;
 
 #define PCAGB_MAXD 17
@@ -420,6 +424,9 @@ typedef struct {
     int      chunk_n[4][4];
     uint32_t chunk_choices[4][4];
     double   launch_rt_ms;
+    double   t_child_lean_ms;          /* per child of a lean level build (the
+                                          last stage's split level: probes and
+                                          links only)                        */
 } pcagb_tuning_t;
 int  pcagb_tuning(pcagb_engine_t *e, pcagb_tuning_t *out);
 

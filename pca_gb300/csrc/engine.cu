@@ -95,6 +95,8 @@ struct Level {
     uint64_t *child_off = nullptr;  /* set when this level is expanded */
     uint64_t children = 0;
     std::vector<uint64_t> hist;     /* [task][128] states per liveness mask */
+    bool lean = false;              /* k_materialize_probe wrote it: links and probes
+                                       only (regs and flags unwritten) */
 };
 
 struct PathGather {
@@ -157,6 +159,7 @@ struct pcagb_engine {
     /* starting values: this engine's costs measured on a GB300 (one- and
        two-input depth-4 searches); every solve refines them */
     double t_child_ms = 1.8e-7;     /* device ms per child of a level build */
+    double t_child_lean_ms = 1.2e-7; /* the same for a lean level (k_materialize_probe) */
     double t_build_fixed_ms = 0.08; /* device ms of a level build's fixed part */
     double t_eval_ms[4] = {0, 1.8e-9, 1.4e-9, 1.3e-9};  /* device ms per value-class
                                                            evaluation, per suffix depth */
@@ -171,6 +174,8 @@ struct pcagb_engine {
     int force_ft = 0, force_chunk = 0;   /* per solve: pcagb_opts_t overrides */
     bool measure = true;                 /* per solve: the GPU is its own (not
                                             shared_gpu), so its times are costs */
+    int lean_K = -1;                     /* per solve: the last depth, whose stage
+                                            reads its split level lean (-1: none) */
 
     /* per batch */
     std::vector<Level> levels;
@@ -206,7 +211,8 @@ namespace {
    what earlier engines measured on the same GPU instead of the defaults. */
 struct CostModel {
     bool set = false;
-    double t_child_ms = 0, t_build_fixed_ms = 0, t_eval_ms[4] = {0, 0, 0, 0}, dedup_ratio = 0;
+    double t_child_ms = 0, t_child_lean_ms = 0, t_build_fixed_ms = 0, t_eval_ms[4] = {0, 0, 0, 0},
+           dedup_ratio = 0;
     double ft_ms[4][4] = {}, ck_ms[4][4] = {}, launch_rt_ms = 0.03;
     int ft_n[4][4] = {}, ck_n[4][4] = {};
 };
@@ -219,6 +225,7 @@ void load_costs(pcagb_engine *e)
     if (e->device < 0 || e->device >= 64 || !g_cost[e->device].set) return;
     const CostModel &c = g_cost[e->device];
     e->t_child_ms = c.t_child_ms;
+    e->t_child_lean_ms = c.t_child_lean_ms;
     e->t_build_fixed_ms = c.t_build_fixed_ms;
     for (int i = 0; i < 4; i++) e->t_eval_ms[i] = c.t_eval_ms[i];
     e->dedup_ratio = c.dedup_ratio;
@@ -235,6 +242,7 @@ void store_costs(const pcagb_engine *e)
     if (e->device < 0 || e->device >= 64) return;
     CostModel &c = g_cost[e->device];
     c.t_child_ms = e->t_child_ms;
+    c.t_child_lean_ms = e->t_child_lean_ms;
     c.t_build_fixed_ms = e->t_build_fixed_ms;
     for (int i = 0; i < 4; i++) c.t_eval_ms[i] = e->t_eval_ms[i];
     c.dedup_ratio = e->dedup_ratio;
@@ -377,8 +385,12 @@ int launch_materialize(pcagb_engine *e, const Level &P, const uint32_t *fcr_up,
 {
     LevelOut out{C.regs, C.flags, C.live, C.task, C.parent, C.cidx, C.rdl, C.own, C.probe};
     const int g = e->grid(e->occ_mat);
-    k_materialize<TPC><<<g, kThreads, 0, e->stream>>>(view(P), e->td, bitmap, word_off, out,
-                                                      split_log2(P.n, g), P.fcr, fcr_up);
+    if (C.lean)
+        k_materialize_probe<TPC><<<g, kThreads, 0, e->stream>>>(view(P), e->td, bitmap, word_off,
+                                                                out, split_log2(P.n, g), fcr_up);
+    else
+        k_materialize<TPC><<<g, kThreads, 0, e->stream>>>(view(P), e->td, bitmap, word_off, out,
+                                                          split_log2(P.n, g), P.fcr, fcr_up);
     return check_launch(e);
 }
 
@@ -391,7 +403,7 @@ int launch_materialize(pcagb_engine *e, const Level &P, const uint32_t *fcr_up,
  * space for every child and its survivor count, status, scan total and
  * histogram come back in one round trip; a larger level reads the survivor
  * count first and allocates exactly. */
-int build_level(pcagb_engine *e, int d)
+int build_level(pcagb_engine *e, int d, bool lean = false)
 {
     const GenTables &gt = gen_tables();
     Level &P = e->levels[d];
@@ -515,6 +527,7 @@ int build_level(pcagb_engine *e, int d)
         }
     }
     Level C;
+    C.lean = lean;
     /* one round trip: space for every child (the ranks of the marked
        children are below their count, whatever the table did) */
     const uint64_t space = one_sync ? children : survivors;
@@ -555,7 +568,8 @@ int build_level(pcagb_engine *e, int d)
         /* a shared GPU: the build's time is the mix's, not a cost */
     } else if (children > 100000) {
         const double per = std::max(0.0, (ms - e->t_build_fixed_ms) / (double)children);
-        e->t_child_ms = 0.7 * e->t_child_ms + 0.3 * per;
+        double &t = lean ? e->t_child_lean_ms : e->t_child_ms;
+        t = 0.7 * t + 0.3 * per;
         if (!e->no_oep) e->dedup_ratio = 0.7 * e->dedup_ratio + 0.3 * ((double)survivors / children);
     } else if (children > 0) {
         e->t_build_fixed_ms = 0.7 * e->t_build_fixed_ms + 0.3 * ms;
@@ -741,11 +755,11 @@ void record_cost(double &ms, int &n, double v)
 
 template <int TPC>
 void launch_suffix_lanes(int ft, int g, cudaStream_t st, const LevelDev &L, const TaskDev &td,
-                         const SolBuf &sb, const PrefixRange &R)
+                         const SolBuf &sb, const PrefixRange &R, const LeanDev &lean)
 {
-    if (ft == 1) k_suffix_lanes<TPC, 1><<<g, kThreads, 0, st>>>(L, td, sb, R);
-    else if (ft == 3) k_suffix_lanes<TPC, 3><<<g, kThreads, 0, st>>>(L, td, sb, R);
-    else k_suffix_lanes<TPC, 2><<<g, kThreads, 0, st>>>(L, td, sb, R);
+    if (ft == 1) k_suffix_lanes<TPC, 1><<<g, kThreads, 0, st>>>(L, td, sb, R, lean);
+    else if (ft == 3) k_suffix_lanes<TPC, 3><<<g, kThreads, 0, st>>>(L, td, sb, R, lean);
+    else k_suffix_lanes<TPC, 2><<<g, kThreads, 0, st>>>(L, td, sb, R, lean);
 }
 
 template <int TPC, int SD>
@@ -821,7 +835,11 @@ int run_stage(pcagb_engine *e, int S, int K, std::vector<TaskRun> &runs, bool fi
         uint32_t chunk = 1;
         /* a lane per prefix needs every prefix's last write: not at the root */
         const bool lanes_ok = s == 1 && S >= 1;
-        if (s >= 2 || lanes_ok) {
+        if (L.lean) {
+            /* a lean level holds no register block: a lane per prefix */
+            ck = 1;
+            chunk = 32;
+        } else if (s >= 2 || lanes_ok) {
             if (e->force_chunk >= 1) {
                 chunk = s == 1 ? (e->force_chunk >= 32 ? 32u : 1u)
                         : e->force_chunk == (int)kLaneShape ? kLaneShape
@@ -854,10 +872,13 @@ int run_stage(pcagb_engine *e, int S, int K, std::vector<TaskRun> &runs, bool fi
             if (s == 1) {
                 if (chunk == 32) {
                     const int gl = e->grid(e->occ_lanes);
+                    LeanDev lean{nullptr, nullptr, nullptr};
+                    if (L.lean)
+                        lean = LeanDev{e->levels[S - 1].regs, e->levels[S - 1].live, L.cidx};
                     /* the kernel's own device time (without the count pass) */
                     cudaEventRecord(e->evk0, e->stream);
-                    if (t16) launch_suffix_lanes<16>(ft, gl, e->stream, V, e->td, sb, R);
-                    else launch_suffix_lanes<32>(ft, gl, e->stream, V, e->td, sb, R);
+                    if (t16) launch_suffix_lanes<16>(ft, gl, e->stream, V, e->td, sb, R, lean);
+                    else launch_suffix_lanes<32>(ft, gl, e->stream, V, e->td, sb, R, lean);
                     cudaEventRecord(e->evk1, e->stream);
                     lane_launches++;
                 } else {
@@ -1162,7 +1183,9 @@ int autotune_split(pcagb_engine *e, int K, const std::vector<uint8_t> &active,
             const double free_b = (double)(e->top - e->bottom);
             bool fits = true;
             for (int d = D + 1; d <= S; d++) {
-                build += kids * e->t_child_ms + e->t_build_fixed_ms;
+                /* the last stage's split level is built lean */
+                const bool lean = d == S && S == K - 1 && K == e->lean_K;
+                build += kids * (lean ? e->t_child_lean_ms : e->t_child_ms) + e->t_build_fixed_ms;
                 double slots = 1024;
                 while (slots < 2 * kids) slots *= 2;
                 const double states = kids * std::min(1.0, 1.5 * e->dedup_ratio);
@@ -1299,6 +1322,12 @@ int run_batch(pcagb_engine *e, std::vector<TaskRun> &runs, const pcagb_opts_t &o
     }
     e->TPC = maxT <= 16 ? 16 : 32;
     e->no_oep = o.oep_mode == PCAGB_OEP_NONE;
+    /* the last depth's split level may be built lean when nothing but its
+       lane-per-prefix stage reads it: not for the reference's counters (every
+       level to K), an ordered solve (its callback sees the level), a forced
+       warp per prefix at depth 1, or a caller that asks for full levels */
+    const bool warp_forced = o.suffix_chunk >= 1 && o.suffix_chunk < 32;
+    e->lean_K = !o.count_levels && !ord && !warp_forced && !o.full_levels ? maxK : -1;
     e->td = TaskDev{e->d_task_T, e->d_task_target, e->d_task_active,
                     o.oep_mode == PCAGB_OEP_EXACT_LIVE, o.oep_mode != PCAGB_OEP_NONE};
     CK(cudaSetDevice(e->device));
@@ -1443,7 +1472,10 @@ int run_batch(pcagb_engine *e, std::vector<TaskRun> &runs, const pcagb_opts_t &o
         while ((int)e->levels.size() - 1 < S_target &&
                (int)e->levels.size() - 1 < e->max_feasible) {
             const int d = (int)e->levels.size() - 1;
-            int rc = build_level(e, d);
+            /* the last depth's split level, read by nothing but its
+               last-position stage, is built lean */
+            const bool lean = K == e->lean_K && d + 1 == S_target && S_target == K - 1;
+            int rc = build_level(e, d, lean);
             if (rc == PCAGB_ENOMEM) {
                 e->max_feasible = d;
                 break;
@@ -2088,6 +2120,7 @@ int pcagb_tuning(pcagb_engine_t *e, pcagb_tuning_t *out)
     memset(out, 0, sizeof *out);
     for (int i = 0; i < 4; i++) out->t_eval_ms[i] = e->t_eval_ms[i];
     out->t_child_ms = e->t_child_ms;
+    out->t_child_lean_ms = e->t_child_lean_ms;
     out->t_build_fixed_ms = e->t_build_fixed_ms;
     out->dedup_ratio = e->dedup_ratio;
     memcpy(out->first_tests_ms, e->ft_ms, sizeof e->ft_ms);

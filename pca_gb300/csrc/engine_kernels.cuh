@@ -103,6 +103,16 @@ struct LevelDev {
     const uint16_t *probe;  /* [n][8][4] r0..r7 on the first four tests, 64 bytes a state */
 };
 
+/* A lean level (k_materialize_probe: links and probes, no register block)
+   reaches its states' registers through their parents: the level above's
+   registers and liveness, and the lean level's own candidate indices.
+   up_regs == nullptr: the level is a full one. */
+struct LeanDev {
+    const uint16_t *up_regs;   /* [n_up][8][TP] */
+    const uint8_t *up_live;    /* [n_up] */
+    const uint16_t *cidx;      /* [n] candidate index of each state in its parent's list */
+};
+
 struct LevelOut {
     uint16_t *regs;
     uint8_t *flags;
@@ -764,6 +774,82 @@ k_materialize(LevelDev P, TaskDev task, const uint32_t *bitmap, const uint64_t *
     }
 }
 
+/* The lean form of k_materialize, for a level that only the last position
+ * reads (the lane-per-prefix scan: each state's 64-byte probe, its links,
+ * and on a hit the registers that k_suffix_lanes recomputes from the
+ * parent). Per kept child it writes live, rdl, task, parent, cidx, own and
+ * the probe, computed from the parent's probe: no register block and no
+ * flags, 64 bytes a state instead of 8 x TPC x 2 + TPC + 64. A warp takes a
+ * parent (or a slice of its 32-candidate groups, as k_materialize), stages
+ * the parent's probe in shared memory, and each lane settles its own
+ * candidate. */
+template <int TPC>
+__global__ void __launch_bounds__(kThreads)
+k_materialize_probe(LevelDev P, TaskDev task, const uint32_t *bitmap, const uint64_t *word_off,
+                    LevelOut C, uint32_t split_log2, const uint32_t *fcr_up)
+{
+    static_assert(TPC == 16 || TPC == 32, "a state holds 16 or 32 tests");
+    __shared__ __align__(16) uint16_t spp[kWarpsPerBlock][8][4];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    uint16_t (&PP)[8][4] = spp[wib];
+    const uint64_t nw = (uint64_t)gridDim.x * kWarpsPerBlock;
+    const uint32_t split = 1u << split_log2;
+    for (uint64_t it = (uint64_t)blockIdx.x * kWarpsPerBlock + wib; it < (P.n << split_log2);
+         it += nw) {
+        const uint64_t q = it >> split_log2;
+        const uint32_t g = (uint32_t)it & (split - 1);
+        const uint32_t tid = P.task[q];
+        if (!task.active[tid]) continue;
+        const int T = task.T[tid];
+        __syncwarp();
+        if (lane < 8)
+            reinterpret_cast<uint2 *>(&PP[0][0])[lane] =
+                reinterpret_cast<const uint2 *>(P.probe + q * 32)[lane];
+        const uint32_t live = P.live[q];
+        __syncwarp();
+        const uint32_t m = (live >> 1) & 127u;
+        const uint32_t base = c_cand_off[m], nc = c_cand_off[m + 1] - base;
+        const uint64_t off = P.child_off[q];
+        const uint32_t W = deadable_writes(P, fcr_up, q);
+        const uint32_t groups = (nc + 31) >> 5;
+        const uint32_t per = (groups + split - 1) >> split_log2;
+        const uint32_t ga = min(groups, g * per), gb = min(groups, ga + per);
+        for (uint32_t c = ga * 32 + lane; c < gb * 32; c += 32) {
+            if (c >= nc) continue;
+            const uint64_t L = off + c;
+            const uint32_t wv = bitmap[L >> 5];
+            if (!((wv >> (L & 31)) & 1u)) continue;
+            const uint64_t rank = word_off[L >> 5] + __popc(wv & ((1u << (L & 31)) - 1u));
+            const uint32_t u = c_cand_uop[base + c];
+            const uint32_t rd = UOP_RD(u), ra = UOP_A(u), rb = UOP_B(u);
+            C.live[rank] = (uint8_t)(live | (1u << rd));
+            C.rdl[rank] = (uint8_t)rd;
+            C.task[rank] = (uint16_t)tid;
+            C.parent[rank] = (uint32_t)q;
+            C.cidx[rank] = (uint16_t)c;
+            C.own[rank] = (uint8_t)((W & ~((1u << ra) | (1u << rb) | (1u << rd)) & 0xFEu) |
+                                    (UOP_OP(u) == PCA_OP_LDI ? 1u : 0u));
+            /* the written register on tests 0..3 (0 past the task's tests,
+               as k_materialize writes them) */
+            uint32_t nv[4];
+#pragma unroll
+            for (int t = 0; t < 4; t++)
+                nv[t] = t < T ? pca_alu(UOP_OP(u), PP[ra][t], PP[rb][t], UOP_IMM(u)) & 0xFFFFu
+                              : 0u;
+            const uint32_t lo = nv[0] | (nv[1] << 16), hi = nv[2] | (nv[3] << 16);
+            uint4 *dst = reinterpret_cast<uint4 *>(C.probe + rank * 32);
+#pragma unroll
+            for (int h = 0; h < 4; h++) {
+                const uint4 old = reinterpret_cast<const uint4 *>(&PP[0][0])[h];
+                uint4 v = old;
+                if (rd == 2u * h) { v.x = lo; v.y = hi; }
+                if (rd == 2u * h + 1) { v.z = lo; v.w = hi; }
+                dst[h] = v;
+            }
+        }
+    }
+}
+
 /* hist[task][mask] += states of that task with that liveness mask. Lanes
    with the same key are counted by one atomic (states of a level are
    grouped by task and mostly by mask). With n_dev set, the level holds
@@ -1218,7 +1304,7 @@ k_suffix(LevelDev P, TaskDev task, SolBuf S, uint32_t chunks_per_prefix, uint32_
  * (w0 = 0) are left to k_suffix. */
 template <int TPC, int FT>
 __global__ void __launch_bounds__(kThreads, 5)
-k_suffix_lanes(LevelDev P, TaskDev task, SolBuf S, PrefixRange R)
+k_suffix_lanes(LevelDev P, TaskDev task, SolBuf S, PrefixRange R, LeanDev lean)
 {
     __shared__ uint32_t sV[kWarpsPerBlock][FT][8][32];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -1300,9 +1386,25 @@ k_suffix_lanes(LevelDev P, TaskDev task, SolBuf S, PrefixRange R)
                 const int TL = task.T[tidL];
                 const uint32_t tgt = lane < TL ? task.target[tidL * 32 + lane] : 0u;
                 uint32_t x = 0, y = 0;
-                if (lane < TL) {
-                    x = P.regs[(qL * 8 + a) * TPC + lane];
-                    y = P.regs[(qL * 8 + b) * TPC + lane];
+                if (!lean.up_regs) {
+                    if (lane < TL) {
+                        x = P.regs[(qL * 8 + a) * TPC + lane];
+                        y = P.regs[(qL * 8 + b) * TPC + lane];
+                    }
+                } else {
+                    /* a lean level: the prefix's registers are its parent's
+                       but for the one its last instruction wrote */
+                    const uint64_t pL = P.parent[qL];
+                    const uint32_t uL = c_cand_uop[c_cand_off[(lean.up_live[pL] >> 1) & 127u] +
+                                                   lean.cidx[qL]];
+                    const uint32_t rdL = UOP_RD(uL);
+                    if (lane < TL) {
+                        const uint16_t *up = lean.up_regs + pL * 8 * TPC + lane;
+                        const uint32_t w = pca_alu(UOP_OP(uL), up[UOP_A(uL) * TPC],
+                                                   up[UOP_B(uL) * TPC], UOP_IMM(uL)) & 0xFFFFu;
+                        x = a == rdL ? w : up[a * TPC];
+                        y = b == rdL ? w : up[b * TPC];
+                    }
                 }
                 const uint32_t vbase = c_vc_off[(liveL >> 1) & 127u];
                 while (hj) {

@@ -66,7 +66,8 @@ class SolveOpts(ctypes.Structure):
                 ("suffix_chunk", ctypes.c_int),
                 ("stage_launch", ctypes.c_int),
                 ("shared_gpu", ctypes.c_int),
-                ("reserved", ctypes.c_int * 2)]
+                ("full_levels", ctypes.c_int),
+                ("reserved", ctypes.c_int * 1)]
 
 
 class SolveResult(ctypes.Structure):
@@ -108,7 +109,8 @@ class Tuning(ctypes.Structure):
                 ("chunk_ms", (ctypes.c_double * 4) * 4),
                 ("chunk_n", (ctypes.c_int * 4) * 4),
                 ("chunk_choices", (ctypes.c_uint32 * 4) * 4),
-                ("launch_rt_ms", ctypes.c_double)]
+                ("launch_rt_ms", ctypes.c_double),
+                ("t_child_lean_ms", ctypes.c_double)]
 
 
 class ServerConfig(ctypes.Structure):
@@ -450,12 +452,13 @@ class Engine:
 
     def solve(self, task: TaskSpec, max_depth=4, oep_mode=OEP_EXACT_LIVE, split_depth=-1,
               count_levels=False, first_only=False, min_depth=0, sol_cap=4096, first_tests=0,
-              suffix_chunk=0, stage_launch=0) -> Solution:
+              suffix_chunk=0, stage_launch=0, full_levels=False) -> Solution:
         o = SolveOpts()
         self.lib.pcagb_default_opts(ctypes.byref(o))
         o.max_depth, o.min_depth, o.split_depth = max_depth, min_depth, split_depth
         o.oep_mode, o.count_levels, o.first_only = oep_mode, int(count_levels), int(first_only)
         o.first_tests, o.suffix_chunk, o.stage_launch = first_tests, suffix_chunk, stage_launch
+        o.full_levels = int(full_levels)
         r = SolveResult()
         progs = (ctypes.c_uint16 * (16 * max(sol_cap, 1)))()
         lens = (ctypes.c_int * max(sol_cap, 1))()
@@ -484,11 +487,12 @@ class Engine:
                 "t_build_fixed_ms": t.t_build_fixed_ms, "dedup_ratio": t.dedup_ratio,
                 "first_tests_ms": grid(t.first_tests_ms), "first_tests_n": grid(t.first_tests_n),
                 "chunk_ms": grid(t.chunk_ms), "chunk_n": grid(t.chunk_n),
-                "chunk_choices": grid(t.chunk_choices), "launch_rt_ms": t.launch_rt_ms}
+                "chunk_choices": grid(t.chunk_choices), "launch_rt_ms": t.launch_rt_ms,
+                "t_child_lean_ms": t.t_child_lean_ms}
 
     def solve_batch(self, tasks, max_depth=4, oep_mode=OEP_EXACT_LIVE, split_depth=-1,
                     count_levels=False, sol_cap=64, on_done=None, first_only=False,
-                    first_tests=0, suffix_chunk=0, shared_gpu=False):
+                    first_tests=0, suffix_chunk=0, shared_gpu=False, full_levels=False):
         """Solve many tasks in shared launches; returns one Solution per task
         (its `seconds` is that task's time-to-proven-optimal in the batch).
         on_done(i, Solution), if given, runs as soon as task i is decided.
@@ -502,6 +506,7 @@ class Engine:
         o.count_levels, o.first_only = int(count_levels), int(first_only)
         o.first_tests, o.suffix_chunk = first_tests, suffix_chunk
         o.shared_gpu = int(shared_gpu)
+        o.full_levels = int(full_levels)
         res = (SolveResult * n)()
         cap = max(sol_cap, 1)
         progs = (ctypes.c_uint16 * (16 * cap * n))()

@@ -85,18 +85,25 @@ def test_tuner_measures_every_choice():
     choice twice before settling on the cheapest, then each shape of the
     last position (a warp or a lane per prefix): after eleven is_power2
     depth-4 solves (their depth-4 stage, suffix depth 1, is large enough)
-    every choice has two measured costs, and the answers never change. A fresh
-    engine on the device starts from the costs earlier engines measured, so
-    the check is on the counts having grown to at least one."""
+    every choice has two measured costs, and the answers never change. The
+    solves build full levels: a lean last level (the default) has no
+    register block for a warp per prefix, so its stage always runs a lane per
+    prefix and explores tests per lane only. A fresh engine on the device
+    starts from the costs earlier engines measured, so the check is on the
+    counts having grown to at least one."""
     from pca_gb300.pcalib import Engine
     t = taskgen.is_power2_task(1)
     eng = Engine(0, 8 << 30)
     try:
-        outs = [eng.solve(t, max_depth=4, split_depth=3, sol_cap=1) for _ in range(11)]
+        outs = [eng.solve(t, max_depth=4, split_depth=3, sol_cap=1, full_levels=True)
+                for _ in range(11)]
+        lean = eng.solve(t, max_depth=4, split_depth=3, sol_cap=1)
         tun = eng.tuning()
     finally:
         eng.close()
-    assert all(o.optimal_depth == -1 for o in outs)
+    assert all(o.optimal_depth == -1 for o in outs + [lean])
+    assert lean.candidates == outs[0].candidates
+    assert tun["t_child_lean_ms"] > 0
     assert all(tun["first_tests_n"][1][ft] >= 2 for ft in (1, 2, 3))
     assert all(tun["first_tests_ms"][1][ft] > 0 for ft in (1, 2, 3))
     assert all(tun["chunk_n"][1][c] >= 2 and tun["chunk_ms"][1][c] > 0 for c in (0, 1))

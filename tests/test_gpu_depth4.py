@@ -9,7 +9,9 @@ oracle's level-synchronous restatement (tests/golden/make_depth4_fixtures.py).
     survivors, the per-depth counters, and no program within kernel depth 4;
   * synthetic tasks with 17-32 tests and one or two inputs: the optimal
     depth, the number of solving programs, the first 64 in depth-first order
-    and a digest of all of them, levels and counters; the depth-first first
+    and a digest of all of them, levels and counters (also with the search
+    capped at the optimal depth, whose split level is then built lean, and
+    with full levels); the depth-first first
     program under the automatic split, alone and in a batch; under the
     regs+flags key, the levels and the first program (one-input tasks)."""
 import hashlib
@@ -44,14 +46,17 @@ def check_levels(sol, want):
     assert sol.pruned_cum[:K + 1] == want["pruned_cum"]
 
 
-@pytest.mark.parametrize("shape", [1, 32], ids=["warp_per_prefix", "lane_per_prefix"])
+@pytest.mark.parametrize("shape,full", [(1, False), (32, False), (32, True)],
+                         ids=["warp_per_prefix", "lane_per_prefix_lean", "lane_per_prefix_full"])
 @pytest.mark.parametrize("mode,key", [(OEP_EXACT_LIVE, "exact_live"), (OEP_EXACT, "exact")])
-def test_is_power2_headline_step(engine, mode, key, shape):
+def test_is_power2_headline_step(engine, mode, key, shape, full):
+    """A warp per prefix reads full levels; a lane per prefix reads the last
+    level lean (the default) or full (full_levels)."""
     fx = D4["is_power2"]
     want = fx[key]
     spec = spec_from_json(fx["task"])
     sol = engine.solve(spec, max_depth=4, split_depth=3, oep_mode=mode, sol_cap=1 << 12,
-                       suffix_chunk=shape)
+                       suffix_chunk=shape, full_levels=full)
     assert sol.optimal_depth == want["optimal_depth"] == -1
     assert sol.total_solutions == 0 and sol.programs == []
     check_levels(sol, want)
@@ -70,6 +75,30 @@ def test_synthetic_depth4_full_set(engine, i, shape):
     sol = engine.solve(spec, max_depth=4, split_depth=3, oep_mode=OEP_EXACT_LIVE, sol_cap=cap,
                        suffix_chunk=shape)
     assert sol.optimal_depth == want["optimal_depth"]
+    assert sol.total_solutions == want["total_solutions"]
+    assert sol.programs[:64] == want["programs"]
+    assert digest(sol.programs) == want["digest"]
+    check_levels(sol, want)
+
+
+@pytest.mark.parametrize("full", [False, True], ids=["lean_last_level", "full_levels"])
+@pytest.mark.parametrize("i", range(len(TASKS)), ids=IDS)
+def test_synthetic_full_set_capped_at_optimal_depth(engine, i, full):
+    """The search capped at each task's optimal depth d (split d - 1, the
+    oracle's split there): the last depth's split level is built lean (links
+    and probes only; a hit's registers recomputed from its parent) unless
+    full_levels is set, and every solving program, the levels and the
+    counters equal the oracle's."""
+    fx = TASKS[i]
+    want = fx["exact_live"]
+    d = want["optimal_depth"]
+    if d < 2:
+        pytest.skip("optimum below kernel depth 2: the last stage reads the root")
+    spec = spec_from_json(fx["task"])
+    cap = max(want["total_solutions"], 1)
+    sol = engine.solve(spec, max_depth=d, split_depth=d - 1, oep_mode=OEP_EXACT_LIVE, sol_cap=cap,
+                       full_levels=full)
+    assert sol.optimal_depth == d
     assert sol.total_solutions == want["total_solutions"]
     assert sol.programs[:64] == want["programs"]
     assert digest(sol.programs) == want["digest"]

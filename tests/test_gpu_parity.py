@@ -101,3 +101,25 @@ def test_suffix_depths_agree(engine, split):
         s = engine.solve(spec, max_depth=3, split_depth=split, sol_cap=1 << 16)
         assert s.optimal_depth == 3
         assert s.programs and all(tuple(p) in full for p in s.programs)
+
+
+@pytest.mark.parametrize("i", FULL, ids=[IDS[i] for i in FULL])
+def test_lean_last_level_matches_full_levels(engine, i):
+    """The reference's task files (up to 16 tests) capped at their optimal
+    depth d with split d - 1: the lean last level (links and probes, a hit's
+    registers from its parent) gives the programs, counts and levels that
+    full levels give, and every program is in the canonical full set."""
+    fx = ENUM[i]
+    d = ref_depth(fx)
+    if d < 2:
+        pytest.skip("optimum below kernel depth 2: the last stage reads the root")
+    spec = spec_from_json(fx["task"])
+    full = {tuple(p) for p in MODES[i]["full"]["programs"]}
+    lean = engine.solve(spec, max_depth=d, split_depth=d - 1, sol_cap=1 << 16)
+    ref = engine.solve(spec, max_depth=d, split_depth=d - 1, sol_cap=1 << 16, full_levels=True)
+    assert lean.optimal_depth == ref.optimal_depth == d
+    assert lean.total_solutions == ref.total_solutions
+    assert lean.programs == ref.programs
+    assert lean.candidates == ref.candidates and lean.evaluations == ref.evaluations
+    assert lean.level_survivors == ref.level_survivors
+    assert lean.programs and all(tuple(p) in full for p in lean.programs)

@@ -49,12 +49,13 @@ CANDIDATES = ("candidates as the reference's enumerator counts them (tools/enume
 # choice there, a lane per prefix with two tests per lane), valid for the
 # kernel source it was taken from (SHA-256 of
 # pca_gb300/csrc/engine_kernels.cuh, first 16 hex).
-SUFFIX_CAPTURE = {"kernel": "k_suffix_lanes<32,2>", "choice": (2, 32), "inst": 313365006, "ms": 0.47264,
-                  "dram_bytes": 436963840 + 3024384, "source_sha16": "45d6c322c421d9ac",
+SUFFIX_CAPTURE = {"kernel": "k_suffix_lanes<32,2>", "choice": (2, 32), "inst": 337644723,
+                  "ms": 0.506912, "dram_bytes": 378862336 + 3662592,
+                  "source_sha16": "303ebd9c82ed1a96",
                   "file": "profiles/k_suffix_lanes_is_power2_t32_k4.md"}
 # The insert kernel's capture (profiles/k_expand_insert_is_power2_t32_level3.md):
 # DRAM bytes read + written by the level-3 launch (99.6% of a solve's children).
-INSERT_CAPTURE = {"dram_bytes": 530220032 + 169304576, "source_sha16": "45d6c322c421d9ac",
+INSERT_CAPTURE = {"dram_bytes": 529865472 + 169544448, "source_sha16": "303ebd9c82ed1a96",
                   "file": "profiles/k_expand_insert_is_power2_t32_level3.md"}
 
 
@@ -89,6 +90,8 @@ def parse():
                     help="kernel depth the headline task's IDDFS continues to after the timing")
     ap.add_argument("--c3-tasks", type=int, default=100,
                     help="synthetic tasks scanned for the CPU/GPU time-to-proven comparison")
+    ap.add_argument("--full-levels", action="store_true",
+                    help="build the last depth's split level with its register block too")
     ap.add_argument("--hbm-gb", type=float, default=0.0,
                     help="engine arena size in GB (0: 60%% of free HBM)")
     ap.add_argument("--workload", default="power2",
@@ -644,9 +647,22 @@ def run_served(args):
     configured rate and at a saturating one: the native server (admission by
     free HBM, concurrent solves on their own streams, queued requests
     batched), the slot server (fixed engines, one batch per slot) and one
-    task at a time."""
+    task at a time. Before the arms, one engine solves 100 other tasks of
+    the mix alone (untimed), so that every arm starts from the same measured
+    autotuner costs."""
     from pca_gb300 import taskgen
+    from pca_gb300.pcalib import Engine
     from pca_gb300.serve import NativeServer, SerialServer, Server, latency_summary, replay
+    # every arm's engines start from the autotuner costs one engine measures
+    # alone on the workload's tasks (untimed): the servers' solves share the
+    # GPU and measure nothing, and the plain arm would otherwise calibrate
+    # during its own measured run
+    cal = Engine(0, 4 << 30)
+    cal_tasks = [t for _, t in taskgen.poisson_stream(100, rate=args.rate, seed=5)]
+    for _ in range(2):
+        for t in cal_tasks:
+            cal.solve(t, max_depth=4, first_only=True, sol_cap=1)
+    cal.close()
     makers = (("native", lambda: NativeServer(workers=8, max_batch=64, max_depth=4)),
               ("slots", lambda: Server(slots=4, max_batch=256, max_depth=4)),
               ("plain", lambda: SerialServer(max_depth=4)))
@@ -675,7 +691,9 @@ def run_served(args):
             "config": {"workload": f"Poisson {args.rate:g} req/s (and {args.sat_rate:g} req/s), "
                                    f"{args.requests} requests, source length mix 4-8, kernel "
                                    "depth <= 4; native: 8 workers, 1 GiB arenas from an 80% "
-                                   "pool, batches of up to 64; slots: 4 engines"},
+                                   "pool, batches of up to 64; slots: 4 engines; every arm "
+                                   "starts from autotuner costs measured alone on 100 other "
+                                   "tasks of the mix"},
             "rates": out}
     print(json.dumps(line), flush=True)
 
@@ -968,11 +986,12 @@ def main():
 
     def step():
         return eng.solve(task, max_depth=args.max_depth, split_depth=args.split,
-                         oep_mode=OEP_EXACT_LIVE, sol_cap=1 << 12)
+                         oep_mode=OEP_EXACT_LIVE, sol_cap=1 << 12, full_levels=args.full_levels)
 
     # the autotuner measures each of its launch choices twice on stages this
-    # size before keeping the cheapest (three tests-per-lane choices, then
-    # two last-position shapes): those solves are untimed calibration
+    # size before keeping the cheapest (three tests-per-lane choices; with
+    # full levels also the two last-position shapes): those solves are
+    # untimed calibration
     for _ in range(12):
         step()
     for _ in range(max(3, args.warmup)):

@@ -369,6 +369,14 @@ def proof_and_time_to_optimal(eng, task, args) -> dict:
             "candidates_decided": int(sum(s.candidates))}
         if args.proof_depth > 5 or s.optimal_depth < 0:
             net, ds, used, losses, t_label, t_train = train_value_net(eng)
+            # untimed: one ordered solve to the headline depth with every
+            # stage ranked whole, so that the first use of the whole-level
+            # ranking (modules loaded and compiled in a fresh process, its
+            # buffers allocated) is not inside the timed solve
+            warm = ValueOrder(net, min_states=1, gain=0.0, full_gain=0.0)
+            eng.solve_ordered(task, warm, chunk=256, max_depth=args.max_depth,
+                              split_depth=args.split, sol_cap=4)
+            warm.close()
             vo = ValueOrder(net, min_states=1, gain=0.0)
             t0 = time.perf_counter()
             s = eng.solve_ordered(task, vo, chunk=256, max_depth=args.proof_depth,

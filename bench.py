@@ -50,12 +50,12 @@ CANDIDATES = ("candidates as the reference's enumerator counts them (tools/enume
 # kernel source it was taken from (SHA-256 of
 # pca_gb300/csrc/engine_kernels.cuh, first 16 hex).
 SUFFIX_CAPTURE = {"kernel": "k_suffix_lanes<32,2>", "choice": (2, 32), "inst": 337644723,
-                  "ms": 0.506912, "dram_bytes": 378862336 + 3662592,
-                  "source_sha16": "303ebd9c82ed1a96",
+                  "ms": 0.509696, "dram_bytes": 378859520 + 3082240,
+                  "source_sha16": "17cc19cb3689daec",
                   "file": "profiles/k_suffix_lanes_is_power2_t32_k4.md"}
 # The insert kernel's capture (profiles/k_expand_insert_is_power2_t32_level3.md):
 # DRAM bytes read + written by the level-3 launch (99.6% of a solve's children).
-INSERT_CAPTURE = {"dram_bytes": 529865472 + 169544448, "source_sha16": "303ebd9c82ed1a96",
+INSERT_CAPTURE = {"dram_bytes": 540317696 + 170325504, "source_sha16": "17cc19cb3689daec",
                   "file": "profiles/k_expand_insert_is_power2_t32_level3.md"}
 
 

@@ -69,8 +69,9 @@ constexpr size_t kArenaExternal = ~size_t(0);
 /* slots of the pinned host buffer */
 constexpr int kPinStatus = 0, kPinSurvivors = 1, kPinTotal = 2, kPinCount = 3, kPinFirst = 4,
               kPinHist = 64;
-/* A level whose children fit in this many bytes of states is written into
-   space for all of them, so its build needs one host round trip. */
+/* A level whose children's states fit in this many bytes, or in an eighth
+   of the arena's free space, is written into space for all of them, so its
+   build needs one host round trip instead of three. */
 constexpr uint64_t kOneSyncBytes = 64ull << 20;
 /* ordered solves with an automatic split (see run_batch) */
 constexpr double kOrderMinStageMs = 2.0;
@@ -131,7 +132,9 @@ struct pcagb_engine {
     char *arena = nullptr;
     size_t cap = 0, bottom = 0, top = 0;
     unsigned long long *d_small = nullptr;   /* [0] sol count [1] first [2] count
-                                                [3] value-class evaluations run */
+                                                [3] value-class evaluations run
+                                                [4] the work counter of the insert and
+                                                lean materialise kernels */
     uint32_t *d_status = nullptr;
     ulonglong2 *d_sol = nullptr;
     uint64_t sol_cap = 1u << 20;
@@ -374,8 +377,12 @@ int launch_expand(pcagb_engine *e, const Level &P, const uint32_t *fcr_up,
                   unsigned long long *table, uint64_t tmask)
 {
     const int g = e->grid(e->occ_insert);
+    /* the work-item counter the kernel's warps draw from */
+    uint32_t *next = reinterpret_cast<uint32_t *>(e->d_small + 4);
+    CK(cudaMemsetAsync(next, 0, 4, e->stream));
     k_expand_insert<TPC><<<g, kThreads, 0, e->stream>>>(view(P), e->td, table, tmask,
-                                                        e->d_status, split_log2(P.n, g), fcr_up);
+                                                        e->d_status, split_log2(P.n, g), fcr_up,
+                                                        next);
     return check_launch(e);
 }
 
@@ -385,10 +392,13 @@ int launch_materialize(pcagb_engine *e, const Level &P, const uint32_t *fcr_up,
 {
     LevelOut out{C.regs, C.flags, C.live, C.task, C.parent, C.cidx, C.rdl, C.own, C.probe};
     const int g = e->grid(e->occ_mat);
-    if (C.lean)
+    if (C.lean) {
+        uint32_t *next = reinterpret_cast<uint32_t *>(e->d_small + 4);
+        CK(cudaMemsetAsync(next, 0, 4, e->stream));
         k_materialize_probe<TPC><<<g, kThreads, 0, e->stream>>>(view(P), e->td, bitmap, word_off,
-                                                                out, split_log2(P.n, g), fcr_up);
-    else
+                                                                out, split_log2(P.n, g), fcr_up,
+                                                                next);
+    } else
         k_materialize<TPC><<<g, kThreads, 0, e->stream>>>(view(P), e->td, bitmap, word_off, out,
                                                           split_log2(P.n, g), P.fcr, fcr_up);
     return check_launch(e);
@@ -399,10 +409,10 @@ int launch_materialize(pcagb_engine *e, const Level &P, const uint32_t *fcr_up,
  *
  * The child count comes from the parent level's histogram on the host (the
  * same sum the device scan forms), so nothing waits before the insert. A
- * level whose children's states fit in kOneSyncBytes is materialised into
- * space for every child and its survivor count, status, scan total and
- * histogram come back in one round trip; a larger level reads the survivor
- * count first and allocates exactly. */
+ * level whose children's states fit in kOneSyncBytes or an eighth of the
+ * free arena is materialised into space for every child and its survivor
+ * count, status, scan total and histogram come back in one round trip; a
+ * larger level reads the survivor count first and allocates exactly. */
 int build_level(pcagb_engine *e, int d, bool lean = false)
 {
     const GenTables &gt = gen_tables();
@@ -444,7 +454,8 @@ int build_level(pcagb_engine *e, int d, bool lean = false)
     if (children >= (1ull << 38)) return fail(PCAGB_ENOMEM);
     const uint64_t words = (children + 31) / 32;
     const uint64_t state_bytes = 8ull * 2 * e->TPC + e->TPC + 1 + 2 + 4 + 2 + 1 + 1 + 1 + 64;
-    const bool one_sync = children * state_bytes <= kOneSyncBytes;
+    const bool one_sync =
+        children * state_bytes <= std::max<uint64_t>(kOneSyncBytes, (e->top - e->bottom) / 8);
 
     cudaEventRecord(e->ev0, e->stream);
     uint32_t *bitmap = (uint32_t *)e->alloc_top(words * 4 + 4);
@@ -2246,8 +2257,12 @@ int pcagb_internal_solve_batch_arena(pcagb_engine_t *e, void *arena, size_t byte
         o.max_depth = max_depths[i];
         if (!make_run(&tasks[i], o, &runs[i])) return PCAGB_EINVAL;
     }
-    e->arena = (char *)arena;
-    e->cap = bytes & ~size_t(255);
+    /* the arena's allocations start on 256-byte boundaries (the kernels'
+       16-byte pieces and vector loads rely on it): align a supplied base */
+    const uintptr_t base = (uintptr_t)arena, aligned = (base + 255) & ~uintptr_t(255);
+    if (bytes < aligned - base) { set_err("arena of %zu bytes", bytes); return PCAGB_EINVAL; }
+    e->arena = (char *)aligned;
+    e->cap = (bytes - (aligned - base)) & ~size_t(255);
     DoneCtx c{tasks, &o, &runs, results, sol_progs, sol_lens, cap, on_done, user, 0};
     int rc = run_batch(e, runs, o, deliver, &c);
     e->arena = nullptr;

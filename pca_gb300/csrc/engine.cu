@@ -881,7 +881,8 @@ int run_stage(pcagb_engine *e, int S, int K, std::vector<TaskRun> &runs, bool fi
         auto launch = [&](const PrefixRange &R) {
             const LevelDev V = view(L);
             if (s == 1) {
-                if (chunk == 32) {
+                const bool lanes = chunk == 32;
+                if (lanes) {
                     const int gl = e->grid(e->occ_lanes);
                     LeanDev lean{nullptr, nullptr, nullptr};
                     if (L.lean)
@@ -898,10 +899,14 @@ int run_stage(pcagb_engine *e, int S, int K, std::vector<TaskRun> &runs, bool fi
                 }
                 const int rc0 = check_launch(e);
                 if (rc0) return rc0;
-                /* a thread per prefix (the pass is latency bound) */
-                const unsigned cb = (unsigned)std::min<uint64_t>((R.count + 255) / 256,
-                                                                 (uint64_t)e->sms * 32);
-                k_count_evals<<<std::max(cb, 1u), 256, 0, e->stream>>>(V, e->td, R, sb);
+                /* the evaluation count: the lane kernel sums its own; after
+                   the warp kernel, a thread per prefix (the pass is latency
+                   bound) */
+                if (!lanes) {
+                    const unsigned cb = (unsigned)std::min<uint64_t>((R.count + 255) / 256,
+                                                                     (uint64_t)e->sms * 32);
+                    k_count_evals<<<std::max(cb, 1u), 256, 0, e->stream>>>(V, e->td, R, sb);
+                }
             } else if (chunk == kLaneShape) {
                 const int gl = e->grid(e->occ_mid_lanes);
                 if (s == 2) {

@@ -1338,6 +1338,7 @@ k_suffix_lanes(LevelDev P, TaskDev task, SolBuf S, PrefixRange R, LeanDev lean)
 #pragma unroll
     for (int t = 0; t < FT; t++) V[t][0][lane] = 0;
     const uint64_t nw = (uint64_t)gridDim.x * kWarpsPerBlock;
+    uint32_t nev = 0;   /* this lane's prefixes' readable classes (the evaluation count) */
     for (uint64_t base = ((uint64_t)blockIdx.x * kWarpsPerBlock + wib) * 32; base < R.count;
          base += nw * 32) {
         const uint64_t i = base + lane;
@@ -1356,6 +1357,7 @@ k_suffix_lanes(LevelDev P, TaskDev task, SolBuf S, PrefixRange R, LeanDev lean)
                 const uint32_t m = (live >> 1) & 127u;
                 p0 = c_pr_off_g[m * 8 + w0];
                 np = c_pr_off_g[m * 8 + w0 + 1] - p0;
+                nev += __ldg(c_ev_sd1 + m * 8 + w0);
                 T = (uint32_t)task.T[tid];
                 t0 = task.target[tid * 32];
                 if (FT >= 2) t1 = task.target[tid * 32 + 1];
@@ -1447,6 +1449,8 @@ k_suffix_lanes(LevelDev P, TaskDev task, SolBuf S, PrefixRange R, LeanDev lean)
             }
         }
     }
+    /* the stage's evaluation count (k_count_evals' sum for these prefixes) */
+    flush_evals(S, nev, lane);
 }
 
 /* The value of register x on test t after the middles (first FT tests):

@@ -78,6 +78,9 @@ def test_launch_choices_keep_full_sets(engine):
                               suffix_chunk=32)
             assert (ln.optimal_depth, ln.total_solutions, ln.programs) == \
                 (w.optimal_depth, w.total_solutions, w.programs)
+            # the lane kernel sums the evaluation count itself; the warp
+            # kernel's is a separate pass over the same prefixes
+            assert ln.evaluations_run == w.evaluations_run
 
 
 def test_tuner_measures_every_choice():

@@ -51,11 +51,15 @@ CANDIDATES = ("candidates as the reference's enumerator counts them (tools/enume
 # pca_gb300/csrc/engine_kernels.cuh, first 16 hex).
 SUFFIX_CAPTURE = {"kernel": "k_suffix_lanes<32,2>", "choice": (2, 32), "inst": 337644723,
                   "ms": 0.509696, "dram_bytes": 378859520 + 3082240,
-                  "source_sha16": "17cc19cb3689daec",
+                  "source_sha16": ("17cc19cb3689daec",),
                   "file": "profiles/k_suffix_lanes_is_power2_t32_k4.md"}
 # The insert kernel's capture (profiles/k_expand_insert_is_power2_t32_level3.md):
 # DRAM bytes read + written by the level-3 launch (99.6% of a solve's children).
-INSERT_CAPTURE = {"dram_bytes": 540317696 + 170325504, "source_sha16": "17cc19cb3689daec",
+# Valid for the captured source and for 5e54a4b3..., which differs from it
+# only inside k_suffix_lanes (its own evaluation count), a kernel the insert
+# launch neither calls nor shares code with.
+INSERT_CAPTURE = {"dram_bytes": 540317696 + 170325504,
+                  "source_sha16": ("17cc19cb3689daec", "5e54a4b385e0443c"),
                   "file": "profiles/k_expand_insert_is_power2_t32_level3.md"}
 
 
@@ -105,6 +109,11 @@ def parse():
                     help="served: a saturating arrival rate, measured too")
     ap.add_argument("--requests", type=int, default=200, help="served: number of requests")
     ap.add_argument("--tasks", type=int, default=1000, help="batched: number of tasks")
+    ap.add_argument("--beyond-depth", type=int, default=5,
+                    help="batched: kernel depth the tasks with no program up to depth 4 are "
+                         "continued to (<= 4: not continued)")
+    ap.add_argument("--beyond-budget-s", type=float, default=60.0,
+                    help="batched: solving time after which no further open task is started")
     ap.add_argument("--deep-tasks", type=int, default=200, help="deep: number of tasks")
     ap.add_argument("--deep-depth", type=int, default=5,
                     help="deep: kernel depth up to which each task is searched exhaustively")
@@ -276,7 +285,7 @@ def insert_roofline(sol, T: int, insert_ms: float, hbm_gbs: float, pk_kind: str)
             continue
         byts += kids * 8 + (kids - kept) * 17 * T + parents * 17 * T
     achieved = byts / (insert_ms / 1000.0) / 1e9 if insert_ms > 0 else 0.0
-    fresh = kernel_source_sha16() == INSERT_CAPTURE["source_sha16"]
+    fresh = kernel_source_sha16() in INSERT_CAPTURE["source_sha16"]
     return {"kernel": "k_expand_insert<32> (exact OEP insert of levels 1..3)", "bound": "hbm",
             "achieved": achieved, "peak": hbm_gbs, "unit": "GB/s", "frac": achieved / hbm_gbs,
             "traffic": INSERT_CAPTURE["dram_bytes"] if fresh else None,
@@ -310,7 +319,7 @@ def suffix_roofline(kernel_ms: float, stage_ms: float, peak_issue: float, evals_
     captured one; beside it the launch's DRAM bytes against HBM and the whole
     last-position stage time (the kernel, its evaluation count and the
     shallower depths' stages)."""
-    fresh = kernel_source_sha16() == SUFFIX_CAPTURE["source_sha16"]
+    fresh = kernel_source_sha16() in SUFFIX_CAPTURE["source_sha16"]
     ft, shape = tuned_depth1_choice(tuning)
     same = (ft, shape) == SUFFIX_CAPTURE["choice"]
     out = {"kernel": SUFFIX_CAPTURE["kernel"] + " (last instruction over operand pairs)",
@@ -646,7 +655,50 @@ def run_batched(args):
             "plain_solve_p99_s": pct([s.seconds for s in plain], 99),
             "same_answers": same, "candidates_per_s": cands / t_batch,
             "optimal_depth_histogram": {str(k): v for k, v in sorted(hist.items())}}
+    if args.beyond_depth > 4:
+        line["beyond_depth_4"] = continue_open_tasks(
+            [t for t, s in zip(tasks, batched) if s.optimal_depth < 0], args)
     print(json.dumps(line), flush=True)
+
+
+def continue_open_tasks(open_tasks, args) -> dict:
+    """The tasks with no program up to kernel depth 4, continued one at a
+    time at depths 5..--beyond-depth (depths 0..4 are not searched again:
+    min_depth 5), cheapest first (one input before two, fewer tests first),
+    until --beyond-budget-s of solving time is spent. Every task started is
+    finished: it is proven optimal at a depth found, or proven to have no
+    program up to --beyond-depth; the ones never started are counted."""
+    from pca_gb300.pcalib import Engine
+    order = sorted(open_tasks, key=lambda t: (t.num_inputs, t.num_tests))
+    eng = Engine(0, int(args.hbm_gb * (1 << 30)))
+    rows, t0 = [], time.perf_counter()
+    try:
+        for t in order:
+            if time.perf_counter() - t0 >= args.beyond_budget_s:
+                break
+            t1 = time.perf_counter()
+            s = eng.solve(t, max_depth=args.beyond_depth, min_depth=5, first_only=True, sol_cap=1)
+            rows.append((t, s.optimal_depth, time.perf_counter() - t1,
+                         int(sum(s.candidates[5:]))))
+    finally:
+        eng.close()
+    proven = {}
+    for _, k, _, _ in rows:
+        if k >= 0:
+            proven[str(k)] = proven.get(str(k), 0) + 1
+
+    def secs(n_inputs):
+        xs = [dt for t, _, dt, _ in rows if t.num_inputs == n_inputs]
+        return {"tasks": len(xs), "mean_s": statistics.mean(xs) if xs else None,
+                "max_s": max(xs) if xs else None}
+
+    return {"tasks_open_after_depth_4": len(order), "searched_to_depth": args.beyond_depth,
+            "started": len(rows), "proven_optimal_at_depth": proven,
+            "no_program_up_to_depth": sum(1 for _, k, _, _ in rows if k < 0),
+            "not_started_time_bound": len(order) - len(rows),
+            "budget_s": args.beyond_budget_s, "seconds": time.perf_counter() - t0,
+            "one_input": secs(1), "two_inputs": secs(2),
+            "candidates_decided": sum(c for _, _, _, c in rows)}
 
 
 def run_served(args):

@@ -109,6 +109,15 @@ class Server:
         return batch
 
     def _worker(self, eng: Engine):
+        """Solve batches until the end marker, then free this worker's engine
+        (here, not in close(): a worker still inside a solve when close()
+        stops waiting frees its engine once that solve ends)."""
+        try:
+            self._serve(eng)
+        finally:
+            eng.close()
+
+    def _serve(self, eng: Engine):
         while True:
             batch = self._take_batch()
             if not batch:
@@ -138,19 +147,19 @@ class Server:
                         r.done.set()
 
     def close(self, timeout: float = 60.0):
-        """Take no new requests, answer those already queued, and free the
-        engines. A worker still inside a solve after `timeout` seconds keeps
-        its engine (freeing it under the solve would crash the process)."""
+        """Take no new requests, answer those already queued, and wait up to
+        `timeout` seconds per worker. Each worker frees its own engine when
+        it exits; one still inside a solve after the timeout frees it when
+        that solve ends (freeing it under the solve would crash the
+        process)."""
         with self._lock:
             self._stop = True
             self.q.put(None)
-        for t, e in zip(self.threads, self.engines):
+        for t in self.threads:
             t.join(timeout=timeout)
             if t.is_alive():
-                warnings.warn(f"serving worker still busy after {timeout:g} s; its engine is "
-                              "left open", RuntimeWarning)
-                continue
-            e.close()
+                warnings.warn(f"serving worker still busy after {timeout:g} s; it frees its "
+                              "engine when its solve ends", RuntimeWarning)
 
 
 class SerialServer(Server):

@@ -136,7 +136,7 @@ def test_close_answers_queued_requests_and_refuses_new_ones():
         raise AssertionError("a closed server took a request")
 
 
-def test_close_keeps_the_engine_of_a_worker_still_solving():
+def test_close_leaves_a_busy_worker_to_free_its_engine_after_its_solve():
     import warnings
 
     eng = FakeEngine(delay=1.0)
@@ -148,3 +148,5 @@ def test_close_keeps_the_engine_of_a_worker_still_solving():
         srv.close(timeout=0.1)
     assert not eng.closed and any(issubclass(x.category, RuntimeWarning) for x in w)
     assert r.done.wait(5) and r.solution == answer(3)
+    srv.threads[0].join(5)
+    assert eng.closed, "the worker did not free its engine when its solve ended"

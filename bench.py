@@ -49,9 +49,9 @@ CANDIDATES = ("candidates as the reference's enumerator counts them (tools/enume
 # choice there, a lane per prefix with two tests per lane), valid for the
 # kernel source it was taken from (SHA-256 of
 # pca_gb300/csrc/engine_kernels.cuh, first 16 hex).
-SUFFIX_CAPTURE = {"kernel": "k_suffix_lanes<32,2>", "choice": (2, 32), "inst": 337644723,
-                  "ms": 0.509696, "dram_bytes": 378859520 + 3082240,
-                  "source_sha16": ("17cc19cb3689daec",),
+SUFFIX_CAPTURE = {"kernel": "k_suffix_lanes<32,2>", "choice": (2, 32), "inst": 336474909,
+                  "ms": 0.521024, "dram_bytes": 379046912 + 266496,
+                  "source_sha16": ("5e54a4b385e0443c",),
                   "file": "profiles/k_suffix_lanes_is_power2_t32_k4.md"}
 # The insert kernel's capture (profiles/k_expand_insert_is_power2_t32_level3.md):
 # DRAM bytes read + written by the level-3 launch (99.6% of a solve's children).

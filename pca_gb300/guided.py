@@ -223,6 +223,12 @@ class ValueOrder:
         self._graphs = {}
         _LIVE_ORDERS.add(self)
 
+    def new_solve(self):
+        """Forget the levels scored so far (Engine.solve_ordered calls this
+        before each solve): levels are keyed by device address, size and
+        depth, which a level of another solve can repeat."""
+        self._cache = {}
+
     def close(self):
         """Release the captured ranking graphs and their buffers (also done
         for every live ValueOrder when the interpreter exits, while the CUDA

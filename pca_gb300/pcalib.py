@@ -557,6 +557,12 @@ class Engine:
         self.lib.pcagb_default_opts(ctypes.byref(o))
         o.max_depth, o.split_depth, o.oep_mode = max_depth, split_depth, oep_mode
         keep, errors = [], []
+        # an order object that keeps per-level state (ValueOrder's scored
+        # levels, keyed by device address) starts every solve afresh: a new
+        # solve's level can sit at a freed level's address
+        new_solve = getattr(order_fn, "new_solve", None)
+        if new_solve is not None:
+            new_solve()
 
         def cb(vp, _user):
             # An exception must not cross the C boundary (ctypes would hand

@@ -100,3 +100,25 @@ def test_order_callback_must_return_a_device_permutation_tensor():
     assert lib.order_returns == [None]
     sol = eng.solve_ordered(taskgen.negate_task(1), lambda view: None)
     assert sol.optimal_depth == 3 and lib.order_returns == [None, None]
+
+
+def test_order_object_starts_every_solve_afresh():
+    """An order object with per-level state (ValueOrder keys scored levels
+    by device address, size and depth) is told before each ordered solve,
+    so a level of a later solve at a freed level's address is scored anew."""
+    eng, _ = _engine()
+    events = []
+
+    class Order:
+        def new_solve(self):
+            events.append("new_solve")
+
+        def __call__(self, view):
+            events.append("order")
+            return None
+
+    order = Order()
+    task = taskgen.negate_task(1)
+    eng.solve_ordered(task, order)
+    eng.solve_ordered(task, order)
+    assert events == ["new_solve", "order", "new_solve", "order"]

@@ -110,10 +110,11 @@ def parse():
     ap.add_argument("--requests", type=int, default=200, help="served: number of requests")
     ap.add_argument("--tasks", type=int, default=1000, help="batched: number of tasks")
     ap.add_argument("--beyond-depth", type=int, default=5,
-                    help="batched: kernel depth the tasks with no program up to depth 4 are "
-                         "continued to (<= 4: not continued)")
+                    help="batched and served: kernel depth the tasks with no program up to "
+                         "depth 4 are continued to, after the timed arms (<= 4: not continued)")
     ap.add_argument("--beyond-budget-s", type=float, default=60.0,
-                    help="batched: solving time after which no further open task is started")
+                    help="batched and served: solving time after which no further open task "
+                         "is started")
     ap.add_argument("--deep-tasks", type=int, default=200, help="deep: number of tasks")
     ap.add_argument("--deep-depth", type=int, default=5,
                     help="deep: kernel depth up to which each task is searched exhaustively")
@@ -727,6 +728,7 @@ def run_served(args):
               ("slots", lambda: Server(slots=4, max_batch=256, max_depth=4)),
               ("plain", lambda: SerialServer(max_depth=4)))
     out = {}
+    open_tasks = []
     for rate in (args.rate, args.sat_rate):
         trace = taskgen.poisson_stream(args.requests, rate=rate, seed=11)
         row = {}
@@ -739,6 +741,9 @@ def run_served(args):
             srv.close()
             row[name] = latency_summary(reqs)
             row[name]["solves"] = len(srv.batches)
+            if name == "native" and rate == args.rate:
+                open_tasks = [r.task for r in reqs
+                              if r.solution is not None and r.solution.optimal_depth < 0]
         for name in ("native", "slots"):
             row[name]["p99_ratio_plain_over_this"] = (row["plain"]["p99_s"] / row[name]["p99_s"]
                                                       if row[name]["p99_s"] else None)
@@ -755,6 +760,8 @@ def run_served(args):
                                    "starts from autotuner costs measured alone on 100 other "
                                    "tasks of the mix"},
             "rates": out}
+    if args.beyond_depth > 4:
+        line["beyond_depth_4"] = continue_open_tasks(open_tasks, args)
     print(json.dumps(line), flush=True)
 
 

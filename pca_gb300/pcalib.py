@@ -552,7 +552,8 @@ class Engine:
         the order order_fn(view) returns (a device tensor of uint32/int32
         prefix indices, or None for DFS order), `chunk` prefixes in the first
         launch of a stage and twice as many in each next one, stopping at the
-        first launch of the optimal depth with a solution."""
+        first launch of the optimal depth with a solution. An order_fn with a
+        new_solve() method has it called before the solve starts."""
         o = SolveOpts()
         self.lib.pcagb_default_opts(ctypes.byref(o))
         o.max_depth, o.split_depth, o.oep_mode = max_depth, split_depth, oep_mode

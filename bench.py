@@ -663,12 +663,13 @@ def run_batched(args):
 
 
 def continue_open_tasks(open_tasks, args) -> dict:
-    """The tasks with no program up to kernel depth 4, continued one at a
-    time at depths 5..--beyond-depth (depths 0..4 are not searched again:
-    min_depth 5), cheapest first (one input before two, fewer tests first),
-    until --beyond-budget-s of solving time is spent. Every task started is
-    finished: it is proven optimal at a depth found, or proven to have no
-    program up to --beyond-depth; the ones never started are counted."""
+    """The tasks with no program up to kernel depth 4, solved again one at a
+    time up to --beyond-depth (the IDDFS repeats depths 1..4, milliseconds
+    against a depth-5 pass of a third of a second or more), cheapest first
+    (one input before two, fewer tests first), until --beyond-budget-s of
+    solving time is spent. Every task started is finished: it is proven
+    optimal at a depth found, or proven to have no program up to
+    --beyond-depth; the ones never started are counted."""
     from pca_gb300.pcalib import Engine
     order = sorted(open_tasks, key=lambda t: (t.num_inputs, t.num_tests))
     eng = Engine(0, int(args.hbm_gb * (1 << 30)))
@@ -678,7 +679,7 @@ def continue_open_tasks(open_tasks, args) -> dict:
             if time.perf_counter() - t0 >= args.beyond_budget_s:
                 break
             t1 = time.perf_counter()
-            s = eng.solve(t, max_depth=args.beyond_depth, min_depth=5, first_only=True, sol_cap=1)
+            s = eng.solve(t, max_depth=args.beyond_depth, first_only=True, sol_cap=1)
             rows.append((t, s.optimal_depth, time.perf_counter() - t1,
                          int(sum(s.candidates[5:]))))
     finally:

@@ -178,7 +178,9 @@ typedef struct pcagb_engine pcagb_engine_t;
 
 typedef struct {
     int max_depth;      /* largest kernel depth K tried (IDDFS 0..max_depth) */
-    int min_depth;      /* first K tried (0 = from the root check)           */
+    int min_depth;      /* 0: start with the root check (K = 0, a live
+                           register already holding the target); > 0: skip
+                           it. Depths 1..max_depth are always searched.      */
     int split_depth;    /* deepest level built with OEP; -1 = automatic      */
     int oep_mode;       /* PCAGB_OEP_*                                       */
     int count_levels;   /* 1: build every level up to K with OEP so that the

@@ -1,6 +1,6 @@
 """Host logic of bench.py's proofs past depth 4 (continue_open_tasks), over a
-stand-in engine: the open tasks are continued cheapest first (one input
-before two, fewer tests first) at depths 5.. only, every task started is
+stand-in engine: the open tasks are solved again to the deeper cap, cheapest
+first (one input before two, fewer tests first), every task started is
 finished, none is started once the time budget is spent, and the counts add
 up."""
 import os
@@ -19,8 +19,8 @@ class FakeEngine:
     def __init__(self, device, budget):
         self.closed = False
 
-    def solve(self, task, max_depth, min_depth, first_only, sol_cap):
-        FakeEngine.calls.append((task.name, max_depth, min_depth))
+    def solve(self, task, max_depth, first_only, sol_cap):
+        FakeEngine.calls.append((task.name, max_depth))
         time.sleep(task.cost)
         k = task.answer
         cands = [0] * 5 + [7] * (max_depth - 4 if k < 0 else k - 4)
@@ -46,7 +46,7 @@ def test_open_tasks_continue_cheapest_first_within_the_budget(monkeypatch):
     # one input first (fewer tests first), then two; the budget is spent
     # during "b", so "d" is never started
     assert [c[0] for c in FakeEngine.calls] == ["c", "a", "b"]
-    assert all(c[1:] == (5, 5) for c in FakeEngine.calls)
+    assert all(c[1] == 5 for c in FakeEngine.calls)
     assert out["tasks_open_after_depth_4"] == 4 and out["started"] == 3
     assert out["proven_optimal_at_depth"] == {"5": 1}
     assert out["no_program_up_to_depth"] == 2 and out["not_started_time_bound"] == 1
